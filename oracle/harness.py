@@ -1,0 +1,267 @@
+"""ctypes harness over the CPU oracle (oracle/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: the oracle is the checker for the CUDA engine and
+is loaded only by tests, __graft_entry__.smoke() and bench.py's CPU-baseline
+leg. It shares the engine's ctypes struct mirrors (the same C layouts) and
+nothing else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import importlib
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+ORACLE_DIR = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(ORACLE_DIR)
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+A = importlib.import_module("cuacd-web_gb300._abi")
+Mesh = importlib.import_module("cuacd-web_gb300.mesh").Mesh
+_lib = None
+
+
+def build_oracle():
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)
+    ref_src = "/root/reference/wasm/quickhull/QuickHull.cpp"
+    if os.path.exists(ref_src):
+        subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref"], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = os.path.join(ORACLE_DIR, "liboracle.so")
+    if not os.path.exists(path):
+        build_oracle()
+    L = C.CDLL(path)
+    P = C.POINTER
+    L.orc_tree_create.restype = C.c_void_p
+    L.orc_tree_create.argtypes = [P(A.TreeConfig)]
+    L.orc_tree_destroy.argtypes = [C.c_void_p]
+    L.orc_plane_slots.argtypes = [C.c_void_p]
+    L.orc_tree_run.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, P(C.c_float), C.c_int, P(A.RunOpts),
+                               P(A.SeedResult), P(A.RunStats)]
+    L.orc_tree_hull_meshes.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, C.c_int, C.c_int, P(C.c_uint32),
+                                       C.c_uint32, P(C.c_float), P(C.c_uint32), P(C.c_int32)]
+    for f in ("orc_read_items", "orc_read_parts", "orc_read_jobs"):
+        getattr(L, f).argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, P(C.c_uint32)]
+    L.orc_read_part_geometry.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float), P(C.c_uint32), P(C.c_uint32)]
+    L.orc_read_plane.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float)]
+    L.orc_last_items.restype = C.c_uint32
+    L.orc_last_items.argtypes = [C.c_void_p]
+    L.orc_last_error.restype = C.c_char_p
+    L.orc_hausdorff_gpu.argtypes = [P(A.MeshRef), P(A.MeshRef), C.c_int, P(C.c_uint32), P(C.c_float)]
+    L.orc_hausdorff_cpu.argtypes = [P(A.MeshRef), P(A.MeshRef), C.c_int, P(C.c_double)]
+    L.orc_sample_gpu.argtypes = [P(A.MeshRef), C.c_uint32, P(C.c_float), C.c_uint32]
+    L.orc_signed_volume.restype = C.c_double
+    L.orc_signed_volume.argtypes = [P(A.MeshRef)]
+    L.orc_is_closed.argtypes = [P(A.MeshRef)]
+    L.orc_plane_cut.argtypes = [P(A.MeshRef), P(C.c_double), P(C.c_float), P(C.c_uint32), P(C.c_float),
+                                P(C.c_uint32), C.c_uint32, C.c_uint32, P(C.c_uint32)]
+    L.orc_concave_planes.argtypes = [P(A.MeshRef), C.c_int, C.c_double, C.c_double, C.c_uint32, P(C.c_float), C.c_int]
+    L.orc_hull_volume.restype = C.c_double
+    L.orc_hull_volume.argtypes = [P(A.MeshRef), C.c_int]
+    L.orc_rv_cost.restype = C.c_float
+    L.orc_rv_cost.argtypes = [C.c_float, C.c_float]
+    L.orc_eval_candidates.argtypes = [P(A.MeshRef), P(C.c_double), C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_double)]
+    L.orc_load_qh_ref.argtypes = [C.c_char_p]
+    ref = os.path.join(ORACLE_DIR, "_ref", "libqh_ref.so")
+    if os.path.exists(ref):
+        try:
+            L.orc_load_qh_ref(ref.encode())
+        except OSError:
+            pass
+    _lib = L
+    return L
+
+
+def qh_ref_loaded() -> bool:
+    return bool(lib().orc_qh_ref_loaded())
+
+
+class OracleTree:
+    """CPU restatement of GpuTree (src/gpu/tree.ts) with the engine's interface."""
+
+    def __init__(self, **cfg):
+        self.cfg = A.make_config(**cfg)
+        self.h = lib().orc_tree_create(C.byref(self.cfg))
+        if not self.h:
+            raise ValueError(lib().orc_last_error().decode())
+        self.plane_slots = lib().orc_plane_slots(self.h)
+
+    def destroy(self):
+        if self.h:
+            lib().orc_tree_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.destroy()
+
+    def run(self, seeds, edge_planes=None, depth=0, width=-1, n_edge_cuts=-1, refine=None):
+        seeds = [A.as_mesh(s) for s in seeds]
+        ma = A.MeshArray(seeds)
+        n = len(seeds)
+        k = self.plane_slots
+        ep = np.zeros((max(n, 1), k, 4), np.float32)
+        if edge_planes is not None:
+            for i, p in enumerate(edge_planes):
+                p = np.asarray(p, np.float32).reshape(-1, 4)[:k]
+                ep[i, : len(p)] = p
+        opts = A.RunOpts(depth=depth, width=width, nEdgeCuts=n_edge_cuts)
+        spacing = None
+        if refine:
+            opts.refineRounds = refine["rounds"]
+            opts.refineProbes = refine["probes"]
+            spacing = np.asarray(refine["spacing"], np.float32)
+            opts.refineSpacing = A.fptr(spacing)
+        out = (A.SeedResult * max(n, 1))()
+        st = A.RunStats()
+        rc = lib().orc_tree_run(self.h, ma.arr, n, A.fptr(ep), k, C.byref(opts), out, C.byref(st))
+        if rc != 0:
+            raise ValueError(lib().orc_last_error().decode())
+        return _result(out, st, n)
+
+    def hull_meshes(self, meshes, hull_stage=0, no_export=False):
+        meshes = [A.as_mesh(m) for m in meshes]
+        ma = A.MeshArray(meshes)
+        n = len(meshes)
+        maxnv = max(m.nv for m in meshes)
+        stride = 3 * 2 * min(self.cfg.hullMaxVerts, maxnv)
+        tris = np.zeros(n * stride, np.uint32)
+        vol = np.zeros(n, np.float32)
+        nt = np.zeros(n, np.uint32)
+        status = np.zeros(n, np.int32)
+        rc = lib().orc_tree_hull_meshes(self.h, ma.arr, n, hull_stage, int(no_export), A.uptr(tris), stride,
+                                        A.fptr(vol), A.uptr(nt), status.ctypes.data_as(C.POINTER(C.c_int32)))
+        if rc != 0:
+            raise ValueError(lib().orc_last_error().decode())
+        out = []
+        for i in range(n):
+            if status[i] != 0:
+                out.append(None)
+            else:
+                out.append(dict(tris=tris[i * stride: i * stride + 3 * nt[i]].reshape(-1, 3).copy(), volume=float(vol[i])))
+        return out, status
+
+    def items(self, first, n):
+        w = np.zeros(20 * n, np.uint32)
+        assert lib().orc_read_items(self.h, first, n, A.uptr(w)) == 0
+        return w.reshape(n, 20)
+
+    def parts(self, first, n):
+        w = np.zeros(16 * n, np.uint32)
+        assert lib().orc_read_parts(self.h, first, n, A.uptr(w)) == 0
+        return w.reshape(n, 16)
+
+    def jobs(self, first, n):
+        w = np.zeros(24 * n, np.uint32)
+        assert lib().orc_read_jobs(self.h, first, n, A.uptr(w)) == 0
+        return w.reshape(n, 24)
+
+    def part_geometry(self, idx):
+        d = self.parts(idx, 1)[0]
+        v = np.zeros(3 * d[1], np.float32)
+        t = np.zeros(3 * d[3], np.uint32)
+        e = np.zeros(8 * d[5], np.uint32)
+        lib().orc_read_part_geometry(self.h, idx, A.fptr(v), A.uptr(t), A.uptr(e))
+        return v.reshape(-1, 3), t.reshape(-1, 3), e.reshape(-1, 8)
+
+    def plane(self, idx):
+        f = np.zeros(4, np.float32)
+        lib().orc_read_plane(self.h, idx, A.fptr(f))
+        return f
+
+
+def _result(out, st, n):
+    seeds = []
+    for i in range(n):
+        s = out[i]
+        seeds.append(dict(bestCut=s.bestCut, bestCost=s.bestCost if s.valid else float("inf"),
+                          plane=list(s.plane) if s.valid else None))
+    return dict(
+        seeds=seeds, overflow=bool(st.overflow), hullFail=bool(st.hullFail), hullFailCount=st.hullFailCount,
+        npOverflow=bool(st.npOverflow), pruned=st.pruned, jobsPerLevel=list(st.jobsPerLevel[: st.nLevels]),
+        validJobs=st.validJobs, hullSlabWords=st.hullSlabWords,
+    )
+
+
+def hausdorff_gpu_form(pairs, caps=None):
+    a = A.MeshArray([A.as_mesh(p[0]) for p in pairs])
+    b = A.MeshArray([A.as_mesh(p[1]) for p in pairs])
+    out = np.zeros(len(pairs), np.float32)
+    cp = None
+    if caps is not None:
+        caps = np.asarray(caps, np.uint32)
+        cp = A.uptr(caps)
+    lib().orc_hausdorff_gpu(a.arr, b.arr, len(pairs), cp, A.fptr(out))
+    return out
+
+
+def hausdorff_cpu(a, b) -> float:
+    ma, mb = A.MeshArray([A.as_mesh(a)]), A.MeshArray([A.as_mesh(b)])
+    out = np.zeros(1, np.float64)
+    lib().orc_hausdorff_cpu(ma.arr, mb.arr, 1, out.ctypes.data_as(C.POINTER(C.c_double)))
+    return float(out[0])
+
+
+def sample_gpu_form(m, cap=0):
+    ma = A.MeshArray([A.as_mesh(m)])
+    n = lib().orc_sample_gpu(ma.arr, cap, None, 0)
+    out = np.zeros(3 * max(n, 1), np.float32)
+    lib().orc_sample_gpu(ma.arr, cap, A.fptr(out), n)
+    return out[: 3 * n].reshape(-1, 3)
+
+
+def plane_cut(m, plane):
+    m = A.as_mesh(m)
+    ma = A.MeshArray([m])
+    cap_v = 4 * m.nv + 4 * m.nt + 64
+    cap_t = 8 * m.nt + 64
+    pv, nvv = np.zeros(3 * cap_v, np.float32), np.zeros(3 * cap_v, np.float32)
+    pt, ntt = np.zeros(3 * cap_t, np.uint32), np.zeros(3 * cap_t, np.uint32)
+    cnt = np.zeros(4, np.uint32)
+    pl = np.asarray(plane, np.float64)
+    rc = lib().orc_plane_cut(ma.arr, pl.ctypes.data_as(C.POINTER(C.c_double)), A.fptr(pv), A.uptr(pt), A.fptr(nvv),
+                             A.uptr(ntt), cap_v, cap_t, A.uptr(cnt))
+    if rc != 0:
+        return None
+    pos = Mesh(pv[: 3 * cnt[0]], pt[: 3 * cnt[1]])
+    neg = Mesh(nvv[: 3 * cnt[2]], ntt[: 3 * cnt[3]])
+    return pos, neg
+
+
+def concave_planes(m, n_concave_edges=16, eps=0.005, thresh=3.49, seed=12345):
+    m = A.as_mesh(m)
+    ma = A.MeshArray([m])
+    cap = 4 * max(n_concave_edges, 1)
+    out = np.zeros(4 * cap, np.float32)
+    n = lib().orc_concave_planes(ma.arr, n_concave_edges, eps, thresh, seed, A.fptr(out), cap)
+    return out[: 4 * min(n, cap)].reshape(-1, 4)
+
+
+def hull_volume(m, use_ref=True) -> float:
+    ma = A.MeshArray([A.as_mesh(m)])
+    return float(lib().orc_hull_volume(ma.arr, int(use_ref)))
+
+
+def is_closed(m) -> bool:
+    ma = A.MeshArray([A.as_mesh(m)])
+    return bool(lib().orc_is_closed(ma.arr))
+
+
+def rv_cost(mv, hv) -> float:
+    return float(lib().orc_rv_cost(mv, hv))
+
+
+def eval_candidates(m, planes, threads=1, with_hd=True, use_ref=True):
+    ma = A.MeshArray([A.as_mesh(m)])
+    pl = np.ascontiguousarray(np.asarray(planes, np.float64).reshape(-1, 4))
+    out = np.zeros((len(pl), 8), np.float64)
+    lib().orc_eval_candidates(ma.arr, pl.ctypes.data_as(C.POINTER(C.c_double)), len(pl), threads, int(with_hd),
+                              int(use_ref), out.ctypes.data_as(C.POINTER(C.c_double)))
+    return out
