@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Cut candidates evaluated per second by the lookahead tree on GB300.
+
+Workload (the staircase configuration): the closed union of 8 boxes (1.0 x
+0.25 x k * 0.125, k = 1..8, 96 triangles in this triangulation), normalised
+to a largest extent of 2 as decompose() does, cut with width 6, width2 3,
+depth 3, 16 concave edges (64 plane slots), threshold 0.1 (minEdgeDist
+0.015) and 2 refinement rounds of 8 probes. One step is one GpuTree.run over
+a batch of maxNCutting = 160 such seeds: the tree, its evaluate kernel and
+both probe rounds. A candidate cut is a job that is valid after plan (all
+levels and rounds); the count comes from the device.
+
+value: candidates per second of device time, seeds resident on the device
+  (one CUDA-graph replay per step, CUDA events on the library's stream, L2
+  flushed by a 256 MiB write between steps, outside the timed events).
+e2e: the same metric through the public C call cuacd_tree_run with host
+  buffers: seed upload, the run and the result readback in the timed region.
+
+--impl reference: the CPU restatement of the same path (the oracle port of
+the reference's kernels) on all host threads, timed on bounded samples.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+THRESHOLD = 0.1
+TREE = dict(width=6, width2=3, depth=3, nConcaveEdges=16, minEdgeDist=min(THRESHOLD / 4, 0.015))
+POOLS = dict(vertexCap=256 << 20, triCap=256 << 20, edgeCap=16 << 20, scratchWords=256 << 20,
+             hullBudgetBytes=4 << 30, hullMaxVerts=4096)
+REFINE_ROUNDS, REFINE_PROBES = 2, 8
+METRIC = "cut candidates evaluated/s"
+UNIT = "candidates/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload(n_seeds):
+    gen = importlib.import_module("cuacd-web_gb300.meshgen")
+    mesh = importlib.import_module("cuacd-web_gb300.mesh")
+    conc = importlib.import_module("cuacd-web_gb300.concave")
+    seed, _, _ = mesh.normalize(gen.staircase(8))
+    planes = conc.concave_edge_planes(seed, TREE["nConcaveEdges"])
+    spacing = conc.refine_spacing([seed], THRESHOLD, TREE["width"])[0]
+    seeds = [seed] * n_seeds
+    refine = dict(rounds=REFINE_ROUNDS, probes=REFINE_PROBES, spacing=[spacing] * n_seeds)
+    return seeds, [planes] * n_seeds, refine
+
+
+def config_dict(n_seeds):
+    return {"workload": f"staircase-8 lookahead tree, {n_seeds} seeds per step", "mesh": "staircase-8 (96 tris, 50 verts)",
+            "seeds": n_seeds, "width": TREE["width"], "width2": TREE["width2"], "depth": TREE["depth"],
+            "nConcaveEdges": TREE["nConcaveEdges"], "threshold": THRESHOLD, "refineRounds": REFINE_ROUNDS,
+            "refineProbes": REFINE_PROBES, "l2": "flushed between timed steps (256 MiB write)"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        mhz, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                mhz.append(float(p[1]))
+                mx = max(mx, float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """dram bytes per launch of a kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", f"{kernel}_staircase160.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":")[1])
+    return None
+
+
+def cpu_tree_rate(seeds, planes, refine, threads):
+    """Oracle restatement of the tree (the CPU port) on host threads: seeds
+    are split over the threads, each with its own tree. Returns (candidates,
+    seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+
+    harness.lib()
+    threads = max(1, min(threads, len(seeds)))
+    chunks = [list(range(i, len(seeds), threads)) for i in range(threads)]
+    results = [None] * threads
+    cfg = dict(TREE, **POOLS)
+    cfg.update(vertexCap=32 << 20, triCap=32 << 20, edgeCap=4 << 20, scratchWords=32 << 20)
+    trees = [harness.OracleTree(**cfg) for _ in range(threads)]
+
+    def work(k):
+        idx = chunks[k]
+        r = trees[k].run([seeds[i] for i in idx], [planes[i] for i in idx],
+                         refine=dict(rounds=refine["rounds"], probes=refine["probes"],
+                                     spacing=[refine["spacing"][i] for i in idx]))
+        results[k] = r["validJobs"]
+
+    t0 = time.perf_counter()
+    th = [threading.Thread(target=work, args=(k,)) for k in range(threads)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    dt = time.perf_counter() - t0
+    return sum(results), dt
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, local = dist_setup(args)
+    if rank != 0:
+        return
+    n = host_threads()
+    sample = max(n, 32)
+    seeds, planes, refine = workload(sample)
+    for _ in range(args.warmup):
+        cpu_tree_rate(seeds[:n], planes[:n], refine, n)
+    cands, secs = 0, 0.0
+    for _ in range(args.steps):
+        c, s = cpu_tree_rate(seeds, planes, refine, n)
+        cands += c
+        secs += s
+    value = cands / secs
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_dict(sample),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": n, "kind": "port",
+                             "sample": f"{sample} staircase seeds per step (the oracle's restatement of the reference "
+                                       f"kernels; the reference's own path is WebGPU, unavailable on this box)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_engine(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    tree_mod = importlib.import_module("cuacd-web_gb300.tree")
+    seeds, planes, refine = workload(args.seeds)
+    g = tree_mod.GpuTree(**TREE, **POOLS)
+    g.set_profile(True)  # per-kernel CUDA events recorded as graph nodes
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- value: seeds resident on the device ----
+    g.prepare(seeds, planes, refine=refine)
+    for _ in range(args.warmup):
+        g.launch()
+        g.collect()
+    barrier()
+    dev_ms, cands = 0.0, 0
+    kms = {k: 0.0 for k in g.KERNELS}
+    kbytes = np.zeros(3, np.float64)
+    lib = tree_mod.load_library()
+    import ctypes as C
+
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            g.launch()
+            r = g.collect()
+            dev_ms += r["gpuMs"]
+            cands += r["validJobs"]
+            for k, v in g.kernel_ms().items():
+                kms[k] += v
+            b = (C.c_uint64 * 3)()
+            lib.cuacd_tree_kernel_bytes(g.h, b)
+            kbytes += np.array(list(b), np.float64)
+    barrier()
+    t_max = dev_ms
+    if world > 1:
+        tt = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * cands / (t_max / 1000.0)
+
+    # ---- e2e: public C call with host buffers ----
+    g.set_profile(False)
+    for _ in range(args.warmup):
+        g.run(seeds, planes, refine=refine)
+    barrier()
+    e2e_s = 0.0
+    e2e_c = 0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = g.run(seeds, planes, refine=refine)
+        e2e_s += time.perf_counter() - t0
+        e2e_c += r["validJobs"]
+    barrier()
+    if world > 1:
+        tt = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    n = len(seeds)
+    ps = g.plane_slots
+    h2d = sum(s.verts.nbytes + s.tris.nbytes for s in seeds) + n * ps * 16 \
+        + n * 64 + n * 80 + (16 + 1024) * 4 + n * ps * 16 + (16 + 4 * n) * 16
+    d2h = (16 + 4 * n) * 16 + 64
+
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel ----
+    dom = max((k for k in kms if k in ("plan", "emit", "hull", "scan", "record")), key=lambda k: kms[k])
+    depth, stages = TREE["depth"], 1 + REFINE_ROUNDS
+    launches_per_step = {"plan": depth * stages, "scan": depth * stages, "emit": depth * stages,
+                         "hull": 2 * depth * stages, "record": depth * stages}
+    byte_idx = {"plan": 0, "emit": 1, "hull": 2}
+    peak, peak_kind = peaks()
+    roof = None
+    if dom in byte_idx:
+        nl = launches_per_step[dom] * args.steps
+        per_launch = kbytes[byte_idx[dom]] / nl
+        avg_s = kms[dom] / 1000.0 / nl
+        achieved = per_launch / avg_s / 1e9
+        roof = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch,
+                "avg_launch_us": avg_s * 1e6, "traffic": ncu_traffic(f"k_{dom}"),
+                "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items()}}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args.seeds),
+            "e2e": {"value": world * e2e_c / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": 1000 * e2e_s / args.steps},
+            "roofline": roof, "clocks": clk.summary(),
+            "gpu_launches": args.steps * stages * (depth * 6 + 1),
+            "candidates_per_step": cands / args.steps}
+    if world == 1 and not args.no_cpu_baseline:
+        nthr = host_threads()
+        sample = 2 * nthr
+        s2, p2, r2 = workload(sample)
+        c, s = cpu_tree_rate(s2, p2, r2, nthr)
+        line["cpu_baseline"] = {"value": c / s, "unit": UNIT, "cores": nthr, "kind": "port",
+                                "sample": f"{sample} staircase seeds, one tree run with {REFINE_ROUNDS} refinement "
+                                          f"rounds on the oracle's CPU restatement ({c} candidates, {s:.1f} s)"}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--seeds", type=int, default=160)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

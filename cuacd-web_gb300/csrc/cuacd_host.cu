@@ -1,0 +1,812 @@
+// cuacd_host.cu — host driver and C ABI of the engine (include/cuacd.h).
+//
+// Mirrors the reference's GpuTree (src/gpu/tree.ts): device pools sized by
+// TreeConfig, per-run tables for up to nSeeds seeds, level layouts of the
+// tree and of the refinement rounds, and one submission per run. The whole
+// run (seed-table reset, every level's plan / scan / emit / hull / record,
+// evaluate, each refinement round) is captured once into a CUDA graph and
+// replayed; a graph is reused while the run's layout is unchanged.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/cuacd.h"
+#include "cuacd_dev.cuh"
+
+namespace cuacd {
+void launch_plan(const Level& P, const Dev& D, bool big, cudaStream_t s);
+void launch_scan(const Level& P, const Dev& D, cudaStream_t s);
+void launch_emit(const Level& P, const Dev& D, bool big, cudaStream_t s);
+void launch_record(const Level& P, const Dev& D, cudaStream_t s);
+void launch_evaluate(uint32_t stateBase, uint32_t headerOff, uint32_t mode, uint32_t nSeeds, uint32_t jobBase,
+                     uint32_t edgePlaneBase, uint32_t edgeStride, const Dev& D, cudaStream_t s);
+void launch_hull(const Level& P, const Dev& D, bool warps, cudaStream_t s);
+void launch_hd(const HdArgs& A, const Dev& D, cudaStream_t s);
+}  // namespace cuacd
+
+using namespace cuacd;
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CK(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) return fail(CUACD_E_CUDA, std::string(#x ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+static const uint32_t VIS_MAX = CUACD_VIS_MAX;
+// parts with at most this many points get a warp per hull, larger ones a block
+static const uint32_t SMALL_NV = 1024;
+// parents with more points than this get a block per plan / emit job
+static const uint32_t BIG_JOB_NV = 2048;
+
+struct LevelLayout {
+  uint32_t itemsInBase, nItemsIn, itemsOutBase, jobBase, partBase, nJobs, width, nEdgeCuts, totalWidth;
+};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need) {
+    if (need <= bytes) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (cudaMalloc(&p, need) != cudaSuccess) return fail(CUACD_E_CUDA, "device allocation failed");
+    bytes = need;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+struct HostBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need) {
+    if (need <= bytes) return 0;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+    if (cudaMallocHost(&p, need) != cudaSuccess) return fail(CUACD_E_CUDA, "pinned allocation failed");
+    bytes = need;
+    return 0;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct Tree {
+  cuacd_tree_config cfg;
+  uint32_t edgeStride = 0;
+  int device = 0, nSM = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool profile = false;
+  // profile mode: eager launches with an event after each kernel; kernel
+  // classes are reset, plan, scan, emit, hull, record, evaluate
+  std::vector<cudaEvent_t> pev;
+  std::vector<int> pcls;
+  float kernelMs[7] = {0, 0, 0, 0, 0, 0, 0};
+  uint64_t bytes[3] = {0, 0, 0};  // algorithmic bytes of plan, emit, hull in the last run
+  void mark(int cls) {
+    if (!profile) return;
+    size_t i = pcls.size();
+    if (i >= pev.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pev.push_back(e);
+    }
+    cudaEventRecord(pev[i], stream);
+    pcls.push_back(cls);
+  }
+  Dev D{};
+  DevBuf bV, bT, bE, bS, bCtr, bSlab, bParts, bItems, bJobs, bPlanes, bSnap, bHd;
+  HostBuf hStage, hRead, hSnap, hMeta;
+  uint32_t capSeeds = 0, capJobs = 0, capItems = 0, capParts = 0, capPlanes = 0;
+  // prepared run
+  bool prepared = false;
+  uint32_t nSeeds = 0, depth = 0, nProbes = 0, rounds = 0;
+  uint32_t vTop = 0, tTop = 0;
+  uint32_t slabWords = 0, slabStride = 0, nSlabsSmall = 0, nSlabsBig = 0;
+  uint32_t maxSeedNv = 0;
+  uint32_t edgePlaneBase = 0, stateBase = 0, lastItems = 0;
+  std::vector<LevelLayout> tree, probe;
+  size_t snapParts = 0, snapItems = 0, snapCtr = 0, snapEdge = 0, snapState = 0, snapBytes = 0;
+  // graph of the prepared run
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<uint64_t> gsig;
+  bool gvalid = false;
+
+  ~Tree() {
+    if (gexec) cudaGraphExecDestroy(gexec);
+    for (DevBuf* b : {&bV, &bT, &bE, &bS, &bCtr, &bSlab, &bParts, &bItems, &bJobs, &bPlanes, &bSnap, &bHd}) b->release();
+    for (HostBuf* b : {&hStage, &hRead, &hSnap, &hMeta}) b->release();
+    for (cudaEvent_t e : pev) cudaEventDestroy(e);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  void bind() {
+    D.V = (float*)bV.p; D.T = (uint32_t*)bT.p; D.E = (uint32_t*)bE.p; D.S = (uint32_t*)bS.p;
+    D.slab = (uint32_t*)bSlab.p; D.parts = (PartDesc*)bParts.p; D.items = (ItemDesc*)bItems.p;
+    D.jobs = (Job*)bJobs.p; D.planes = (float4*)bPlanes.p; D.ctr = (uint32_t*)bCtr.p;
+    D.vCap = cfg.vertexCap; D.tCap = cfg.triCap; D.eCap = cfg.edgeCap; D.sCap = cfg.scratchWords;
+  }
+  // tree.ts:191-213
+  int ensureTables(uint32_t n) {
+    if (n <= capSeeds) return 0;
+    uint64_t w0 = (uint64_t)cfg.width + edgeStride, nIn = n, totalJobs = 0;
+    for (int l = 0; l < cfg.depth; l++) {
+      uint64_t w = l == 0 ? w0 : (uint64_t)cfg.width2;
+      totalJobs += nIn * w;
+      nIn *= w;
+    }
+    uint64_t nItems = n + totalJobs;
+    uint64_t nParts = std::max<uint64_t>(n + 2 * totalJobs, capParts);
+    uint64_t nPlanes = totalJobs + (uint64_t)n * edgeStride + 16 + 4 * (uint64_t)n;
+    if (nItems > 0xffffffffull / 2 || nParts > 0xffffffffull / 2) return fail(CUACD_E_CAPACITY, "tree tables exceed 32-bit indexing");
+    int rc;
+    if ((rc = bParts.ensure(nParts * sizeof(PartDesc)))) return rc;
+    if ((rc = bItems.ensure(nItems * sizeof(ItemDesc)))) return rc;
+    if ((rc = bJobs.ensure(std::max<uint64_t>(totalJobs, 1) * sizeof(Job)))) return rc;
+    if ((rc = bPlanes.ensure(std::max<uint64_t>(nPlanes, 1) * 16))) return rc;
+    capSeeds = n; capJobs = (uint32_t)totalJobs; capItems = (uint32_t)nItems; capParts = (uint32_t)nParts;
+    capPlanes = (uint32_t)nPlanes;
+    gvalid = false;
+    bind();
+    return 0;
+  }
+  int ensurePartSlots(uint32_t n) {
+    if (n <= capParts) return 0;
+    int rc = bParts.ensure((size_t)n * sizeof(PartDesc));
+    if (rc) return rc;
+    capParts = n;
+    gvalid = false;
+    bind();
+    return 0;
+  }
+  // hull slab of the run (tree.ts:300-312) and the number of slabs in flight
+  int planSlabs(uint32_t maxNv, uint32_t nParts) {
+    uint32_t fmax = 2 * std::min<uint32_t>((uint32_t)cfg.hullMaxVerts, maxNv) + 3 * VIS_MAX + 1024;
+    slabWords = ((2 * maxNv + std::max(maxNv, 80u) + 7) & ~7u) + 16 * fmax;
+    slabStride = (slabWords + 2 * VIS_MAX + 63) & ~63u;
+    uint64_t byBudget = std::max<uint64_t>(1, cfg.hullBudgetBytes / ((uint64_t)slabStride * 4));
+    nSlabsSmall = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * 32, (uint64_t)std::max(nParts, 1u)});
+    nSlabsBig = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * 2, (uint64_t)std::max(nParts, 1u)});
+    size_t need = (size_t)std::max(nSlabsSmall, nSlabsBig) * slabStride * 4;
+    if (bSlab.bytes < need) {
+      gvalid = false;
+      int rc = bSlab.ensure(need);
+      if (rc) return rc;
+      bind();
+    }
+    return 0;
+  }
+  Level baseLevel() const {
+    Level P;
+    std::memset(&P, 0, sizeof(P));
+    P.edgeStride = edgeStride;
+    P.minEdgeDist = cfg.minEdgeDist;
+    P.hullSlabWords = slabWords;
+    P.slabStride = slabStride;
+    P.smallNv = SMALL_NV;
+    return P;
+  }
+  void hullLaunch(Level P) {
+    P.nSlabs = nSlabsSmall;
+    launch_hull(P, D, true, stream);
+    P.nSlabs = nSlabsBig;
+    launch_hull(P, D, false, stream);
+  }
+  // upload meshes at the start of the pools and write their part descriptors
+  // (tree.ts:233-278); returns the host-side descriptors in parts
+  int uploadMeshes(const cuacd_mesh* m, uint32_t n, std::vector<PartDesc>& parts) {
+    uint64_t totV = 0, totT = 0;
+    for (uint32_t k = 0; k < n; k++) {
+      if (m[k].nv && !m[k].verts) return fail(CUACD_E_INVALID, "mesh has vertices but no vertex pointer");
+      if (m[k].nt && !m[k].tris) return fail(CUACD_E_INVALID, "mesh has triangles but no index pointer");
+      totV += 3ull * m[k].nv;
+      totT += 3ull * m[k].nt;
+    }
+    if (totV > cfg.vertexCap || totT > cfg.triCap) return fail(CUACD_E_CAPACITY, "seed meshes exceed pool capacity");
+    int rc = hStage.ensure(std::max<size_t>((totV + totT) * 4, 64));
+    if (rc) return rc;
+    float* hv = (float*)hStage.p;
+    uint32_t* ht = (uint32_t*)(hv + totV);
+    parts.assign(n, PartDesc{});
+    uint32_t vt = 0, tt = 0;
+    for (uint32_t k = 0; k < n; k++) {
+      std::memcpy(hv + vt, m[k].verts, 12ull * m[k].nv);
+      if (m[k].nt) std::memcpy(ht + tt, m[k].tris, 12ull * m[k].nt);
+      PartDesc& p = parts[k];
+      std::memset(&p, 0, sizeof(p));
+      p.vOff = vt; p.nv = m[k].nv; p.tOff = tt; p.nt = m[k].nt;
+      p.planeIds[0] = p.planeIds[1] = p.planeIds[2] = p.planeIds[3] = CUACD_NONE;
+      p.flags = m[k].nt == 0 ? 2u : 0u;
+      vt += 3 * m[k].nv;
+      tt += 3 * m[k].nt;
+    }
+    if (totV) CK(cudaMemcpyAsync(D.V, hv, totV * 4, cudaMemcpyHostToDevice, stream));
+    if (totT) CK(cudaMemcpyAsync(D.T, ht, totT * 4, cudaMemcpyHostToDevice, stream));
+    vTop = vt;
+    tTop = tt;
+    return 0;
+  }
+
+  std::vector<LevelLayout> layout(uint32_t n, uint32_t dep, uint32_t w0, uint32_t ne0) const {
+    std::vector<LevelLayout> lv;
+    uint32_t itemsInBase = 0, nItemsIn = n, itemsOutBase = n, jobBase = 0;
+    for (uint32_t l = 0; l < dep; l++) {
+      uint32_t width = l == 0 ? w0 : (uint32_t)cfg.width2;
+      uint32_t nEdge = l == 0 ? ne0 : 0;
+      uint32_t tw = width + nEdge;
+      uint32_t nJobs = nItemsIn * tw;
+      lv.push_back(LevelLayout{itemsInBase, nItemsIn, itemsOutBase, jobBase, n + 2 * jobBase, nJobs, width, nEdge, tw});
+      itemsInBase = itemsOutBase;
+      nItemsIn = nJobs;
+      itemsOutBase += nJobs;
+      jobBase += nJobs;
+    }
+    return lv;
+  }
+
+  int prepare(const cuacd_mesh* seeds, int n, const float* edgePlanes, int planesPerSeed, const cuacd_run_opts* o) {
+    CK(cudaStreamSynchronize(stream));
+    prepared = false;
+    cuacd_run_opts def;
+    std::memset(&def, 0, sizeof(def));
+    def.width = -1;
+    def.nEdgeCuts = -1;
+    if (!o) o = &def;
+    if (n < 0) return fail(CUACD_E_INVALID, "negative seed count");
+    uint32_t dep = o->depth > 0 ? (uint32_t)o->depth : (uint32_t)cfg.depth;
+    uint32_t width0 = o->width >= 0 ? (uint32_t)o->width : (uint32_t)cfg.width;
+    uint32_t nEdge0 = std::min<uint32_t>(o->nEdgeCuts >= 0 ? (uint32_t)o->nEdgeCuts : edgeStride, edgeStride);
+    if (width0 % 3 != 0 || width0 > (uint32_t)cfg.width) return fail(CUACD_E_INVALID, "width override must be a multiple of 3 and <= configured width");
+    if (dep < 1 || dep > (uint32_t)cfg.depth) return fail(CUACD_E_INVALID, "depth out of range for this tree");
+    nSeeds = (uint32_t)n;
+    depth = dep;
+    if (n == 0) { prepared = true; return 0; }
+    bool refine = o->refineRounds > 0 && o->refineProbes >= 3;
+    nProbes = refine ? std::min<uint32_t>((uint32_t)o->refineProbes, edgeStride) : 0;
+    rounds = refine ? (uint32_t)o->refineRounds : 0;
+    int rc = ensureTables(nSeeds);
+    if (rc) return rc;
+    maxSeedNv = 0;
+    for (int k = 0; k < n; k++) maxSeedNv = std::max(maxSeedNv, seeds[k].nv);
+    tree = layout(nSeeds, depth, width0, nEdge0);
+    probe = refine ? layout(nSeeds, depth, 0, nProbes) : std::vector<LevelLayout>();
+    uint32_t maxChild = 0;
+    for (auto& L : tree) maxChild = std::max(maxChild, 2 * L.nJobs);
+    for (auto& L : probe) maxChild = std::max(maxChild, 2 * L.nJobs);
+    if ((rc = planSlabs(maxSeedNv, maxChild))) return rc;
+    std::vector<PartDesc> parts;
+    if ((rc = uploadMeshes(seeds, nSeeds, parts))) return rc;
+    edgePlaneBase = capJobs;
+    stateBase = edgePlaneBase + capSeeds * edgeStride;
+    // snapshot: seed parts | seed items | counters | edge planes | evaluate state
+    snapParts = 0;
+    snapItems = snapParts + (size_t)nSeeds * sizeof(PartDesc);
+    snapCtr = snapItems + (size_t)nSeeds * sizeof(ItemDesc);
+    snapEdge = snapCtr + CTR_WORDS * 4;
+    snapState = snapEdge + (size_t)nSeeds * edgeStride * 16;
+    snapBytes = snapState + (16 + 4 * (size_t)nSeeds) * 16;
+    if ((rc = hSnap.ensure(snapBytes))) return rc;
+    uint8_t* h = (uint8_t*)hSnap.p;
+    std::memset(h, 0, snapBytes);
+    std::memcpy(h + snapParts, parts.data(), (size_t)nSeeds * sizeof(PartDesc));
+    ItemDesc* items = (ItemDesc*)(h + snapItems);
+    for (uint32_t k = 0; k < nSeeds; k++) {
+      items[k].partIds[0] = k;
+      items[k].np = 1;
+      items[k].srcPart = k;
+      items[k].initialCut = CUACD_NONE;
+      items[k].nLevels = 0;
+      items[k].flags = 1;
+      items[k].parentItem = CUACD_NONE;
+    }
+    uint32_t* ctr = (uint32_t*)(h + snapCtr);
+    ctr[CTR_V] = vTop;
+    ctr[CTR_T] = tTop;
+    float* ep = (float*)(h + snapEdge);
+    if (edgePlanes && planesPerSeed > 0) {
+      uint32_t k0 = std::min<uint32_t>((uint32_t)planesPerSeed, edgeStride);
+      for (uint32_t k = 0; k < nSeeds; k++)
+        std::memcpy(ep + (size_t)4 * k * edgeStride, edgePlanes + (size_t)4 * k * planesPerSeed, 16ull * k0);
+    }
+    uint32_t* su = (uint32_t*)(h + snapState);
+    float* sf = (float*)su;
+    auto header = [&](uint32_t at, const std::vector<LevelLayout>& L) {
+      su[at] = depth; su[at + 1] = nSeeds; su[at + 2] = L[0].totalWidth; su[at + 3] = nProbes;
+      for (size_t l = 0; l < L.size(); l++) { su[at + 4 + 4 * l] = L[l].itemsOutBase; su[at + 5 + 4 * l] = L[l].nJobs; }
+    };
+    header(0, tree);
+    if (refine) header(20, probe);
+    for (uint32_t k = 0; k < nSeeds; k++) sf[(16 + 4 * k + 2) * 4] = (refine && o->refineSpacing) ? o->refineSpacing[k] : 0.0f;
+    if ((rc = bSnap.ensure(snapBytes))) return rc;
+    CK(cudaMemcpyAsync(bSnap.p, h, snapBytes, cudaMemcpyHostToDevice, stream));
+    const std::vector<LevelLayout>& last = refine ? probe : tree;
+    lastItems = last.back().itemsOutBase + last.back().nJobs;
+    prepared = true;
+    return 0;
+  }
+
+  // the whole run on the stream (tree.ts:559-594)
+  void enqueue() {
+    mark(-1);
+    uint8_t* snap = (uint8_t*)bSnap.p;
+    cudaMemcpyAsync(D.parts, snap + snapParts, (size_t)nSeeds * sizeof(PartDesc), cudaMemcpyDeviceToDevice, stream);
+    cudaMemcpyAsync(D.items, snap + snapItems, (size_t)nSeeds * sizeof(ItemDesc), cudaMemcpyDeviceToDevice, stream);
+    cudaMemcpyAsync(D.ctr, snap + snapCtr, CTR_WORDS * 4, cudaMemcpyDeviceToDevice, stream);
+    cudaMemcpyAsync(D.planes + edgePlaneBase, snap + snapEdge, (size_t)nSeeds * edgeStride * 16, cudaMemcpyDeviceToDevice, stream);
+    cudaMemcpyAsync(D.planes + stateBase, snap + snapState, (16 + 4 * (size_t)nSeeds) * 16, cudaMemcpyDeviceToDevice, stream);
+    mark(0);
+    auto stage = [&](const std::vector<LevelLayout>& L, uint32_t mode, uint32_t headerOff) {
+      for (uint32_t l = 0; l < L.size(); l++) {
+        const LevelLayout& v = L[l];
+        Level P = baseLevel();
+        P.itemsInBase = v.itemsInBase; P.nItemsIn = v.nItemsIn; P.itemsOutBase = v.itemsOutBase; P.jobBase = v.jobBase;
+        P.width = v.width; P.nEdgeCuts = v.nEdgeCuts; P.totalWidth = v.totalWidth;
+        P.level = l; P.totalLevels = depth; P.partBase = v.partBase;
+        P.edgePlaneBase = edgePlaneBase; P.nChildParts = 2 * v.nJobs; P.nJobs = v.nJobs;
+        P.lastLevel = l == depth - 1 ? 1u : 0u;
+        P.nSeeds = cfg.pruneLastLevel ? nSeeds : 0;
+        // parents shrink roughly by half per level
+        bool big = (maxSeedNv >> l) > BIG_JOB_NV;
+        launch_plan(P, D, big, stream);
+        mark(1);
+        launch_scan(P, D, stream);
+        mark(2);
+        launch_emit(P, D, big, stream);
+        mark(3);
+        hullLaunch(P);
+        mark(4);
+        launch_record(P, D, stream);
+        mark(5);
+      }
+      launch_evaluate(stateBase, headerOff, mode, nSeeds, L[0].jobBase, edgePlaneBase, edgeStride, D, stream);
+      mark(6);
+    };
+    stage(tree, 0, 0);
+    for (uint32_t r = 0; r < rounds; r++) {
+      cudaMemcpyAsync(D.ctr, snap + snapCtr, 4 * 4, cudaMemcpyDeviceToDevice, stream);
+      mark(0);
+      stage(probe, 1, 5);
+    }
+  }
+  std::vector<uint64_t> signature() const {
+    std::vector<uint64_t> s = {nSeeds, depth, nProbes, rounds, slabWords, slabStride, nSlabsSmall, nSlabsBig,
+                               maxSeedNv > BIG_JOB_NV ? maxSeedNv : 0, edgePlaneBase, stateBase, (uint64_t)bSnap.p,
+                               (uint64_t)bSlab.p, (uint64_t)bParts.p, (uint64_t)bItems.p, (uint64_t)bJobs.p,
+                               (uint64_t)bPlanes.p, (uint64_t)bCtr.p, snapBytes};
+    for (auto& L : tree) { s.push_back(L.nJobs); s.push_back(L.totalWidth); s.push_back(L.width); }
+    for (uint32_t l = 0; l < depth; l++) s.push_back((maxSeedNv >> l) > BIG_JOB_NV);
+    return s;
+  }
+  int launch() {
+    if (!prepared) return fail(CUACD_E_INVALID, "launch before prepare");
+    if (nSeeds == 0) return 0;
+    std::vector<uint64_t> sig = signature();
+    sig.push_back(profile ? 1 : 0);
+    if (!gvalid || sig != gsig) {
+      pcls.clear();
+      if (gexec) { cudaGraphExecDestroy(gexec); gexec = nullptr; }
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      enqueue();
+      CK(cudaStreamEndCapture(stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return fail(CUACD_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+      gsig = sig;
+      gvalid = true;
+    }
+    CK(cudaEventRecord(ev0, stream));
+    CK(cudaGraphLaunch(gexec, stream));
+    CK(cudaEventRecord(ev1, stream));
+    return 0;
+  }
+  int collect(cuacd_seed_result* out, cuacd_run_stats* st) {
+    if (!prepared) return fail(CUACD_E_INVALID, "collect before prepare");
+    if (st) std::memset(st, 0, sizeof(*st));
+    if (nSeeds == 0) return 0;
+    size_t stateBytes = (16 + 4 * (size_t)nSeeds) * 16;
+    int rc = hRead.ensure(stateBytes + 64 * 4);
+    if (rc) return rc;
+    uint8_t* h = (uint8_t*)hRead.p;
+    CK(cudaMemcpyAsync(h, D.planes + stateBase, stateBytes, cudaMemcpyDeviceToHost, stream));
+    CK(cudaMemcpyAsync(h + stateBytes, D.ctr, 16 * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaGetLastError());
+    const float* sf = (const float*)h;
+    const uint32_t* sw = (const uint32_t*)h;
+    const uint32_t* ctr = (const uint32_t*)(h + stateBytes);
+    for (uint32_t k = 0; k < nSeeds && out; k++) {
+      size_t o = (16 + 4 * (size_t)k) * 4;
+      bool valid = (sw[o + 7] & 1) != 0;
+      out[k].valid = valid ? 1 : 0;
+      out[k].bestCut = valid ? (int32_t)sw[o + 6] : -1;
+      out[k].bestCost = valid ? sf[o + 4] : INFINITY;
+      for (int a = 0; a < 4; a++) out[k].plane[a] = valid ? sf[o + a] : 0.0f;
+      out[k].reserved = 0;
+    }
+    if (st) {
+      st->overflow = ctr[CTR_OVERFLOW] != 0;
+      st->hullFail = ctr[CTR_HULLFAIL] != 0;
+      st->hullFailCount = ctr[CTR_HULLFAIL];
+      st->npOverflow = ctr[CTR_NPOVER] != 0;
+      st->pruned = ctr[CTR_PRUNED];
+      st->nLevels = (uint32_t)tree.size();
+      for (size_t l = 0; l < tree.size() && l < 4; l++) st->jobsPerLevel[l] = tree[l].nJobs;
+      st->validJobs = (uint64_t)ctr[CTR_VALID_LO] | ((uint64_t)ctr[CTR_VALID_HI] << 32);
+      st->hullSlabWords = slabWords;
+      st->hullChunkSize = nSlabsSmall;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, ev0, ev1);
+      st->gpuMs = ms;
+    }
+    for (int c = 0; c < 7; c++) kernelMs[c] = 0;
+    std::memcpy(bytes, ctr + CTR_BYTES_PLAN, sizeof(bytes));
+    if (profile) {
+      for (size_t i = 1; i < pcls.size(); i++) {
+        float d = 0;
+        cudaEventElapsedTime(&d, pev[i - 1], pev[i]);
+        if (pcls[i] >= 0) kernelMs[pcls[i]] += d;
+      }
+    }
+    return 0;
+  }
+
+  // ---- hull batches (tree.ts:382-443, 671-756) ----
+  int hulls(const cuacd_mesh* m, int n, int hullStage, uint32_t* trisOut, uint32_t exportStrideOut, float* volOut,
+            uint32_t* ntOut, int32_t* status, float* hdOut) {
+    if (n < 0) return fail(CUACD_E_INVALID, "negative mesh count");
+    if (n == 0) return 0;
+    CK(cudaStreamSynchronize(stream));
+    bool withHd = hdOut != nullptr;
+    if (withHd && n > CUACD_HD_MAX_PAIRS) return fail(CUACD_E_INVALID, "hullsWithHausdorff: at most 1024 meshes per call");
+    int rc = ensureTables(1);
+    if (rc) return rc;
+    if ((rc = ensurePartSlots(withHd ? 2 * n : n))) return rc;
+    uint32_t maxNv = 0;
+    for (int k = 0; k < n; k++) maxNv = std::max(maxNv, m[k].nv);
+    if ((rc = planSlabs(maxNv, (uint32_t)n))) return rc;
+    std::vector<PartDesc> parts;
+    if ((rc = uploadMeshes(m, (uint32_t)n, parts))) return rc;
+    const bool doExport = trisOut != nullptr || withHd;
+    uint32_t stride = doExport ? 3 * 2 * std::min<uint32_t>((uint32_t)cfg.hullMaxVerts, maxNv) : 0;
+    if ((uint64_t)tTop + (uint64_t)n * stride > cfg.triCap) return fail(CUACD_E_CAPACITY, "hull export exceeds triangle pool");
+    // sample scratch of the fused Hausdorff (tree.ts:686-698)
+    std::vector<uint32_t> capOff, capN;
+    uint64_t totalCap = 0;
+    uint32_t maxSide = 0;
+    if (withHd) {
+      capOff.resize(2 * n);
+      capN.resize(2 * n);
+      uint64_t off = 0;
+      for (int k = 0; k < n; k++) {
+        double area = mesh_area(m[k]);
+        uint64_t res = std::max<uint64_t>(1000, (uint64_t)std::floor(2000.0 * area));
+        uint64_t cap = 2 * (2 * res + std::max<uint64_t>(m[k].nt, 2ull * m[k].nv) + 16);
+        if (3 * (off + cap) > cfg.scratchWords) return fail(CUACD_E_SCRATCH, "hausdorff sample scratch exceeds capacity");
+        uint32_t ca = (uint32_t)(cap / 2), cb = (uint32_t)(cap - cap / 2);
+        capOff[k] = (uint32_t)off; capN[k] = ca;
+        capOff[n + k] = (uint32_t)(off + ca); capN[n + k] = cb;
+        off += cap;
+        maxSide = std::max(maxSide, std::max(ca, cb));
+      }
+      totalCap = off;
+    }
+    CK(cudaMemcpyAsync(D.parts, parts.data(), (size_t)n * sizeof(PartDesc), cudaMemcpyHostToDevice, stream));
+    if (withHd) CK(cudaMemsetAsync(D.parts + n, 0, (size_t)n * sizeof(PartDesc), stream));
+    CK(cudaMemsetAsync(D.ctr, 0, CTR_WORDS * 4, stream));
+    Level P = baseLevel();
+    P.nItemsIn = n; P.itemsOutBase = n; P.totalLevels = 1;
+    P.edgePlaneBase = capJobs; P.nChildParts = n; P.nJobs = 0;
+    P.exportBase = tTop; P.exportStride = stride; P.hullStage = (uint32_t)hullStage;
+    P.hdDescBase = withHd ? (uint32_t)n : 0;
+    CK(cudaEventRecord(ev0, stream));
+    hullLaunch(P);
+    if (withHd) {
+      if ((rc = runHd((uint32_t)n, 0, capOff, capN, totalCap, maxSide))) return rc;
+    }
+    CK(cudaEventRecord(ev1, stream));
+    CK(cudaGetLastError());
+    size_t pb = (size_t)n * sizeof(PartDesc), tb = (size_t)n * stride * 4;
+    if ((rc = hRead.ensure(pb + tb + 4 * (size_t)n + 64))) return rc;
+    uint8_t* h = (uint8_t*)hRead.p;
+    CK(cudaMemcpyAsync(h, D.parts, pb, cudaMemcpyDeviceToHost, stream));
+    if (tb) CK(cudaMemcpyAsync(h + pb, D.T + tTop, tb, cudaMemcpyDeviceToHost, stream));
+    if (withHd) CK(cudaMemcpyAsync(h + pb + tb, D.ctr + CTR_HD, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    const PartDesc* pd = (const PartDesc*)h;
+    const uint32_t* tw = (const uint32_t*)(h + pb);
+    const uint32_t* hdw = (const uint32_t*)(h + pb + tb);
+    for (int k = 0; k < n; k++) {
+      float vol = pd[k].hullVol;
+      uint32_t nf = doExport ? pd[k].pad0 : 4;
+      int32_t s = 0;
+      if (vol < 0.0f) s = (pd[k].flags & 3) ? (int32_t)(pd[k].flags & 3) : 9;
+      else if (nf < 4) s = 8;
+      if (status) status[k] = s;
+      if (volOut) volOut[k] = vol;
+      if (ntOut) ntOut[k] = s == 0 && doExport ? nf : 0;
+      if (trisOut && s == 0 && exportStrideOut) {
+        uint32_t cpy = std::min(3 * nf, exportStrideOut);
+        std::memcpy(trisOut + (size_t)k * exportStrideOut, tw + (size_t)k * stride, 4ull * cpy);
+      }
+      if (withHd) {
+        float w;
+        std::memcpy(&w, &hdw[k], 4);
+        hdOut[k] = std::sqrt(w);
+      }
+    }
+    return 0;
+  }
+  static double mesh_area(const cuacd_mesh& m) {
+    double area = 0;
+    for (uint32_t t = 0; t < m.nt; t++) {
+      const float* a = m.verts + 3 * m.tris[3 * t];
+      const float* b = m.verts + 3 * m.tris[3 * t + 1];
+      const float* c = m.verts + 3 * m.tris[3 * t + 2];
+      double abx = (double)b[0] - a[0], aby = (double)b[1] - a[1], abz = (double)b[2] - a[2];
+      double acx = (double)c[0] - a[0], acy = (double)c[1] - a[1], acz = (double)c[2] - a[2];
+      double nx = aby * acz - abz * acy, ny = abz * acx - abx * acz, nz = abx * acy - aby * acx;
+      area += 0.5 * std::sqrt(nx * nx + ny * ny + nz * nz);
+    }
+    return area;
+  }
+  int runHd(uint32_t nPairs, uint32_t partBase, const std::vector<uint32_t>& capOff, const std::vector<uint32_t>& capN,
+            uint64_t totalCap, uint32_t maxSide) {
+    size_t metaBytes = (size_t)(3 * 2 * nPairs) * 4;
+    size_t need = metaBytes + 256 + (size_t)totalCap * 16;
+    int rc = bHd.ensure(need);
+    if (rc) return rc;
+    uint32_t* meta = (uint32_t*)bHd.p;
+    float4* samples = (float4*)((uint8_t*)bHd.p + ((metaBytes + 255) & ~(size_t)255));
+    std::vector<uint32_t> hm(4 * nPairs);
+    std::memcpy(hm.data(), capOff.data(), 4ull * 2 * nPairs);
+    std::memcpy(hm.data() + 2 * nPairs, capN.data(), 4ull * 2 * nPairs);
+    if ((rc = hMeta.ensure(hm.size() * 4))) return rc;
+    std::memcpy(hMeta.p, hm.data(), hm.size() * 4);
+    CK(cudaMemcpyAsync(meta, hMeta.p, hm.size() * 4, cudaMemcpyHostToDevice, stream));
+    HdArgs A;
+    A.nPairs = nPairs;
+    A.nMeshes = 2 * nPairs;
+    A.capOff = meta;
+    A.capN = meta + 2 * nPairs;
+    A.ns = meta + 4 * nPairs;
+    A.samples = samples;
+    A.partBase = partBase;
+    A.maxSide = maxSide;
+    launch_hd(A, D, stream);
+    return 0;
+  }
+  // GpuTree.hausdorff (tree.ts:318-372)
+  int hausdorff(const cuacd_mesh* a, const cuacd_mesh* b, int n, float* out) {
+    if (n < 0) return fail(CUACD_E_INVALID, "negative pair count");
+    if (n == 0) return 0;
+    if (n > CUACD_HD_MAX_PAIRS) return fail(CUACD_E_INVALID, "hausdorff: at most 1024 pairs per call");
+    CK(cudaStreamSynchronize(stream));
+    int rc = ensureTables(1);
+    if (rc) return rc;
+    if ((rc = ensurePartSlots(2 * n))) return rc;
+    std::vector<cuacd_mesh> all(2 * n);
+    for (int k = 0; k < n; k++) { all[k] = a[k]; all[n + k] = b[k]; }
+    std::vector<PartDesc> parts;
+    if ((rc = uploadMeshes(all.data(), 2 * n, parts))) return rc;
+    auto bound = [](const cuacd_mesh& m) {
+      uint64_t res = std::max<uint64_t>(1000, (uint64_t)std::floor(2000.0 * mesh_area(m)));
+      return 2 * res + m.nt + 16;
+    };
+    std::vector<uint32_t> capOff(2 * n), capN(2 * n);
+    uint64_t off = 0;
+    uint32_t maxSide = 0;
+    for (int k = 0; k < n; k++) {
+      uint64_t cap = 2 * std::max(bound(a[k]), bound(b[k]));
+      if (3 * (off + cap) > cfg.scratchWords) return fail(CUACD_E_SCRATCH, "hausdorff sample scratch exceeds capacity");
+      uint32_t ca = (uint32_t)(cap / 2), cb = (uint32_t)(cap - cap / 2);
+      capOff[k] = (uint32_t)off; capN[k] = ca;
+      capOff[n + k] = (uint32_t)(off + ca); capN[n + k] = cb;
+      off += cap;
+      maxSide = std::max(maxSide, std::max(ca, cb));
+    }
+    CK(cudaMemcpyAsync(D.parts, parts.data(), 2ull * n * sizeof(PartDesc), cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(D.ctr + CTR_HD, 0, 4ull * n, stream));
+    CK(cudaEventRecord(ev0, stream));
+    if ((rc = runHd((uint32_t)n, 0, capOff, capN, off, maxSide))) return rc;
+    CK(cudaEventRecord(ev1, stream));
+    CK(cudaGetLastError());
+    if ((rc = hRead.ensure(4ull * n))) return rc;
+    CK(cudaMemcpyAsync(hRead.p, D.ctr + CTR_HD, 4ull * n, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    const uint32_t* w = (const uint32_t*)hRead.p;
+    for (int k = 0; k < n; k++) {
+      float f;
+      std::memcpy(&f, &w[k], 4);
+      out[k] = std::sqrt(f);
+    }
+    return 0;
+  }
+  int readBack(void* dst, const void* src, size_t bytes) {
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost));
+    return 0;
+  }
+};
+
+extern "C" {
+
+const char* cuacd_last_error(void) { return g_err.c_str(); }
+
+void cuacd_tree_config_default(cuacd_tree_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->width = 60;
+  c->width2 = 3;
+  c->depth = 2;
+  c->nConcaveEdges = 32;
+  c->minEdgeDist = 0.0125f;
+  c->hullMaxVerts = 4096;
+  c->vertexCap = 64ull << 20;
+  c->triCap = 64ull << 20;
+  c->edgeCap = 1ull << 20;
+  c->scratchWords = 48ull << 20;
+  c->hullBudgetBytes = 256ull << 20;
+  c->pruneLastLevel = 1;
+}
+
+void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
+  auto bad = [&](int code, const char* msg) -> void* {
+    g_err = msg;
+    if (err) *err = code;
+    return nullptr;
+  };
+  if (!c) return bad(CUACD_E_INVALID, "null config");
+  if (c->width % 3 != 0 || c->width2 % 3 != 0 || c->width < 0 || c->width2 < 0)
+    return bad(CUACD_E_INVALID, "width and width2 must be multiples of 3");
+  if (c->depth < 1 || c->depth > 4) return bad(CUACD_E_INVALID, "depth must be in 1..4");
+  if (c->vertexCap >= (1ull << 32) || c->triCap >= (1ull << 32) || c->edgeCap >= (1ull << 28) || c->scratchWords >= (1ull << 32))
+    return bad(CUACD_E_INVALID, "pool capacities must fit 32-bit offsets");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return bad(CUACD_E_NODEVICE, "no CUDA device");
+  Tree* t = new Tree();
+  t->cfg = *c;
+  t->edgeStride = (uint32_t)std::max(4 * c->nConcaveEdges, 32);
+  cudaGetDevice(&t->device);
+  cudaDeviceGetAttribute(&t->nSM, cudaDevAttrMultiProcessorCount, t->device);
+  int rc = 0;
+  if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&t->ev0) != cudaSuccess || cudaEventCreate(&t->ev1) != cudaSuccess) {
+    delete t;
+    return bad(CUACD_E_CUDA, "stream or event creation failed");
+  }
+  if ((rc = t->bV.ensure(std::max<uint64_t>(c->vertexCap, 4) * 4)) || (rc = t->bT.ensure(std::max<uint64_t>(c->triCap, 4) * 4)) ||
+      (rc = t->bE.ensure(std::max<uint64_t>(c->edgeCap, 1) * 32)) || (rc = t->bS.ensure(std::max<uint64_t>(c->scratchWords, 4) * 4)) ||
+      (rc = t->bCtr.ensure(CTR_WORDS * 4))) {
+    std::string m = g_err;
+    delete t;
+    return bad(rc, m.c_str());
+  }
+  t->bind();
+  if ((rc = t->ensureTables(16))) {
+    std::string m = g_err;
+    delete t;
+    return bad(rc, m.c_str());
+  }
+  if (err) *err = 0;
+  return t;
+}
+
+void cuacd_tree_destroy(void* t) { delete (Tree*)t; }
+int cuacd_plane_slots(const void* t) { return (int)((const Tree*)t)->edgeStride; }
+int cuacd_vis_max(void) { return CUACD_VIS_MAX; }
+void cuacd_set_profile(void* t, int on) {
+  Tree* tr = (Tree*)t;
+  tr->profile = on != 0;
+  // events are created before any capture: a profiled run records up to
+  // 2 + (1 + rounds) * (5 * depth + 2) of them as graph nodes
+  while (tr->profile && tr->pev.size() < 256) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) break;
+    tr->pev.push_back(e);
+  }
+}
+int cuacd_tree_kernel_bytes(void* t, uint64_t* bytes3) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  std::memcpy(bytes3, ((Tree*)t)->bytes, sizeof(uint64_t) * 3);
+  return 0;
+}
+int cuacd_tree_kernel_ms(void* t, float* ms7) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  std::memcpy(ms7, ((Tree*)t)->kernelMs, sizeof(float) * 7);
+  return 0;
+}
+
+int cuacd_tree_prepare(void* t, const cuacd_mesh* seeds, int n, const float* edgePlanes, int planesPerSeed,
+                       const cuacd_run_opts* opts) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  return ((Tree*)t)->prepare(seeds, n, edgePlanes, planesPerSeed, opts);
+}
+int cuacd_tree_launch(void* t) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  return ((Tree*)t)->launch();
+}
+int cuacd_tree_collect(void* t, cuacd_seed_result* out, cuacd_run_stats* st) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  return ((Tree*)t)->collect(out, st);
+}
+int cuacd_tree_run(void* t, const cuacd_mesh* seeds, int n, const float* edgePlanes, int planesPerSeed,
+                   const cuacd_run_opts* opts, cuacd_seed_result* out, cuacd_run_stats* st) {
+  int rc = cuacd_tree_prepare(t, seeds, n, edgePlanes, planesPerSeed, opts);
+  if (rc) return rc;
+  if ((rc = cuacd_tree_launch(t))) return rc;
+  return cuacd_tree_collect(t, out, st);
+}
+int cuacd_tree_hausdorff(void* t, const cuacd_mesh* a, const cuacd_mesh* b, int n, float* out) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  return ((Tree*)t)->hausdorff(a, b, n, out);
+}
+int cuacd_tree_hull_meshes(void* t, const cuacd_mesh* m, int n, int hullStage, uint32_t* trisOut, uint32_t exportStride,
+                           float* volOut, uint32_t* ntOut, int32_t* status) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  return ((Tree*)t)->hulls(m, n, hullStage, trisOut, exportStride, volOut, ntOut, status, nullptr);
+}
+int cuacd_tree_hulls_with_hausdorff(void* t, const cuacd_mesh* m, int n, uint32_t* trisOut, uint32_t exportStride,
+                                    float* volOut, uint32_t* ntOut, float* hdOut, int32_t* status) {
+  if (!t) return fail(CUACD_E_INVALID, "null tree");
+  if (!hdOut) return fail(CUACD_E_INVALID, "null Hausdorff output");
+  return ((Tree*)t)->hulls(m, n, 0, trisOut, exportStride, volOut, ntOut, status, hdOut);
+}
+int cuacd_tree_read_items(void* tp, uint32_t first, uint32_t n, uint32_t* out) {
+  Tree* t = (Tree*)tp;
+  if ((uint64_t)first + n > t->capItems) return fail(CUACD_E_INVALID, "item range out of bounds");
+  return t->readBack(out, t->D.items + first, (size_t)n * sizeof(ItemDesc));
+}
+int cuacd_tree_read_parts(void* tp, uint32_t first, uint32_t n, uint32_t* out) {
+  Tree* t = (Tree*)tp;
+  if ((uint64_t)first + n > t->capParts) return fail(CUACD_E_INVALID, "part range out of bounds");
+  return t->readBack(out, t->D.parts + first, (size_t)n * sizeof(PartDesc));
+}
+int cuacd_tree_read_jobs(void* tp, uint32_t first, uint32_t n, uint32_t* out) {
+  Tree* t = (Tree*)tp;
+  if ((uint64_t)first + n > std::max<uint32_t>(t->capJobs, 1)) return fail(CUACD_E_INVALID, "job range out of bounds");
+  return t->readBack(out, t->D.jobs + first, (size_t)n * sizeof(Job));
+}
+int cuacd_tree_read_part_geometry(void* tp, uint32_t part, float* verts, uint32_t* tris, uint32_t* edges) {
+  Tree* t = (Tree*)tp;
+  if (part >= t->capParts) return fail(CUACD_E_INVALID, "part out of bounds");
+  PartDesc pd;
+  int rc = t->readBack(&pd, t->D.parts + part, sizeof(pd));
+  if (rc) return rc;
+  if ((uint64_t)pd.vOff + 3ull * pd.nv > t->cfg.vertexCap || (uint64_t)pd.tOff + 3ull * pd.nt > t->cfg.triCap ||
+      (uint64_t)pd.eOff + pd.ne > t->cfg.edgeCap)
+    return fail(CUACD_E_INVALID, "part geometry out of pool bounds");
+  if (verts && pd.nv && (rc = t->readBack(verts, t->D.V + pd.vOff, 12ull * pd.nv))) return rc;
+  if (tris && pd.nt && (rc = t->readBack(tris, t->D.T + pd.tOff, 12ull * pd.nt))) return rc;
+  if (edges && pd.ne && (rc = t->readBack(edges, t->D.E + 8ull * pd.eOff, 32ull * pd.ne))) return rc;
+  return 0;
+}
+int cuacd_tree_read_plane(void* tp, uint32_t idx, float* out4) {
+  Tree* t = (Tree*)tp;
+  if (idx >= t->capPlanes) return fail(CUACD_E_INVALID, "plane out of bounds");
+  return t->readBack(out4, t->D.planes + idx, 16);
+}
+
+}  // extern "C"

@@ -1,0 +1,638 @@
+// hull_kernel.cu — exact incremental convex hulls of the tree's child parts
+// (the reference's hull kernel, src/gpu/shaders.ts:752-1401), on sm_103a.
+//
+// Per part: quantise to a 2^21 grid across the largest bbox extent, take the
+// extremes along 40 fixed axes as 80 seeds, build a simplex, insert the
+// seeds farthest-first, then every point still outside, farthest-first.
+// Orientation signs come from a float32 determinant when it clears a
+// rigorous rounding bound and from an exact 64/128-bit integer determinant
+// otherwise (the reference uses three 32-bit limbs; the sign is the same).
+//
+// GB300 design:
+//   * one group per part: a warp for parts up to smallNv points, a 256-thread
+//     block above; persistent groups walk the level's parts round-robin, each
+//     with its own scratch slab (owner, dist, candidates, faces, visible list)
+//   * visible faces are listed in slot order and new faces are created in
+//     horizon-edge order with group prefix sums, so the face sets are
+//     deterministic (the reference uses atomicAdd order); the most visible
+//     face and the next point break ties by the lowest index
+//   * the hull volume is an exact 128-bit sum of integer determinants
+//
+// Compiled with --fmad=false: face ranking values match the CPU oracle bit
+// for bit, and with them the insertion order and the face sets.
+#include "cuacd_dev.cuh"
+
+namespace cuacd {
+
+#define HULL_VIS_MAX 2048u
+#define ALIVE 0x80000000u
+
+// k-DOP seed axes (shaders.ts:769-810): the same table, so the seeds are the
+// same extreme points as the reference picks
+__constant__ float c_kdop[40][3] = {
+    {-0.5786893f, 0.7696723f, 0.2696723f}, {-0.7696723f, 0.2696723f, 0.5786893f},
+    {-0.2696723f, 0.5786893f, 0.7696723f}, {-0.5773503f, 0.5773503f, 0.5773503f},
+    {-0.3090170f, 0.9363390f, 0.1666667f}, {0.0000000f, 0.7453560f, 0.6666667f},
+    {0.3090170f, 0.9363390f, 0.1666667f},  {0.0000000f, 0.9341724f, 0.3568221f},
+    {-0.3090170f, 0.9363390f, -0.1666667f}, {0.3090170f, 0.9363390f, -0.1666667f},
+    {0.0000000f, 0.7453560f, -0.6666667f}, {0.0000000f, 0.9341724f, -0.3568221f},
+    {-0.5786893f, 0.7696723f, -0.2696723f}, {-0.2696723f, 0.5786893f, -0.7696723f},
+    {-0.7696723f, 0.2696723f, -0.5786893f}, {-0.5773503f, 0.5773503f, -0.5773503f},
+    {-0.7453560f, 0.6666667f, 0.0000000f}, {-0.9363390f, 0.1666667f, -0.3090170f},
+    {-0.9363390f, 0.1666667f, 0.3090170f}, {-0.9341724f, 0.3568221f, 0.0000000f},
+    {0.5786893f, 0.7696723f, 0.2696723f},  {0.2696723f, 0.5786893f, 0.7696723f},
+    {0.7696723f, 0.2696723f, 0.5786893f},  {0.5773503f, 0.5773503f, 0.5773503f},
+    {-0.1666667f, 0.3090170f, 0.9363390f}, {-0.6666667f, 0.0000000f, 0.7453560f},
+    {-0.1666667f, -0.3090170f, 0.9363390f}, {-0.3568221f, 0.0000000f, 0.9341724f},
+    {-0.9363390f, -0.1666667f, 0.3090170f}, {-0.9363390f, -0.1666667f, -0.3090170f},
+    {-0.7453560f, -0.6666667f, 0.0000000f}, {-0.9341724f, -0.3568221f, 0.0000000f},
+    {-0.6666667f, 0.0000000f, -0.7453560f}, {-0.1666667f, 0.3090170f, -0.9363390f},
+    {-0.1666667f, -0.3090170f, -0.9363390f}, {-0.3568221f, 0.0000000f, -0.9341724f},
+    {0.2696723f, 0.5786893f, -0.7696723f}, {0.5786893f, 0.7696723f, -0.2696723f},
+    {0.7696723f, 0.2696723f, -0.5786893f}, {0.5773503f, 0.5773503f, -0.5773503f},
+};
+
+struct HullSm {
+  uint32_t seed[80];
+  uint32_t nf, nalive, fail, compacted;
+  uint32_t ncand, ok;
+  uint32_t pad[2];
+};
+
+// exact sign of det[e1; e2; d] for integer vectors below 2^23 (shaders.ts:868-876)
+__device__ __forceinline__ int orient_exact(f3 e1f, f3 e2f, f3 df) {
+  long long e1x = (long long)e1f.x, e1y = (long long)e1f.y, e1z = (long long)e1f.z;
+  long long e2x = (long long)e2f.x, e2y = (long long)e2f.y, e2z = (long long)e2f.z;
+  long long dx = (long long)df.x, dy = (long long)df.y, dz = (long long)df.z;
+  long long cx = e1y * e2z - e1z * e2y;
+  long long cy = e1z * e2x - e1x * e2z;
+  long long cz = e1x * e2y - e1y * e2x;
+  __int128 det = (__int128)cx * dx + (__int128)cy * dy + (__int128)cz * dz;
+  return det > 0 ? 1 : (det < 0 ? -1 : 0);
+}
+// filtered orientation (shaders.ts:878-884)
+__device__ __forceinline__ int orient_filtered(f3 n, f3 e1, f3 e2, f3 d) {
+  float det = dot(n, d);
+  float bound = ((1e-6f * l1(e1)) * l1(e2)) * l1(d);
+  if (det > bound) return 1;
+  if (det < -bound) return -1;
+  return orient_exact(e1, e2, d);
+}
+
+struct HullCtx {
+  const float* V;
+  uint32_t vOff, nv;
+  f3 qlo;
+  float qs;
+  uint32_t fmax;
+  uint32_t* owner;
+  float* dist;
+  uint32_t* cand;
+  uint32_t* F;     // face records, 16 words each
+  uint32_t* vis;   // visible face slots (HULL_VIS_MAX)
+  uint32_t* conn;  // connected flags of the visible list (HULL_VIS_MAX)
+
+  __device__ __forceinline__ f3 qvert(uint32_t i) const {
+    f3 v = ldv(V, (size_t)vOff + 3 * (size_t)i) - qlo;
+    return mk3(rintf(v.x * qs), rintf(v.y * qs), rintf(v.z * qs));
+  }
+  __device__ __forceinline__ uint4* rec(uint32_t f) const { return reinterpret_cast<uint4*>(F + 16 * (size_t)f); }
+  __device__ __forceinline__ bool alive(uint32_t f) const { return (F[16 * (size_t)f] & ALIVE) != 0; }
+  __device__ __forceinline__ void abc(uint32_t f, uint32_t& a, uint32_t& b, uint32_t& c) const {
+    uint4 w = rec(f)[0];
+    a = w.x & 0x7fffffffu; b = w.y; c = w.z;
+  }
+  // face record: ia|alive ib ic bf | nx ny nz ax | ay az bx by | bz cx cy cz
+  __device__ __forceinline__ void face_write(uint32_t f, uint32_t a, uint32_t b, uint32_t c) const {
+    f3 pa = qvert(a), pb = qvert(b), pc = qvert(c);
+    f3 e1 = pb - pa, e2 = pc - pa;
+    f3 n = cross(e1, e2);
+    float bf = l1(e1) * l1(e2);
+    uint4* w = rec(f);
+    w[0] = make_uint4(a | ALIVE, b, c, __float_as_uint(bf));
+    w[1] = make_uint4(__float_as_uint(n.x), __float_as_uint(n.y), __float_as_uint(n.z), __float_as_uint(pa.x));
+    w[2] = make_uint4(__float_as_uint(pa.y), __float_as_uint(pa.z), __float_as_uint(pb.x), __float_as_uint(pb.y));
+    w[3] = make_uint4(__float_as_uint(pb.z), __float_as_uint(pc.x), __float_as_uint(pc.y), __float_as_uint(pc.z));
+  }
+  // positive: visible (ranking value); negative: not visible (shaders.ts:906-921)
+  __device__ __forceinline__ float face_eval(uint32_t f, f3 p) const {
+    const uint4* w = rec(f);
+    uint4 a = w[0];
+    if ((a.x & ALIVE) == 0) return -1e30f;
+    uint4 b = w[1], c = w[2];
+    f3 n = mk3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z));
+    f3 pa = mk3(__uint_as_float(b.w), __uint_as_float(c.x), __uint_as_float(c.y));
+    f3 d = p - pa;
+    float det = dot(n, d);
+    float bound = (1e-6f * __uint_as_float(a.w)) * l1(d);
+    if (det > bound) return det / fmaxf(sqrtf(dot(n, n)), 1e-30f);
+    if (det < -bound) return -1.0f;
+    uint4 e = w[3];
+    f3 pb = mk3(__uint_as_float(c.z), __uint_as_float(c.w), __uint_as_float(e.x));
+    f3 pc = mk3(__uint_as_float(e.y), __uint_as_float(e.z), __uint_as_float(e.w));
+    return orient_exact(pb - pa, pc - pa, d) > 0 ? 1e-30f : -1.0f;
+  }
+  __device__ __forceinline__ void assign(uint32_t i, uint32_t f0, uint32_t f1) const {
+    f3 pt = qvert(i);
+    uint32_t bestF = CUACD_NONE;
+    float bestD = -1.0f;
+    for (uint32_t f = f0; f < f1; f++) {
+      float dd = face_eval(f, pt);
+      if (dd > 0.0f && dd > bestD) { bestD = dd; bestF = f; }
+    }
+    owner[i] = bestF;
+    dist[i] = bestF != CUACD_NONE ? bestD : 0.0f;
+  }
+};
+
+__device__ __forceinline__ bool shares_edge(uint32_t f0, uint32_t f1, uint32_t f2, uint32_t g0, uint32_t g1, uint32_t g2) {
+  uint32_t f[3] = {f0, f1, f2};
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    uint32_t a = f[k], b = f[k == 2 ? 0 : k + 1];
+    if ((g0 == b && g1 == a) || (g1 == b && g2 == a) || (g2 == b && g0 == a)) return true;
+  }
+  return false;
+}
+
+// remove dead face slots, keeping slot order (shaders.ts:946-969)
+template <int G>
+__device__ void hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
+  const int lid = Grp<G>::lid();
+  const uint32_t nf = hs.nf;
+  uint32_t run = 0;
+  for (uint32_t c = 0; c * G < nf; c++) {
+    const uint32_t f = c * G + lid;
+    uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0, w2 = w0, w3 = w0;
+    uint32_t al = 0;
+    if (f < nf) {
+      const uint4* r = h.rec(f);
+      w0 = r[0]; w1 = r[1]; w2 = r[2]; w3 = r[3];
+      al = (w0.x & ALIVE) ? 1u : 0u;
+    }
+    uint32_t tot;
+    uint32_t pre = grp_scan_u<G>(al, &tot, sm);
+    Grp<G>::sync();
+    if (al) {
+      uint4* r = h.rec(run + pre);
+      r[0] = w0; r[1] = w1; r[2] = w2; r[3] = w3;
+    }
+    run += tot;
+    Grp<G>::sync();
+  }
+  if (lid == 0) { hs.nf = run; hs.compacted = 1; }
+  Grp<G>::sync();
+}
+
+// insert point pIdx (shaders.ts:975-1055) with the deterministic order
+template <int G>
+__device__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t pIdx) {
+  const int lid = Grp<G>::lid();
+  const f3 p = h.qvert(pIdx);
+  uint32_t nf = hs.nf;
+  const uint32_t nalive = hs.nalive;
+  if (nf + 3 * HULL_VIS_MAX > h.fmax || nf > 2 * nalive + 512) {
+    hull_compact<G>(h, hs, sm);
+    nf = hs.nf;
+  }
+  // visible faces in slot order; most visible face, lowest list position on ties
+  uint32_t nvis = 0;
+  float bd = -1.0f;
+  uint32_t bk = CUACD_NONE;
+  for (uint32_t c = 0; c * G < nf; c++) {
+    const uint32_t f = c * G + lid;
+    float dd = f < nf ? h.face_eval(f, p) : -1.0f;
+    uint32_t v = dd > 0.0f ? 1u : 0u;
+    uint32_t tot;
+    uint32_t pre = grp_scan_u<G>(v, &tot, sm);
+    if (v) {
+      uint32_t k = nvis + pre;
+      if (k < HULL_VIS_MAX) h.vis[k] = f;
+      am_merge(bd, bk, dd, k);
+    }
+    nvis += tot;
+  }
+  Grp<G>::sync();
+  if (nvis == 0) return;
+  if (nvis > HULL_VIS_MAX) {
+    if (lid == 0) hs.fail = 1;
+    Grp<G>::sync();
+    return;
+  }
+  grp_argmax<G>(bd, bk, sm);
+  const uint32_t seedK = bk;
+  for (uint32_t k = lid; k < nvis; k += G) h.conn[k] = k == seedK ? 1u : 0u;
+  Grp<G>::sync();
+  // edge-connected component of the most visible face
+  for (;;) {
+    bool changed = false;
+    for (uint32_t i = lid; i < nvis; i += G) {
+      if (h.conn[i]) continue;
+      uint32_t a, b, c;
+      h.abc(h.vis[i], a, b, c);
+      for (uint32_t j = 0; j < nvis; j++) {
+        if (j == i || !h.conn[j]) continue;
+        uint32_t x, y, z;
+        h.abc(h.vis[j], x, y, z);
+        if (shares_edge(a, b, c, x, y, z)) { h.conn[i] = 1; changed = true; break; }
+      }
+    }
+    bool any = grp_any<G>(changed, sm);
+    Grp<G>::sync();
+    if (!any) break;
+  }
+  if (nf + 3 * nvis > h.fmax) {
+    if (lid == 0) hs.fail = 2;
+    Grp<G>::sync();
+    return;
+  }
+  // horizon edges in order e = 3 * listPos + k become new faces (a, b, p)
+  uint32_t nnew = 0;
+  for (uint32_t c = 0; c * G < 3 * nvis; c++) {
+    const uint32_t e = c * G + lid;
+    uint32_t isNew = 0, a = 0, b = 0;
+    if (e < 3 * nvis) {
+      const uint32_t vi = e / 3, k = e % 3;
+      if (h.conn[vi]) {
+        uint32_t fa, fb, fc;
+        h.abc(h.vis[vi], fa, fb, fc);
+        a = k == 0 ? fa : (k == 1 ? fb : fc);
+        b = k == 0 ? fb : (k == 1 ? fc : fa);
+        bool found = false;
+        for (uint32_t j = 0; j < nvis && !found; j++) {
+          if (!h.conn[j]) continue;
+          uint32_t g0, g1, g2;
+          h.abc(h.vis[j], g0, g1, g2);
+          if ((g0 == b && g1 == a) || (g1 == b && g2 == a) || (g2 == b && g0 == a)) found = true;
+        }
+        isNew = found ? 0u : 1u;
+      }
+    }
+    uint32_t tot;
+    uint32_t pre = grp_scan_u<G>(isNew, &tot, sm);
+    if (isNew) h.face_write(nf + nnew + pre, a, b, pIdx);
+    nnew += tot;
+  }
+  Grp<G>::sync();
+  uint32_t killed = 0;
+  for (uint32_t vi = lid; vi < nvis; vi += G) {
+    if (h.conn[vi]) {
+      h.F[16 * (size_t)h.vis[vi]] &= 0x7fffffffu;
+      killed++;
+    }
+  }
+  killed = grp_sum_u<G>(killed, sm);
+  if (lid == 0) {
+    hs.nf = nf + nnew;
+    hs.nalive = nalive + nnew - killed;
+  }
+  Grp<G>::sync();
+}
+
+// farthest-first insertion of the candidate list (shaders.ts:1060-1129)
+template <int G>
+__device__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t nfPrev, uint32_t maxIter) {
+  const int lid = Grp<G>::lid();
+  uint32_t ncand = hs.ncand;
+  uint32_t sinceCompact = 0, nIns = 0;
+  for (uint32_t iter = 0; iter < maxIter; iter++) {
+    if (ncand == 0) break;
+    float md = -1.0f;
+    uint32_t mi = CUACD_NONE;
+    for (uint32_t k = lid; k < ncand; k += G) {
+      uint32_t i = h.cand[k];
+      if (h.owner[i] != CUACD_NONE) am_merge(md, mi, h.dist[i], i);
+    }
+    grp_argmax<G>(md, mi, sm);
+    if (md < 0.0f) break;
+    const uint32_t pick = mi;
+    if (lid == 0) hs.compacted = 0;
+    Grp<G>::sync();
+    hull_insert<G>(h, hs, sm, pick);
+    nIns++;
+    if (hs.fail) break;
+    const uint32_t nfNow = hs.nf;
+    const bool compacted = hs.compacted != 0;
+    if (lid == 0) { h.owner[pick] = CUACD_NONE; h.dist[pick] = 0.0f; }
+    Grp<G>::sync();
+    for (uint32_t k = lid; k < ncand; k += G) {
+      uint32_t i = h.cand[k];
+      uint32_t own = h.owner[i];
+      if (own == CUACD_NONE) continue;
+      if (!compacted && h.alive(own)) continue;
+      h.assign(i, compacted ? 0 : nfPrev, nfNow);
+    }
+    Grp<G>::sync();
+    nfPrev = nfNow;
+    if (++sinceCompact >= 4) {
+      sinceCompact = 0;
+      uint32_t nc = 0;
+      for (uint32_t c = 0; c * G < ncand; c++) {
+        const uint32_t k = c * G + lid;
+        uint32_t keep = 0, i = 0;
+        if (k < ncand) { i = h.cand[k]; keep = h.owner[i] != CUACD_NONE ? 1u : 0u; }
+        uint32_t tot;
+        uint32_t pre = grp_scan_u<G>(keep, &tot, sm);
+        Grp<G>::sync();
+        if (keep) h.cand[nc + pre] = i;
+        nc += tot;
+        Grp<G>::sync();
+      }
+      ncand = nc;
+    }
+  }
+  if (lid == 0) hs.ncand = ncand;
+  Grp<G>::sync();
+  return nIns;
+}
+
+// exact volume of the alive faces, in grid units
+template <int G>
+__device__ double hull_volume_grid(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
+  const int lid = Grp<G>::lid();
+  uint32_t a0, b0, c0;
+  h.abc(0, a0, b0, c0);
+  const f3 of = h.qvert(a0);
+  const long long ox = (long long)of.x, oy = (long long)of.y, oz = (long long)of.z;
+  __int128 v6 = 0;
+  const uint32_t nf = hs.nf;
+  for (uint32_t f = lid; f < nf; f += G) {
+    if (!h.alive(f)) continue;
+    uint32_t a, b, c;
+    h.abc(f, a, b, c);
+    f3 pa = h.qvert(a), pb = h.qvert(b), pc = h.qvert(c);
+    long long ax = (long long)pa.x - ox, ay = (long long)pa.y - oy, az = (long long)pa.z - oz;
+    long long bx = (long long)pb.x - ox, by = (long long)pb.y - oy, bz = (long long)pb.z - oz;
+    long long cx = (long long)pc.x - ox, cy = (long long)pc.y - oy, cz = (long long)pc.z - oz;
+    long long nx = by * cz - bz * cy, ny = bz * cx - bx * cz, nz = bx * cy - by * cx;
+    v6 += (__int128)ax * nx + (__int128)ay * ny + (__int128)az * nz;
+  }
+  // group sum of the 128-bit partials
+  unsigned long long lo = (unsigned long long)v6;
+  long long hi = (long long)(v6 >> 64);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long lo2 = __shfl_xor_sync(FULLMASK, lo, o);
+    long long hi2 = __shfl_xor_sync(FULLMASK, hi, o);
+    __int128 s = ((__int128)hi << 64 | (__int128)lo) + ((__int128)hi2 << 64 | (__int128)lo2);
+    lo = (unsigned long long)s;
+    hi = (long long)(s >> 64);
+  }
+  __int128 tot = (__int128)hi << 64 | (__int128)lo;
+  if (G > 32) {
+    __shared__ unsigned long long vs[8][2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0) { vs[w][0] = lo; vs[w][1] = (unsigned long long)hi; }
+    __syncthreads();
+    tot = 0;
+    for (int i = 0; i < G / 32; i++) tot += ((__int128)(long long)vs[i][1] << 64) | (__int128)vs[i][0];
+    __syncthreads();
+  }
+  if (tot < 0) tot = -tot;
+  long long th = (long long)(tot >> 32);
+  uint32_t tl = (uint32_t)(tot & 0xffffffffu);
+  return ((double)th * 4294967296.0 + (double)tl) / 6.0;
+}
+
+template <int G>
+__device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* slab, HullSm& hs, GrpSmem& sm) {
+  const int lid = Grp<G>::lid();
+  const uint32_t partIdx = P.partBase + idx;
+  PartDesc* pdp = D.parts + partIdx;
+  const uint32_t nv = pdp->nv, nt = pdp->nt, vOff = pdp->vOff, flags = pdp->flags;
+  const float meshVol = pdp->meshVol;
+  if (!(nv >= 4 && (nt > 0 || (flags & 2) != 0))) {
+    if (lid == 0) pdp->hullVol = 0.0f;
+    return;
+  }
+  const uint32_t fb = (2 * nv + max(nv, 80u) + 7) & ~7u;
+  const uint32_t fmax = P.hullSlabWords > fb ? (P.hullSlabWords - fb) / 16 : 0;
+  if (fmax < 64) {
+    if (lid == 0) { pdp->hullVol = -1.0f; pdp->flags = 3; atomicAdd(D.ctr + CTR_HULLFAIL, 1u); }
+    return;
+  }
+  if (lid == 0) add_bytes(D.ctr, CTR_BYTES_HULL, 12ull * nv);
+  HullCtx h;
+  h.V = D.V; h.vOff = vOff; h.nv = nv; h.fmax = fmax;
+  h.owner = slab;
+  h.dist = reinterpret_cast<float*>(slab + nv);
+  h.cand = slab + 2 * nv;
+  h.F = slab + fb;
+  h.vis = slab + P.hullSlabWords;
+  h.conn = h.vis + HULL_VIS_MAX;
+  // quantisation grid: 2^21 cells across the largest extent
+  f3 lo = mk3(1e30f, 1e30f, 1e30f), hi = mk3(-1e30f, -1e30f, -1e30f);
+  for (uint32_t i = lid; i < nv; i += G) {
+    f3 p = ldv(D.V, (size_t)vOff + 3 * (size_t)i);
+    lo = vmin3(lo, p);
+    hi = vmax3(hi, p);
+  }
+  lo.x = grp_min_f<G>(lo.x, sm); lo.y = grp_min_f<G>(lo.y, sm); lo.z = grp_min_f<G>(lo.z, sm);
+  hi.x = grp_max_f<G>(hi.x, sm); hi.y = grp_max_f<G>(hi.y, sm); hi.z = grp_max_f<G>(hi.z, sm);
+  const f3 ext = hi - lo;
+  const float scale = fmaxf(fmaxf(fmaxf(ext.x, ext.y), ext.z), 1e-30f);
+  h.qlo = lo;
+  h.qs = 2097152.0f / scale;
+  const float cell = scale / 2097152.0f;
+  const float volScale = (cell * cell) * cell;
+  // 80 seeds: max and min along 40 axes, lowest index on ties
+  for (int ps = 0; ps < 20; ps++) {
+    const f3 a0 = mk3(c_kdop[2 * ps][0], c_kdop[2 * ps][1], c_kdop[2 * ps][2]);
+    const f3 a1 = mk3(c_kdop[2 * ps + 1][0], c_kdop[2 * ps + 1][1], c_kdop[2 * ps + 1][2]);
+    float mx0 = -1e30f, mx1 = -1e30f, mn0 = -1e30f, mn1 = -1e30f;  // mins stored negated
+    uint32_t ix0 = CUACD_NONE, ix1 = CUACD_NONE, in0 = CUACD_NONE, in1 = CUACD_NONE;
+    for (uint32_t i = lid; i < nv; i += G) {
+      f3 v = h.qvert(i);
+      float d0 = dot(a0, v), d1 = dot(a1, v);
+      am_merge(mx0, ix0, d0, i);
+      am_merge(mn0, in0, -d0, i);
+      am_merge(mx1, ix1, d1, i);
+      am_merge(mn1, in1, -d1, i);
+    }
+    grp_argmax<G>(mx0, ix0, sm);
+    grp_argmax<G>(mn0, in0, sm);
+    grp_argmax<G>(mx1, ix1, sm);
+    grp_argmax<G>(mn1, in1, sm);
+    if (lid == 0) { hs.seed[4 * ps] = ix0; hs.seed[4 * ps + 1] = in0; hs.seed[4 * ps + 2] = ix1; hs.seed[4 * ps + 3] = in1; }
+  }
+  Grp<G>::sync();
+  if (P.hullStage == 1) {
+    if (lid == 0) pdp->hullVol = 0.0f;
+    return;
+  }
+  // initial simplex (shaders.ts:1227-1263), serial on lane 0
+  if (lid == 0) {
+    hs.ok = 0;
+    hs.fail = 0;
+    const uint32_t i0 = hs.seed[1], i1 = hs.seed[0];
+    const f3 p0 = h.qvert(i0), p1 = h.qvert(i1);
+    const f3 d01 = p1 - p0;
+    uint32_t i2 = CUACD_NONE;
+    float best = 0.0f;
+    for (int k = 0; k < 80; k++) {
+      f3 c = cross(d01, h.qvert(hs.seed[k]) - p0);
+      float v = dot(c, c);
+      if (v > best) { best = v; i2 = hs.seed[k]; }
+    }
+    if (i2 != CUACD_NONE) {
+      const f3 e2 = h.qvert(i2) - p0;
+      const f3 n = cross(d01, e2);
+      float bd = 0.0f;
+      int bs = 0;
+      uint32_t i3 = CUACD_NONE;
+      for (int k = 0; k < 80; k++) {
+        f3 dk = h.qvert(hs.seed[k]) - p0;
+        float v = fabsf(dot(n, dk));
+        if (v > bd) {
+          int sgn = orient_filtered(n, d01, e2, dk);
+          if (sgn != 0) { bd = v; i3 = hs.seed[k]; bs = sgn; }
+        }
+      }
+      if (i3 != CUACD_NONE) {
+        uint32_t a = i0, b = i1, c = i2;
+        if (bs > 0) { b = i2; c = i1; }
+        h.face_write(0, a, b, c);
+        h.face_write(1, a, i3, b);
+        h.face_write(2, b, i3, c);
+        h.face_write(3, c, i3, a);
+        hs.nf = 4;
+        hs.nalive = 4;
+        hs.ok = 1;
+      }
+    }
+  }
+  Grp<G>::sync();
+  if (!hs.ok) {
+    if (lid == 0) pdp->hullVol = 0.0f;
+    return;
+  }
+  // seeds first
+  for (uint32_t k = lid; k < 80; k += G) {
+    const uint32_t i = hs.seed[k];
+    h.assign(i, 0, 4);
+    h.cand[k] = i;
+  }
+  if (lid == 0) hs.ncand = 80;
+  Grp<G>::sync();
+  uint32_t nIns = hull_grow<G>(h, hs, sm, 4, 80);
+  const uint32_t fail0 = hs.fail;
+  const uint32_t nfPrev = hs.nf;
+  // last-level branch and bound (shaders.ts:1300-1331)
+  if (P.lastLevel == 1 && P.level > 0 && P.nSeeds > 0 && P.exportStride == 0 && fail0 == 0) {
+    const Job* jb = D.jobs + P.jobBase + idx / 2;
+    const ItemDesc* pit = D.items + P.itemsInBase + jb->parentItem;
+    float ssum = 0.0f;
+    for (uint32_t l = 0; l < pit->nLevels; l++) ssum += pit->levelCosts[l];
+    const uint32_t perSeed = P.nItemsIn / P.nSeeds;
+    const uint32_t srcPart = pit->srcPart;
+    float ubMin = 1e30f;
+    for (uint32_t i = lid; i < perSeed; i += G) {
+      const ItemDesc* it = D.items + P.itemsInBase + srcPart * perSeed + i;
+      if (it->flags == 1 && it->nLevels > 0) {
+        float ps = 0.0f;
+        for (uint32_t l = 0; l < it->nLevels; l++) ps += it->levelCosts[l];
+        float u = ps + it->levelCosts[it->nLevels - 1] * (float)(P.totalLevels - it->nLevels);
+        ubMin = fminf(ubMin, u);
+      }
+    }
+    const float ub = grp_min_f<G>(ubMin, sm);
+    const float vRough = (float)(hull_volume_grid<G>(h, hs, sm) * (double)volScale);
+    const float bound = ssum + rv_cost(meshVol, vRough);
+    if (bound > ub) {
+      if (lid == 0) {
+        pdp->hullVol = vRough;
+        pdp->flags = pdp->flags | 4u;
+        atomicAdd(D.ctr + CTR_PRUNED, 1u);
+      }
+      return;
+    }
+  }
+  // every point against the rough hull; candidates = points outside it
+  uint32_t ncand = 0;
+  for (uint32_t c = 0; c * G < nv; c++) {
+    const uint32_t i = c * G + lid;
+    uint32_t outside = 0;
+    if (i < nv && fail0 == 0) {
+      h.assign(i, 0, nfPrev);
+      outside = h.owner[i] != CUACD_NONE ? 1u : 0u;
+    }
+    uint32_t tot;
+    uint32_t pre = grp_scan_u<G>(outside, &tot, sm);
+    if (outside) h.cand[ncand + pre] = i;
+    ncand += tot;
+  }
+  if (lid == 0) {
+    hs.ncand = ncand;
+    if (P.exportStride == 0) pdp->pad0 = ncand;
+  }
+  Grp<G>::sync();
+  const uint32_t maxIter = (P.hullStage == 2 || P.hullStage == 3 || fail0 != 0) ? 0 : nv;
+  nIns += hull_grow<G>(h, hs, sm, nfPrev, maxIter);
+  if (hs.fail) {
+    if (lid == 0) {
+      pdp->hullVol = -1.0f;
+      pdp->flags = hs.fail;
+      atomicAdd(D.ctr + CTR_HULLFAIL, 1u);
+    }
+    return;
+  }
+  const float vol = (float)(hull_volume_grid<G>(h, hs, sm) * (double)volScale);
+  if (lid == 0) { pdp->hullVol = vol; pdp->pad1 = nIns; }
+  if (P.exportStride != 0) {
+    const uint32_t nf = hs.nf;
+    uint32_t run = 0;
+    const size_t base = (size_t)P.exportBase + (size_t)idx * P.exportStride;
+    for (uint32_t c = 0; c * G < nf; c++) {
+      const uint32_t f = c * G + lid;
+      uint32_t al = 0, a = 0, b = 0, cc = 0;
+      if (f < nf && h.alive(f)) { al = 1; h.abc(f, a, b, cc); }
+      uint32_t tot;
+      uint32_t pre = grp_scan_u<G>(al, &tot, sm);
+      if (al && 3 * (run + pre) + 3 <= P.exportStride) {
+        uint32_t* w = D.T + base + 3 * (size_t)(run + pre);
+        w[0] = a; w[1] = b; w[2] = cc;
+      }
+      run += tot;
+    }
+    if (lid == 0) {
+      const uint32_t nx = min(run, P.exportStride / 3);
+      pdp->pad0 = nx;
+      if (P.hdDescBase != 0) {
+        PartDesc hd;
+        hd.vOff = vOff; hd.nv = nv; hd.tOff = (uint32_t)base; hd.nt = nx;
+        hd.eOff = 0; hd.ne = 0; hd.meshVol = 0.0f; hd.hullVol = vol;
+        hd.planeIds[0] = hd.planeIds[1] = hd.planeIds[2] = hd.planeIds[3] = CUACD_NONE;
+        hd.nPlanes = 0; hd.flags = 2; hd.pad0 = 0; hd.pad1 = 0;
+        D.parts[partIdx + P.hdDescBase] = hd;
+      }
+    }
+  }
+}
+
+// Persistent groups: group s owns slab s and walks parts s, s + nSlabs, ...
+// Warp groups take parts with nv <= smallNv, block groups the others.
+template <int G>
+__global__ void __launch_bounds__(256) k_hull(const Level P, const Dev D) {
+  __shared__ GrpSmem gsm[Grp<G>::PER_BLOCK];
+  __shared__ HullSm hsm[Grp<G>::PER_BLOCK];
+  const int gi = Grp<G>::gid();
+  const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
+  if (s >= P.nSlabs) return;
+  uint32_t* slab = D.slab + (size_t)s * P.slabStride;
+  for (uint32_t idx = s; idx < P.nChildParts; idx += P.nSlabs) {
+    const uint32_t nv = D.parts[P.partBase + idx].nv;
+    const bool small = nv <= P.smallNv;
+    if (small != (G == 32)) continue;
+    hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi]);
+    Grp<G>::sync();
+  }
+}
+
+void launch_hull(const Level& P, const Dev& D, bool warps, cudaStream_t s) {
+  if (P.nChildParts == 0 || P.nSlabs == 0) return;
+  if (warps) k_hull<32><<<(P.nSlabs + 7) / 8, 256, 0, s>>>(P, D);
+  else k_hull<256><<<P.nSlabs, 256, 0, s>>>(P, D);
+}
+
+}  // namespace cuacd

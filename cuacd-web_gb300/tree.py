@@ -1,0 +1,286 @@
+"""GpuTree over libcuacd.so — the reference's GpuTree (src/gpu/tree.ts) on the
+GB300 engine.
+
+Method names follow the reference: run, hausdorff, hull_meshes,
+hulls_with_hausdorff, plane_slots, read_part, read_plane; table readers
+return the reference's word layouts. There is no fallback: if libcuacd.so is
+missing or no CUDA device is present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import _abi as A
+from .mesh import Mesh, mesh_area
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+HD_MAX_PAIRS = 1024
+_lib = None
+
+
+class CuacdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"cuacd error {code}: {msg}")
+        self.code = code
+
+
+class ScratchError(CuacdError):
+    """Hausdorff sample scratch exceeded. The message contains "scratch", as
+    the reference's Error does (tree.ts:345), so merge-style callers can halve
+    the batch on it (merge.ts:405)."""
+
+
+def library_path() -> str:
+    return os.path.join(HERE, "libcuacd.so")
+
+
+def load_library():
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build() or cuacd-web_gb300/build.py")
+    L = C.CDLL(path)
+    P = C.POINTER
+    L.cuacd_last_error.restype = C.c_char_p
+    L.cuacd_tree_config_default.argtypes = [P(A.TreeConfig)]
+    L.cuacd_tree_create.restype = C.c_void_p
+    L.cuacd_tree_create.argtypes = [P(A.TreeConfig), P(C.c_int)]
+    L.cuacd_tree_destroy.argtypes = [C.c_void_p]
+    L.cuacd_plane_slots.argtypes = [C.c_void_p]
+    L.cuacd_set_profile.argtypes = [C.c_void_p, C.c_int]
+    L.cuacd_tree_kernel_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    run_args = [C.c_void_p, P(A.MeshRef), C.c_int, P(C.c_float), C.c_int, P(A.RunOpts)]
+    L.cuacd_tree_run.argtypes = run_args + [P(A.SeedResult), P(A.RunStats)]
+    L.cuacd_tree_prepare.argtypes = run_args
+    L.cuacd_tree_launch.argtypes = [C.c_void_p]
+    L.cuacd_tree_collect.argtypes = [C.c_void_p, P(A.SeedResult), P(A.RunStats)]
+    L.cuacd_tree_hausdorff.argtypes = [C.c_void_p, P(A.MeshRef), P(A.MeshRef), C.c_int, P(C.c_float)]
+    L.cuacd_tree_hull_meshes.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, C.c_int, P(C.c_uint32), C.c_uint32,
+                                         P(C.c_float), P(C.c_uint32), P(C.c_int32)]
+    L.cuacd_tree_hulls_with_hausdorff.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, P(C.c_uint32), C.c_uint32,
+                                                  P(C.c_float), P(C.c_uint32), P(C.c_float), P(C.c_int32)]
+    for f in ("cuacd_tree_read_items", "cuacd_tree_read_parts", "cuacd_tree_read_jobs"):
+        getattr(L, f).argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, P(C.c_uint32)]
+    L.cuacd_tree_read_part_geometry.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float), P(C.c_uint32), P(C.c_uint32)]
+    L.cuacd_tree_read_plane.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float)]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        msg = load_library().cuacd_last_error().decode()
+        if rc == -3:
+            raise ScratchError(rc, msg)
+        raise CuacdError(rc, msg)
+
+
+def _int32p(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+class GpuTree:
+    """Lookahead tree search, hulls and Hausdorff distances on the GB300."""
+
+    def __init__(self, **cfg):
+        L = load_library()
+        self.cfg = A.make_config(**cfg)
+        err = C.c_int(0)
+        self.h = L.cuacd_tree_create(C.byref(self.cfg), C.byref(err))
+        if not self.h:
+            raise CuacdError(err.value, L.cuacd_last_error().decode())
+        self.plane_slots = L.cuacd_plane_slots(self.h)
+        self.last_hull_fails = []
+
+    def destroy(self):
+        if getattr(self, "h", None):
+            load_library().cuacd_tree_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    @property
+    def vis_max(self):
+        return 2048
+
+    def set_profile(self, on: bool):
+        load_library().cuacd_set_profile(self.h, int(on))
+
+    KERNELS = ("reset", "plan", "scan", "emit", "hull", "record", "evaluate")
+
+    def kernel_ms(self) -> dict:
+        """Per-kernel device time of the last profiled run (stats.kernelMs)."""
+        ms = np.zeros(7, np.float32)
+        _check(load_library().cuacd_tree_kernel_ms(self.h, A.fptr(ms)))
+        return {k: float(v) for k, v in zip(self.KERNELS, ms)}
+
+    # ---- GpuTree.run (tree.ts:449-661) ----
+    def _args(self, seeds, edge_planes, depth, width, n_edge_cuts, refine):
+        seeds = [A.as_mesh(s) for s in seeds]
+        ma = A.MeshArray(seeds)
+        n = len(seeds)
+        k = self.plane_slots
+        ep = np.zeros((max(n, 1), k, 4), np.float32)
+        if edge_planes is not None:
+            for i, p in enumerate(edge_planes):
+                p = np.asarray(p, np.float32).reshape(-1, 4)[:k]
+                ep[i, : len(p)] = p
+        opts = A.RunOpts(depth=depth, width=width, nEdgeCuts=n_edge_cuts)
+        keep = [ma, ep]
+        if refine:
+            opts.refineRounds = refine["rounds"]
+            opts.refineProbes = refine["probes"]
+            sp = np.asarray(refine["spacing"], np.float32)
+            keep.append(sp)
+            opts.refineSpacing = A.fptr(sp)
+        return ma, n, ep, opts, keep
+
+    def run(self, seeds, edge_planes=None, depth=0, width=-1, n_edge_cuts=-1, refine=None):
+        ma, n, ep, opts, keep = self._args(seeds, edge_planes, depth, width, n_edge_cuts, refine)
+        out = (A.SeedResult * max(n, 1))()
+        st = A.RunStats()
+        _check(load_library().cuacd_tree_run(self.h, ma.arr, n, A.fptr(ep), self.plane_slots, C.byref(opts), out, C.byref(st)))
+        return _result(out, st, n)
+
+    def prepare(self, seeds, edge_planes=None, depth=0, width=-1, n_edge_cuts=-1, refine=None):
+        """Upload seeds and planes once; launch() reruns the tree on them."""
+        ma, n, ep, opts, keep = self._args(seeds, edge_planes, depth, width, n_edge_cuts, refine)
+        _check(load_library().cuacd_tree_prepare(self.h, ma.arr, n, A.fptr(ep), self.plane_slots, C.byref(opts)))
+        self._n = n
+
+    def launch(self):
+        _check(load_library().cuacd_tree_launch(self.h))
+
+    def collect(self):
+        n = self._n
+        out = (A.SeedResult * max(n, 1))()
+        st = A.RunStats()
+        _check(load_library().cuacd_tree_collect(self.h, out, C.byref(st)))
+        return _result(out, st, n)
+
+    # ---- GpuTree.hullMeshes (tree.ts:382-443) ----
+    def hull_meshes(self, meshes, hull_stage=0, no_export=False):
+        meshes = [A.as_mesh(m) for m in meshes]
+        n = len(meshes)
+        if n == 0:
+            return [], np.zeros(0, np.int32)
+        ma = A.MeshArray(meshes)
+        maxnv = max(m.nv for m in meshes)
+        stride = 3 * 2 * min(self.cfg.hullMaxVerts, maxnv)
+        tris = np.zeros(max(n * stride, 1), np.uint32)
+        vol = np.zeros(n, np.float32)
+        nt = np.zeros(n, np.uint32)
+        status = np.zeros(n, np.int32)
+        _check(load_library().cuacd_tree_hull_meshes(self.h, ma.arr, n, hull_stage, None if no_export else A.uptr(tris),
+                                                     stride, A.fptr(vol), A.uptr(nt), _int32p(status)))
+        out = []
+        for i in range(n):
+            if status[i] != 0:
+                out.append(None)
+            else:
+                out.append(dict(tris=tris[i * stride: i * stride + 3 * nt[i]].reshape(-1, 3).copy(), volume=float(vol[i])))
+        return out, status
+
+    # ---- GpuTree.hullsWithHausdorff (tree.ts:671-756) ----
+    def hulls_with_hausdorff(self, meshes):
+        meshes = [A.as_mesh(m) for m in meshes]
+        n = len(meshes)
+        if n == 0:
+            return []
+        if n > HD_MAX_PAIRS:
+            raise ValueError(f"hullsWithHausdorff: at most {HD_MAX_PAIRS} meshes per call")
+        ma = A.MeshArray(meshes)
+        maxnv = max(m.nv for m in meshes)
+        stride = 3 * 2 * min(self.cfg.hullMaxVerts, maxnv)
+        tris = np.zeros(max(n * stride, 1), np.uint32)
+        vol = np.zeros(n, np.float32)
+        nt = np.zeros(n, np.uint32)
+        hd = np.zeros(n, np.float32)
+        status = np.zeros(n, np.int32)
+        _check(load_library().cuacd_tree_hulls_with_hausdorff(self.h, ma.arr, n, A.uptr(tris), stride, A.fptr(vol),
+                                                              A.uptr(nt), A.fptr(hd), _int32p(status)))
+        self.last_hull_fails = [int(s) for s in status]
+        out = []
+        for i in range(n):
+            if status[i] != 0:
+                out.append(None)
+            else:
+                out.append(dict(tris=tris[i * stride: i * stride + 3 * nt[i]].reshape(-1, 3).copy(), volume=float(vol[i]),
+                                hausdorff=float(hd[i])))
+        return out
+
+    # ---- GpuTree.hausdorff (tree.ts:318-372) ----
+    def hausdorff(self, pairs):
+        n = len(pairs)
+        if n == 0:
+            return np.zeros(0, np.float32)
+        if n > HD_MAX_PAIRS:
+            raise ValueError(f"hausdorff: at most {HD_MAX_PAIRS} pairs per call")
+        a = A.MeshArray([A.as_mesh(p[0]) for p in pairs])
+        b = A.MeshArray([A.as_mesh(p[1]) for p in pairs])
+        out = np.zeros(n, np.float32)
+        _check(load_library().cuacd_tree_hausdorff(self.h, a.arr, b.arr, n, A.fptr(out)))
+        return out
+
+    # ---- debug readers (tree.ts:764-807) ----
+    def items(self, first, n):
+        w = np.zeros(20 * n, np.uint32)
+        _check(load_library().cuacd_tree_read_items(self.h, first, n, A.uptr(w)))
+        return w.reshape(n, 20)
+
+    def parts(self, first, n):
+        w = np.zeros(16 * n, np.uint32)
+        _check(load_library().cuacd_tree_read_parts(self.h, first, n, A.uptr(w)))
+        return w.reshape(n, 16)
+
+    def jobs(self, first, n):
+        w = np.zeros(24 * n, np.uint32)
+        _check(load_library().cuacd_tree_read_jobs(self.h, first, n, A.uptr(w)))
+        return w.reshape(n, 24)
+
+    def part_geometry(self, idx):
+        d = self.parts(idx, 1)[0]
+        v = np.zeros(3 * d[1], np.float32)
+        t = np.zeros(3 * d[3], np.uint32)
+        e = np.zeros(8 * d[5], np.uint32)
+        _check(load_library().cuacd_tree_read_part_geometry(self.h, idx, A.fptr(v), A.uptr(t), A.uptr(e)))
+        return v.reshape(-1, 3), t.reshape(-1, 3), e.reshape(-1, 8)
+
+    def read_part(self, idx):
+        d = self.parts(idx, 1)[0]
+        f = d.view(np.float32)
+        v, t, e = self.part_geometry(idx)
+        return dict(mesh=Mesh(v, t), edges=e, meshVol=float(f[6]), hullVol=float(f[7]), nPlanes=int(d[12]),
+                    planeIds=[int(x) for x in d[8: 8 + d[12]]])
+
+    def plane(self, idx):
+        f = np.zeros(4, np.float32)
+        _check(load_library().cuacd_tree_read_plane(self.h, idx, A.fptr(f)))
+        return f
+
+    read_plane = plane
+
+
+def _result(out, st, n):
+    seeds = []
+    for i in range(n):
+        s = out[i]
+        seeds.append(dict(bestCut=s.bestCut, bestCost=s.bestCost if s.valid else float("inf"),
+                          plane=list(s.plane) if s.valid else None))
+    return dict(
+        seeds=seeds, overflow=bool(st.overflow), hullFail=bool(st.hullFail), hullFailCount=st.hullFailCount,
+        npOverflow=bool(st.npOverflow), pruned=st.pruned, jobsPerLevel=list(st.jobsPerLevel[: st.nLevels]),
+        validJobs=st.validJobs, hullSlabWords=st.hullSlabWords, hullChunkSize=st.hullChunkSize, gpuMs=st.gpuMs,
+    )
+
+
+__all__ = ["GpuTree", "HD_MAX_PAIRS", "load_library", "library_path", "CuacdError", "ScratchError", "mesh_area"]

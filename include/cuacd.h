@@ -1,0 +1,192 @@
+/* cuacd.h — C ABI of the cuacd GB300 engine (libcuacd.so).
+ *
+ * The engine replaces the WebGPU hot path of cuacd-web: the lookahead tree
+ * that GpuTree drives (src/gpu/tree.ts with the plan / scan / emit / hull /
+ * record / evaluate kernels of src/gpu/shaders.ts), the sampled Hausdorff
+ * kernel (src/gpu/hausdorff_shader.ts) and the GPU hull and Hausdorff
+ * batches of the merge pass (src/merge.ts:357-416). Every entry point below
+ * names the reference interface it stands in for.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only. Inputs are borrowed for the duration of
+ *     the call and copied; outputs are caller-allocated.
+ *   - Return codes: CUACD_OK (0) or a negative CUACD_E_* code; the message
+ *     of the last failure on the calling thread is cuacd_last_error().
+ *   - Recoverable conditions of a tree run (pool overflow, hull failures,
+ *     too many parts per item) are result flags, not errors, as in
+ *     TreeRunResult (tree.ts:75-85): the caller halves the batch and retries
+ *     (decompose.ts:316-321).
+ *   - One handle owns one CUDA stream and its device pools; calls on one
+ *     handle must not overlap (the reference serialises GpuTree calls with
+ *     await). Different handles may be used from different threads.
+ *   - Nothing here aborts the process or traps the device.
+ */
+#ifndef CUACD_H
+#define CUACD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUACD_OK 0
+#define CUACD_E_INVALID (-1)  /* bad argument or configuration */
+#define CUACD_E_CAPACITY (-2) /* input exceeds a configured pool */
+#define CUACD_E_SCRATCH (-3)  /* Hausdorff sample scratch exceeded (tree.ts:345) */
+#define CUACD_E_CUDA (-4)     /* CUDA runtime error (allocation, launch) */
+#define CUACD_E_NODEVICE (-5) /* no CUDA device */
+
+/* Maximum pairs of one Hausdorff call (HD_MAX_PAIRS, tree.ts:12). */
+#define CUACD_HD_MAX_PAIRS 1024
+/* Visible-face limit of one hull insertion (VIS_MAX, shaders.ts:27). */
+#define CUACD_VIS_MAX 2048
+
+/* TreeConfig (tree.ts:14-46). Capacities keep the reference's units:
+ * vertexCap in floats (3 per vertex), triCap in u32 (3 per triangle),
+ * edgeCap in open edges, scratchWords in u32. */
+typedef struct {
+  int32_t width;         /* axis-aligned cuts at level 0 (multiple of 3) */
+  int32_t width2;        /* axis-aligned cuts at deeper levels (multiple of 3) */
+  int32_t depth;         /* full levels, 1..4 */
+  int32_t nConcaveEdges; /* edge planes per seed = max(4 * nConcaveEdges, 32) */
+  float minEdgeDist;
+  int32_t hullMaxVerts;  /* hull export bound per part */
+  uint64_t vertexCap;
+  uint64_t triCap;
+  uint64_t edgeCap;
+  uint64_t scratchWords;
+  uint64_t hullBudgetBytes; /* bytes of hull scratch slabs in flight */
+  int32_t pruneLastLevel;   /* last-level branch and bound (tree.ts:29-30) */
+  int32_t reserved;
+} cuacd_tree_config;
+
+/* Mesh (mesh.ts:7-10): nv vertices (3 floats each), nt triangles (3 u32). */
+typedef struct {
+  const float* verts;
+  const uint32_t* tris;
+  uint32_t nv;
+  uint32_t nt;
+} cuacd_mesh;
+
+/* GpuTree.run opts (tree.ts:449-453) and RefineRequest (tree.ts:60-67). */
+typedef struct {
+  int32_t depth;        /* <= 0: configured depth */
+  int32_t width;        /* < 0: configured width */
+  int32_t nEdgeCuts;    /* < 0: every plane slot */
+  int32_t refineRounds; /* probe rounds after the tree, 0 = none */
+  int32_t refineProbes; /* probes per round (>= 3) */
+  int32_t reserved;
+  const float* refineSpacing; /* per seed initial half-width, or NULL */
+} cuacd_run_opts;
+
+/* SeedResult (tree.ts:69-73). */
+typedef struct {
+  int32_t bestCut; /* index into the seed's candidate planes, -1 if none */
+  float bestCost;  /* +inf when no cut */
+  float plane[4];  /* a, b, c, d with a x + b y + c z + d = 0 */
+  int32_t valid;
+  int32_t reserved;
+} cuacd_seed_result;
+
+/* TreeRunResult flags and stats (tree.ts:75-85). */
+typedef struct {
+  uint32_t overflow;
+  uint32_t hullFail;
+  uint32_t hullFailCount;
+  uint32_t npOverflow;
+  uint32_t pruned;
+  uint32_t nLevels;
+  uint32_t jobsPerLevel[4];
+  uint64_t validJobs; /* candidate cuts evaluated (jobs valid after plan, all stages) */
+  uint32_t hullSlabWords;
+  uint32_t hullChunkSize; /* hull scratch slabs in flight */
+  float gpuMs;            /* device time of the run */
+  uint32_t reserved;
+} cuacd_run_stats;
+
+/* DEFAULT_TREE_CONFIG (tree.ts:33-46), with width2 = 3 (decompose.ts:91). */
+void cuacd_tree_config_default(cuacd_tree_config* cfg);
+
+/* new GpuTree(device, cfg) (tree.ts:139-178): validates width/width2 (multiples
+ * of 3) and depth (1..4), allocates the device pools on the current device.
+ * Returns NULL and sets *err on failure. */
+void* cuacd_tree_create(const cuacd_tree_config* cfg, int* err);
+
+/* GpuTree.destroy (tree.ts:813-815). */
+void cuacd_tree_destroy(void* tree);
+
+/* GpuTree.planeSlots (tree.ts:759-761): plane slots per seed. */
+int cuacd_plane_slots(const void* tree);
+
+/* GpuTree.visMax (tree.ts:809-811). */
+int cuacd_vis_max(void);
+
+/* GpuTree.profile (tree.ts:133-134): when on, runs launch kernel by kernel
+ * with CUDA events between them instead of replaying a CUDA graph. */
+void cuacd_set_profile(void* tree, int on);
+
+/* stats.kernelMs of the last profiled run (tree.ts:82, 610-615): device time
+ * per kernel class, summed over levels and rounds, in ms: [0] table reset,
+ * [1] plan, [2] scan, [3] emit, [4] hull, [5] record, [6] evaluate. */
+int cuacd_tree_kernel_ms(void* tree, float* ms7);
+
+/* GpuTree.run (tree.ts:449-661). edgePlanes holds planesPerSeed planes
+ * (4 floats) per seed; zero planes are skipped; planes beyond planeSlots are
+ * ignored. out receives nSeeds results. */
+int cuacd_tree_run(void* tree, const cuacd_mesh* seeds, int nSeeds, const float* edgePlanes, int planesPerSeed,
+                   const cuacd_run_opts* opts, cuacd_seed_result* out, cuacd_run_stats* stats);
+
+/* The two halves of cuacd_tree_run for device-resident reruns: prepare
+ * uploads seeds and planes (tree.ts:470-557); launch enqueues the whole tree,
+ * evaluate and refinement rounds on the handle's stream, starting from the
+ * prepared seeds (tree.ts:559-594); collect waits and reads the results
+ * (tree.ts:596-661). launch may be called any number of times after one
+ * prepare. */
+int cuacd_tree_prepare(void* tree, const cuacd_mesh* seeds, int nSeeds, const float* edgePlanes, int planesPerSeed,
+                       const cuacd_run_opts* opts);
+int cuacd_tree_launch(void* tree);
+int cuacd_tree_collect(void* tree, cuacd_seed_result* out, cuacd_run_stats* stats);
+
+/* GpuTree.hausdorff (tree.ts:318-372): bidirectional sampled Hausdorff of n
+ * pairs (n <= CUACD_HD_MAX_PAIRS). Returns CUACD_E_SCRATCH when the pairs'
+ * sample capacity exceeds scratchWords (the reference throws an Error whose
+ * message contains "scratch"; merge.ts:405 halves the batch on it). */
+int cuacd_tree_hausdorff(void* tree, const cuacd_mesh* a, const cuacd_mesh* b, int n, float* out);
+
+/* GpuTree.hullMeshes (tree.ts:382-443): exact convex hulls of n meshes or
+ * point sets (nt = 0). For mesh k, up to exportStride u32 of outward hull
+ * triangles over its own vertex indices go to trisOut + k * exportStride,
+ * the triangle count to ntOut[k], the volume to volOut[k], and status[k] is
+ * 0, or the reference's failure code (lastHullFails, tree.ts:668, 752):
+ * 1 visible-set overflow, 2 face slots exhausted, 3 slab too small,
+ * 8 fewer than 4 faces, 9 other. hullStage 1/2/3 stop after the seeds,
+ * the seed insertion or the first assignment (tests/bench_hull.ts:2-4).
+ * trisOut may be NULL (noExport). */
+int cuacd_tree_hull_meshes(void* tree, const cuacd_mesh* meshes, int n, int hullStage, uint32_t* trisOut,
+                           uint32_t exportStride, float* volOut, uint32_t* ntOut, int32_t* status);
+
+/* GpuTree.hullsWithHausdorff (tree.ts:671-756): hulls as above plus the
+ * Hausdorff distance of each mesh to its hull, in one submission. */
+int cuacd_tree_hulls_with_hausdorff(void* tree, const cuacd_mesh* meshes, int n, uint32_t* trisOut,
+                                    uint32_t exportStride, float* volOut, uint32_t* ntOut, float* hdOut,
+                                    int32_t* status);
+
+/* Debug readers of the last run's tables, in the reference's word layouts
+ * (shaders.ts:41-60): items 20 words, parts 16 words, jobs 24 words. Part
+ * offsets keep the reference's units (vOff in floats, tOff in u32, eOff in
+ * edges). GpuTree.readPart / readPlane / levels (tree.ts:764-807, 621-639). */
+int cuacd_tree_read_items(void* tree, uint32_t first, uint32_t n, uint32_t* out);
+int cuacd_tree_read_parts(void* tree, uint32_t first, uint32_t n, uint32_t* out);
+int cuacd_tree_read_jobs(void* tree, uint32_t first, uint32_t n, uint32_t* out);
+int cuacd_tree_read_part_geometry(void* tree, uint32_t part, float* verts, uint32_t* tris, uint32_t* edges);
+int cuacd_tree_read_plane(void* tree, uint32_t index, float* out4);
+
+/* Message of the last failure on the calling thread. */
+const char* cuacd_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUACD_H */

@@ -378,6 +378,7 @@ HullResult hull_points(const f3* pts, uint32_t nv, uint32_t slabWords, const Hul
     }
   }
   r.ncand = ncand;
+  r.assigned = true;
   uint32_t maxIter = (o.hullStage == 2 || o.hullStage == 3 || fail0 != 0) ? 0 : nv;
   nIns += h.grow(ncand, nfPrev, maxIter);
   if (h.fail) { r.hullVol = -1.0f; r.status = h.fail; r.nIns = nIns; return r; }

@@ -29,6 +29,7 @@ struct HullResult {
   float hullVol = 0.0f;
   uint32_t status = 0;  // 1 visible-set overflow, 2 face slots exhausted, 3 slab too small
   bool pruned = false;
+  bool assigned = false;  // reached the full assignment pass (the kernel records ncand there)
   uint32_t nIns = 0, ncand = 0;
   std::vector<uint32_t> faces;  // alive faces in slot order, (a, b, c) per face
 };

@@ -551,6 +551,7 @@ struct Tree {
         ctr[CTR_PRUNED]++;
         continue;
       }
+      if (r.assigned && P.exportStride == 0) pd[14] = r.ncand;
       if (r.status != 0) {
         pd[7] = fbits(-1.0f);
         pd[13] = r.status;
@@ -558,7 +559,6 @@ struct Tree {
         continue;
       }
       pd[7] = fbits(r.hullVol);
-      if (P.exportStride == 0) pd[14] = r.ncand;
       pd[15] = r.nIns;
       if (P.exportStride != 0) {
         uint32_t nfx = (uint32_t)r.faces.size() / 3;

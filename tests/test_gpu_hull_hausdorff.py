@@ -1,0 +1,130 @@
+"""Parity of the CUDA hull and Hausdorff batches (GpuTree.hullMeshes,
+hausdorff, hullsWithHausdorff) with the CPU oracle, through the C ABI.
+
+Hull face sets are compared exactly (same faces in the same order); volumes
+to 1e-6 relative, and to the reference's own quickhull within the 2^21
+grid's quantisation (3e-5). Hausdorff distances agree with the oracle's
+float32 form within 1e-5 + 1e-4 d, and with the reference's CPU helper within
+its own test tolerance, 1e-4 + 1e-3 d (tests/cpu.test.ts:97-111)."""
+import importlib
+
+import numpy as np
+import pytest
+
+from fixtures import M, l_prism, square_torus, stairs
+
+pytestmark = pytest.mark.gpu
+gen = importlib.import_module("cuacd-web_gb300.meshgen")
+
+
+@pytest.fixture(scope="module")
+def tree_mod():
+    return importlib.import_module("cuacd-web_gb300.tree")
+
+
+def point_sets():
+    rng = np.random.default_rng(7)
+    out = [
+        M.unit_cube(), M.l_shape(), square_torus(), stairs(), gen.staircase(8), gen.noisy_icosphere(3, seed=1),
+        M.Mesh(rng.normal(size=(500, 3)).astype(np.float32), np.zeros((0, 3), np.uint32)),
+        M.Mesh(rng.uniform(-1, 1, size=(2000, 3)).astype(np.float32), np.zeros((0, 3), np.uint32)),
+        # coplanar grid plus one apex: many exactly coplanar points
+        M.Mesh(np.concatenate([np.stack(np.meshgrid(np.arange(8), np.arange(8), [0.0]), -1).reshape(-1, 3),
+                               [[3.5, 3.5, 2.0]]]).astype(np.float32), np.zeros((0, 3), np.uint32)),
+        # duplicated points
+        M.Mesh(np.repeat(rng.normal(size=(40, 3)), 3, axis=0).astype(np.float32), np.zeros((0, 3), np.uint32)),
+        # fewer than 4 points, and a flat set: no hull
+        M.Mesh(np.eye(3, dtype=np.float32), np.zeros((0, 3), np.uint32)),
+        M.Mesh(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [0.5, 0.5, 0]], np.float32), np.zeros((0, 3), np.uint32)),
+    ]
+    return out
+
+
+def test_hull_faces_match_oracle(tree_mod, oracle):
+    cfg = dict(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    g = tree_mod.GpuTree(**cfg)
+    o = oracle.OracleTree(**cfg)
+    sets = point_sets()
+    rg, sg = g.hull_meshes(sets)
+    ro, so = o.hull_meshes(sets)
+    assert list(sg) == list(so)
+    for i, (a, b) in enumerate(zip(rg, ro)):
+        assert (a is None) == (b is None), i
+        if a is None:
+            continue
+        assert np.array_equal(a["tris"], b["tris"]), i
+        assert np.float32(a["volume"]).view(np.uint32) == np.float32(b["volume"]).view(np.uint32), (i, a["volume"], b["volume"])
+        h = M.Mesh(sets[i].verts, a["tris"])
+        assert M.is_closed(h) and M.signed_volume(h) > 0, i
+        if oracle.qh_ref_loaded():
+            ref = oracle.hull_volume(sets[i], True)
+            assert abs(a["volume"] - ref) <= 3e-5 * ref, (i, a["volume"], ref)
+
+
+def test_hull_stages_and_large_parts(tree_mod, oracle):
+    """Large point sets run on block groups; the staged variants of
+    tests/bench_hull.ts stop early."""
+    cfg = dict(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    g = tree_mod.GpuTree(**cfg)
+    o = oracle.OracleTree(**cfg)
+    big = gen.noisy_icosphere(5, seed=2)  # 10242 points
+    for stage in (0, 2):
+        rg, sg = g.hull_meshes([big, big], hull_stage=stage)
+        ro, so = o.hull_meshes([big, big], hull_stage=stage)
+        assert list(sg) == list(so)
+        for a, b in zip(rg, ro):
+            assert (a is None) == (b is None)
+            if a is not None:
+                assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"]
+
+
+def hd_pairs(oracle):
+    t = oracle.OracleTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    pairs = []
+    for m in (M.l_shape(), square_torus(), stairs(), l_prism(), gen.staircase(8), gen.noisy_icosphere(3, seed=5)):
+        h = t.hull_meshes([m])[0][0]
+        pairs.append((m, M.Mesh(m.verts, h["tris"])))
+    pairs.append((M.unit_cube(), M.make_box((0.1, 0, 0), (1.1, 1, 1))))
+    return pairs
+
+
+def test_hausdorff_matches_oracle_and_cpu(tree_mod, oracle):
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0)
+    pairs = hd_pairs(oracle)
+    hg = g.hausdorff(pairs)
+    ho = oracle.hausdorff_gpu_form(pairs)
+    for i, (a, b) in enumerate(pairs):
+        assert abs(hg[i] - ho[i]) <= 1e-5 + 1e-4 * ho[i], (i, hg[i], ho[i])
+        c = oracle.hausdorff_cpu(a, b)
+        assert abs(hg[i] - c) <= 1e-4 + 1e-3 * c, (i, hg[i], c)
+    # known answers (tests/cpu.test.ts:78-87)
+    assert 0.3 < hg[0] < 0.6
+    assert abs(hg[-1] - 0.1) < 0.02
+
+
+def test_hulls_with_hausdorff(tree_mod, oracle):
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    o = oracle.OracleTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    meshes = [M.unit_cube(), M.l_shape(), square_torus(), stairs(), gen.staircase(8)]
+    rg = g.hulls_with_hausdorff(meshes)
+    ro, _ = o.hull_meshes(meshes)
+    for m, a, b in zip(meshes, rg, ro):
+        assert a is not None and b is not None
+        assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"]
+        ref = oracle.hausdorff_gpu_form([(m, M.Mesh(m.verts, b["tris"]))])[0]
+        assert abs(a["hausdorff"] - ref) <= 1e-5 + 1e-4 * ref
+    assert rg[0]["hausdorff"] < 1e-6
+
+
+def test_hausdorff_scratch_error(tree_mod):
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, scratchWords=1000)
+    with pytest.raises(tree_mod.ScratchError) as e:
+        g.hausdorff([(M.unit_cube(), M.unit_cube())])
+    assert "scratch" in str(e.value)
+
+
+def test_empty_batches(tree_mod):
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0)
+    assert len(g.hausdorff([])) == 0
+    assert g.hull_meshes([])[0] == []
+    assert g.hulls_with_hausdorff([]) == []
