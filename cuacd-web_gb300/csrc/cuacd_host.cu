@@ -113,7 +113,8 @@ struct Tree {
       cudaEventCreate(&e);
       pev.push_back(e);
     }
-    cudaEventRecord(pev[i], stream);
+    // inside a stream capture only an external record becomes an event node
+    cudaEventRecordWithFlags(pev[i], stream, cudaEventRecordExternal);
     pcls.push_back(cls);
   }
   Dev D{};
@@ -467,7 +468,10 @@ struct Tree {
     if (profile) {
       for (size_t i = 1; i < pcls.size(); i++) {
         float d = 0;
-        cudaEventElapsedTime(&d, pev[i - 1], pev[i]);
+        if (cudaEventElapsedTime(&d, pev[i - 1], pev[i]) != cudaSuccess) {
+          cudaGetLastError();  // a timing failure must not poison later calls
+          d = 0;
+        }
         if (pcls[i] >= 0) kernelMs[pcls[i]] += d;
       }
     }

@@ -110,6 +110,8 @@ class OracleTree:
         ep = np.zeros((max(n, 1), k, 4), np.float32)
         if edge_planes is not None:
             for i, p in enumerate(edge_planes):
+                if p is None:
+                    continue
                 p = np.asarray(p, np.float32).reshape(-1, 4)[:k]
                 ep[i, : len(p)] = p
         opts = A.RunOpts(depth=depth, width=width, nEdgeCuts=n_edge_cuts)

@@ -27,11 +27,11 @@ def test_reference_known_answers(GpuTree, case):
     case(GpuTree)
 
 
-def run_both(GpuTree, oracle, seeds, planes=None, refine=None, depth=0, **cfg):
+def run_both(GpuTree, oracle, seeds, planes=None, refine=None, run_depth=0, **cfg):
     g = GpuTree(**cfg)
     o = oracle.OracleTree(**cfg)
-    rg = g.run(seeds, planes, depth=depth, refine=refine)
-    ro = o.run(seeds, planes, depth=depth, refine=refine)
+    rg = g.run(seeds, planes, depth=run_depth, refine=refine)
+    ro = o.run(seeds, planes, depth=run_depth, refine=refine)
     return g, o, rg, ro
 
 
