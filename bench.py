@@ -36,8 +36,8 @@ sys.path.insert(0, ROOT)
 
 THRESHOLD = 0.1
 TREE = dict(width=6, width2=3, depth=3, nConcaveEdges=16, minEdgeDist=min(THRESHOLD / 4, 0.015))
-POOLS = dict(vertexCap=256 << 20, triCap=256 << 20, edgeCap=16 << 20, scratchWords=256 << 20,
-             hullBudgetBytes=4 << 30, hullMaxVerts=4096)
+POOLS = dict(vertexCap=64 << 20, triCap=64 << 20, edgeCap=4 << 20, scratchWords=64 << 20,
+             hullBudgetBytes=2 << 30, hullMaxVerts=4096)
 REFINE_ROUNDS, REFINE_PROBES = 2, 8
 METRIC = "cut candidates evaluated/s"
 UNIT = "candidates/s"
@@ -233,7 +233,9 @@ def run_engine(args):
     g.prepare(seeds, planes, refine=refine)
     for _ in range(args.warmup):
         g.launch()
-        g.collect()
+        r = g.collect()
+        # a run that overflowed a pool evaluated fewer candidates: not a valid step
+        assert not r["overflow"] and not r["npOverflow"], "pool overflow: raise the pool capacities"
     barrier()
     dev_ms, cands = 0.0, 0
     kms = {k: 0.0 for k in g.KERNELS}

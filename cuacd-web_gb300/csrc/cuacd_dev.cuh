@@ -64,6 +64,8 @@ struct Dev {
   Job* jobs;
   float4* planes;
   uint32_t* ctr;
+  unsigned long long* scanTmp;  // scan bases and per-block sums (3 + 3 * blocks)
+  uint32_t* work;               // hull work counters, one per hull launch of a run
   uint64_t vCap, tCap, eCap, sCap;
 };
 
@@ -81,6 +83,8 @@ struct Level {
   uint32_t exportBase, exportStride;  // hull face export into T (u32 offsets)
   uint32_t lastLevel, hullStage, nSeeds;
   uint32_t hdDescBase;      // != 0: write a Hausdorff descriptor at part + hdDescBase
+  uint32_t workSlot;        // hull work counter of this launch (D.work)
+  uint32_t maxNvHint;       // largest part the host knows of, or 0: read D.work[32 + workSlot]
 };
 
 // Hausdorff batch: mesh m's descriptor at parts[partBase + m]; pair k is
@@ -216,6 +220,29 @@ template <int G> __device__ __forceinline__ uint32_t grp_scan_u(uint32_t v, uint
   *tot = all;
   return before + inc - v;
 }
+// exclusive scan of 0/1 flags in lane order (ballot and popcount per warp)
+template <int G> __device__ __forceinline__ uint32_t grp_scan_bit(bool b, uint32_t* tot, GrpSmem& sm) {
+  const unsigned m = __ballot_sync(FULLMASK, b);
+  const int lane = threadIdx.x & 31;
+  const uint32_t pre = __popc(m & ((1u << lane) - 1u));
+  if (G == 32) {
+    *tot = __popc(m);
+    return pre;
+  }
+  const int w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sm.u[w][1] = __popc(m);
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+#pragma unroll
+  for (int i = 0; i < G / 32; i++) {
+    uint32_t t = sm.u[i][1];
+    if (i < w) before += t;
+    all += t;
+  }
+  *tot = all;
+  return before + pre;
+}
 // argmax of (value, index): largest value, lowest index on ties
 __device__ __forceinline__ void am_merge(float& v, uint32_t& i, float v2, uint32_t i2) {
   if (v2 > v || (v2 == v && i2 < i)) { v = v2; i = i2; }
@@ -236,6 +263,22 @@ template <int G> __device__ __forceinline__ void grp_argmax(float& v, uint32_t& 
   i = sm.u[0][2];
 #pragma unroll
   for (int k = 1; k < G / 32; k++) am_merge(v, i, sm.f[k][1], sm.u[k][2]);
+}
+// argmax over lanes whose value is positive: largest value, lowest index on
+// ties; lanes with v <= 0 take no part. Positive floats order like their
+// bits, so a warp needs two redux instructions. With no positive value the
+// result is v = -1, i = NONE.
+template <int G> __device__ __forceinline__ void grp_argmax_pos(float& v, uint32_t& i, GrpSmem& sm) {
+  if (G == 32) {
+    const uint32_t key = v > 0.0f ? __float_as_uint(v) : 0u;
+    const uint32_t mk = __reduce_max_sync(FULLMASK, key);
+    const uint32_t mi = __reduce_min_sync(FULLMASK, (key == mk && mk != 0u) ? i : 0xffffffffu);
+    v = mk != 0u ? __uint_as_float(mk) : -1.0f;
+    i = mk != 0u ? mi : 0xffffffffu;
+    return;
+  }
+  if (!(v > 0.0f)) { v = -1.0f; i = 0xffffffffu; }
+  grp_argmax<G>(v, i, sm);
 }
 // broadcast a value from lane 0 of the group
 template <int G> __device__ __forceinline__ uint32_t grp_bcast_u(uint32_t v, GrpSmem& sm) {

@@ -28,6 +28,7 @@ void launch_evaluate(uint32_t stateBase, uint32_t headerOff, uint32_t mode, uint
                      uint32_t edgePlaneBase, uint32_t edgeStride, const Dev& D, cudaStream_t s);
 void launch_hull(const Level& P, const Dev& D, bool warps, cudaStream_t s);
 void launch_hd(const HdArgs& A, const Dev& D, cudaStream_t s);
+int hull_blocks_per_sm(bool warps);
 }  // namespace cuacd
 
 using namespace cuacd;
@@ -95,7 +96,7 @@ struct HostBuf {
 struct Tree {
   cuacd_tree_config cfg;
   uint32_t edgeStride = 0;
-  int device = 0, nSM = 0;
+  int device = 0, nSM = 0, bpsSmall = 1, bpsBig = 1;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool profile = false;
@@ -118,7 +119,8 @@ struct Tree {
     pcls.push_back(cls);
   }
   Dev D{};
-  DevBuf bV, bT, bE, bS, bCtr, bSlab, bParts, bItems, bJobs, bPlanes, bSnap, bHd;
+  DevBuf bV, bT, bE, bS, bCtr, bSlab, bParts, bItems, bJobs, bPlanes, bSnap, bHd, bScan, bWork;
+  uint32_t workSlots = 0;  // hull launches of the prepared run
   HostBuf hStage, hRead, hSnap, hMeta;
   uint32_t capSeeds = 0, capJobs = 0, capItems = 0, capParts = 0, capPlanes = 0;
   // prepared run
@@ -137,7 +139,7 @@ struct Tree {
 
   ~Tree() {
     if (gexec) cudaGraphExecDestroy(gexec);
-    for (DevBuf* b : {&bV, &bT, &bE, &bS, &bCtr, &bSlab, &bParts, &bItems, &bJobs, &bPlanes, &bSnap, &bHd}) b->release();
+    for (DevBuf* b : {&bV, &bT, &bE, &bS, &bCtr, &bSlab, &bParts, &bItems, &bJobs, &bPlanes, &bSnap, &bHd, &bScan, &bWork}) b->release();
     for (HostBuf* b : {&hStage, &hRead, &hSnap, &hMeta}) b->release();
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
     if (ev0) cudaEventDestroy(ev0);
@@ -148,6 +150,7 @@ struct Tree {
     D.V = (float*)bV.p; D.T = (uint32_t*)bT.p; D.E = (uint32_t*)bE.p; D.S = (uint32_t*)bS.p;
     D.slab = (uint32_t*)bSlab.p; D.parts = (PartDesc*)bParts.p; D.items = (ItemDesc*)bItems.p;
     D.jobs = (Job*)bJobs.p; D.planes = (float4*)bPlanes.p; D.ctr = (uint32_t*)bCtr.p;
+    D.scanTmp = (unsigned long long*)bScan.p; D.work = (uint32_t*)bWork.p;
     D.vCap = cfg.vertexCap; D.tCap = cfg.triCap; D.eCap = cfg.edgeCap; D.sCap = cfg.scratchWords;
   }
   // tree.ts:191-213
@@ -189,8 +192,8 @@ struct Tree {
     slabWords = ((2 * maxNv + std::max(maxNv, 80u) + 7) & ~7u) + 16 * fmax;
     slabStride = (slabWords + 2 * VIS_MAX + 63) & ~63u;
     uint64_t byBudget = std::max<uint64_t>(1, cfg.hullBudgetBytes / ((uint64_t)slabStride * 4));
-    nSlabsSmall = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * 32, (uint64_t)std::max(nParts, 1u)});
-    nSlabsBig = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * 2, (uint64_t)std::max(nParts, 1u)});
+    nSlabsSmall = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * bpsSmall * 8, (uint64_t)std::max(nParts, 1u)});
+    nSlabsBig = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * bpsBig, (uint64_t)std::max(nParts, 1u)});
     size_t need = (size_t)std::max(nSlabsSmall, nSlabsBig) * slabStride * 4;
     if (bSlab.bytes < need) {
       gvalid = false;
@@ -210,7 +213,9 @@ struct Tree {
     P.smallNv = SMALL_NV;
     return P;
   }
-  void hullLaunch(Level P) {
+  // hull launches of one level; work counter `slot` must be zero beforehand
+  void hullLaunch(Level P, uint32_t slot) {
+    P.workSlot = slot;
     P.nSlabs = nSlabsSmall;
     launch_hull(P, D, true, stream);
     P.nSlabs = nSlabsBig;
@@ -298,6 +303,16 @@ struct Tree {
     for (auto& L : tree) maxChild = std::max(maxChild, 2 * L.nJobs);
     for (auto& L : probe) maxChild = std::max(maxChild, 2 * L.nJobs);
     if ((rc = planSlabs(maxSeedNv, maxChild))) return rc;
+    // scan bases and per-block sums of the largest level
+    uint32_t maxJobs = 0;
+    for (auto& L : tree) maxJobs = std::max(maxJobs, L.nJobs);
+    for (auto& L : probe) maxJobs = std::max(maxJobs, L.nJobs);
+    size_t scanBytes = (3 + 3 * (size_t)((maxJobs + 1023) / 1024)) * 8;
+    if (scanBytes > bScan.bytes) {
+      if ((rc = bScan.ensure(scanBytes))) return rc;
+      gvalid = false;
+      bind();
+    }
     std::vector<PartDesc> parts;
     if ((rc = uploadMeshes(seeds, nSeeds, parts))) return rc;
     edgePlaneBase = capJobs;
@@ -360,6 +375,9 @@ struct Tree {
     cudaMemcpyAsync(D.planes + stateBase, snap + snapState, (16 + 4 * (size_t)nSeeds) * 16, cudaMemcpyDeviceToDevice, stream);
     mark(0);
     auto stage = [&](const std::vector<LevelLayout>& L, uint32_t mode, uint32_t headerOff) {
+      // one hull work counter per level of the stage
+      // (work[l]: the level's hull counter; work[32 + l]: its largest child)
+      cudaMemsetAsync(D.work, 0, 64 * 4, stream);
       for (uint32_t l = 0; l < L.size(); l++) {
         const LevelLayout& v = L[l];
         Level P = baseLevel();
@@ -369,6 +387,7 @@ struct Tree {
         P.edgePlaneBase = edgePlaneBase; P.nChildParts = 2 * v.nJobs; P.nJobs = v.nJobs;
         P.lastLevel = l == depth - 1 ? 1u : 0u;
         P.nSeeds = cfg.pruneLastLevel ? nSeeds : 0;
+        P.workSlot = l;
         // parents shrink roughly by half per level
         bool big = (maxSeedNv >> l) > BIG_JOB_NV;
         launch_plan(P, D, big, stream);
@@ -377,7 +396,7 @@ struct Tree {
         mark(2);
         launch_emit(P, D, big, stream);
         mark(3);
-        hullLaunch(P);
+        hullLaunch(P, l);
         mark(4);
         launch_record(P, D, stream);
         mark(5);
@@ -396,7 +415,8 @@ struct Tree {
     std::vector<uint64_t> s = {nSeeds, depth, nProbes, rounds, slabWords, slabStride, nSlabsSmall, nSlabsBig,
                                maxSeedNv > BIG_JOB_NV ? maxSeedNv : 0, edgePlaneBase, stateBase, (uint64_t)bSnap.p,
                                (uint64_t)bSlab.p, (uint64_t)bParts.p, (uint64_t)bItems.p, (uint64_t)bJobs.p,
-                               (uint64_t)bPlanes.p, (uint64_t)bCtr.p, snapBytes};
+                               (uint64_t)bPlanes.p, (uint64_t)bCtr.p, snapBytes, (uint64_t)bScan.p,
+                               (uint64_t)bWork.p};
     for (auto& L : tree) { s.push_back(L.nJobs); s.push_back(L.totalWidth); s.push_back(L.width); }
     for (uint32_t l = 0; l < depth; l++) s.push_back((maxSeedNv >> l) > BIG_JOB_NV);
     return s;
@@ -526,8 +546,10 @@ struct Tree {
     P.edgePlaneBase = capJobs; P.nChildParts = n; P.nJobs = 0;
     P.exportBase = tTop; P.exportStride = stride; P.hullStage = (uint32_t)hullStage;
     P.hdDescBase = withHd ? (uint32_t)n : 0;
+    P.maxNvHint = std::max(maxNv, 1u);
+    CK(cudaMemsetAsync(D.work, 0, 4, stream));
     CK(cudaEventRecord(ev0, stream));
-    hullLaunch(P);
+    hullLaunch(P, 0);
     if (withHd) {
       if ((rc = runHd((uint32_t)n, 0, capOff, capN, totalCap, maxSide))) return rc;
     }
@@ -695,6 +717,8 @@ void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
   t->edgeStride = (uint32_t)std::max(4 * c->nConcaveEdges, 32);
   cudaGetDevice(&t->device);
   cudaDeviceGetAttribute(&t->nSM, cudaDevAttrMultiProcessorCount, t->device);
+  t->bpsSmall = hull_blocks_per_sm(true);
+  t->bpsBig = hull_blocks_per_sm(false);
   int rc = 0;
   if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&t->ev0) != cudaSuccess || cudaEventCreate(&t->ev1) != cudaSuccess) {
@@ -703,7 +727,7 @@ void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
   }
   if ((rc = t->bV.ensure(std::max<uint64_t>(c->vertexCap, 4) * 4)) || (rc = t->bT.ensure(std::max<uint64_t>(c->triCap, 4) * 4)) ||
       (rc = t->bE.ensure(std::max<uint64_t>(c->edgeCap, 1) * 32)) || (rc = t->bS.ensure(std::max<uint64_t>(c->scratchWords, 4) * 4)) ||
-      (rc = t->bCtr.ensure(CTR_WORDS * 4))) {
+      (rc = t->bCtr.ensure(CTR_WORDS * 4)) || (rc = t->bWork.ensure(256 * 4)) || (rc = t->bScan.ensure(64 * 8))) {
     std::string m = g_err;
     delete t;
     return bad(rc, m.c_str());

@@ -26,6 +26,8 @@ namespace cuacd {
 
 #define HULL_VIS_MAX 2048u
 #define ALIVE 0x80000000u
+// points a warp group keeps in shared memory (3 floats each)
+#define QC_MAX 256u
 
 // k-DOP seed axes (shaders.ts:769-810): the same table, so the seeds are the
 // same extreme points as the reference picks
@@ -60,7 +62,7 @@ struct HullSm {
 };
 
 // exact sign of det[e1; e2; d] for integer vectors below 2^23 (shaders.ts:868-876)
-__device__ __forceinline__ int orient_exact(f3 e1f, f3 e2f, f3 df) {
+__device__ __noinline__ int orient_exact(f3 e1f, f3 e2f, f3 df) {
   long long e1x = (long long)e1f.x, e1y = (long long)e1f.y, e1z = (long long)e1f.z;
   long long e2x = (long long)e2f.x, e2y = (long long)e2f.y, e2z = (long long)e2f.z;
   long long dx = (long long)df.x, dy = (long long)df.y, dz = (long long)df.z;
@@ -91,8 +93,10 @@ struct HullCtx {
   uint32_t* F;     // face records, 16 words each
   uint32_t* vis;   // visible face slots (HULL_VIS_MAX)
   uint32_t* conn;  // connected flags of the visible list (HULL_VIS_MAX)
+  const float* qc;  // quantised points in shared memory, or null
 
   __device__ __forceinline__ f3 qvert(uint32_t i) const {
+    if (qc) return mk3(qc[3 * i], qc[3 * i + 1], qc[3 * i + 2]);
     f3 v = ldv(V, (size_t)vOff + 3 * (size_t)i) - qlo;
     return mk3(rintf(v.x * qs), rintf(v.y * qs), rintf(v.z * qs));
   }
@@ -119,17 +123,32 @@ struct HullCtx {
     const uint4* w = rec(f);
     uint4 a = w[0];
     if ((a.x & ALIVE) == 0) return -1e30f;
-    uint4 b = w[1], c = w[2];
+    uint4 b = w[1];
     f3 n = mk3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z));
-    f3 pa = mk3(__uint_as_float(b.w), __uint_as_float(c.x), __uint_as_float(c.y));
+    // the corners are the quantised points: from the shared-memory copy
+    // when the part has one (same values as the record holds)
+    f3 pa;
+    uint4 c;
+    if (qc) {
+      pa = qvert(a.x & 0x7fffffffu);
+    } else {
+      c = w[2];
+      pa = mk3(__uint_as_float(b.w), __uint_as_float(c.x), __uint_as_float(c.y));
+    }
     f3 d = p - pa;
     float det = dot(n, d);
     float bound = (1e-6f * __uint_as_float(a.w)) * l1(d);
     if (det > bound) return det / fmaxf(sqrtf(dot(n, n)), 1e-30f);
     if (det < -bound) return -1.0f;
-    uint4 e = w[3];
-    f3 pb = mk3(__uint_as_float(c.z), __uint_as_float(c.w), __uint_as_float(e.x));
-    f3 pc = mk3(__uint_as_float(e.y), __uint_as_float(e.z), __uint_as_float(e.w));
+    f3 pb, pc;
+    if (qc) {
+      pb = qvert(a.y);
+      pc = qvert(a.z);
+    } else {
+      uint4 e = w[3];
+      pb = mk3(__uint_as_float(c.z), __uint_as_float(c.w), __uint_as_float(e.x));
+      pc = mk3(__uint_as_float(e.y), __uint_as_float(e.z), __uint_as_float(e.w));
+    }
     return orient_exact(pb - pa, pc - pa, d) > 0 ? 1e-30f : -1.0f;
   }
   __device__ __forceinline__ void assign(uint32_t i, uint32_t f0, uint32_t f1) const {
@@ -157,7 +176,7 @@ __device__ __forceinline__ bool shares_edge(uint32_t f0, uint32_t f1, uint32_t f
 
 // remove dead face slots, keeping slot order (shaders.ts:946-969)
 template <int G>
-__device__ void hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
+__device__ __noinline__ void hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
   const int lid = Grp<G>::lid();
   const uint32_t nf = hs.nf;
   uint32_t run = 0;
@@ -171,7 +190,7 @@ __device__ void hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
       al = (w0.x & ALIVE) ? 1u : 0u;
     }
     uint32_t tot;
-    uint32_t pre = grp_scan_u<G>(al, &tot, sm);
+    uint32_t pre = grp_scan_bit<G>(al != 0, &tot, sm);
     Grp<G>::sync();
     if (al) {
       uint4* r = h.rec(run + pre);
@@ -186,7 +205,7 @@ __device__ void hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
 
 // insert point pIdx (shaders.ts:975-1055) with the deterministic order
 template <int G>
-__device__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t pIdx) {
+__device__ __noinline__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t pIdx) {
   const int lid = Grp<G>::lid();
   const f3 p = h.qvert(pIdx);
   uint32_t nf = hs.nf;
@@ -204,7 +223,7 @@ __device__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t 
     float dd = f < nf ? h.face_eval(f, p) : -1.0f;
     uint32_t v = dd > 0.0f ? 1u : 0u;
     uint32_t tot;
-    uint32_t pre = grp_scan_u<G>(v, &tot, sm);
+    uint32_t pre = grp_scan_bit<G>(v != 0, &tot, sm);
     if (v) {
       uint32_t k = nvis + pre;
       if (k < HULL_VIS_MAX) h.vis[k] = f;
@@ -219,7 +238,7 @@ __device__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t 
     Grp<G>::sync();
     return;
   }
-  grp_argmax<G>(bd, bk, sm);
+  grp_argmax_pos<G>(bd, bk, sm);
   const uint32_t seedK = bk;
   for (uint32_t k = lid; k < nvis; k += G) h.conn[k] = k == seedK ? 1u : 0u;
   Grp<G>::sync();
@@ -269,7 +288,7 @@ __device__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t 
       }
     }
     uint32_t tot;
-    uint32_t pre = grp_scan_u<G>(isNew, &tot, sm);
+    uint32_t pre = grp_scan_bit<G>(isNew != 0, &tot, sm);
     if (isNew) h.face_write(nf + nnew + pre, a, b, pIdx);
     nnew += tot;
   }
@@ -291,7 +310,7 @@ __device__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t 
 
 // farthest-first insertion of the candidate list (shaders.ts:1060-1129)
 template <int G>
-__device__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t nfPrev, uint32_t maxIter) {
+__device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t nfPrev, uint32_t maxIter) {
   const int lid = Grp<G>::lid();
   uint32_t ncand = hs.ncand;
   uint32_t sinceCompact = 0, nIns = 0;
@@ -303,7 +322,7 @@ __device__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_
       uint32_t i = h.cand[k];
       if (h.owner[i] != CUACD_NONE) am_merge(md, mi, h.dist[i], i);
     }
-    grp_argmax<G>(md, mi, sm);
+    grp_argmax_pos<G>(md, mi, sm);
     if (md < 0.0f) break;
     const uint32_t pick = mi;
     if (lid == 0) hs.compacted = 0;
@@ -332,7 +351,7 @@ __device__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_
         uint32_t keep = 0, i = 0;
         if (k < ncand) { i = h.cand[k]; keep = h.owner[i] != CUACD_NONE ? 1u : 0u; }
         uint32_t tot;
-        uint32_t pre = grp_scan_u<G>(keep, &tot, sm);
+        uint32_t pre = grp_scan_bit<G>(keep != 0, &tot, sm);
         Grp<G>::sync();
         if (keep) h.cand[nc + pre] = i;
         nc += tot;
@@ -396,7 +415,8 @@ __device__ double hull_volume_grid(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
 }
 
 template <int G>
-__device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* slab, HullSm& hs, GrpSmem& sm) {
+__device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* slab, HullSm& hs, GrpSmem& sm,
+                         float* qcache) {
   const int lid = Grp<G>::lid();
   const uint32_t partIdx = P.partBase + idx;
   PartDesc* pdp = D.parts + partIdx;
@@ -414,6 +434,7 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
   }
   if (lid == 0) add_bytes(D.ctr, CTR_BYTES_HULL, 12ull * nv);
   HullCtx h;
+  h.qc = nullptr;
   h.V = D.V; h.vOff = vOff; h.nv = nv; h.fmax = fmax;
   h.owner = slab;
   h.dist = reinterpret_cast<float*>(slab + nv);
@@ -436,7 +457,34 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
   h.qs = 2097152.0f / scale;
   const float cell = scale / 2097152.0f;
   const float volScale = (cell * cell) * cell;
-  // 80 seeds: max and min along 40 axes, lowest index on ties
+  // small parts keep their quantised points in shared memory
+  if (G == 32 && qcache != nullptr && nv <= QC_MAX) {
+    for (uint32_t i = lid; i < nv; i += G) {
+      f3 v = ldv(D.V, (size_t)vOff + 3 * (size_t)i) - lo;
+      qcache[3 * i] = rintf(v.x * h.qs);
+      qcache[3 * i + 1] = rintf(v.y * h.qs);
+      qcache[3 * i + 2] = rintf(v.z * h.qs);
+    }
+    h.qc = qcache;
+    Grp<G>::sync();
+  }
+  // 80 seeds: max and min along 40 axes, lowest index on ties; seed 2a is
+  // the maximum along axis a, seed 2a + 1 the minimum
+  if (h.qc != nullptr) {
+    // one lane per axis, each scanning every point in index order
+    for (uint32_t a = lid; a < 40; a += G) {
+      const f3 ax = mk3(c_kdop[a][0], c_kdop[a][1], c_kdop[a][2]);
+      float mx = -1e30f, mn = 1e30f;
+      uint32_t ix = 0, in = 0;
+      for (uint32_t i = 0; i < nv; i++) {
+        const float d = dot(ax, h.qvert(i));
+        if (d > mx) { mx = d; ix = i; }
+        if (d < mn) { mn = d; in = i; }
+      }
+      hs.seed[2 * a] = ix;
+      hs.seed[2 * a + 1] = in;
+    }
+  } else
   for (int ps = 0; ps < 20; ps++) {
     const f3 a0 = mk3(c_kdop[2 * ps][0], c_kdop[2 * ps][1], c_kdop[2 * ps][2]);
     const f3 a1 = mk3(c_kdop[2 * ps + 1][0], c_kdop[2 * ps + 1][1], c_kdop[2 * ps + 1][2]);
@@ -461,45 +509,54 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
     if (lid == 0) pdp->hullVol = 0.0f;
     return;
   }
-  // initial simplex (shaders.ts:1227-1263), serial on lane 0
-  if (lid == 0) {
-    hs.ok = 0;
-    hs.fail = 0;
+  // initial simplex (shaders.ts:1227-1263). The reference scans the 80 seeds
+  // serially with strict comparisons, so each choice is the first seed
+  // position reaching the maximum: here every lane scans its positions in
+  // order and the group argmax breaks ties by the lowest position.
+  {
     const uint32_t i0 = hs.seed[1], i1 = hs.seed[0];
     const f3 p0 = h.qvert(i0), p1 = h.qvert(i1);
     const f3 d01 = p1 - p0;
-    uint32_t i2 = CUACD_NONE;
     float best = 0.0f;
-    for (int k = 0; k < 80; k++) {
-      f3 c = cross(d01, h.qvert(hs.seed[k]) - p0);
-      float v = dot(c, c);
-      if (v > best) { best = v; i2 = hs.seed[k]; }
+    uint32_t bk = CUACD_NONE;
+    for (uint32_t k = lid; k < 80; k += G) {
+      const f3 c = cross(d01, h.qvert(hs.seed[k]) - p0);
+      const float v = dot(c, c);
+      if (v > best) { best = v; bk = k; }
     }
-    if (i2 != CUACD_NONE) {
+    grp_argmax<G>(best, bk, sm);
+    uint32_t i3 = CUACD_NONE, i2 = CUACD_NONE;
+    int bs = 0;
+    if (bk != CUACD_NONE) {
+      i2 = hs.seed[bk];
       const f3 e2 = h.qvert(i2) - p0;
       const f3 n = cross(d01, e2);
       float bd = 0.0f;
-      int bs = 0;
-      uint32_t i3 = CUACD_NONE;
-      for (int k = 0; k < 80; k++) {
-        f3 dk = h.qvert(hs.seed[k]) - p0;
-        float v = fabsf(dot(n, dk));
-        if (v > bd) {
-          int sgn = orient_filtered(n, d01, e2, dk);
-          if (sgn != 0) { bd = v; i3 = hs.seed[k]; bs = sgn; }
-        }
+      uint32_t k3 = CUACD_NONE;
+      for (uint32_t k = lid; k < 80; k += G) {
+        const f3 dk = h.qvert(hs.seed[k]) - p0;
+        const float v = fabsf(dot(n, dk));
+        if (v > bd && orient_filtered(n, d01, e2, dk) != 0) { bd = v; k3 = k; }
       }
-      if (i3 != CUACD_NONE) {
-        uint32_t a = i0, b = i1, c = i2;
-        if (bs > 0) { b = i2; c = i1; }
-        h.face_write(0, a, b, c);
-        h.face_write(1, a, i3, b);
-        h.face_write(2, b, i3, c);
-        h.face_write(3, c, i3, a);
-        hs.nf = 4;
-        hs.nalive = 4;
-        hs.ok = 1;
+      grp_argmax<G>(bd, k3, sm);
+      if (k3 != CUACD_NONE) {
+        i3 = hs.seed[k3];
+        bs = orient_filtered(n, d01, e2, h.qvert(i3) - p0);
       }
+    }
+    if (lid < 4 && i3 != CUACD_NONE) {
+      uint32_t a = i0, b = i1, c = i2;
+      if (bs > 0) { b = i2; c = i1; }
+      if (lid == 0) h.face_write(0, a, b, c);
+      if (lid == 1) h.face_write(1, a, i3, b);
+      if (lid == 2) h.face_write(2, b, i3, c);
+      if (lid == 3) h.face_write(3, c, i3, a);
+    }
+    if (lid == 0) {
+      hs.fail = 0;
+      hs.ok = i3 != CUACD_NONE ? 1u : 0u;
+      hs.nf = 4;
+      hs.nalive = 4;
     }
   }
   Grp<G>::sync();
@@ -558,7 +615,7 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
       outside = h.owner[i] != CUACD_NONE ? 1u : 0u;
     }
     uint32_t tot;
-    uint32_t pre = grp_scan_u<G>(outside, &tot, sm);
+    uint32_t pre = grp_scan_bit<G>(outside != 0, &tot, sm);
     if (outside) h.cand[ncand + pre] = i;
     ncand += tot;
   }
@@ -588,7 +645,7 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
       uint32_t al = 0, a = 0, b = 0, cc = 0;
       if (f < nf && h.alive(f)) { al = 1; h.abc(f, a, b, cc); }
       uint32_t tot;
-      uint32_t pre = grp_scan_u<G>(al, &tot, sm);
+      uint32_t pre = grp_scan_bit<G>(al != 0, &tot, sm);
       if (al && 3 * (run + pre) + 3 <= P.exportStride) {
         uint32_t* w = D.T + base + 3 * (size_t)(run + pre);
         w[0] = a; w[1] = b; w[2] = cc;
@@ -613,20 +670,47 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
 // Persistent groups: group s owns slab s and walks parts s, s + nSlabs, ...
 // Warp groups take parts with nv <= smallNv, block groups the others.
 template <int G>
-__global__ void __launch_bounds__(256) k_hull(const Level P, const Dev D) {
+__global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
   __shared__ GrpSmem gsm[Grp<G>::PER_BLOCK];
   __shared__ HullSm hsm[Grp<G>::PER_BLOCK];
+  __shared__ float qcs[G == 32 ? 8 * 3 * QC_MAX : 1];
   const int gi = Grp<G>::gid();
   const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
   if (s >= P.nSlabs) return;
-  uint32_t* slab = D.slab + (size_t)s * P.slabStride;
-  for (uint32_t idx = s; idx < P.nChildParts; idx += P.nSlabs) {
-    const uint32_t nv = D.parts[P.partBase + idx].nv;
-    const bool small = nv <= P.smallNv;
-    if (small != (G == 32)) continue;
-    hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi]);
-    Grp<G>::sync();
+  if (G != 32) {
+    // block groups only serve parts above smallNv: leave at once when the
+    // level has none (the scan recorded its largest child)
+    const uint32_t mx = P.maxNvHint ? P.maxNvHint : D.work[32 + P.workSlot];
+    if (mx <= P.smallNv) return;
   }
+  uint32_t* slab = D.slab + (size_t)s * P.slabStride;
+  if (G == 32) {
+    // warp groups take the next part from the launch's counter, so parts of
+    // uneven size balance across the GPU
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+      uint32_t idx = 0;
+      if (lane == 0) idx = atomicAdd(D.work + P.workSlot, 1u);
+      idx = __shfl_sync(FULLMASK, idx, 0);
+      if (idx >= P.nChildParts) break;
+      if (D.parts[P.partBase + idx].nv > P.smallNv) continue;
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], G == 32 ? qcs + gi * 3 * QC_MAX : nullptr);
+      Grp<G>::sync();
+    }
+  } else {
+    for (uint32_t idx = s; idx < P.nChildParts; idx += P.nSlabs) {
+      if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], G == 32 ? qcs + gi * 3 * QC_MAX : nullptr);
+      Grp<G>::sync();
+    }
+  }
+}
+
+int hull_blocks_per_sm(bool warps) {
+  int n = 0;
+  if (warps) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<32>, 256, 0);
+  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<256>, 256, 0);
+  return n > 0 ? n : 1;
 }
 
 void launch_hull(const Level& P, const Dev& D, bool warps, cudaStream_t s) {

@@ -236,17 +236,68 @@ __global__ void __launch_bounds__(256) k_plan(const Level P, const Dev D) {
 }
 
 // ======================= scan (shaders.ts:446-554) =======================
-// One block of 1024 threads walks the level's jobs in chunks of 1024 with
-// block-wide exclusive scans of the vertex, triangle and edge needs.
+// The reference runs this as one serial workgroup. Here it is device-wide:
+// k_scan_sums writes each 1024-job block's vertex, triangle and edge needs
+// (and the pool tops as the bases); k_scan then gives every block its offset
+// from the sums of the blocks before it and scans within the block.
+__device__ __forceinline__ void job_needs(const Level& P, const Dev& D, uint32_t j, uint32_t need[3]) {
+  need[0] = need[1] = need[2] = 0;
+  if (j >= P.nJobs) return;
+  const Job* J = D.jobs + P.jobBase + j;
+  if (J->valid != 1) return;
+  const uint4* cw = reinterpret_cast<const uint4*>(J->cnt);
+  uint4 a = cw[0], b = cw[1];
+  need[0] = 3 * (a.x + a.w);
+  if (P.lastLevel == 0) {
+    need[1] = 3 * (a.y + b.x);
+    need[2] = a.z + b.y;
+  }
+}
+__global__ void __launch_bounds__(1024) k_scan_sums(const Level P, const Dev D) {
+  __shared__ unsigned long long ws[3][32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  uint32_t need[3];
+  job_needs(P, D, blockIdx.x * 1024 + tid, need);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    uint32_t s = warp_sum_u(need[k]);
+    if (lane == 0) ws[k][w] = s;
+  }
+  __syncthreads();
+  if (tid < 3) {
+    unsigned long long s = 0;
+    for (int i = 0; i < 32; i++) s += ws[tid][i];
+    D.scanTmp[3 + 3 * blockIdx.x + tid] = s;
+    if (blockIdx.x == 0) D.scanTmp[tid] = D.ctr[CTR_V + tid];
+  }
+}
 __global__ void __launch_bounds__(1024) k_scan(const Level P, const Dev D) {
   __shared__ uint32_t wsum[3][32];
   __shared__ unsigned long long run[3];
+  __shared__ unsigned long long bsum[3][32];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
-  if (tid == 0) { run[0] = D.ctr[CTR_V]; run[1] = D.ctr[CTR_T]; run[2] = D.ctr[CTR_E]; }
-  __syncthreads();
+  {
+    // base = pool tops + needs of all earlier blocks
+    unsigned long long s[3] = {0, 0, 0};
+    for (uint32_t b = tid; b < blockIdx.x; b += 1024)
+      for (int k = 0; k < 3; k++) s[k] += D.scanTmp[3 + 3 * b + k];
+    for (int k = 0; k < 3; k++) {
+      unsigned long long v = s[k];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULLMASK, v, o);
+      if (lane == 0) bsum[k][w] = v;
+    }
+    __syncthreads();
+    if (tid < 3) {
+      unsigned long long v = D.scanTmp[tid];
+      for (int i = 0; i < 32; i++) v += bsum[tid][i];
+      run[tid] = v;
+    }
+    __syncthreads();
+  }
   const bool keepTopo = P.lastLevel == 0;
-  const uint32_t nChunks = (P.nJobs + 1023) / 1024;
-  for (uint32_t c = 0; c < nChunks; c++) {
+  uint32_t childMax = 0;
+  {
+    const uint32_t c = blockIdx.x;
     const uint32_t j = c * 1024 + tid;
     const bool inRange = j < P.nJobs;
     Job* J = D.jobs + P.jobBase + (inRange ? j : 0);
@@ -318,6 +369,7 @@ __global__ void __launch_bounds__(1024) k_scan(const Level P, const Dev D) {
         neg.nt = keepTopo ? cnt[4] : 0; neg.eOff = keepTopo ? eOff + cnt[2] : eOff; neg.ne = keepTopo ? cnt[5] : 0;
         D.parts[posP] = pos;
         D.parts[negP] = neg;
+        childMax = max(cnt[0], cnt[3]);
         const bool bothNonEmpty = cnt[0] > 0 && cnt[1] > 0 && cnt[3] > 0 && cnt[4] > 0;
         it = parent;
         if (parent.np >= 8) {
@@ -347,7 +399,13 @@ __global__ void __launch_bounds__(1024) k_scan(const Level P, const Dev D) {
     }
     __syncthreads();
   }
-  if (tid == 0) {
+  // the level's largest child: hull launches for large parts skip levels
+  // without any
+  childMax = __reduce_max_sync(FULLMASK, childMax);
+  if (lane == 0 && childMax != 0) atomicMax(D.work + 32 + P.workSlot, childMax);
+  if (tid == 0 && blockIdx.x == gridDim.x - 1) {
+    // the last block holds the level's totals; the bases were read from the
+    // copy k_scan_sums made, so the counters can move now
     D.ctr[CTR_V] = (uint32_t)min(run[0], (unsigned long long)D.vCap);
     D.ctr[CTR_T] = (uint32_t)min(run[1], (unsigned long long)D.tCap);
     D.ctr[CTR_E] = (uint32_t)min(run[2], (unsigned long long)D.eCap);
@@ -677,7 +735,9 @@ void launch_plan(const Level& P, const Dev& D, bool big, cudaStream_t s) {
 }
 void launch_scan(const Level& P, const Dev& D, cudaStream_t s) {
   if (P.nJobs == 0) return;
-  k_scan<<<1, 1024, 0, s>>>(P, D);
+  const uint32_t blocks = (P.nJobs + 1023) / 1024;
+  k_scan_sums<<<blocks, 1024, 0, s>>>(P, D);
+  k_scan<<<blocks, 1024, 0, s>>>(P, D);
 }
 void launch_emit(const Level& P, const Dev& D, bool big, cudaStream_t s) {
   if (P.nJobs == 0) return;
