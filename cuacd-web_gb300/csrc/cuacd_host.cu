@@ -39,6 +39,11 @@ static int fail(int code, const std::string& msg) {
   g_err = msg;
   return code;
 }
+namespace cuacd {
+// records the message of a failed call for cuacd_last_error (used by entry
+// points defined next to their kernels)
+int set_error(int code, const char* msg) { return fail(code, msg); }
+}  // namespace cuacd
 
 #define CK(x)                                                                                   \
   do {                                                                                          \

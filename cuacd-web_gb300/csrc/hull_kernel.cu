@@ -719,4 +719,119 @@ void launch_hull(const Level& P, const Dev& D, bool warps, cudaStream_t s) {
   else k_hull<256><<<P.nSlabs, 256, 0, s>>>(P, D);
 }
 
+// ---------------------------------------------------------------------------
+// Hull of one point set without any device allocation.
+//
+// Some callers cannot allocate device memory at the moment they need a hull:
+// a host application that hands every byte of the GPU to its own arena or
+// caching allocator, or an interactive loop where cudaMalloc and cudaFree
+// would stall work already running on the device. cuacd_tree_create
+// allocates pools, so such callers get this entry point instead: they pass
+// device buffers they already own for the points and the results, and the
+// scratch the hull kernel needs (one slab, one part descriptor and the
+// counters) comes from the fixed array below, which every GPU that loads the
+// library holds until the process exits.
+// ---------------------------------------------------------------------------
+
+int set_error(int code, const char* msg);
+
+// largest point set the fixed scratch holds
+#define NOALLOC_MAX_POINTS 4096u
+// one slab for NOALLOC_MAX_POINTS points with hullMaxVerts 4096, sized as the
+// tree's slabs: ((2 n + n + 7) & ~7) + 16 (2 n + 3 * 2048 + 1024) words
+// = 258048, plus the visible list and its flags (2 * 2048 words)
+#define NOALLOC_SLAB_WORDS 262144u
+#define NOALLOC_PART_OFF NOALLOC_SLAB_WORDS
+#define NOALLOC_CTR_OFF (NOALLOC_PART_OFF + 16u)
+#define NOALLOC_WORK_OFF (NOALLOC_CTR_OFF + (uint32_t)CTR_WORDS)
+#define NOALLOC_WORDS (NOALLOC_WORK_OFF + 64u)
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[NOALLOC_WORDS];
+
+// the part descriptor of the point set, zeroed counters
+__global__ void k_noalloc_setup(uint32_t* scratch, uint32_t nv) {
+  const int t = threadIdx.x;
+  PartDesc* pd = reinterpret_cast<PartDesc*>(scratch + NOALLOC_PART_OFF);
+  if (t == 0) {
+    PartDesc p;
+    p.vOff = 0; p.nv = nv; p.tOff = 0; p.nt = 0; p.eOff = 0; p.ne = 0;
+    p.meshVol = 0.0f; p.hullVol = 0.0f;
+    p.planeIds[0] = p.planeIds[1] = p.planeIds[2] = p.planeIds[3] = CUACD_NONE;
+    p.nPlanes = 0; p.flags = 2; p.pad0 = 0; p.pad1 = 0;
+    *pd = p;
+  }
+  for (uint32_t i = t; i < (uint32_t)CTR_WORDS; i += blockDim.x) scratch[NOALLOC_CTR_OFF + i] = 0;
+  for (uint32_t i = t; i < 64; i += blockDim.x) scratch[NOALLOC_WORK_OFF + i] = 0;
+}
+// results with the status rule of the hull batches (tree.ts:750-753)
+__global__ void k_noalloc_finish(const uint32_t* scratch, float* volume, uint32_t* ntris, int32_t* status) {
+  const PartDesc* pd = reinterpret_cast<const PartDesc*>(scratch + NOALLOC_PART_OFF);
+  const float vol = pd->hullVol;
+  int32_t s = 0;
+  if (vol < 0.0f) s = (pd->flags & 3) ? (int32_t)(pd->flags & 3) : 9;
+  else if (pd->pad0 < 4) s = 8;
+  *volume = vol;
+  *ntris = s == 0 ? pd->pad0 : 0;
+  *status = s;
+}
+
 }  // namespace cuacd
+
+using namespace cuacd;
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+extern "C" int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint32_t* tris, uint32_t trisCap,
+                                         float* volume, uint32_t* ntris, int32_t* status, void* stream) {
+  if (!points || !tris || !volume || !ntris || !status) return set_error(-1, "cuacd_hull_points_noalloc: null buffer");
+  if (nv > NOALLOC_MAX_POINTS)
+    return set_error(-2, "cuacd_hull_points_noalloc: at most 4096 points (the fixed scratch holds one 4096-point slab)");
+  if (trisCap < 12) return set_error(-1, "cuacd_hull_points_noalloc: trisCap must hold at least 4 triangles (12 u32)");
+  // the scratch array's device address, looked up once per device with that
+  // device current (in host code its name is only a stand-in)
+  static std::mutex mu;
+  static uint32_t* addr[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return set_error(-4, "cuacd_hull_points_noalloc: no current device");
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess) return set_error(-4, cudaGetErrorString(e));
+      addr[dev] = (uint32_t*)p;
+    }
+  }
+  uint32_t* scratch = addr[dev];
+  cudaStream_t s = (cudaStream_t)stream;
+  const uint32_t maxNv = std::max(nv, 1u);
+  const uint32_t fmax = 2 * std::min(4096u, maxNv) + 3 * HULL_VIS_MAX + 1024;
+  Level P;
+  memset(&P, 0, sizeof(P));
+  P.totalLevels = 1;
+  P.nChildParts = 1;
+  P.hullSlabWords = ((2 * maxNv + std::max(maxNv, 80u) + 7) & ~7u) + 16 * fmax;
+  P.slabStride = NOALLOC_SLAB_WORDS;
+  P.nSlabs = 1;
+  P.smallNv = 1024;
+  P.exportBase = 0;
+  P.exportStride = trisCap;
+  P.maxNvHint = maxNv;
+  Dev D;
+  memset(&D, 0, sizeof(D));
+  D.V = const_cast<float*>(points);
+  D.T = tris;
+  D.slab = scratch;
+  D.parts = reinterpret_cast<PartDesc*>(scratch + NOALLOC_PART_OFF);
+  D.ctr = scratch + NOALLOC_CTR_OFF;
+  D.work = scratch + NOALLOC_WORK_OFF;
+  k_noalloc_setup<<<1, 64, 0, s>>>(scratch, nv);
+  if (nv <= P.smallNv) k_hull<32><<<1, 256, 0, s>>>(P, D);
+  else k_hull<256><<<1, 256, 0, s>>>(P, D);
+  k_noalloc_finish<<<1, 1, 0, s>>>(scratch, volume, ntris, status);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return set_error(-4, cudaGetErrorString(e));
+  return 0;
+}

@@ -182,6 +182,26 @@ int cuacd_tree_read_jobs(void* tree, uint32_t first, uint32_t n, uint32_t* out);
 int cuacd_tree_read_part_geometry(void* tree, uint32_t part, float* verts, uint32_t* tris, uint32_t* edges);
 int cuacd_tree_read_plane(void* tree, uint32_t index, float* out4);
 
+/* Convex hull of one point set without allocating device memory. No
+ * counterpart in the reference: it serves callers that cannot allocate at
+ * the moment they need a hull (a host application whose own arena or
+ * caching allocator owns the device memory, or an interactive loop that
+ * must not stall running work on cudaMalloc / cudaFree). The caller passes
+ * device buffers it owns: points (nv * 3 floats), tris (trisCap u32, at
+ * least 12), and one float, one u32 and one i32 for the volume, the
+ * triangle count and the status (as cuacd_tree_hull_meshes: 0 or the
+ * failure code). The kernel's scratch is a fixed array of about 1 MiB inside
+ * the library, which every GPU that loads the library keeps until exit; it
+ * holds at most 4096 points, and larger sets are rejected with
+ * CUACD_E_CAPACITY. Work is queued on `stream` (a cudaStream_t, NULL for
+ * the default stream); results are valid once that stream has completed.
+ * The first call on a device looks up the array's device address (with
+ * that device current), so make the first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (different
+ * streams, or different host threads) race and must be serialised. */
+int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint32_t* tris, uint32_t trisCap, float* volume,
+                              uint32_t* ntris, int32_t* status, void* stream);
+
 /* Message of the last failure on the calling thread. */
 const char* cuacd_last_error(void);
 
