@@ -327,6 +327,74 @@ def run_engine(args):
     print(json.dumps(line), flush=True)
 
 
+def sample_counts(m):
+    """Samples per mesh by the reference's rule (hausdorff_shader.ts:57-78)."""
+    import numpy as np
+
+    v = m.verts.astype(np.float32)
+    a, b, c = v[m.tris[:, 0]], v[m.tris[:, 1]], v[m.tris[:, 2]]
+    ar = 0.5 * np.linalg.norm(np.cross(b - a, c - a), axis=1).astype(np.float32)
+    total = np.float32(ar.astype(np.float64).sum())
+    res = max(np.float32(1000.0), np.floor(np.float32(2000.0) * total))
+    cnt = np.floor((res / total) * ar).astype(np.int64)
+    nt = len(ar)
+    if nt > res:
+        step = max(nt // int(res), 1)
+        fill = (np.arange(nt) % step) == 0
+    else:
+        fill = (np.arange(nt) % 2) == 0
+    cnt = np.where(cnt > 0, cnt, fill.astype(np.int64))
+    return int(cnt.sum())
+
+
+def run_secondary(args):
+    """Hausdorff or hull batches (the merge pass's GPU work) on one GPU."""
+    import numpy as np
+    import torch
+
+    tree_mod = importlib.import_module("cuacd-web_gb300.tree")
+    gen = importlib.import_module("cuacd-web_gb300.meshgen")
+    mesh = importlib.import_module("cuacd-web_gb300.mesh")
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096, hullBudgetBytes=2 << 30,
+                         scratchWords=256 << 20)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    n = args.pairs
+    parts = [gen.noisy_icosphere(3, noise=0.15, seed=s) for s in range(n)]
+    hulls, _ = g.hull_meshes(parts)
+    if args.workload == "hausdorff":
+        pairs = [(m, mesh.Mesh(m.verts, h["tris"])) for m, h in zip(parts, hulls)]
+        evals = sum(sample_counts(a) * b.nt + sample_counts(b) * a.nt for a, b in pairs)
+        call = lambda: g.hausdorff(pairs)  # noqa: E731
+        metric, unit, units = "point-triangle distance evaluations/s", "evals/s", evals
+        cfg = {"workload": f"Hausdorff of {n} (noisy icosphere L3, its hull) pairs", "tris_per_mesh": parts[0].nt,
+               "samples": "max(1000, floor(2000 area)) per mesh"}
+    else:
+        pts = [mesh.Mesh(m.verts, np.zeros((0, 3), np.uint32)) for m in parts]
+        call = lambda: g.hull_meshes(pts)  # noqa: E731
+        metric, unit, units = "convex hulls/s", "hulls/s", n
+        cfg = {"workload": f"hulls of {n} point sets of {parts[0].nv} points (noisy icosphere L3)"}
+    for _ in range(args.warmup):
+        call()
+    ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        call()
+        ms += g.last_gpu_ms
+    value = units * args.steps / (ms / 1000.0)
+    line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "f32", "data": "synthetic", "config": cfg}
+    if args.workload == "hausdorff":
+        # float32 operations counted from hd_tri_sq's source: 67 on the face
+        # interior branch, 150 through the three edge tests; nominal FP32 peak
+        # 152 SMs x 128 lanes x 2 x 2.07 GHz
+        peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        for c, name in ((67, "flops_face_interior"), (150, "flops_edge_tests")):
+            line.setdefault("fp32", {})[name] = c * value / 1e12
+        line["fp32"]["peak_tflops_nominal"] = peak
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -335,9 +403,13 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--seeds", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls"])
+    ap.add_argument("--pairs", type=int, default=256)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "tree":
+        run_secondary(args)
     else:
         run_engine(args)
 

@@ -761,6 +761,17 @@ void cuacd_set_profile(void* t, int on) {
     tr->pev.push_back(e);
   }
 }
+float cuacd_tree_last_gpu_ms(void* t) {
+  // device time between the last call's two events (a run, a hull batch or
+  // a Hausdorff batch); 0 when the call has not completed
+  Tree* tr = (Tree*)t;
+  float ms = 0;
+  if (!tr || cudaEventElapsedTime(&ms, tr->ev0, tr->ev1) != cudaSuccess) {
+    cudaGetLastError();
+    return 0.0f;
+  }
+  return ms;
+}
 int cuacd_tree_kernel_bytes(void* t, uint64_t* bytes3) {
   if (!t) return fail(CUACD_E_INVALID, "null tree");
   std::memcpy(bytes3, ((Tree*)t)->bytes, sizeof(uint64_t) * 3);

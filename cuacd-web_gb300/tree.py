@@ -54,6 +54,9 @@ def load_library():
     L.cuacd_plane_slots.argtypes = [C.c_void_p]
     L.cuacd_set_profile.argtypes = [C.c_void_p, C.c_int]
     L.cuacd_tree_kernel_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
+    L.cuacd_tree_kernel_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
+    L.cuacd_tree_last_gpu_ms.restype = C.c_float
+    L.cuacd_tree_last_gpu_ms.argtypes = [C.c_void_p]
     run_args = [C.c_void_p, P(A.MeshRef), C.c_int, P(C.c_float), C.c_int, P(A.RunOpts)]
     L.cuacd_tree_run.argtypes = run_args + [P(A.SeedResult), P(A.RunStats)]
     L.cuacd_tree_prepare.argtypes = run_args
@@ -114,6 +117,17 @@ class GpuTree:
 
     def set_profile(self, on: bool):
         load_library().cuacd_set_profile(self.h, int(on))
+
+    @property
+    def last_gpu_ms(self) -> float:
+        """Device time of the last call (GpuTree.lastHullGpuMs, tree.ts:380)."""
+        return float(load_library().cuacd_tree_last_gpu_ms(self.h))
+
+    def kernel_bytes(self):
+        """Algorithmic bytes of the last run's plan, emit and hull kernels."""
+        b = (C.c_uint64 * 3)()
+        _check(load_library().cuacd_tree_kernel_bytes(self.h, b))
+        return [int(x) for x in b]
 
     KERNELS = ("reset", "plan", "scan", "emit", "hull", "record", "evaluate")
 

@@ -131,6 +131,15 @@ void cuacd_set_profile(void* tree, int on);
  * [1] plan, [2] scan, [3] emit, [4] hull, [5] record, [6] evaluate. */
 int cuacd_tree_kernel_ms(void* tree, float* ms7);
 
+/* Algorithmic bytes of the last run's plan, emit and hull kernels: each
+ * candidate reads its parent once (12 nv + 12 nt + 32 ne), writes its
+ * children once, and each child's points are read once by its hull. */
+int cuacd_tree_kernel_bytes(void* tree, uint64_t* bytes3);
+
+/* GpuTree.lastHullGpuMs (tree.ts:380): device time of the last completed
+ * call on this handle (tree run, hull batch or Hausdorff batch), in ms. */
+float cuacd_tree_last_gpu_ms(void* tree);
+
 /* GpuTree.run (tree.ts:449-661). edgePlanes holds planesPerSeed planes
  * (4 floats) per seed; zero planes are skipped; planes beyond planeSlots are
  * ignored. out receives nSeeds results. */
