@@ -37,7 +37,7 @@ sys.path.insert(0, ROOT)
 THRESHOLD = 0.1
 TREE = dict(width=6, width2=3, depth=3, nConcaveEdges=16, minEdgeDist=min(THRESHOLD / 4, 0.015))
 POOLS = dict(vertexCap=64 << 20, triCap=64 << 20, edgeCap=4 << 20, scratchWords=64 << 20,
-             hullBudgetBytes=2 << 30, hullMaxVerts=4096)
+             hullBudgetBytes=6 << 30, hullMaxVerts=4096)
 REFINE_ROUNDS, REFINE_PROBES = 2, 8
 METRIC = "cut candidates evaluated/s"
 UNIT = "candidates/s"
@@ -355,7 +355,7 @@ def run_secondary(args):
     tree_mod = importlib.import_module("cuacd-web_gb300.tree")
     gen = importlib.import_module("cuacd-web_gb300.meshgen")
     mesh = importlib.import_module("cuacd-web_gb300.mesh")
-    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096, hullBudgetBytes=2 << 30,
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096, hullBudgetBytes=6 << 30,
                          scratchWords=256 << 20)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     n = args.pairs

@@ -100,6 +100,15 @@ struct HdArgs {
   uint32_t maxSide;          // largest per-side capacity
 };
 
+// Physical words of one hull slab whose reference size (which fixes the face
+// limit fmax) is W words. After the W words a part of nv points needs the
+// visible list and walk queue (2 * 2048), adjacency (4 fmax), two bitmap
+// arrays (2 ceil(fmax / 32)) and two horizon maps (2 nv). With fmax <= (W -
+// 3 nv) / 16 and nv <= (W - 1024) / 3 that is below 3672 + 0.671 W.
+__host__ __device__ constexpr uint32_t hull_slab_stride(uint32_t W) {
+  return (W + 4096u + (uint32_t)(((uint64_t)W * 2) / 3) + W / 128 + 64u + 63u) & ~63u;
+}
+
 // ---------------- group primitives ----------------
 template <int G> struct Grp;
 

@@ -195,7 +195,7 @@ struct Tree {
   int planSlabs(uint32_t maxNv, uint32_t nParts) {
     uint32_t fmax = 2 * std::min<uint32_t>((uint32_t)cfg.hullMaxVerts, maxNv) + 3 * VIS_MAX + 1024;
     slabWords = ((2 * maxNv + std::max(maxNv, 80u) + 7) & ~7u) + 16 * fmax;
-    slabStride = (slabWords + 2 * VIS_MAX + 63) & ~63u;
+    slabStride = hull_slab_stride(slabWords);
     uint64_t byBudget = std::max<uint64_t>(1, cfg.hullBudgetBytes / ((uint64_t)slabStride * 4));
     nSlabsSmall = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * bpsSmall * 8, (uint64_t)std::max(nParts, 1u)});
     nSlabsBig = (uint32_t)std::min<uint64_t>({byBudget, (uint64_t)nSM * bpsBig, (uint64_t)std::max(nParts, 1u)});

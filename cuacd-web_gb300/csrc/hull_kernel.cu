@@ -57,8 +57,8 @@ __constant__ float c_kdop[40][3] = {
 struct HullSm {
   uint32_t seed[80];
   uint32_t nf, nalive, fail, compacted;
-  uint32_t ncand, ok;
-  uint32_t pad[2];
+  uint32_t ncand, ok, nvis;
+  uint32_t pad;
 };
 
 // exact sign of det[e1; e2; d] for integer vectors below 2^23 (shaders.ts:868-876)
@@ -91,8 +91,13 @@ struct HullCtx {
   float* dist;
   uint32_t* cand;
   uint32_t* F;     // face records, 16 words each
-  uint32_t* vis;   // visible face slots (HULL_VIS_MAX)
-  uint32_t* conn;  // connected flags of the visible list (HULL_VIS_MAX)
+  uint32_t* vis;   // visible face slots in slot order (HULL_VIS_MAX)
+  uint32_t* q;     // walk queue (HULL_VIS_MAX)
+  uint32_t* nbr;   // 4 words per face slot: the faces across its 3 edges
+  uint32_t* bm;    // one bit per face slot
+  uint32_t* wp;    // compaction: alive faces before each bitmap word
+  uint32_t* hA;    // per point: new face whose horizon edge starts there
+  uint32_t* hB;    // per point: new face whose horizon edge ends there
   const float* qc;  // quantised points in shared memory, or null
 
   __device__ __forceinline__ f3 qvert(uint32_t i) const {
@@ -151,6 +156,17 @@ struct HullCtx {
     }
     return orient_exact(pb - pa, pc - pa, d) > 0 ? 1e-30f : -1.0f;
   }
+  // the most visible face of [f0, f1) for point i (first slot on ties)
+  __device__ __forceinline__ void best_face(uint32_t i, uint32_t f0, uint32_t f1, uint32_t& bestF, float& bestD) const {
+    const f3 pt = qvert(i);
+    bestF = CUACD_NONE;
+    bestD = -1.0f;
+    for (uint32_t f = f0; f < f1; f++) {
+      const float dd = face_eval(f, pt);
+      if (dd > 0.0f && dd > bestD) { bestD = dd; bestF = f; }
+    }
+    if (bestF == CUACD_NONE) bestD = 0.0f;
+  }
   __device__ __forceinline__ void assign(uint32_t i, uint32_t f0, uint32_t f1) const {
     f3 pt = qvert(i);
     uint32_t bestF = CUACD_NONE;
@@ -174,138 +190,231 @@ __device__ __forceinline__ bool shares_edge(uint32_t f0, uint32_t f1, uint32_t f
   return false;
 }
 
-// remove dead face slots, keeping slot order (shaders.ts:946-969)
+// Adjacency: nbr[4 f + k] is the face across edge k of face f, edges being
+// (a, b), (b, c), (c, a). The bitmap bm marks the faces visible from the
+// point being inserted (and, during a compaction, the alive faces).
+__device__ __forceinline__ bool bm_test(const uint32_t* bm, uint32_t f) { return (bm[f >> 5] >> (f & 31)) & 1u; }
+
+// remove dead face slots, keeping slot order (shaders.ts:946-969). Face
+// f's new slot is its rank among alive faces: the alive bitmap's word
+// prefix plus the bits below f in its word. Neighbour slots are renumbered
+// the same way. Returns the new slot of `track`.
 template <int G>
-__device__ __noinline__ void hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
+__device__ __noinline__ uint32_t hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t track) {
   const int lid = Grp<G>::lid();
   const uint32_t nf = hs.nf;
-  uint32_t run = 0;
+  const uint32_t nw = (nf + 31) / 32;
+  // alive bitmap, one ballot per 32 slots
   for (uint32_t c = 0; c * G < nf; c++) {
     const uint32_t f = c * G + lid;
-    uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0, w2 = w0, w3 = w0;
-    uint32_t al = 0;
+    const bool al = f < nf && h.alive(f);
+    const unsigned m = __ballot_sync(FULLMASK, al);
+    if ((threadIdx.x & 31) == 0 && (f >> 5) < nw) h.bm[f >> 5] = m;
+  }
+  Grp<G>::sync();
+  uint32_t run = 0;
+  for (uint32_t c = 0; c * G < nw; c++) {
+    const uint32_t w = c * G + lid;
+    const uint32_t cnt = w < nw ? __popc(h.bm[w]) : 0u;
+    uint32_t tot;
+    const uint32_t pre = grp_scan_u<G>(cnt, &tot, sm);
+    if (w < nw) h.wp[w] = run + pre;
+    run += tot;
+  }
+  Grp<G>::sync();
+  auto rank = [&](uint32_t f) { return h.wp[f >> 5] + __popc(h.bm[f >> 5] & ((1u << (f & 31)) - 1u)); };
+  for (uint32_t c = 0; c * G < nf; c++) {
+    const uint32_t f = c * G + lid;
+    uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0, w2 = w0, w3 = w0, nb = w0;
+    bool al = false;
     if (f < nf) {
       const uint4* r = h.rec(f);
-      w0 = r[0]; w1 = r[1]; w2 = r[2]; w3 = r[3];
-      al = (w0.x & ALIVE) ? 1u : 0u;
+      w0 = r[0];
+      al = (w0.x & ALIVE) != 0;
+      if (al) {
+        w1 = r[1]; w2 = r[2]; w3 = r[3];
+        nb = *reinterpret_cast<const uint4*>(h.nbr + 4 * (size_t)f);
+        if (nb.x < nf) nb.x = rank(nb.x);
+        if (nb.y < nf) nb.y = rank(nb.y);
+        if (nb.z < nf) nb.z = rank(nb.z);
+      }
     }
-    uint32_t tot;
-    uint32_t pre = grp_scan_bit<G>(al != 0, &tot, sm);
     Grp<G>::sync();
     if (al) {
-      uint4* r = h.rec(run + pre);
+      const uint32_t r0 = rank(f);
+      uint4* r = h.rec(r0);
       r[0] = w0; r[1] = w1; r[2] = w2; r[3] = w3;
+      *reinterpret_cast<uint4*>(h.nbr + 4 * (size_t)r0) = nb;
     }
-    run += tot;
     Grp<G>::sync();
   }
+  const uint32_t tracked = track < nf ? rank(track) : track;
+  Grp<G>::sync();
+  for (uint32_t w = lid; w < nw; w += G) h.bm[w] = 0;
   if (lid == 0) { hs.nf = run; hs.compacted = 1; }
   Grp<G>::sync();
+  return tracked;
 }
 
-// insert point pIdx (shaders.ts:975-1055) with the deterministic order
+// Insert point pIdx (shaders.ts:975-1055). The reference scans every face
+// slot for visible faces and keeps the edge-connected component of the
+// most visible one; with exact predicates the visible faces of a convex
+// hull form one connected patch, so here the patch is walked from the
+// point's owner face (a visible face) across neighbours, and the bitmap of
+// the patch is then listed in slot order: the visible list, the horizon
+// order and the new face slots are the reference's deterministic ones.
+// The bitmap stays set for hull_grow's reassignment and is cleared there.
 template <int G>
-__device__ __noinline__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t pIdx) {
+__device__ __noinline__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t pIdx, uint32_t start) {
   const int lid = Grp<G>::lid();
   const f3 p = h.qvert(pIdx);
   uint32_t nf = hs.nf;
   const uint32_t nalive = hs.nalive;
   if (nf + 3 * HULL_VIS_MAX > h.fmax || nf > 2 * nalive + 512) {
-    hull_compact<G>(h, hs, sm);
+    start = hull_compact<G>(h, hs, sm, start);
     nf = hs.nf;
   }
-  // visible faces in slot order; most visible face, lowest list position on ties
-  uint32_t nvis = 0;
-  float bd = -1.0f;
-  uint32_t bk = CUACD_NONE;
-  for (uint32_t c = 0; c * G < nf; c++) {
-    const uint32_t f = c * G + lid;
-    float dd = f < nf ? h.face_eval(f, p) : -1.0f;
-    uint32_t v = dd > 0.0f ? 1u : 0u;
-    uint32_t tot;
-    uint32_t pre = grp_scan_bit<G>(v != 0, &tot, sm);
-    if (v) {
-      uint32_t k = nvis + pre;
-      if (k < HULL_VIS_MAX) h.vis[k] = f;
-      am_merge(bd, bk, dd, k);
-    }
-    nvis += tot;
+  // breadth-first walk over visible neighbours, claiming faces in bm
+  if (lid == 0) {
+    h.q[0] = start;
+    h.bm[start >> 5] |= 1u << (start & 31);
   }
   Grp<G>::sync();
-  if (nvis == 0) return;
-  if (nvis > HULL_VIS_MAX) {
-    if (lid == 0) hs.fail = 1;
-    Grp<G>::sync();
-    return;
-  }
-  grp_argmax_pos<G>(bd, bk, sm);
-  const uint32_t seedK = bk;
-  for (uint32_t k = lid; k < nvis; k += G) h.conn[k] = k == seedK ? 1u : 0u;
-  Grp<G>::sync();
-  // edge-connected component of the most visible face
-  for (;;) {
-    bool changed = false;
-    for (uint32_t i = lid; i < nvis; i += G) {
-      if (h.conn[i]) continue;
-      uint32_t a, b, c;
-      h.abc(h.vis[i], a, b, c);
-      for (uint32_t j = 0; j < nvis; j++) {
-        if (j == i || !h.conn[j]) continue;
-        uint32_t x, y, z;
-        h.abc(h.vis[j], x, y, z);
-        if (shares_edge(a, b, c, x, y, z)) { h.conn[i] = 1; changed = true; break; }
+  uint32_t head = 0, qn = 1;
+  bool overflow = false;
+  while (head < qn) {
+    const uint32_t tasks = 3 * (qn - head);
+    uint32_t added = 0;
+    for (uint32_t t0 = 0; t0 < tasks; t0 += G) {
+      const uint32_t t = t0 + lid;
+      uint32_t g = 0;
+      bool claimed = false;
+      if (t < tasks) {
+        g = h.nbr[4 * (size_t)h.q[head + t / 3] + t % 3];
+        if (g < nf && !bm_test(h.bm, g) && h.face_eval(g, p) > 0.0f) {
+          const uint32_t bit = 1u << (g & 31);
+          claimed = (atomicOr(h.bm + (g >> 5), bit) & bit) == 0;
+        }
       }
+      uint32_t tot;
+      const uint32_t pre = grp_scan_bit<G>(claimed, &tot, sm);
+      if (claimed && qn + added + pre < HULL_VIS_MAX) h.q[qn + added + pre] = g;
+      added += tot;
     }
-    bool any = grp_any<G>(changed, sm);
     Grp<G>::sync();
-    if (!any) break;
+    head = qn;
+    qn += added;
+    if (qn > HULL_VIS_MAX) { overflow = true; break; }
   }
-  if (nf + 3 * nvis > h.fmax) {
-    if (lid == 0) hs.fail = 2;
+  const uint32_t nw = (nf + 31) / 32;
+  if (overflow || nf + 3 * qn > h.fmax) {
+    // visible-set overflow (code 1) or face slots exhausted (code 2)
+    for (uint32_t w = lid; w < nw; w += G) h.bm[w] = 0;
+    if (lid == 0) hs.fail = overflow ? 1u : 2u;
     Grp<G>::sync();
     return;
   }
-  // horizon edges in order e = 3 * listPos + k become new faces (a, b, p)
+  const uint32_t nvis = qn;
+  // the visible faces in slot order
+  uint32_t pos = 0;
+  for (uint32_t c = 0; c * G < nw; c++) {
+    const uint32_t w = c * G + lid;
+    uint32_t bits = w < nw ? h.bm[w] : 0u;
+    uint32_t tot;
+    uint32_t at = pos + grp_scan_u<G>(__popc(bits), &tot, sm);
+    while (bits) {
+      const uint32_t b = __ffs(bits) - 1;
+      h.vis[at++] = 32 * w + b;
+      bits &= bits - 1;
+    }
+    pos += tot;
+  }
+  Grp<G>::sync();
+  // horizon edges in order e = 3 * listPos + k become new faces (a, b, p):
+  // an edge is on the horizon when the face across it is not visible
   uint32_t nnew = 0;
   for (uint32_t c = 0; c * G < 3 * nvis; c++) {
     const uint32_t e = c * G + lid;
-    uint32_t isNew = 0, a = 0, b = 0;
+    bool isNew = false;
+    uint32_t a = 0, b = 0, f = 0, twin = 0;
     if (e < 3 * nvis) {
       const uint32_t vi = e / 3, k = e % 3;
-      if (h.conn[vi]) {
+      f = h.vis[vi];
+      twin = h.nbr[4 * (size_t)f + k];
+      if (twin >= nf || !bm_test(h.bm, twin)) {
+        isNew = true;
         uint32_t fa, fb, fc;
-        h.abc(h.vis[vi], fa, fb, fc);
+        h.abc(f, fa, fb, fc);
         a = k == 0 ? fa : (k == 1 ? fb : fc);
         b = k == 0 ? fb : (k == 1 ? fc : fa);
-        bool found = false;
-        for (uint32_t j = 0; j < nvis && !found; j++) {
-          if (!h.conn[j]) continue;
-          uint32_t g0, g1, g2;
-          h.abc(h.vis[j], g0, g1, g2);
-          if ((g0 == b && g1 == a) || (g1 == b && g2 == a) || (g2 == b && g0 == a)) found = true;
-        }
-        isNew = found ? 0u : 1u;
       }
     }
     uint32_t tot;
-    uint32_t pre = grp_scan_bit<G>(isNew != 0, &tot, sm);
-    if (isNew) h.face_write(nf + nnew + pre, a, b, pIdx);
+    const uint32_t pre = grp_scan_bit<G>(isNew, &tot, sm);
+    if (isNew) {
+      const uint32_t s = nf + nnew + pre;
+      h.face_write(s, a, b, pIdx);
+      h.nbr[4 * (size_t)s] = twin;
+      if (twin < nf) {
+        uint32_t* tn = h.nbr + 4 * (size_t)twin;
+        for (int j = 0; j < 3; j++) if (tn[j] == f) tn[j] = s;
+      }
+      h.hA[a] = s;
+      h.hB[b] = s;
+    }
     nnew += tot;
   }
   Grp<G>::sync();
-  uint32_t killed = 0;
-  for (uint32_t vi = lid; vi < nvis; vi += G) {
-    if (h.conn[vi]) {
-      h.F[16 * (size_t)h.vis[vi]] &= 0x7fffffffu;
-      killed++;
-    }
+  // new faces around the horizon loop: (b, p) borders the face starting at
+  // b, (p, a) the face ending at a
+  for (uint32_t s = nf + lid; s < nf + nnew; s += G) {
+    uint32_t a, b, c;
+    h.abc(s, a, b, c);
+    h.nbr[4 * (size_t)s + 1] = h.hA[b];
+    h.nbr[4 * (size_t)s + 2] = h.hB[a];
   }
-  killed = grp_sum_u<G>(killed, sm);
+  for (uint32_t vi = lid; vi < nvis; vi += G) h.F[16 * (size_t)h.vis[vi]] &= 0x7fffffffu;
   if (lid == 0) {
     hs.nf = nf + nnew;
-    hs.nalive = nalive + nnew - killed;
+    hs.nalive = nalive + nnew - nvis;
+    hs.nvis = nvis;
   }
   Grp<G>::sync();
+}
+
+// hull_grow for a warp whose candidate list fits its lanes: lane k holds
+// candidate k (point ci, owner co, distance cd) in registers. The pick (the
+// largest distance, lowest point index on ties) is two redux operations and
+// reassignment is per lane; dropping inside points from the list is not
+// needed because the pick does not depend on list order. Same result as
+// hull_grow; the owner and distance arrays are not kept up to date.
+__device__ __noinline__ uint32_t hull_grow_lanes(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t nfPrev,
+                                                 uint32_t maxIter, uint32_t ci, uint32_t co, float cd) {
+  const int lane = threadIdx.x & 31;
+  uint32_t nIns = 0;
+  for (uint32_t iter = 0; iter < maxIter; iter++) {
+    const uint32_t key = co != CUACD_NONE ? __float_as_uint(cd) : 0u;
+    const uint32_t mk = __reduce_max_sync(FULLMASK, key);
+    if (mk == 0u) break;
+    const uint32_t pick = __reduce_min_sync(FULLMASK, key == mk ? ci : CUACD_NONE);
+    const unsigned holder = __ballot_sync(FULLMASK, key == mk && ci == pick);
+    const uint32_t start = __shfl_sync(FULLMASK, co, __ffs(holder) - 1);
+    if (lane == 0) hs.compacted = 0;
+    __syncwarp();
+    hull_insert<32>(h, hs, sm, pick, start);
+    nIns++;
+    if (hs.fail) break;
+    const uint32_t nfNow = hs.nf;
+    const bool compacted = hs.compacted != 0;
+    if (ci == pick) co = CUACD_NONE;
+    if (co != CUACD_NONE && (compacted || bm_test(h.bm, co))) h.best_face(ci, compacted ? 0 : nfPrev, nfNow, co, cd);
+    __syncwarp();
+    for (uint32_t vi = lane; vi < hs.nvis; vi += 32) h.bm[h.vis[vi] >> 5] = 0;
+    __syncwarp();
+    nfPrev = nfNow;
+  }
+  __syncwarp();
+  return nIns;
 }
 
 // farthest-first insertion of the candidate list (shaders.ts:1060-1129)
@@ -327,20 +436,23 @@ __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem
     const uint32_t pick = mi;
     if (lid == 0) hs.compacted = 0;
     Grp<G>::sync();
-    hull_insert<G>(h, hs, sm, pick);
+    hull_insert<G>(h, hs, sm, pick, h.owner[pick]);
     nIns++;
     if (hs.fail) break;
     const uint32_t nfNow = hs.nf;
     const bool compacted = hs.compacted != 0;
     if (lid == 0) { h.owner[pick] = CUACD_NONE; h.dist[pick] = 0.0f; }
     Grp<G>::sync();
+    // an owner face died in this insertion exactly when it was visible
     for (uint32_t k = lid; k < ncand; k += G) {
       uint32_t i = h.cand[k];
       uint32_t own = h.owner[i];
       if (own == CUACD_NONE) continue;
-      if (!compacted && h.alive(own)) continue;
+      if (!compacted && !bm_test(h.bm, own)) continue;
       h.assign(i, compacted ? 0 : nfPrev, nfNow);
     }
+    Grp<G>::sync();
+    for (uint32_t vi = lid; vi < hs.nvis; vi += G) h.bm[h.vis[vi] >> 5] = 0;
     Grp<G>::sync();
     nfPrev = nfNow;
     if (++sinceCompact >= 4) {
@@ -432,6 +544,12 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
     if (lid == 0) { pdp->hullVol = -1.0f; pdp->flags = 3; atomicAdd(D.ctr + CTR_HULLFAIL, 1u); }
     return;
   }
+  // the walk's arrays after the reference's slab words must fit the slab
+  // (always true for hull_slab_stride; checked so a slab is never overrun)
+  if ((uint64_t)P.hullSlabWords + 2 * HULL_VIS_MAX + 4ull * fmax + 2 * ((fmax + 31) / 32) + 2ull * nv > P.slabStride) {
+    if (lid == 0) { pdp->hullVol = -1.0f; pdp->flags = 3; atomicAdd(D.ctr + CTR_HULLFAIL, 1u); }
+    return;
+  }
   if (lid == 0) add_bytes(D.ctr, CTR_BYTES_HULL, 12ull * nv);
   HullCtx h;
   h.qc = nullptr;
@@ -440,8 +558,17 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
   h.dist = reinterpret_cast<float*>(slab + nv);
   h.cand = slab + 2 * nv;
   h.F = slab + fb;
+  // after the reference's slab words (which fix fmax): visible list, walk
+  // queue, adjacency, bitmap, word prefix, horizon maps (hull_slab_stride)
   h.vis = slab + P.hullSlabWords;
-  h.conn = h.vis + HULL_VIS_MAX;
+  h.q = h.vis + HULL_VIS_MAX;
+  h.nbr = h.q + HULL_VIS_MAX;
+  const uint32_t nw = (fmax + 31) / 32;
+  h.bm = h.nbr + 4 * (size_t)fmax;
+  h.wp = h.bm + nw;
+  h.hA = h.wp + nw;
+  h.hB = h.hA + nv;
+  for (uint32_t w = lid; w < nw; w += G) h.bm[w] = 0;
   // quantisation grid: 2^21 cells across the largest extent
   f3 lo = mk3(1e30f, 1e30f, 1e30f), hi = mk3(-1e30f, -1e30f, -1e30f);
   for (uint32_t i = lid; i < nv; i += G) {
@@ -551,6 +678,9 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
       if (lid == 1) h.face_write(1, a, i3, b);
       if (lid == 2) h.face_write(2, b, i3, c);
       if (lid == 3) h.face_write(3, c, i3, a);
+      // faces across each edge of the tetrahedron
+      const uint4 nb[4] = {make_uint4(1, 2, 3, 0), make_uint4(3, 2, 0, 0), make_uint4(1, 3, 0, 0), make_uint4(2, 1, 0, 0)};
+      *reinterpret_cast<uint4*>(h.nbr + 4 * lid) = nb[lid];
     }
     if (lid == 0) {
       hs.fail = 0;
@@ -564,15 +694,40 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
     if (lid == 0) pdp->hullVol = 0.0f;
     return;
   }
-  // seeds first
-  for (uint32_t k = lid; k < 80; k += G) {
-    const uint32_t i = hs.seed[k];
-    h.assign(i, 0, 4);
-    h.cand[k] = i;
+  // seeds first. A point can be the extreme of several axes; its repeats in
+  // the list have the same distance and index, so they never change a pick
+  // or an owner, and the list keeps first occurrences only.
+  uint32_t nuniq = 0;
+  for (uint32_t c = 0; c * G < 80; c++) {
+    const uint32_t k = c * G + lid;
+    bool keep = false;
+    uint32_t s = 0;
+    if (k < 80) {
+      s = hs.seed[k];
+      keep = true;
+      for (uint32_t j = 0; j < k; j++) if (hs.seed[j] == s) { keep = false; break; }
+    }
+    uint32_t tot;
+    const uint32_t pre = grp_scan_bit<G>(keep, &tot, sm);
+    if (keep) h.cand[nuniq + pre] = s;
+    nuniq += tot;
   }
-  if (lid == 0) hs.ncand = 80;
   Grp<G>::sync();
-  uint32_t nIns = hull_grow<G>(h, hs, sm, 4, 80);
+  uint32_t nIns;
+  if (G == 32 && nuniq <= 32) {
+    uint32_t ci = 0, co = CUACD_NONE;
+    float cd = 0.0f;
+    if ((uint32_t)lid < nuniq) {
+      ci = h.cand[lid];
+      h.best_face(ci, 0, 4, co, cd);
+    }
+    nIns = hull_grow_lanes(h, hs, sm, 4, 80, ci, co, cd);
+  } else {
+    for (uint32_t k = lid; k < nuniq; k += G) h.assign(h.cand[k], 0, 4);
+    if (lid == 0) hs.ncand = nuniq;
+    Grp<G>::sync();
+    nIns = hull_grow<G>(h, hs, sm, 4, 80);
+  }
   const uint32_t fail0 = hs.fail;
   const uint32_t nfPrev = hs.nf;
   // last-level branch and bound (shaders.ts:1300-1331)
@@ -625,7 +780,18 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
   }
   Grp<G>::sync();
   const uint32_t maxIter = (P.hullStage == 2 || P.hullStage == 3 || fail0 != 0) ? 0 : nv;
-  nIns += hull_grow<G>(h, hs, sm, nfPrev, maxIter);
+  if (G == 32 && ncand <= 32) {
+    uint32_t ci = 0, co = CUACD_NONE;
+    float cd = 0.0f;
+    if ((uint32_t)lid < ncand) {
+      ci = h.cand[lid];
+      co = h.owner[ci];
+      cd = h.dist[ci];
+    }
+    nIns += hull_grow_lanes(h, hs, sm, nfPrev, maxIter, ci, co, cd);
+  } else {
+    nIns += hull_grow<G>(h, hs, sm, nfPrev, maxIter);
+  }
   if (hs.fail) {
     if (lid == 0) {
       pdp->hullVol = -1.0f;
@@ -739,8 +905,8 @@ int set_error(int code, const char* msg);
 #define NOALLOC_MAX_POINTS 4096u
 // one slab for NOALLOC_MAX_POINTS points with hullMaxVerts 4096, sized as the
 // tree's slabs: ((2 n + n + 7) & ~7) + 16 (2 n + 3 * 2048 + 1024) words
-// = 258048, plus the visible list and its flags (2 * 2048 words)
-#define NOALLOC_SLAB_WORDS 262144u
+// = 258048, plus the walk's arrays (hull_slab_stride): 436288 words, 1.7 MiB
+#define NOALLOC_SLAB_WORDS hull_slab_stride(258048u)
 #define NOALLOC_PART_OFF NOALLOC_SLAB_WORDS
 #define NOALLOC_CTR_OFF (NOALLOC_PART_OFF + 16u)
 #define NOALLOC_WORK_OFF (NOALLOC_CTR_OFF + (uint32_t)CTR_WORDS)

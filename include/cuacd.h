@@ -199,7 +199,7 @@ int cuacd_tree_read_plane(void* tree, uint32_t index, float* out4);
  * device buffers it owns: points (nv * 3 floats), tris (trisCap u32, at
  * least 12), and one float, one u32 and one i32 for the volume, the
  * triangle count and the status (as cuacd_tree_hull_meshes: 0 or the
- * failure code). The kernel's scratch is a fixed array of about 1 MiB inside
+ * failure code). The kernel's scratch is a fixed array of about 1.7 MiB inside
  * the library, which every GPU that loads the library keeps until exit; it
  * holds at most 4096 points, and larger sets are rejected with
  * CUACD_E_CAPACITY. Work is queued on `stream` (a cudaStream_t, NULL for
