@@ -111,72 +111,95 @@ struct HullCtx {
     uint4 w = rec(f)[0];
     a = w.x & 0x7fffffffu; b = w.y; c = w.z;
   }
-  // face record: ia|alive ib ic bf | nx ny nz ax | ay az bx by | bz cx cy cz
+  // face record (16-word slots):
+  //   ia|alive ib ic kb | nx ny nz s | ax ay az Nx.lo | Ny.lo Nz.lo Nx.hi|Ny.hi<<16 Nz.hi
+  // kb = 1e-6 * |e1|_1 * |e2|_1 is the rounding-bound factor of the filtered
+  // predicate and s = max(|n|, 1e-30) the ranking divisor, both rounded
+  // exactly as the predicate rounds them when it forms them itself. N is the
+  // exact integer normal e1 x e2: grid differences are at most 2^21, so each
+  // component is below 2^43 and splits into a low word and a 16-bit high part.
   __device__ __forceinline__ void face_write(uint32_t f, uint32_t a, uint32_t b, uint32_t c) const {
     f3 pa = qvert(a), pb = qvert(b), pc = qvert(c);
     f3 e1 = pb - pa, e2 = pc - pa;
     f3 n = cross(e1, e2);
-    float bf = l1(e1) * l1(e2);
+    const float kb = 1e-6f * (l1(e1) * l1(e2));
+    const float s = fmaxf(sqrtf(dot(n, n)), 1e-30f);
+    const long long e1x = (long long)e1.x, e1y = (long long)e1.y, e1z = (long long)e1.z;
+    const long long e2x = (long long)e2.x, e2y = (long long)e2.y, e2z = (long long)e2.z;
+    const long long Nx = e1y * e2z - e1z * e2y, Ny = e1z * e2x - e1x * e2z, Nz = e1x * e2y - e1y * e2x;
+    const uint32_t hx = (uint32_t)(Nx >> 32) & 0xffffu, hy = (uint32_t)(Ny >> 32) & 0xffffu;
     uint4* w = rec(f);
-    w[0] = make_uint4(a | ALIVE, b, c, __float_as_uint(bf));
-    w[1] = make_uint4(__float_as_uint(n.x), __float_as_uint(n.y), __float_as_uint(n.z), __float_as_uint(pa.x));
-    w[2] = make_uint4(__float_as_uint(pa.y), __float_as_uint(pa.z), __float_as_uint(pb.x), __float_as_uint(pb.y));
-    w[3] = make_uint4(__float_as_uint(pb.z), __float_as_uint(pc.x), __float_as_uint(pc.y), __float_as_uint(pc.z));
+    w[0] = make_uint4(a | ALIVE, b, c, __float_as_uint(kb));
+    w[1] = make_uint4(__float_as_uint(n.x), __float_as_uint(n.y), __float_as_uint(n.z), __float_as_uint(s));
+    w[2] = make_uint4(__float_as_uint(pa.x), __float_as_uint(pa.y), __float_as_uint(pa.z), (uint32_t)Nx);
+    w[3] = make_uint4((uint32_t)Ny, (uint32_t)Nz, hx | (hy << 16), (uint32_t)(Nz >> 32));
   }
-  // positive: visible (ranking value); negative: not visible (shaders.ts:906-921)
-  __device__ __forceinline__ float face_eval(uint32_t f, f3 p) const {
-    const uint4* w = rec(f);
-    uint4 a = w[0];
-    if ((a.x & ALIVE) == 0) return -1e30f;
-    uint4 b = w[1];
-    f3 n = mk3(__uint_as_float(b.x), __uint_as_float(b.y), __uint_as_float(b.z));
-    // the corners are the quantised points: from the shared-memory copy
-    // when the part has one (same values as the record holds)
-    f3 pa;
-    uint4 c;
-    if (qc) {
-      pa = qvert(a.x & 0x7fffffffu);
-    } else {
-      c = w[2];
-      pa = mk3(__uint_as_float(b.w), __uint_as_float(c.x), __uint_as_float(c.y));
-    }
-    f3 d = p - pa;
-    float det = dot(n, d);
-    float bound = (1e-6f * __uint_as_float(a.w)) * l1(d);
-    if (det > bound) return det / fmaxf(sqrtf(dot(n, n)), 1e-30f);
+  // the float32 filter on loaded record words: the ranking value det/|n|
+  // when the point is visible beyond the rounding bound, -1 when it is
+  // behind it, 0 when the sign needs the exact determinant. Grid
+  // coordinates are integers, so a nonzero det is at least 1 and det/|n|
+  // is above 2^-46: the exact test's 1e-30 is below every filtered value.
+  // A corner of the face itself (point index pi) is never visible: its
+  // determinant is exactly zero, and the float32 one stays inside the bound
+  // (its rounding error is below 5 * 2^-24 * |e1|_1^2 * |e2|_1), so the
+  // filter would hand it to the exact test, which returns zero.
+  __device__ __forceinline__ float face_filter(uint4 w0, uint4 w1, uint4 w2, f3 p, uint32_t pi) const {
+    const f3 n = mk3(__uint_as_float(w1.x), __uint_as_float(w1.y), __uint_as_float(w1.z));
+    const f3 d = p - mk3(__uint_as_float(w2.x), __uint_as_float(w2.y), __uint_as_float(w2.z));
+    const float det = dot(n, d);
+    const float bound = __uint_as_float(w0.w) * l1(d);
+    if (det > bound) return det / __uint_as_float(w1.w);
     if (det < -bound) return -1.0f;
-    f3 pb, pc;
-    if (qc) {
-      pb = qvert(a.y);
-      pc = qvert(a.z);
-    } else {
-      uint4 e = w[3];
-      pb = mk3(__uint_as_float(c.z), __uint_as_float(c.w), __uint_as_float(e.x));
-      pc = mk3(__uint_as_float(e.y), __uint_as_float(e.z), __uint_as_float(e.w));
-    }
-    return orient_exact(pb - pa, pc - pa, d) > 0 ? 1e-30f : -1.0f;
+    return ((w0.x & 0x7fffffffu) == pi || w0.y == pi || w0.z == pi) ? -1.0f : 0.0f;
   }
-  // the most visible face of [f0, f1) for point i (first slot on ties)
+  // exact visibility of p from the face (shaders.ts:868-876): the sign of
+  // N . (p - a) with the stored integer normal. With N = 2^32 h + l (l the
+  // unsigned low word) the determinant is 2^32 A + B, A = h . d below 2^37
+  // and B = l . d below 2^57; folding B's high part into A leaves
+  // 2^32 A' + r with 0 <= r < 2^32, whose sign is A''s, or r's when A' = 0.
+  __device__ __forceinline__ bool face_exact(uint4 w2, uint4 w3, f3 p) const {
+    const long long dx = (long long)(p.x - __uint_as_float(w2.x));
+    const long long dy = (long long)(p.y - __uint_as_float(w2.y));
+    const long long dz = (long long)(p.z - __uint_as_float(w2.z));
+    const long long hx = (short)(w3.z & 0xffffu), hy = (short)(w3.z >> 16), hz = (short)w3.w;
+    const long long A = hx * dx + hy * dy + hz * dz;
+    const long long B = (long long)w2.w * dx + (long long)w3.x * dy + (long long)w3.y * dz;
+    const long long A2 = A + (B >> 32);
+    return A2 > 0 || (A2 == 0 && (uint32_t)B != 0u);
+  }
+  // the predicate (shaders.ts:906-921): positive = visible (ranking value),
+  // negative = not visible
+  __device__ __forceinline__ float face_eval(uint32_t f, f3 p, uint32_t pi) const {
+    const uint4* w = rec(f);
+    const uint4 w0 = w[0];
+    if ((w0.x & ALIVE) == 0) return -1e30f;
+    const uint4 w2 = w[2];
+    const float v = face_filter(w0, w[1], w2, p, pi);
+    return v != 0.0f ? v : (face_exact(w2, w[3], p) ? 1e-30f : -1.0f);
+  }
+  // the most visible face of [f0, f1) for point i (first slot on ties;
+  // distance 0 when none). An exact-visible face ranks 1e-30, below every
+  // filtered value, so the exact test only runs while no face is visible.
   __device__ __forceinline__ void best_face(uint32_t i, uint32_t f0, uint32_t f1, uint32_t& bestF, float& bestD) const {
     const f3 pt = qvert(i);
     bestF = CUACD_NONE;
-    bestD = -1.0f;
+    bestD = 0.0f;
     for (uint32_t f = f0; f < f1; f++) {
-      const float dd = face_eval(f, pt);
-      if (dd > 0.0f && dd > bestD) { bestD = dd; bestF = f; }
+      const uint4* w = rec(f);
+      const uint4 w0 = w[0];
+      if ((w0.x & ALIVE) == 0) continue;
+      const uint4 w2 = w[2];
+      const float dd = face_filter(w0, w[1], w2, pt, i);
+      if (dd > bestD) { bestD = dd; bestF = f; }
+      if (dd == 0.0f && bestF == CUACD_NONE && face_exact(w2, w[3], pt)) { bestD = 1e-30f; bestF = f; }
     }
-    if (bestF == CUACD_NONE) bestD = 0.0f;
   }
   __device__ __forceinline__ void assign(uint32_t i, uint32_t f0, uint32_t f1) const {
-    f3 pt = qvert(i);
-    uint32_t bestF = CUACD_NONE;
-    float bestD = -1.0f;
-    for (uint32_t f = f0; f < f1; f++) {
-      float dd = face_eval(f, pt);
-      if (dd > 0.0f && dd > bestD) { bestD = dd; bestF = f; }
-    }
+    uint32_t bestF;
+    float bestD;
+    best_face(i, f0, f1, bestF, bestD);
     owner[i] = bestF;
-    dist[i] = bestF != CUACD_NONE ? bestD : 0.0f;
+    dist[i] = bestD;
   }
 };
 
@@ -291,7 +314,7 @@ __device__ __noinline__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& 
       bool claimed = false;
       if (t < tasks) {
         g = h.nbr[4 * (size_t)h.q[head + t / 3] + t % 3];
-        if (g < nf && !bm_test(h.bm, g) && h.face_eval(g, p) > 0.0f) {
+        if (g < nf && !bm_test(h.bm, g) && h.face_eval(g, p, pIdx) > 0.0f) {
           const uint32_t bit = 1u << (g & 31);
           claimed = (atomicOr(h.bm + (g >> 5), bit) & bit) == 0;
         }
@@ -475,6 +498,65 @@ __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem
   if (lid == 0) hs.ncand = ncand;
   Grp<G>::sync();
   return nIns;
+}
+
+// Every point against the face slots [0, nf) (shaders.ts:1332-1354): owner =
+// the first slot of largest positive ranking value, candidates = the points
+// with an owner, in index order. Each thread holds up to ASSIGN_K points in
+// registers and the slots are read once per ASSIGN_K * G points, the next
+// slot's record loading while the current one is evaluated.
+#define ASSIGN_K 4
+template <int G>
+__device__ __noinline__ uint32_t hull_assign_all(const HullCtx& h, GrpSmem& sm, uint32_t nf) {
+  const int lid = Grp<G>::lid();
+  const uint32_t nv = h.nv;
+  uint32_t ncand = 0;
+  for (uint32_t base = 0; base < nv; base += ASSIGN_K * G) {
+    f3 p[ASSIGN_K];
+    float bd[ASSIGN_K];
+    uint32_t bo[ASSIGN_K];
+#pragma unroll
+    for (int k = 0; k < ASSIGN_K; k++) {
+      const uint32_t i = base + k * G + lid;
+      p[k] = h.qvert(i < nv ? i : 0u);
+      bd[k] = 0.0f;
+      bo[k] = CUACD_NONE;
+    }
+    uint4 n0 = nf > 0 ? h.rec(0)[0] : make_uint4(0, 0, 0, 0);
+    for (uint32_t f = 0; f < nf; f++) {
+      const uint4 w0 = n0;
+      if (f + 1 < nf) n0 = h.rec(f + 1)[0];
+      if ((w0.x & ALIVE) == 0) continue;
+      const uint4* w = h.rec(f);
+      const uint4 w1 = w[1], w2 = w[2];
+#pragma unroll
+      for (int k = 0; k < ASSIGN_K; k++) {
+        if (base + k * G < nv) {
+          const float dd = h.face_filter(w0, w1, w2, p[k], base + k * G + lid);
+          if (dd > bd[k]) { bd[k] = dd; bo[k] = f; }
+          // an exact-visible face ranks 1e-30, below every filtered value:
+          // it only matters while the point has no owner
+          if (dd == 0.0f && bo[k] == CUACD_NONE && h.face_exact(w2, w[3], p[k])) { bd[k] = 1e-30f; bo[k] = f; }
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < ASSIGN_K; k++) {
+      if (base + k * G < nv) {
+        const uint32_t i = base + k * G + lid;
+        const bool outside = i < nv && bo[k] != CUACD_NONE;
+        if (i < nv) {
+          h.owner[i] = bo[k];
+          h.dist[i] = bd[k];
+        }
+        uint32_t tot;
+        const uint32_t pre = grp_scan_bit<G>(outside, &tot, sm);
+        if (outside) h.cand[ncand + pre] = i;
+        ncand += tot;
+      }
+    }
+  }
+  return ncand;
 }
 
 // exact volume of the alive faces, in grid units
@@ -761,19 +843,7 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
     }
   }
   // every point against the rough hull; candidates = points outside it
-  uint32_t ncand = 0;
-  for (uint32_t c = 0; c * G < nv; c++) {
-    const uint32_t i = c * G + lid;
-    uint32_t outside = 0;
-    if (i < nv && fail0 == 0) {
-      h.assign(i, 0, nfPrev);
-      outside = h.owner[i] != CUACD_NONE ? 1u : 0u;
-    }
-    uint32_t tot;
-    uint32_t pre = grp_scan_bit<G>(outside != 0, &tot, sm);
-    if (outside) h.cand[ncand + pre] = i;
-    ncand += tot;
-  }
+  const uint32_t ncand = fail0 == 0 ? hull_assign_all<G>(h, sm, nfPrev) : 0u;
   if (lid == 0) {
     hs.ncand = ncand;
     if (P.exportStride == 0) pdp->pad0 = ncand;
