@@ -58,7 +58,19 @@ struct HullSm {
   uint32_t seed[80];
   uint32_t nf, nalive, fail, compacted;
   uint32_t ncand, ok, nvis;
-  uint32_t pad;
+  uint32_t nfRef;  // register hull: the slot count the slot-array form would have
+};
+
+// Register hull (one warp, up to TINY_FACES faces, face k in lane k): the
+// staging area for the faces an insertion creates and the horizon maps.
+#define TINY_FACES 32u
+// parts whose distinct seeds exceed this go straight to the slot-array form
+// (a hull with F <= 32 faces has at most 18 vertices)
+#define TINY_SEEDS 24u
+struct TinySm {
+  uint32_t stage[3 * TINY_FACES];  // new face j: a, b, old lane of the face across (a, b)
+  uint8_t hA[QC_MAX];              // per point: lane of the new face starting there
+  uint8_t hB[QC_MAX];              // per point: lane of the new face ending there
 };
 
 // exact sign of det[e1; e2; d] for integer vectors below 2^23 (shaders.ts:868-876)
@@ -118,7 +130,8 @@ struct HullCtx {
   // exactly as the predicate rounds them when it forms them itself. N is the
   // exact integer normal e1 x e2: grid differences are at most 2^21, so each
   // component is below 2^43 and splits into a low word and a 16-bit high part.
-  __device__ __forceinline__ void face_write(uint32_t f, uint32_t a, uint32_t b, uint32_t c) const {
+  __device__ __forceinline__ void face_make(uint32_t a, uint32_t b, uint32_t c, uint4& w0, uint4& w1, uint4& w2,
+                                            uint4& w3) const {
     f3 pa = qvert(a), pb = qvert(b), pc = qvert(c);
     f3 e1 = pb - pa, e2 = pc - pa;
     f3 n = cross(e1, e2);
@@ -128,11 +141,16 @@ struct HullCtx {
     const long long e2x = (long long)e2.x, e2y = (long long)e2.y, e2z = (long long)e2.z;
     const long long Nx = e1y * e2z - e1z * e2y, Ny = e1z * e2x - e1x * e2z, Nz = e1x * e2y - e1y * e2x;
     const uint32_t hx = (uint32_t)(Nx >> 32) & 0xffffu, hy = (uint32_t)(Ny >> 32) & 0xffffu;
+    w0 = make_uint4(a | ALIVE, b, c, __float_as_uint(kb));
+    w1 = make_uint4(__float_as_uint(n.x), __float_as_uint(n.y), __float_as_uint(n.z), __float_as_uint(s));
+    w2 = make_uint4(__float_as_uint(pa.x), __float_as_uint(pa.y), __float_as_uint(pa.z), (uint32_t)Nx);
+    w3 = make_uint4((uint32_t)Ny, (uint32_t)Nz, hx | (hy << 16), (uint32_t)(Nz >> 32));
+  }
+  __device__ __forceinline__ void face_write(uint32_t f, uint32_t a, uint32_t b, uint32_t c) const {
+    uint4 w0, w1, w2, w3;
+    face_make(a, b, c, w0, w1, w2, w3);
     uint4* w = rec(f);
-    w[0] = make_uint4(a | ALIVE, b, c, __float_as_uint(kb));
-    w[1] = make_uint4(__float_as_uint(n.x), __float_as_uint(n.y), __float_as_uint(n.z), __float_as_uint(s));
-    w[2] = make_uint4(__float_as_uint(pa.x), __float_as_uint(pa.y), __float_as_uint(pa.z), (uint32_t)Nx);
-    w[3] = make_uint4((uint32_t)Ny, (uint32_t)Nz, hx | (hy << 16), (uint32_t)(Nz >> 32));
+    w[0] = w0; w[1] = w1; w[2] = w2; w[3] = w3;
   }
   // the float32 filter on loaded record words: the ranking value det/|n|
   // when the point is visible beyond the rounding bound, -1 when it is
@@ -440,6 +458,189 @@ __device__ __noinline__ uint32_t hull_grow_lanes(const HullCtx& h, HullSm& hs, G
   return nIns;
 }
 
+// ---------------------------------------------------------------------------
+// Register hull: the same insertion sequence as hull_grow_lanes + hull_insert
+// for a hull of at most 32 alive faces, with face k held by lane k. The
+// lanes keep the alive faces in slot order (survivors in order, then the new
+// faces in horizon order), which is all the slot order decides: the first
+// slot on ranking ties and the visible-list order. The slot counter of the
+// slot-array form (nfRef) is carried along because it decides when that
+// form compacts, which makes the next reassignment scan every face, and the
+// face-slot failure. The faces live in the slot array densely (slots 0 ..
+// nalive-1) before and after each call.
+
+struct TinyFace {
+  uint4 w0, w1, w2, w3;    // face record words
+  uint32_t nb0, nb1, nb2;  // lanes across edges (a, b), (b, c), (c, a)
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+// bit position of the (k+1)-th set bit of m, for k < popc(m)
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t k) {
+  uint32_t pos = 0;
+#pragma unroll
+  for (int w = 16; w >= 1; w >>= 1) {
+    const uint32_t c = __popc(m & ((1u << w) - 1u));
+    if (k >= c) { k -= c; m >>= w; pos += w; }
+  }
+  return pos;
+}
+__device__ __forceinline__ float tiny_eval(const HullCtx& h, const TinyFace& F, f3 p, uint32_t pi) {
+  const float v = h.face_filter(F.w0, F.w1, F.w2, p, pi);
+  return v != 0.0f ? v : (h.face_exact(F.w2, F.w3, p) ? 1e-30f : -1.0f);
+}
+__device__ __forceinline__ uint4 shfl4(uint4 v, uint32_t src) {
+  v.x = __shfl_sync(FULLMASK, v.x, src);
+  v.y = __shfl_sync(FULLMASK, v.y, src);
+  v.z = __shfl_sync(FULLMASK, v.z, src);
+  v.w = __shfl_sync(FULLMASK, v.w, src);
+  return v;
+}
+
+// Returns the number of insertions, or CUACD_NONE when the hull outgrows
+// the warp (the caller then builds it again in the slot-array form). A
+// face-slot failure sets hs.fail = 2 as hull_insert does.
+__device__ __noinline__ uint32_t hull_tiny_grow(const HullCtx& h, HullSm& hs, TinySm& ts, uint32_t maxIter,
+                                                uint32_t ci, uint32_t co, float cd) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lt = lanemask_lt();
+  uint32_t nalive = hs.nalive, nfRef = hs.nfRef;
+  TinyFace F;
+  F.w0 = F.w1 = F.w2 = F.w3 = make_uint4(0, 0, 0, 0);
+  F.nb0 = F.nb1 = F.nb2 = 0;
+  if (lane < nalive) {
+    const uint4* r = h.rec(lane);
+    F.w0 = r[0]; F.w1 = r[1]; F.w2 = r[2]; F.w3 = r[3];
+    const uint4 nb = *reinterpret_cast<const uint4*>(h.nbr + 4 * lane);
+    F.nb0 = nb.x; F.nb1 = nb.y; F.nb2 = nb.z;
+  }
+  uint32_t nIns = 0;
+  bool outgrown = false;
+  for (uint32_t iter = 0; iter < maxIter; iter++) {
+    // the farthest candidate, lowest point index on ties
+    const uint32_t key = co != CUACD_NONE ? __float_as_uint(cd) : 0u;
+    const uint32_t mk = __reduce_max_sync(FULLMASK, key);
+    if (mk == 0u) break;
+    const uint32_t pick = __reduce_min_sync(FULLMASK, key == mk ? ci : CUACD_NONE);
+    const unsigned holder = __ballot_sync(FULLMASK, key == mk && ci == pick);
+    const uint32_t start = __shfl_sync(FULLMASK, co, __ffs(holder) - 1);
+    const f3 pp = h.qvert(pick);
+    nIns++;
+    // the slot-array form compacts here (hull_insert's condition)
+    bool compacted = false;
+    if (nfRef + 3 * HULL_VIS_MAX > h.fmax || nfRef > 2 * nalive + 512) {
+      nfRef = nalive;
+      compacted = true;
+    }
+    // visible faces, and the edge-connected patch of the start face
+    const bool live = lane < nalive;
+    const uint32_t V = __ballot_sync(FULLMASK, live && tiny_eval(h, F, pp, pick) > 0.0f);
+    uint32_t C = 1u << start;
+    for (uint32_t it = 0; it < TINY_FACES; it++) {
+      const bool nin = (((C >> (F.nb0 & 31u)) | (C >> (F.nb1 & 31u)) | (C >> (F.nb2 & 31u))) & 1u) != 0;
+      const uint32_t C2 = C | __ballot_sync(FULLMASK, ((V >> lane) & 1u) && nin);
+      if (C2 == C) break;
+      C = C2;
+    }
+    const uint32_t qn = __popc(C);
+    if (nfRef + 3 * qn > h.fmax) {
+      if (lane == 0) hs.fail = 2;
+      break;
+    }
+    // horizon edges in order 3 * listPos + k become new faces (a, b, pick)
+    const bool inC = ((C >> lane) & 1u) != 0;
+    const bool e0 = inC && !((C >> (F.nb0 & 31u)) & 1u);
+    const bool e1 = inC && !((C >> (F.nb1 & 31u)) & 1u);
+    const bool e2 = inC && !((C >> (F.nb2 & 31u)) & 1u);
+    const uint32_t cnt = (uint32_t)e0 + (uint32_t)e1 + (uint32_t)e2;
+    const uint32_t B0 = __ballot_sync(FULLMASK, cnt & 1u), B1 = __ballot_sync(FULLMASK, (cnt & 2u) != 0);
+    const uint32_t nnew = __popc(B0) + 2 * __popc(B1);
+    const uint32_t alive = nalive >= 32 ? FULLMASK : ((1u << nalive) - 1u);
+    const uint32_t S = alive & ~C;
+    const uint32_t nS = __popc(S);
+    if (nS + nnew > TINY_FACES) {
+      outgrown = true;
+      break;
+    }
+    if (inC) {
+      uint32_t j = __popc(B0 & lt) + 2 * __popc(B1 & lt);
+      const uint32_t a = F.w0.x & 0x7fffffffu, b = F.w0.y, c = F.w0.z;
+      if (e0) { ts.stage[3 * j] = a; ts.stage[3 * j + 1] = b; ts.stage[3 * j + 2] = F.nb0; ts.hA[a] = (uint8_t)(nS + j); ts.hB[b] = (uint8_t)(nS + j); j++; }
+      if (e1) { ts.stage[3 * j] = b; ts.stage[3 * j + 1] = c; ts.stage[3 * j + 2] = F.nb1; ts.hA[b] = (uint8_t)(nS + j); ts.hB[c] = (uint8_t)(nS + j); j++; }
+      if (e2) { ts.stage[3 * j] = c; ts.stage[3 * j + 1] = a; ts.stage[3 * j + 2] = F.nb2; ts.hA[c] = (uint8_t)(nS + j); ts.hB[a] = (uint8_t)(nS + j); }
+    }
+    __syncwarp();
+    // survivors move down in order, new faces follow
+    const uint32_t src = lane < nS ? nth_set_bit(S, lane) : lane;
+    F.w0 = shfl4(F.w0, src); F.w1 = shfl4(F.w1, src); F.w2 = shfl4(F.w2, src); F.w3 = shfl4(F.w3, src);
+    F.nb0 = __shfl_sync(FULLMASK, F.nb0, src);
+    F.nb1 = __shfl_sync(FULLMASK, F.nb1, src);
+    F.nb2 = __shfl_sync(FULLMASK, F.nb2, src);
+    if (lane < nS) {
+      // a neighbour that died is replaced by the new face on that edge,
+      // which starts at this edge's end point
+      const uint32_t a = F.w0.x & 0x7fffffffu, b = F.w0.y, c = F.w0.z;
+      F.nb0 = ((C >> F.nb0) & 1u) ? ts.hA[b] : __popc(S & ((1u << F.nb0) - 1u));
+      F.nb1 = ((C >> F.nb1) & 1u) ? ts.hA[c] : __popc(S & ((1u << F.nb1) - 1u));
+      F.nb2 = ((C >> F.nb2) & 1u) ? ts.hA[a] : __popc(S & ((1u << F.nb2) - 1u));
+    } else if (lane < nS + nnew) {
+      const uint32_t j = lane - nS;
+      const uint32_t a = ts.stage[3 * j], b = ts.stage[3 * j + 1], tw = ts.stage[3 * j + 2];
+      h.face_make(a, b, pick, F.w0, F.w1, F.w2, F.w3);
+      F.nb0 = __popc(S & ((1u << tw) - 1u));
+      F.nb1 = ts.hA[b];
+      F.nb2 = ts.hB[a];
+    }
+    __syncwarp();
+    const uint32_t nNow = nS + nnew;
+    // reassign the candidates whose owner died (all of them after a
+    // compaction) over the new faces (every face after a compaction)
+    if (ci == pick) co = CUACD_NONE;
+    bool need = false;
+    if (co != CUACD_NONE) {
+      if (compacted || ((C >> co) & 1u)) need = true;
+      else co = __popc(S & ((1u << co) - 1u));
+    }
+    uint32_t R = __ballot_sync(FULLMASK, need);
+    const uint32_t lo = compacted ? 0u : nS;
+    while (R) {
+      const uint32_t r = __ffs(R) - 1;
+      R &= R - 1;
+      const uint32_t pr = __shfl_sync(FULLMASK, ci, r);
+      float v = -1.0f;
+      if (lane >= lo && lane < nNow) v = tiny_eval(h, F, h.qvert(pr), pr);
+      const uint32_t vk = v > 0.0f ? __float_as_uint(v) : 0u;
+      const uint32_t best = __reduce_max_sync(FULLMASK, vk);
+      const unsigned at = __ballot_sync(FULLMASK, best != 0u && vk == best);
+      if (lane == r) {
+        co = best != 0u ? (uint32_t)(__ffs(at) - 1) : CUACD_NONE;
+        cd = best != 0u ? __uint_as_float(best) : 0.0f;
+      }
+    }
+    nalive = nNow;
+    nfRef += nnew;
+  }
+  __syncwarp();
+  if (outgrown) return CUACD_NONE;
+  // back to the slot array, densely
+  if (lane < nalive) {
+    uint4* r = h.rec(lane);
+    r[0] = F.w0; r[1] = F.w1; r[2] = F.w2; r[3] = F.w3;
+    *reinterpret_cast<uint4*>(h.nbr + 4 * lane) = make_uint4(F.nb0, F.nb1, F.nb2, 0u);
+  }
+  if (lane == 0) {
+    hs.nf = nalive;
+    hs.nalive = nalive;
+    hs.nfRef = nfRef;
+  }
+  __syncwarp();
+  return nIns;
+}
+
 // farthest-first insertion of the candidate list (shaders.ts:1060-1129)
 template <int G>
 __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t nfPrev, uint32_t maxIter) {
@@ -610,7 +811,7 @@ __device__ double hull_volume_grid(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
 
 template <int G>
 __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* slab, HullSm& hs, GrpSmem& sm,
-                         float* qcache) {
+                         float* qcache, TinySm* ts) {
   const int lid = Grp<G>::lid();
   const uint32_t partIdx = P.partBase + idx;
   PartDesc* pdp = D.parts + partIdx;
@@ -718,6 +919,11 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
     if (lid == 0) pdp->hullVol = 0.0f;
     return;
   }
+  // the register hull first when the part's points are in shared memory; a
+  // hull that outgrows the warp is built again from the simplex in the
+  // slot-array form (the same sequence, so the same result)
+  bool tiny = G == 32 && ts != nullptr && h.qc != nullptr;
+restart:
   // initial simplex (shaders.ts:1227-1263). The reference scans the 80 seeds
   // serially with strict comparisons, so each choice is the first seed
   // position reaching the maximum: here every lane scans its positions in
@@ -796,7 +1002,23 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
   }
   Grp<G>::sync();
   uint32_t nIns;
-  if (G == 32 && nuniq <= 32) {
+  bool tinyUsed = false;
+  if (tiny && nuniq <= TINY_SEEDS) {
+    uint32_t ci = 0, co = CUACD_NONE;
+    float cd = 0.0f;
+    if ((uint32_t)lid < nuniq) {
+      ci = h.cand[lid];
+      h.best_face(ci, 0, 4, co, cd);
+    }
+    if (lid == 0) hs.nfRef = 4;
+    __syncwarp();
+    nIns = hull_tiny_grow(h, hs, *ts, 80, ci, co, cd);
+    if (nIns == CUACD_NONE) {
+      tiny = false;
+      goto restart;
+    }
+    tinyUsed = true;
+  } else if (G == 32 && nuniq <= 32) {
     uint32_t ci = 0, co = CUACD_NONE;
     float cd = 0.0f;
     if ((uint32_t)lid < nuniq) {
@@ -850,7 +1072,25 @@ __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* s
   }
   Grp<G>::sync();
   const uint32_t maxIter = (P.hullStage == 2 || P.hullStage == 3 || fail0 != 0) ? 0 : nv;
-  if (G == 32 && ncand <= 32) {
+  if (tinyUsed && fail0 == 0) {
+    if (ncand > 32) {
+      tiny = false;
+      goto restart;
+    }
+    uint32_t ci = 0, co = CUACD_NONE;
+    float cd = 0.0f;
+    if ((uint32_t)lid < ncand) {
+      ci = h.cand[lid];
+      co = h.owner[ci];
+      cd = h.dist[ci];
+    }
+    const uint32_t n2 = hull_tiny_grow(h, hs, *ts, maxIter, ci, co, cd);
+    if (n2 == CUACD_NONE) {
+      tiny = false;
+      goto restart;
+    }
+    nIns += n2;
+  } else if (G == 32 && ncand <= 32) {
     uint32_t ci = 0, co = CUACD_NONE;
     float cd = 0.0f;
     if ((uint32_t)lid < ncand) {
@@ -910,6 +1150,7 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
   __shared__ GrpSmem gsm[Grp<G>::PER_BLOCK];
   __shared__ HullSm hsm[Grp<G>::PER_BLOCK];
   __shared__ float qcs[G == 32 ? 8 * 3 * QC_MAX : 1];
+  __shared__ TinySm tsm[G == 32 ? 8 : 1];
   const int gi = Grp<G>::gid();
   const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
   if (s >= P.nSlabs) return;
@@ -930,13 +1171,13 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
       idx = __shfl_sync(FULLMASK, idx, 0);
       if (idx >= P.nChildParts) break;
       if (D.parts[P.partBase + idx].nv > P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], G == 32 ? qcs + gi * 3 * QC_MAX : nullptr);
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], qcs + gi * 3 * QC_MAX, tsm + gi);
       Grp<G>::sync();
     }
   } else {
     for (uint32_t idx = s; idx < P.nChildParts; idx += P.nSlabs) {
       if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], G == 32 ? qcs + gi * 3 * QC_MAX : nullptr);
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr);
       Grp<G>::sync();
     }
   }
