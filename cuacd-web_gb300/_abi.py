@@ -153,3 +153,78 @@ def item_view(w: np.ndarray) -> dict:
 
 def as_mesh(x) -> Mesh:
     return x if isinstance(x, Mesh) else Mesh(*x)
+
+
+class DecomposeOpts(C.Structure):
+    """cuacd_decompose_opts — DecomposeOptions (decompose.ts:26-78)."""
+
+    _fields_ = [
+        ("threshold", C.c_float),
+        ("maxIters", C.c_int32),
+        ("width", C.c_int32),
+        ("width2", C.c_int32),
+        ("depth", C.c_int32),
+        ("maxNCutting", C.c_int32),
+        ("nConcaveEdges", C.c_int32),
+        ("concaveEps", C.c_float),
+        ("concaveThreshold", C.c_float),
+        ("concaveIters", C.c_int32),
+        ("normalize", C.c_int32),
+        ("requireClosed", C.c_int32),
+        ("validateCuts", C.c_int32),
+        ("refineRounds", C.c_int32),
+        ("refineProbes", C.c_int32),
+        ("mergeHulls", C.c_int32),
+        ("mergeRounds", C.c_int32),
+        ("mergePlaneTol", C.c_float),
+        ("profile", C.c_int32),
+        ("threads", C.c_int32),
+        ("tree", TreeConfig),
+    ]
+
+
+class PartView(C.Structure):
+    """cuacd_part_view — one Part (part.ts:9-22) of a result."""
+
+    _fields_ = [
+        ("verts", C.POINTER(C.c_float)),
+        ("tris", C.POINTER(C.c_uint32)),
+        ("hullVerts", C.POINTER(C.c_float)),
+        ("hullTris", C.POINTER(C.c_uint32)),
+        ("seams", C.POINTER(C.c_double)),
+        ("nv", C.c_uint32),
+        ("nt", C.c_uint32),
+        ("hullNv", C.c_uint32),
+        ("hullNt", C.c_uint32),
+        ("nSeams", C.c_uint32),
+        ("stuck", C.c_int32),
+        ("stuckReason", C.c_int32),
+        ("merged", C.c_int32),
+        ("meshVol", C.c_double),
+        ("hullVol", C.c_double),
+        ("hausdorff", C.c_double),
+    ]
+
+
+class DecomposeStats(C.Structure):
+    """cuacd_decompose_stats — DecomposeResult.stats + MergeStats."""
+
+    _fields_ = [
+        ("iterations", C.c_int32),
+        ("treeRuns", C.c_int32),
+        ("hullFailRuns", C.c_int32),
+        ("nParts", C.c_int32),
+        ("mergeRounds", C.c_int32),
+        ("merges", C.c_int32),
+        ("pairsHulled", C.c_int32),
+        ("pairsHausdorff", C.c_int32),
+        ("candidates", C.c_uint64),
+        ("totalMs", C.c_double),
+        ("treeMs", C.c_double),
+        ("cutMs", C.c_double),
+        ("concaveMs", C.c_double),
+        ("hullMs", C.c_double),
+        ("hausdorffMs", C.c_double),
+        ("mergeMs", C.c_double),
+        ("gpuMs", C.c_double),
+    ]

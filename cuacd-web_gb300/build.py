@@ -27,8 +27,13 @@ UNITS = {
     "hull_kernel.cu": ["--fmad=false"],
     "hausdorff_kernels.cu": [],
     "cuacd_host.cu": [],
+    # host geometry of the decomposition loop: double arithmetic rounded as
+    # the reference's JavaScript rounds it, so no contraction into FMA
+    "host_mesh.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "plane_cut.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "decompose.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["cuacd_dev.cuh"]
+HEADERS = ["cuacd_dev.cuh", "host_mesh.h"]
 
 
 def nvcc() -> str:
@@ -52,7 +57,7 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
     objs = []
     for unit, flags in UNITS.items():
         src = os.path.join(CSRC, unit)
-        obj = os.path.join(OBJ, unit.replace(".cu", ".o"))
+        obj = os.path.join(OBJ, os.path.splitext(unit)[0] + ".o")
         objs.append(obj)
         if force or _stale(obj, [src, __file__] + hdrs):
             cmd = [nvcc()] + ARCH + COMMON + flags + list(extra or []) + ["-c", src, "-o", obj]

@@ -1,0 +1,975 @@
+// decompose.cpp — the decomposition loop (src/decompose.ts) and the hull
+// merging pass (src/merge.ts) on the host, driving the GPU tree, hull and
+// Hausdorff entry points of this library.
+//
+// One Engine owns one GPU tree. A call decomposes n meshes: one after
+// another, or all together, when every iteration gathers the cutting parts
+// of all meshes into one tree run, the new halves of all meshes into one
+// hull + Hausdorff submission, and every merge round's pairs into shared hull
+// and Hausdorff batches. The GPU work per seed and per part does not depend
+// on its batch, so both ways give the same parts. Host geometry (capped cuts,
+// concave planes, seam planes) runs on a thread pool.
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/cuacd.h"
+#include "host_mesh.h"
+
+namespace cuacd {
+int set_error(int code, const char* msg);
+}
+
+namespace cuacd {
+namespace dec {
+
+using host::Mesh;
+using host::Plane;
+
+constexpr double K_RV = 0.3;  // part.ts:7
+
+// rvCost (part.ts:24-26)
+inline double rv_cost(double meshVol, double hullVol) {
+  return K_RV * std::cbrt((3.0 / (4.0 * M_PI)) * std::max(hullVol - meshVol, 0.0));
+}
+
+struct Part {
+  Mesh mesh, hull;
+  double meshVol = 0, hullVol = 0;
+  double hd = 0;
+  bool hasHd = false;
+  bool stuck = false;
+  int stuckReason = 0;
+  std::vector<Plane> seams;
+  int merged = 1;
+  uint64_t id = 0;  // identity for the merge pass's pair cache
+};
+
+// partCost (part.ts:27-29)
+inline double part_cost(const Part& p) { return std::max(rv_cost(p.meshVol, p.hullVol), p.hasHd ? p.hd : 0.0); }
+
+struct Failure {
+  int code;
+  std::string msg;
+};
+
+using Clock = std::chrono::steady_clock;
+inline double ms_since(Clock::time_point t) {
+  return std::chrono::duration<double, std::milli>(Clock::now() - t).count();
+}
+
+// ---------------------------------------------------------------------------
+// thread pool for host geometry
+
+template <class F>
+void parallel_for(size_t n, int threads, F&& fn) {
+  if (n == 0) return;
+  const size_t nt = std::min<size_t>(n, (size_t)std::max(threads, 1));
+  if (nt <= 1) {
+    for (size_t i = 0; i < n; i++) fn(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (size_t t = 0; t < nt; t++)
+    pool.emplace_back([&]() {
+      for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
+    });
+  for (auto& th : pool) th.join();
+}
+
+// ---------------------------------------------------------------------------
+// one decomposition in flight
+
+struct Job {
+  Mesh input;
+  Mesh mesh;  // normalised
+  host::Normalization norm{1.0, {0, 0, 0}};
+  bool normalized = false;
+  std::vector<Part> parts;
+  bool cutting_done = false;
+  bool merging = false;
+  cuacd_decompose_stats st{};
+  // merge state
+  std::map<std::pair<uint64_t, uint64_t>, size_t> cache;  // pair -> eval index
+};
+
+struct PairEval {
+  double cost = 0;
+  bool hasHull = false;
+  Mesh hull;
+  double hullVol = 0;
+  double hd = 0;
+  bool hasSeam = false;
+  Plane seam{0, 0, 0, 0};
+};
+
+struct Result {
+  std::vector<std::vector<Part>> parts;
+  std::vector<cuacd_decompose_stats> stats;
+};
+
+class Engine {
+ public:
+  cuacd_decompose_opts o;
+  void* tree = nullptr;
+  int planeSlots = 0;
+  int threads = 1;
+  uint64_t nextId = 1;
+  std::vector<PairEval> evals;  // merge pair evaluations of the current call
+  // whole-call timings
+  double treeMs = 0, cutMs = 0, concaveMs = 0, hullMs = 0, hdMs = 0, mergeMs = 0, gpuMs = 0;
+
+  ~Engine() {
+    if (tree) cuacd_tree_destroy(tree);
+  }
+
+  [[noreturn]] void cuda_fail(int rc, const char* what) {
+    throw Failure{rc, std::string(what) + ": " + cuacd_last_error()};
+  }
+
+  // ---- GPU services ------------------------------------------------------
+
+  // hulls (and, when withHd, Hausdorff distances to them) of meshes, in
+  // chunks of at most 256 (decompose.ts:180), halved when a chunk's hull
+  // export does not fit the triangle pool. A failed hull is an error unless
+  // allowFail, when the part gets a NaN hull volume.
+  void hulls(const std::vector<const Mesh*>& ms, bool withHd, std::vector<Part>& out, bool allowFail = false) {
+    out.resize(ms.size());
+    size_t chunk = 256;
+    for (size_t s = 0; s < ms.size();) {
+      const size_t n = std::min(chunk, ms.size() - s);
+      std::vector<cuacd_mesh> cm(n);
+      uint32_t maxNv = 0;
+      for (size_t k = 0; k < n; k++) {
+        const Mesh& m = *ms[s + k];
+        cm[k] = cuacd_mesh{m.v.data(), m.t.data(), (uint32_t)m.nv(), (uint32_t)m.nt()};
+        maxNv = std::max(maxNv, (uint32_t)m.nv());
+      }
+      const uint32_t stride = 3 * 2 * std::min<uint32_t>((uint32_t)o.tree.hullMaxVerts, maxNv);
+      std::vector<uint32_t> tris((size_t)n * stride + 1);
+      std::vector<float> vol(n), hd(n);
+      std::vector<uint32_t> ntri(n);
+      std::vector<int32_t> status(n);
+      const auto t0 = Clock::now();
+      const int rc = withHd ? cuacd_tree_hulls_with_hausdorff(tree, cm.data(), (int)n, tris.data(), stride, vol.data(),
+                                                              ntri.data(), hd.data(), status.data())
+                            : cuacd_tree_hull_meshes(tree, cm.data(), (int)n, 0, tris.data(), stride, vol.data(),
+                                                     ntri.data(), status.data());
+      gpuMs += ms_since(t0);
+      if (rc == CUACD_E_CAPACITY && n > 1) {
+        chunk = std::max<size_t>(1, n / 2);
+        continue;
+      }
+      if (rc != CUACD_OK) cuda_fail(rc, "hull batch");
+      parallel_for(n, threads, [&](size_t k) {
+        Part& p = out[s + k];
+        const Mesh& m = *ms[s + k];
+        p.mesh = m;
+        p.meshVol = host::volume(m);
+        if (status[k] != 0) {
+          p.hullVol = NAN;
+          return;
+        }
+        p.hull = host::compact_hull(m.v.data(), tris.data() + (size_t)k * stride, ntri[k], nullptr);
+        p.hullVol = vol[k];
+        if (withHd && std::isfinite(hd[k])) {
+          p.hd = hd[k];
+          p.hasHd = true;
+        }
+      });
+      for (size_t k = 0; k < n && !allowFail; k++)
+        if (std::isnan(out[s + k].hullVol)) {
+          char msg[160];
+          snprintf(msg, sizeof msg, "GPU hull failed (code %d) for a part with %u vertices", status[k], cm[k].nv);
+          throw Failure{CUACD_E_CAPACITY, msg};
+        }
+      s += n;
+    }
+  }
+
+  // Hausdorff distances of pairs (a_k, b_k); batches of up to 1024, halved
+  // when the sample scratch overflows (merge.ts:399-409); non-finite
+  // results fall back to the CPU (decompose.ts:168)
+  void hausdorff(const std::vector<const Mesh*>& a, const std::vector<const Mesh*>& b, std::vector<double>& out) {
+    out.assign(a.size(), 0.0);
+    size_t batch = CUACD_HD_MAX_PAIRS;
+    for (size_t s = 0; s < a.size();) {
+      const size_t n = std::min(batch, a.size() - s);
+      std::vector<cuacd_mesh> ca(n), cb(n);
+      for (size_t k = 0; k < n; k++) {
+        ca[k] = cuacd_mesh{a[s + k]->v.data(), a[s + k]->t.data(), (uint32_t)a[s + k]->nv(), (uint32_t)a[s + k]->nt()};
+        cb[k] = cuacd_mesh{b[s + k]->v.data(), b[s + k]->t.data(), (uint32_t)b[s + k]->nv(), (uint32_t)b[s + k]->nt()};
+      }
+      std::vector<float> r(n);
+      const auto t0 = Clock::now();
+      const int rc = cuacd_tree_hausdorff(tree, ca.data(), cb.data(), (int)n, r.data());
+      gpuMs += ms_since(t0);
+      if ((rc == CUACD_E_SCRATCH || rc == CUACD_E_CAPACITY) && n > 1) {
+        batch = std::max<size_t>(1, n / 2);
+        continue;
+      }
+      if (rc != CUACD_OK) cuda_fail(rc, "hausdorff batch");
+      parallel_for(n, threads, [&](size_t k) {
+        out[s + k] = std::isfinite(r[k]) ? (double)r[k] : host::hausdorff_cpu(*a[s + k], *b[s + k]);
+      });
+      s += n;
+    }
+  }
+
+  // Hausdorff(part, hull) for parts that lack it (decompose.ts:159-170)
+  void fill_hausdorff(const std::vector<Part*>& ps) {
+    std::vector<const Mesh*> a, b;
+    std::vector<Part*> todo;
+    for (Part* p : ps)
+      if (!p->hasHd) {
+        todo.push_back(p);
+        a.push_back(&p->mesh);
+        b.push_back(&p->hull);
+      }
+    if (todo.empty()) return;
+    const auto t0 = Clock::now();
+    std::vector<double> hd;
+    hausdorff(a, b, hd);
+    for (size_t k = 0; k < todo.size(); k++) {
+      todo[k]->hd = hd[k];
+      todo[k]->hasHd = true;
+    }
+    hdMs += ms_since(t0);
+  }
+
+  // refineSpacing (decompose.ts:199-211)
+  double refine_spacing(const Mesh& m) const {
+    const double minEdge = std::min((double)o.threshold / 4, 0.015);
+    const int cpa = std::max(1, o.width / 3);
+    float lo[3], hi[3];
+    host::bbox(m, lo, hi);
+    double s = INFINITY;
+    for (int a = 0; a < 3; a++) {
+      const double valid = (double)hi[a] - (double)lo[a] - 2 * minEdge;
+      if (valid > 0) s = std::min(s, valid / (cpa + 1));
+    }
+    return std::isfinite(s) ? s : 0.0;
+  }
+
+  // ---- one decomposition iteration over all active jobs ------------------
+
+  // returns false when no job had a part to cut
+  bool iterate(std::vector<Job*>& jobs, int iter) {
+    // Hausdorff of the parts that lack it
+    {
+      std::vector<Part*> ps;
+      for (Job* j : jobs)
+        if (!j->cutting_done)
+          for (Part& p : j->parts) ps.push_back(&p);
+      fill_hausdorff(ps);
+    }
+    struct Seed {
+      Job* job;
+      size_t part;
+    };
+    std::vector<Seed> seeds;
+    for (Job* j : jobs) {
+      if (j->cutting_done) continue;
+      j->st.iterations = iter + 1;
+      // ascending by cost; the last maxNCutting above the threshold
+      std::vector<std::pair<double, size_t>> order;
+      for (size_t i = 0; i < j->parts.size(); i++) order.push_back({part_cost(j->parts[i]), i});
+      std::stable_sort(order.begin(), order.end(),
+                       [](const std::pair<double, size_t>& x, const std::pair<double, size_t>& y) {
+                         return x.first < y.first;
+                       });
+      std::vector<size_t> above;
+      for (const auto& e : order)
+        if (e.first >= o.threshold && !j->parts[e.second].stuck) above.push_back(e.second);
+      const size_t from = above.size() > (size_t)o.maxNCutting ? above.size() - (size_t)o.maxNCutting : 0;
+      if (from == above.size()) {
+        j->cutting_done = true;
+        continue;
+      }
+      for (size_t k = from; k < above.size(); k++) seeds.push_back(Seed{j, above[k]});
+    }
+    if (seeds.empty()) return false;
+    // concave-edge planes of every cutting part (decompose.ts:276-281)
+    const auto tc = Clock::now();
+    std::vector<std::vector<float>> planes(seeds.size());
+    parallel_for(seeds.size(), threads, [&](size_t k) {
+      if (iter < o.concaveIters && o.nConcaveEdges > 0)
+        planes[k] = host::concave_edge_planes(seeds[k].job->parts[seeds[k].part].mesh, o.nConcaveEdges, o.concaveEps,
+                                              o.concaveThreshold, (uint32_t)(iter * 7919 + (int)seeds[k].part));
+    });
+    concaveMs += ms_since(tc);
+    // the tree over all cutting parts, halving the batch on pool overflow
+    // (decompose.ts:288-320)
+    std::vector<cuacd_seed_result> best(seeds.size());
+    const int nProbes = std::min(o.refineProbes, planeSlots);
+    const bool refine = o.refineRounds > 0 && nProbes >= 3;
+    size_t batch = seeds.size();
+    for (size_t start = 0; start < seeds.size();) {
+      const size_t n = std::min(batch, seeds.size() - start);
+      std::vector<cuacd_mesh> cm(n);
+      std::vector<float> spacing(n);
+      size_t per = 0;
+      for (size_t k = 0; k < n; k++) per = std::max(per, planes[start + k].size() / 4);
+      std::vector<float> flat(std::max<size_t>(n * per * 4, 1), 0.0f);
+      for (size_t k = 0; k < n; k++) {
+        const Mesh& m = seeds[start + k].job->parts[seeds[start + k].part].mesh;
+        cm[k] = cuacd_mesh{m.v.data(), m.t.data(), (uint32_t)m.nv(), (uint32_t)m.nt()};
+        spacing[k] = refine ? (float)refine_spacing(m) : 0.0f;
+        std::copy(planes[start + k].begin(), planes[start + k].end(), flat.begin() + k * per * 4);
+      }
+      cuacd_run_opts ro{};
+      ro.depth = 0;
+      ro.width = -1;
+      ro.nEdgeCuts = -1;
+      ro.refineRounds = refine ? o.refineRounds : 0;
+      ro.refineProbes = refine ? nProbes : 0;
+      ro.refineSpacing = refine ? spacing.data() : nullptr;
+      cuacd_run_stats rs{};
+      const auto t0 = Clock::now();
+      const int rc = cuacd_tree_run(tree, cm.data(), (int)n, flat.data(), (int)per, &ro, best.data() + start, &rs);
+      const double dt = ms_since(t0);
+      treeMs += dt;
+      gpuMs += rs.gpuMs;
+      if (rc == CUACD_E_CAPACITY && n > 1) {
+        batch = std::max<size_t>(1, n / 2);
+        continue;
+      }
+      if (rc != CUACD_OK) cuda_fail(rc, "tree run");
+      if (rs.overflow) {
+        if (n == 1) throw Failure{CUACD_E_CAPACITY, "GPU pool overflow with a single part; increase tree pool sizes"};
+        batch = std::max<size_t>(1, n >> 1);
+        continue;
+      }
+      if (rs.npOverflow) throw Failure{CUACD_E_CAPACITY, "tree depth exceeds LA_MAX_PARTS"};
+      // every job whose seeds were in this run counts the run once and the
+      // run's candidates in proportion to its seeds
+      std::vector<Job*> seen;
+      for (size_t k = 0; k < n; k++) {
+        Job* j = seeds[start + k].job;
+        if (std::find(seen.begin(), seen.end(), j) == seen.end()) {
+          seen.push_back(j);
+          j->st.treeRuns++;
+          if (rs.hullFail) j->st.hullFailRuns++;
+        }
+        j->st.candidates += rs.validJobs / n;
+      }
+      start += n;
+    }
+    // apply the winning cuts (decompose.ts:327-343)
+    const auto ta = Clock::now();
+    struct Cut {
+      bool ok = false;
+      Mesh pos, neg;
+    };
+    std::vector<Cut> cuts(seeds.size());
+    parallel_for(seeds.size(), threads, [&](size_t k) {
+      Part& p = seeds[k].job->parts[seeds[k].part];
+      const cuacd_seed_result& r = best[k];
+      if (!(r.valid & 1)) {
+        p.stuck = true;
+        p.stuckReason = 1;
+        return;
+      }
+      const Plane pl{r.plane[0], r.plane[1], r.plane[2], r.plane[3]};
+      host::CutResult c = host::plane_cut(p.mesh, pl);
+      if (!c.ok) {
+        p.stuck = true;
+        p.stuckReason = 2;
+        return;
+      }
+      if (c.pos.v.size() < 12 || c.neg.v.size() < 12) {
+        p.stuck = true;
+        p.stuckReason = 4;
+        return;
+      }
+      if (o.validateCuts && (!host::is_closed(c.pos) || !host::is_closed(c.neg))) {
+        p.stuck = true;
+        p.stuckReason = 3;
+        return;
+      }
+      cuts[k].ok = true;
+      cuts[k].pos = std::move(c.pos);
+      cuts[k].neg = std::move(c.neg);
+    });
+    cutMs += ms_since(ta);
+    // hulls and Hausdorff distances of every new half in one submission
+    std::vector<const Mesh*> halves;
+    std::vector<size_t> which;
+    for (size_t k = 0; k < seeds.size(); k++)
+      if (cuts[k].ok) {
+        halves.push_back(&cuts[k].pos);
+        halves.push_back(&cuts[k].neg);
+        which.push_back(k);
+      }
+    const auto th = Clock::now();
+    std::vector<Part> made;
+    hulls(halves, true, made);
+    hullMs += ms_since(th);
+    // per job, in cutting order: the positive half replaces the part, the
+    // negative half is appended
+    for (size_t q = 0; q < which.size(); q++) {
+      const Seed& sd = seeds[which[q]];
+      made[2 * q].id = nextId++;
+      made[2 * q + 1].id = nextId++;
+      sd.job->parts[sd.part] = std::move(made[2 * q]);
+      sd.job->parts.push_back(std::move(made[2 * q + 1]));
+    }
+    return true;
+  }
+
+  // ---- merge pass (merge.ts:189-303), all jobs' rounds in lockstep --------
+
+  static void bbox_of(const Mesh& m, float lo[3], float hi[3]) { host::bbox(m, lo, hi); }
+
+  static bool tri_coplanar(const Mesh& m, size_t t, const Plane& p, double tol) {
+    for (int e = 0; e < 3; e++) {
+      const float* v = &m.v[3 * (size_t)m.t[t + e]];
+      if (std::fabs(p.a * v[0] + p.b * v[1] + p.c * v[2] + p.d) > tol) return false;
+    }
+    return true;
+  }
+
+  static double coplanar_area(const Mesh& m, const Plane& p, double tol) {
+    double area = 0;
+    for (size_t t = 0; t < m.t.size(); t += 3) {
+      if (!tri_coplanar(m, t, p, tol)) continue;
+      const float* A = &m.v[3 * (size_t)m.t[t]];
+      const float* B = &m.v[3 * (size_t)m.t[t + 1]];
+      const float* C = &m.v[3 * (size_t)m.t[t + 2]];
+      const double abx = (double)B[0] - A[0], aby = (double)B[1] - A[1], abz = (double)B[2] - A[2];
+      const double acx = (double)C[0] - A[0], acy = (double)C[1] - A[1], acz = (double)C[2] - A[2];
+      area += 0.5 * std::hypot(aby * acz - abz * acy, abz * acx - abx * acz, abx * acy - aby * acx);
+    }
+    return area;
+  }
+
+  // seamPlane (merge.ts:112-140): a face plane of A's hull with B's hull on
+  // its outer side, carrying the most coplanar mesh area of A and B
+  static bool seam_plane(const Part& A, const Part& B, double tol, Plane& out) {
+    const std::vector<float>& hv = A.hull.v;
+    const std::vector<uint32_t>& ht = A.hull.t;
+    const std::vector<float>& bv = B.hull.v;
+    std::vector<std::array<int64_t, 4>> seen;
+    bool found = false;
+    double bestArea = 0;
+    auto jsround = [](double x) { return (int64_t)std::floor(x + 0.5); };
+    for (size_t t = 0; t < ht.size(); t += 3) {
+      const size_t i0 = 3 * (size_t)ht[t], i1 = 3 * (size_t)ht[t + 1], i2 = 3 * (size_t)ht[t + 2];
+      const double e1x = (double)hv[i1] - hv[i0], e1y = (double)hv[i1 + 1] - hv[i0 + 1], e1z = (double)hv[i1 + 2] - hv[i0 + 2];
+      const double e2x = (double)hv[i2] - hv[i0], e2y = (double)hv[i2 + 1] - hv[i0 + 1], e2z = (double)hv[i2 + 2] - hv[i0 + 2];
+      double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+      const double len = std::hypot(nx, ny, nz);
+      if (len < 1e-20) continue;
+      nx /= len;
+      ny /= len;
+      nz /= len;
+      const double d = nx * hv[i0] + ny * hv[i0 + 1] + nz * hv[i0 + 2];
+      const std::array<int64_t, 4> key{jsround(nx * 2000), jsround(ny * 2000), jsround(nz * 2000), jsround(d * 2000)};
+      if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+      seen.push_back(key);
+      bool ok = true;
+      for (size_t j = 0; j < bv.size(); j += 3)
+        if (nx * bv[j] + ny * bv[j + 1] + nz * bv[j + 2] - d < -tol) {
+          ok = false;
+          break;
+        }
+      if (!ok) continue;
+      const Plane p{nx, ny, nz, -d};
+      const double area = coplanar_area(A.mesh, p, tol) + coplanar_area(B.mesh, p, tol);
+      if (area > bestArea) {
+        bestArea = area;
+        out = p;
+        found = true;
+      }
+    }
+    return found;
+  }
+
+  // filteredConcat (merge.ts:143-157)
+  static Mesh filtered_concat(const Mesh& a, const Mesh& b, const std::vector<Plane>& planes, double tol) {
+    Mesh m = host::merge_meshes(a, b);
+    if (planes.empty()) return m;
+    std::vector<uint32_t> keep;
+    keep.reserve(m.t.size());
+    for (size_t t = 0; t < m.t.size(); t += 3) {
+      bool drop = false;
+      for (const Plane& p : planes)
+        if (tri_coplanar(m, t, p, tol)) {
+          drop = true;
+          break;
+        }
+      if (!drop) keep.insert(keep.end(), m.t.begin() + t, m.t.begin() + t + 3);
+    }
+    m.t.swap(keep);
+    return m;
+  }
+
+  void merge(std::vector<Job*>& all) {
+    const auto tm = Clock::now();
+    std::vector<Job*> jobs;
+    for (Job* j : all)
+      if (o.mergeHulls && j->parts.size() > 1) {
+        j->merging = true;
+        jobs.push_back(j);
+      }
+    const double halfT2 = ((double)o.threshold / 2) * ((double)o.threshold / 2);
+    for (int round = 0; round < o.mergeRounds; round++) {
+      struct Pair {
+        Job* job;
+        size_t i, j;
+      };
+      std::vector<Pair> todo;
+      std::vector<std::vector<Pair>> cands(jobs.size());
+      bool any = false;
+      for (size_t q = 0; q < jobs.size(); q++) {
+        Job* jb = jobs[q];
+        if (!jb->merging) continue;
+        if (jb->parts.size() <= 1) {
+          jb->merging = false;
+          continue;
+        }
+        any = true;
+        jb->st.mergeRounds = round + 1;
+        std::vector<std::array<float, 6>> box(jb->parts.size());
+        for (size_t i = 0; i < jb->parts.size(); i++) bbox_of(jb->parts[i].mesh, &box[i][0], &box[i][3]);
+        for (size_t i = 0; i < jb->parts.size(); i++)
+          for (size_t j = i + 1; j < jb->parts.size(); j++) {
+            const Part& A = jb->parts[i];
+            const Part& B = jb->parts[j];
+            const auto key = std::make_pair(std::min(A.id, B.id), std::max(A.id, B.id));
+            if (jb->cache.count(key)) {
+              cands[q].push_back(Pair{jb, i, j});
+              continue;
+            }
+            if (rv_cost(A.meshVol + B.meshVol, A.hullVol + B.hullVol) >= o.threshold) continue;
+            double g2 = 0;
+            for (int k = 0; k < 3; k++) {
+              const double g = std::max({0.0, (double)box[i][k] - box[j][3 + k], (double)box[j][k] - box[i][3 + k]});
+              g2 += g * g;
+            }
+            if (g2 >= halfT2) continue;
+            todo.push_back(Pair{jb, i, j});
+            cands[q].push_back(Pair{jb, i, j});
+          }
+      }
+      if (!any) break;
+      // merged hulls of the pairs' hull points, one batch for every job
+      std::vector<Mesh> pts(todo.size());
+      for (size_t k = 0; k < todo.size(); k++) {
+        const Part& A = todo[k].job->parts[todo[k].i];
+        const Part& B = todo[k].job->parts[todo[k].j];
+        pts[k].v = A.hull.v;
+        pts[k].v.insert(pts[k].v.end(), B.hull.v.begin(), B.hull.v.end());
+      }
+      const auto th = Clock::now();
+      std::vector<Part> hp;
+      {
+        std::vector<const Mesh*> ptr(todo.size());
+        for (size_t k = 0; k < todo.size(); k++) ptr[k] = &pts[k];
+        hulls(ptr, false, hp, true);
+      }
+      hullMs += ms_since(th);
+      const size_t base = evals.size();
+      evals.resize(base + todo.size());
+      for (size_t k = 0; k < todo.size(); k++) {
+        const Part& A = todo[k].job->parts[todo[k].i];
+        const Part& B = todo[k].job->parts[todo[k].j];
+        PairEval& ev = evals[base + k];
+        ev.hullVol = hp[k].hullVol;
+        // a merged hull that failed on the GPU leaves the pair unmerged
+        ev.cost = std::isnan(ev.hullVol) ? INFINITY : rv_cost(A.meshVol + B.meshVol, ev.hullVol);
+        ev.hasHull = ev.cost < o.threshold;
+        if (ev.hasHull) ev.hull = std::move(hp[k].hull);
+        todo[k].job->st.pairsHulled++;
+      }
+      // Hausdorff(filtered union, merged hull) of pairs still under the threshold
+      std::vector<size_t> hdIdx;
+      for (size_t k = 0; k < todo.size(); k++)
+        if (evals[base + k].hasHull) hdIdx.push_back(k);
+      std::vector<Mesh> unions(hdIdx.size());
+      std::vector<char> nonEmpty(hdIdx.size(), 0);
+      parallel_for(hdIdx.size(), threads, [&](size_t q) {
+        const size_t k = hdIdx[q];
+        const Part& A = todo[k].job->parts[todo[k].i];
+        const Part& B = todo[k].job->parts[todo[k].j];
+        PairEval& ev = evals[base + k];
+        Plane sp;
+        ev.hasSeam = seam_plane(A, B, o.mergePlaneTol, sp);
+        if (ev.hasSeam) ev.seam = sp;
+        std::vector<Plane> planes;
+        if (ev.hasSeam) planes.push_back(ev.seam);
+        planes.insert(planes.end(), A.seams.begin(), A.seams.end());
+        planes.insert(planes.end(), B.seams.begin(), B.seams.end());
+        unions[q] = filtered_concat(A.mesh, B.mesh, planes, o.mergePlaneTol);
+        nonEmpty[q] = !unions[q].t.empty();
+      });
+      std::vector<const Mesh*> ha, hb;
+      std::vector<size_t> hk;
+      for (size_t q = 0; q < hdIdx.size(); q++)
+        if (nonEmpty[q]) {
+          ha.push_back(&unions[q]);
+          hb.push_back(&evals[base + hdIdx[q]].hull);
+          hk.push_back(hdIdx[q]);
+        }
+      const auto thd = Clock::now();
+      std::vector<double> hd;
+      hausdorff(ha, hb, hd);
+      hdMs += ms_since(thd);
+      for (size_t q = 0; q < hk.size(); q++) {
+        PairEval& ev = evals[base + hk[q]];
+        ev.hd = hd[q];
+        ev.cost = std::max(ev.cost, hd[q]);
+        if (ev.cost >= o.threshold) {
+          ev.hasHull = false;
+          ev.hull = Mesh();
+        }
+        todo[hk[q]].job->st.pairsHausdorff++;
+      }
+      for (size_t k = 0; k < todo.size(); k++) {
+        const Part& A = todo[k].job->parts[todo[k].i];
+        const Part& B = todo[k].job->parts[todo[k].j];
+        todo[k].job->cache[std::make_pair(std::min(A.id, B.id), std::max(A.id, B.id))] = base + k;
+      }
+      // greedy min-cost matching per job
+      for (size_t q = 0; q < jobs.size(); q++) {
+        Job* jb = jobs[q];
+        if (!jb->merging) continue;
+        struct Ranked {
+          size_t i, j;
+          size_t ev;
+        };
+        std::vector<Ranked> ranked;
+        for (const Pair& c : cands[q]) {
+          const Part& A = jb->parts[c.i];
+          const Part& B = jb->parts[c.j];
+          const size_t e = jb->cache[std::make_pair(std::min(A.id, B.id), std::max(A.id, B.id))];
+          if (evals[e].cost < o.threshold && evals[e].hasHull) ranked.push_back(Ranked{c.i, c.j, e});
+        }
+        std::stable_sort(ranked.begin(), ranked.end(),
+                         [&](const Ranked& x, const Ranked& y) { return evals[x.ev].cost < evals[y.ev].cost; });
+        std::vector<char> used(jb->parts.size(), 0);
+        std::vector<Part> next;
+        int merges = 0;
+        for (const Ranked& c : ranked) {
+          if (used[c.i] || used[c.j]) continue;
+          used[c.i] = used[c.j] = 1;
+          const Part& A = jb->parts[c.i];
+          const Part& B = jb->parts[c.j];
+          const PairEval& ev = evals[c.ev];
+          Part m;
+          m.mesh = host::merge_meshes(A.mesh, B.mesh);
+          m.hull = ev.hull;
+          m.meshVol = A.meshVol + B.meshVol;
+          m.hullVol = ev.hullVol;
+          m.hd = ev.hd;
+          m.hasHd = true;
+          m.seams = A.seams;
+          m.seams.insert(m.seams.end(), B.seams.begin(), B.seams.end());
+          if (ev.hasSeam) m.seams.push_back(ev.seam);
+          m.merged = A.merged + B.merged;
+          m.id = nextId++;
+          next.push_back(std::move(m));
+          merges++;
+        }
+        if (merges == 0) {
+          jb->merging = false;
+          continue;
+        }
+        for (size_t i = 0; i < jb->parts.size(); i++)
+          if (!used[i]) next.push_back(std::move(jb->parts[i]));
+        jb->parts = std::move(next);
+        jb->st.merges += merges;
+      }
+    }
+    mergeMs += ms_since(tm);
+  }
+
+  // ---- the whole decomposition of a set of jobs ---------------------------
+
+  void run(std::vector<Job*>& jobs) {
+    for (Job* j : jobs) {
+      if (o.requireClosed && !host::is_closed(j->input))
+        throw Failure{CUACD_E_INVALID,
+                      "input mesh is not closed (open or non-manifold edges); repair or remesh it first, or set "
+                      "requireClosed: false"};
+      if (o.normalize) {
+        j->mesh = host::normalize(j->input, j->norm);
+        j->normalized = true;
+      } else {
+        j->mesh = j->input;
+      }
+    }
+    // the first part of every job: the whole mesh with its hull
+    {
+      std::vector<const Mesh*> ms;
+      for (Job* j : jobs) ms.push_back(&j->mesh);
+      std::vector<Part> made;
+      const auto th = Clock::now();
+      hulls(ms, true, made);
+      hullMs += ms_since(th);
+      for (size_t k = 0; k < jobs.size(); k++) {
+        made[k].id = nextId++;
+        jobs[k]->parts.push_back(std::move(made[k]));
+      }
+    }
+    for (int iter = 0; iter < o.maxIters; iter++)
+      if (!iterate(jobs, iter)) break;
+    {
+      std::vector<Part*> ps;
+      for (Job* j : jobs)
+        for (Part& p : j->parts) ps.push_back(&p);
+      fill_hausdorff(ps);
+    }
+    merge(jobs);
+    for (Job* j : jobs) {
+      if (!j->normalized) continue;
+      for (Part& p : j->parts) {
+        p.mesh = host::denormalize(p.mesh, j->norm);
+        p.hull = host::denormalize(p.hull, j->norm);
+        for (Plane& s : p.seams) s = host::denormalize_plane(s, j->norm);
+      }
+    }
+  }
+};
+
+}  // namespace dec
+}  // namespace cuacd
+
+using namespace cuacd;
+using namespace cuacd::dec;
+
+extern "C" {
+
+void cuacd_decompose_opts_default(cuacd_decompose_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof *o);
+  o->threshold = 0.05f;
+  o->maxIters = 100;
+  o->width = 30;
+  o->width2 = 3;
+  o->depth = 2;
+  o->maxNCutting = 16;
+  o->nConcaveEdges = 16;
+  o->concaveEps = 0.005f;
+  o->concaveThreshold = 3.49f;
+  o->concaveIters = 10;
+  o->normalize = 1;
+  o->requireClosed = 1;
+  o->validateCuts = 1;
+  o->refineRounds = 2;
+  o->refineProbes = 8;
+  o->mergeHulls = 1;
+  o->mergeRounds = 32;
+  o->mergePlaneTol = 1e-3f;
+  o->profile = 0;
+  o->threads = 0;
+  cuacd_tree_config_default(&o->tree);
+}
+
+void* cuacd_decomposer_create(const cuacd_decompose_opts* o, int* err) {
+  auto setErr = [&](int c) {
+    if (err) *err = c;
+  };
+  if (!o) {
+    setErr(set_error(CUACD_E_INVALID, "cuacd_decomposer_create: null options"));
+    return nullptr;
+  }
+  if (o->width % 3 != 0 || o->width2 % 3 != 0) {
+    setErr(set_error(CUACD_E_INVALID, "width and width2 must be multiples of 3"));
+    return nullptr;
+  }
+  if (!(o->threshold > 0) || o->maxNCutting < 1 || o->maxIters < 0 || o->mergeRounds < 0) {
+    setErr(set_error(CUACD_E_INVALID, "cuacd_decomposer_create: invalid option"));
+    return nullptr;
+  }
+  std::unique_ptr<Engine> e(new Engine());
+  e->o = *o;
+  cuacd_tree_config cfg = o->tree;
+  cfg.width = o->width;
+  cfg.width2 = o->width2;
+  cfg.depth = o->depth;
+  cfg.nConcaveEdges = o->nConcaveEdges;
+  cfg.minEdgeDist = std::min(o->threshold / 4.0f, 0.015f);
+  int rc = 0;
+  e->tree = cuacd_tree_create(&cfg, &rc);
+  if (!e->tree) {
+    setErr(rc ? rc : CUACD_E_INVALID);
+    return nullptr;
+  }
+  e->o.tree = cfg;
+  cuacd_set_profile(e->tree, o->profile);
+  e->planeSlots = cuacd_plane_slots(e->tree);
+  const unsigned hc = std::thread::hardware_concurrency();
+  e->threads = o->threads > 0 ? o->threads : (int)std::max(1u, hc);
+  setErr(CUACD_OK);
+  return e.release();
+}
+
+void cuacd_decomposer_destroy(void* d) { delete static_cast<Engine*>(d); }
+
+int cuacd_decompose(void* d, const cuacd_mesh* meshes, int n, int batched, void** result) {
+  if (!d || !meshes || n < 1 || !result) return set_error(CUACD_E_INVALID, "cuacd_decompose: invalid argument");
+  Engine* e = static_cast<Engine*>(d);
+  *result = nullptr;
+  std::vector<std::unique_ptr<Job>> jobs;
+  for (int k = 0; k < n; k++) {
+    const cuacd_mesh& m = meshes[k];
+    if ((m.nv && !m.verts) || (m.nt && !m.tris)) return set_error(CUACD_E_INVALID, "cuacd_decompose: null mesh arrays");
+    std::unique_ptr<Job> j(new Job());
+    j->input.v.assign(m.verts, m.verts + 3 * (size_t)m.nv);
+    j->input.t.assign(m.tris, m.tris + 3 * (size_t)m.nt);
+    jobs.push_back(std::move(j));
+  }
+  std::unique_ptr<Result> res(new Result());
+  try {
+    e->evals.clear();
+    e->treeMs = e->cutMs = e->concaveMs = e->hullMs = e->hdMs = e->mergeMs = e->gpuMs = 0;
+    const auto t0 = Clock::now();
+    if (batched) {
+      std::vector<Job*> all;
+      for (auto& j : jobs) all.push_back(j.get());
+      e->run(all);
+    } else {
+      for (auto& j : jobs) {
+        std::vector<Job*> one{j.get()};
+        e->evals.clear();
+        e->run(one);
+      }
+    }
+    const double total = ms_since(t0);
+    for (auto& j : jobs) {
+      cuacd_decompose_stats s = j->st;
+      s.nParts = (int32_t)j->parts.size();
+      s.totalMs = total;
+      s.treeMs = e->treeMs;
+      s.cutMs = e->cutMs;
+      s.concaveMs = e->concaveMs;
+      s.hullMs = e->hullMs;
+      s.hausdorffMs = e->hdMs;
+      s.mergeMs = e->mergeMs;
+      s.gpuMs = e->gpuMs;
+      res->stats.push_back(s);
+      res->parts.push_back(std::move(j->parts));
+    }
+    e->evals.clear();
+  } catch (const Failure& f) {
+    e->evals.clear();
+    return set_error(f.code, f.msg.c_str());
+  } catch (const std::bad_alloc&) {
+    e->evals.clear();
+    return set_error(CUACD_E_CAPACITY, "cuacd_decompose: host memory exhausted");
+  }
+  *result = res.release();
+  return CUACD_OK;
+}
+
+int cuacd_result_meshes(const void* r) { return r ? (int)static_cast<const Result*>(r)->parts.size() : 0; }
+
+int cuacd_result_parts(const void* r, int mesh) {
+  const Result* R = static_cast<const Result*>(r);
+  if (!R || mesh < 0 || (size_t)mesh >= R->parts.size()) return set_error(CUACD_E_INVALID, "cuacd_result_parts: bad mesh");
+  return (int)R->parts[(size_t)mesh].size();
+}
+
+int cuacd_result_part(const void* r, int mesh, int part, cuacd_part_view* out) {
+  const Result* R = static_cast<const Result*>(r);
+  if (!R || !out || mesh < 0 || (size_t)mesh >= R->parts.size() || part < 0 ||
+      (size_t)part >= R->parts[(size_t)mesh].size())
+    return set_error(CUACD_E_INVALID, "cuacd_result_part: bad index");
+  const Part& p = R->parts[(size_t)mesh][(size_t)part];
+  out->verts = p.mesh.v.data();
+  out->tris = p.mesh.t.data();
+  out->hullVerts = p.hull.v.data();
+  out->hullTris = p.hull.t.data();
+  out->seams = p.seams.empty() ? nullptr : &p.seams[0].a;
+  out->nv = (uint32_t)p.mesh.nv();
+  out->nt = (uint32_t)p.mesh.nt();
+  out->hullNv = (uint32_t)p.hull.nv();
+  out->hullNt = (uint32_t)p.hull.nt();
+  out->nSeams = (uint32_t)p.seams.size();
+  out->stuck = p.stuck ? 1 : 0;
+  out->stuckReason = p.stuckReason;
+  out->merged = p.merged;
+  out->meshVol = p.meshVol;
+  out->hullVol = p.hullVol;
+  out->hausdorff = p.hasHd ? p.hd : NAN;
+  return CUACD_OK;
+}
+
+int cuacd_result_stats(const void* r, int mesh, cuacd_decompose_stats* out) {
+  const Result* R = static_cast<const Result*>(r);
+  if (!R || !out || mesh < 0 || (size_t)mesh >= R->stats.size())
+    return set_error(CUACD_E_INVALID, "cuacd_result_stats: bad mesh");
+  *out = R->stats[(size_t)mesh];
+  return CUACD_OK;
+}
+
+void cuacd_result_free(void* r) { delete static_cast<Result*>(r); }
+
+// ---- host geometry entry points ----------------------------------------
+
+namespace {
+struct Halves {
+  host::Mesh h[2];
+};
+host::Mesh to_mesh(const cuacd_mesh* m) {
+  host::Mesh r;
+  r.v.assign(m->verts, m->verts + 3 * (size_t)m->nv);
+  r.t.assign(m->tris, m->tris + 3 * (size_t)m->nt);
+  return r;
+}
+}  // namespace
+
+int cuacd_plane_cut(const cuacd_mesh* mesh, const double* plane, void** halves) {
+  if (!mesh || !plane || !halves || (mesh->nv && !mesh->verts) || (mesh->nt && !mesh->tris))
+    return set_error(CUACD_E_INVALID, "cuacd_plane_cut: invalid argument");
+  *halves = nullptr;
+  const host::Mesh m = to_mesh(mesh);
+  for (uint32_t x : m.t)
+    if (x >= m.nv()) return set_error(CUACD_E_INVALID, "cuacd_plane_cut: triangle index out of range");
+  host::CutResult r = host::plane_cut(m, Plane{plane[0], plane[1], plane[2], plane[3]});
+  if (!r.ok) return set_error(CUACD_E_INVALID, r.reason ? r.reason : "cut failed");
+  Halves* h = new Halves();
+  h->h[0] = std::move(r.pos);
+  h->h[1] = std::move(r.neg);
+  *halves = h;
+  return CUACD_OK;
+}
+
+int cuacd_cut_half(const void* halves, int side, const float** verts, uint32_t* nv, const uint32_t** tris,
+                   uint32_t* nt) {
+  const Halves* h = static_cast<const Halves*>(halves);
+  if (!h || side < 0 || side > 1 || !verts || !nv || !tris || !nt)
+    return set_error(CUACD_E_INVALID, "cuacd_cut_half: invalid argument");
+  *verts = h->h[side].v.data();
+  *nv = (uint32_t)h->h[side].nv();
+  *tris = h->h[side].t.data();
+  *nt = (uint32_t)h->h[side].nt();
+  return CUACD_OK;
+}
+
+void cuacd_cut_free(void* halves) { delete static_cast<Halves*>(halves); }
+
+int cuacd_concave_planes(const cuacd_mesh* mesh, int nConcaveEdges, double concaveEps, double concaveThreshold,
+                         uint32_t seed, float* out, int cap) {
+  if (!mesh || (mesh->nv && !mesh->verts) || (mesh->nt && !mesh->tris) || cap < 0 || (cap > 0 && !out))
+    return set_error(CUACD_E_INVALID, "cuacd_concave_planes: invalid argument");
+  const host::Mesh m = to_mesh(mesh);
+  for (uint32_t x : m.t)
+    if (x >= m.nv()) return set_error(CUACD_E_INVALID, "cuacd_concave_planes: triangle index out of range");
+  const std::vector<float> p = host::concave_edge_planes(m, nConcaveEdges, concaveEps, concaveThreshold, seed);
+  const int n = (int)(p.size() / 4);
+  std::copy(p.begin(), p.begin() + 4 * (size_t)std::min(n, cap), out);
+  return n;
+}
+
+}  // extern "C"

@@ -1,0 +1,231 @@
+"""decompose(mesh, options) over libcuacd.so — the reference's public API
+(src/decompose.ts:404-415, Decomposer at :128-392) with its options
+(DecomposeOptions, :26-78) and result (DecomposeResult, :107-121).
+
+The loop itself runs inside the library (csrc/decompose.cpp): capped cuts,
+concave-edge planes and merge geometry on host threads, the tree search,
+hulls and Hausdorff distances on the GPU. `decompose_batch` decomposes many
+meshes in one call; with batched=True every iteration and merge round
+serves all meshes with shared GPU launches, which gives the same parts as
+decomposing them one at a time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _abi as A
+from .mesh import Mesh
+from .tree import CuacdError, _check, load_library
+
+# DEFAULT_OPTIONS (decompose.ts:83-106)
+DEFAULT_OPTIONS = dict(
+    threshold=0.05,
+    maxIters=100,
+    width=30,
+    width2=3,
+    depth=2,
+    maxNCutting=16,
+    nConcaveEdges=16,
+    concaveEps=0.005,
+    concaveThreshold=3.49,
+    concaveIters=10,
+    normalize=True,
+    requireClosed=True,
+    validateCuts=True,
+    refineRounds=2,
+    refineProbes=8,
+    mergeHulls=True,
+    mergeRounds=32,
+    mergePlaneTol=1e-3,
+    profile=False,
+    threads=0,
+)
+
+STUCK_REASONS = {0: None, 1: "no-plane", 2: "cut-failed", 3: "not-closed", 4: "degenerate"}
+
+_bound = False
+
+
+def _lib():
+    global _bound
+    L = load_library()
+    if not _bound:
+        P = C.POINTER
+        L.cuacd_decompose_opts_default.argtypes = [P(A.DecomposeOpts)]
+        L.cuacd_decomposer_create.restype = C.c_void_p
+        L.cuacd_decomposer_create.argtypes = [P(A.DecomposeOpts), P(C.c_int)]
+        L.cuacd_decomposer_destroy.argtypes = [C.c_void_p]
+        L.cuacd_decompose.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, C.c_int, P(C.c_void_p)]
+        L.cuacd_result_meshes.argtypes = [C.c_void_p]
+        L.cuacd_result_parts.argtypes = [C.c_void_p, C.c_int]
+        L.cuacd_result_part.argtypes = [C.c_void_p, C.c_int, C.c_int, P(A.PartView)]
+        L.cuacd_result_stats.argtypes = [C.c_void_p, C.c_int, P(A.DecomposeStats)]
+        L.cuacd_result_free.argtypes = [C.c_void_p]
+        L.cuacd_plane_cut.argtypes = [P(A.MeshRef), P(C.c_double), P(C.c_void_p)]
+        L.cuacd_cut_half.argtypes = [C.c_void_p, C.c_int, P(P(C.c_float)), P(C.c_uint32), P(P(C.c_uint32)),
+                                     P(C.c_uint32)]
+        L.cuacd_cut_free.argtypes = [C.c_void_p]
+        L.cuacd_concave_planes.argtypes = [P(A.MeshRef), C.c_int, C.c_double, C.c_double, C.c_uint32, P(C.c_float),
+                                           C.c_int]
+        _bound = True
+    return L
+
+
+@dataclass
+class Part:
+    """Part (part.ts:9-22)."""
+
+    mesh: Mesh
+    hull: Mesh
+    meshVol: float
+    hullVol: float
+    hausdorff: float | None
+    stuck: bool = False
+    stuckReason: str | None = None
+    seams: list = field(default_factory=list)
+    merged: int = 1
+
+
+@dataclass
+class DecomposeResult:
+    """DecomposeResult (decompose.ts:107-121)."""
+
+    parts: list
+    iterations: int
+    stats: dict
+
+
+def _opts(kw) -> A.DecomposeOpts:
+    L = _lib()
+    o = A.DecomposeOpts()
+    L.cuacd_decompose_opts_default(C.byref(o))
+    tree = dict(kw.pop("tree", {}) or {})
+    for k, v in kw.items():
+        if k not in DEFAULT_OPTIONS:
+            raise KeyError(f"unknown decompose option {k!r}")
+        cur = getattr(o, k)
+        setattr(o, k, float(v) if isinstance(cur, float) else int(v))
+    for k, v in tree.items():
+        if not hasattr(o.tree, k):
+            raise KeyError(f"unknown tree config field {k!r}")
+        setattr(o.tree, k, float(v) if k == "minEdgeDist" else int(v))
+    return o
+
+
+def _arr(ptr, n, dtype, width):
+    if n == 0:
+        return np.zeros((0, width), dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n * width,)).astype(dtype, copy=True).reshape(n, width)
+
+
+class Decomposer:
+    """Decomposer (decompose.ts:128-392): one GPU tree, reused across calls."""
+
+    def __init__(self, **options):
+        L = _lib()
+        self.opts = _opts(dict(options))
+        err = C.c_int(0)
+        self.h = L.cuacd_decomposer_create(C.byref(self.opts), C.byref(err))
+        if not self.h:
+            raise CuacdError(err.value, L.cuacd_last_error().decode())
+
+    def destroy(self):
+        if getattr(self, "h", None):
+            _lib().cuacd_decomposer_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def decompose_many(self, meshes, batched: bool = True) -> list:
+        L = _lib()
+        ma = A.MeshArray([A.as_mesh(m) for m in meshes])
+        res = C.c_void_p()
+        _check(L.cuacd_decompose(self.h, ma.arr, ma.n, int(batched), C.byref(res)))
+        try:
+            out = []
+            for k in range(ma.n):
+                parts = []
+                for p in range(L.cuacd_result_parts(res, k)):
+                    v = A.PartView()
+                    _check(L.cuacd_result_part(res, k, p, C.byref(v)))
+                    seams = _arr(v.seams, v.nSeams, np.float64, 4)
+                    parts.append(Part(
+                        mesh=Mesh(_arr(v.verts, v.nv, np.float32, 3), _arr(v.tris, v.nt, np.uint32, 3)),
+                        hull=Mesh(_arr(v.hullVerts, v.hullNv, np.float32, 3), _arr(v.hullTris, v.hullNt, np.uint32, 3)),
+                        meshVol=float(v.meshVol), hullVol=float(v.hullVol),
+                        hausdorff=None if math.isnan(v.hausdorff) else float(v.hausdorff),
+                        stuck=bool(v.stuck), stuckReason=STUCK_REASONS.get(v.stuckReason),
+                        seams=[tuple(float(x) for x in s) for s in seams], merged=int(v.merged)))
+                st = A.DecomposeStats()
+                _check(L.cuacd_result_stats(res, k, C.byref(st)))
+                stats = {name: getattr(st, name) for name, _ in A.DecomposeStats._fields_}
+                out.append(DecomposeResult(parts=parts, iterations=int(st.iterations), stats=stats))
+            return out
+        finally:
+            L.cuacd_result_free(res)
+
+    def decompose(self, mesh) -> DecomposeResult:
+        return self.decompose_many([mesh], batched=False)[0]
+
+
+def decompose(mesh, **options) -> DecomposeResult:
+    """decompose(mesh, opts) (decompose.ts:404-415)."""
+    d = Decomposer(**options)
+    try:
+        return d.decompose(mesh)
+    finally:
+        d.destroy()
+
+
+def decompose_batch(meshes, batched: bool = True, **options) -> list:
+    """Decomposes many meshes in one call (same parts as one at a time)."""
+    d = Decomposer(**options)
+    try:
+        return d.decompose_many(meshes, batched=batched)
+    finally:
+        d.destroy()
+
+
+def plane_cut(mesh, plane):
+    """planeCut with caps (src/cpu/cut.ts:33-315) on the library's host path.
+    Returns (pos, neg) meshes, or raises CuacdError with the reference's
+    reason when the cut fails."""
+    L = _lib()
+    ma = A.MeshArray([A.as_mesh(mesh)])
+    pl = (C.c_double * 4)(*[float(x) for x in plane])
+    h = C.c_void_p()
+    _check(L.cuacd_plane_cut(ma.arr, pl, C.byref(h)))
+    try:
+        out = []
+        for side in (0, 1):
+            v = C.POINTER(C.c_float)()
+            t = C.POINTER(C.c_uint32)()
+            nv = C.c_uint32()
+            nt = C.c_uint32()
+            _check(L.cuacd_cut_half(h, side, C.byref(v), C.byref(nv), C.byref(t), C.byref(nt)))
+            out.append(Mesh(_arr(v, nv.value, np.float32, 3), _arr(t, nt.value, np.uint32, 3)))
+        return out[0], out[1]
+    finally:
+        L.cuacd_cut_free(h)
+
+
+def concave_planes(mesh, n_concave_edges=16, concave_eps=0.005, concave_threshold=3.49, seed=12345) -> np.ndarray:
+    """concaveEdgePlanes (src/cpu/concave.ts:25-92) on the library's host
+    path: (n, 4) float32 planes."""
+    L = _lib()
+    ma = A.MeshArray([A.as_mesh(mesh)])
+    cap = 4 * max(n_concave_edges, 0)
+    out = np.zeros(max(4 * cap, 4), np.float32)
+    n = L.cuacd_concave_planes(ma.arr, int(n_concave_edges), float(concave_eps), float(concave_threshold),
+                               int(seed) & 0xFFFFFFFF, A.fptr(out), cap)
+    if n < 0:
+        _check(n)
+    return out[: 4 * min(n, cap)].reshape(-1, 4).copy()

@@ -211,6 +211,104 @@ int cuacd_tree_read_plane(void* tree, uint32_t index, float* out4);
 int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint32_t* tris, uint32_t trisCap, float* volume,
                               uint32_t* ntris, int32_t* status, void* stream);
 
+/* ---- decomposition (src/decompose.ts, src/merge.ts) -------------------- */
+
+/* DecomposeOptions (decompose.ts:26-78) with DEFAULT_OPTIONS (decompose.ts:
+ * 83-106). The GPU tree of the decomposer is built from `tree` with width,
+ * width2, depth and nConcaveEdges taken from the options and minEdgeDist =
+ * min(threshold / 4, 0.015) (decompose.ts:141-147). Hulls and Hausdorff
+ * distances always run on the GPU (hullBackend / hausdorffBackend "gpu"). */
+typedef struct {
+  float threshold;
+  int32_t maxIters;
+  int32_t width;
+  int32_t width2;
+  int32_t depth;
+  int32_t maxNCutting;
+  int32_t nConcaveEdges;
+  float concaveEps;
+  float concaveThreshold;
+  int32_t concaveIters;
+  int32_t normalize;     /* centre and scale to extent 2 */
+  int32_t requireClosed; /* reject input that is not a closed manifold */
+  int32_t validateCuts;  /* a cut whose halves are not closed leaves the part */
+  int32_t refineRounds;
+  int32_t refineProbes;
+  int32_t mergeHulls;
+  int32_t mergeRounds;
+  float mergePlaneTol;
+  int32_t profile;
+  int32_t threads; /* host threads for cuts and merge geometry, 0 = all cores */
+  cuacd_tree_config tree;
+} cuacd_decompose_opts;
+
+/* Part (part.ts:9-22) of a finished decomposition, in input units. The
+ * pointers stay valid until cuacd_result_free. hausdorff is NaN when unset.
+ * stuckReason: 0 none, 1 no-plane, 2 cut-failed, 3 not-closed, 4 degenerate. */
+typedef struct {
+  const float* verts;
+  const uint32_t* tris;
+  const float* hullVerts;
+  const uint32_t* hullTris;
+  const double* seams; /* 4 doubles per seam plane */
+  uint32_t nv, nt, hullNv, hullNt, nSeams;
+  int32_t stuck;
+  int32_t stuckReason;
+  int32_t merged;
+  double meshVol;
+  double hullVol;
+  double hausdorff;
+} cuacd_part_view;
+
+/* DecomposeResult.stats and MergeStats (decompose.ts:112-120, merge.ts:
+ * 53-66) of one mesh. Times are of the whole call (every mesh of a batched
+ * call shares them). candidates = cut candidates the tree evaluated. */
+typedef struct {
+  int32_t iterations;
+  int32_t treeRuns;
+  int32_t hullFailRuns;
+  int32_t nParts;
+  int32_t mergeRounds;
+  int32_t merges;
+  int32_t pairsHulled;
+  int32_t pairsHausdorff;
+  uint64_t candidates;
+  double totalMs, treeMs, cutMs, concaveMs, hullMs, hausdorffMs, mergeMs, gpuMs;
+} cuacd_decompose_stats;
+
+void cuacd_decompose_opts_default(cuacd_decompose_opts* o);
+/* new Decomposer(device, opts) (decompose.ts:128-149): validates the options
+ * and creates the GPU tree. NULL on failure (err set). */
+void* cuacd_decomposer_create(const cuacd_decompose_opts* o, int* err);
+void cuacd_decomposer_destroy(void* d);
+/* Decomposer.decompose (decompose.ts:213-392) of n meshes. batched = 0 runs
+ * them one after another; batched != 0 advances all of them together, so one
+ * tree launch per iteration serves the cutting parts of every mesh and hull,
+ * Hausdorff and merge batches are shared. The results are the same either
+ * way. On success *result receives a handle for the accessors below. */
+int cuacd_decompose(void* d, const cuacd_mesh* meshes, int n, int batched, void** result);
+int cuacd_result_meshes(const void* result);
+int cuacd_result_parts(const void* result, int mesh);
+int cuacd_result_part(const void* result, int mesh, int part, cuacd_part_view* out);
+int cuacd_result_stats(const void* result, int mesh, cuacd_decompose_stats* out);
+void cuacd_result_free(void* result);
+
+/* planeCut with caps (src/cpu/cut.ts:33-315) on the host, for callers that
+ * apply a cut themselves. plane = a, b, c, d (a x + b y + c z + d = 0). On
+ * success the two halves are returned in a handle read with
+ * cuacd_cut_half (0 = positive side, 1 = negative side). Returns
+ * CUACD_E_INVALID with the reference's reason when the plane does not split
+ * the mesh or a boundary loop cannot be closed. */
+int cuacd_plane_cut(const cuacd_mesh* mesh, const double* plane, void** halves);
+int cuacd_cut_half(const void* halves, int side, const float** verts, uint32_t* nv, const uint32_t** tris,
+                   uint32_t* nt);
+void cuacd_cut_free(void* halves);
+
+/* concaveEdgePlanes (src/cpu/concave.ts:25-92): writes up to cap planes (4
+ * floats each) and returns their count (or a negative error). */
+int cuacd_concave_planes(const cuacd_mesh* mesh, int nConcaveEdges, double concaveEps, double concaveThreshold,
+                         uint32_t seed, float* out, int cap);
+
 /* Message of the last failure on the calling thread. */
 const char* cuacd_last_error(void);
 

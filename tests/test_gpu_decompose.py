@@ -1,0 +1,94 @@
+"""decompose(mesh, options) end to end on the GPU: the reference's known
+answers (tests/decompose.test.ts:10-53, tests/merge.test.ts:76-97) and the
+batched form against one mesh at a time (same parts, bit for bit)."""
+import numpy as np
+import pytest
+
+from conftest import pkg
+from fixtures import M, square_torus, stairs
+
+D = pkg("decompose")
+G = pkg("meshgen")
+P = pkg("part")
+
+# smallTree (tests/decompose.test.ts:8)
+SMALL_TREE = dict(vertexCap=4 << 20, triCap=4 << 20, edgeCap=1 << 18, scratchWords=4 << 20, hullBudgetBytes=32 << 20,
+                  hullMaxVerts=1024)
+
+pytestmark = pytest.mark.gpu
+
+
+def _cost(p):
+    return P.part_cost(p.meshVol, p.hullVol, p.hausdorff)
+
+
+def _check_parts(r, vol, thr):
+    total = 0.0
+    for p in r.parts:
+        assert M.is_closed(p.mesh)
+        assert _cost(p) < thr + 1e-6 or p.stuck, _cost(p)
+        total += M.volume(p.mesh)
+    assert abs(total - vol) < 1e-4, total
+
+
+def test_cube_stays_one_part():
+    r = D.decompose(M.unit_cube(), maxIters=5, threshold=0.05, tree=SMALL_TREE)
+    assert len(r.parts) == 1
+    assert abs(M.volume(r.parts[0].mesh) - 1) < 1e-6
+    assert r.iterations == 1
+
+
+def test_l_shape_two_parts():
+    r = D.decompose(M.l_shape(), maxIters=50, threshold=0.05, width=30, tree=SMALL_TREE, mergeHulls=False)
+    assert 2 <= len(r.parts) <= 10, len(r.parts)
+    _check_parts(r, 1.5, 0.05)
+    # with the merge pass the L ends at exactly 2 parts (merge.test.ts:89-97)
+    r = D.decompose(M.l_shape(), maxIters=50, threshold=0.05, width=30, tree=SMALL_TREE, mergeHulls=True)
+    assert len(r.parts) == 2, len(r.parts)
+    _check_parts(r, 1.5, 0.05)
+
+
+def test_stairs_and_torus():
+    r = D.decompose(stairs(), maxIters=50, threshold=0.05, width=30, tree=SMALL_TREE)
+    assert 3 <= len(r.parts) <= 6, len(r.parts)
+    _check_parts(r, 6.0, 0.05)
+    r = D.decompose(square_torus(), maxIters=50, threshold=0.05, width=30, tree=SMALL_TREE)
+    assert len(r.parts) >= 4, len(r.parts)
+    _check_parts(r, 1.5, 0.05)
+
+
+def _same(ra, rb):
+    assert len(ra.parts) == len(rb.parts)
+    assert ra.iterations == rb.iterations
+    for a, b in zip(ra.parts, rb.parts):
+        assert np.array_equal(a.mesh.verts, b.mesh.verts) and np.array_equal(a.mesh.tris, b.mesh.tris)
+        assert np.array_equal(a.hull.verts, b.hull.verts) and np.array_equal(a.hull.tris, b.hull.tris)
+        assert a.meshVol == b.meshVol and a.hullVol == b.hullVol and a.hausdorff == b.hausdorff
+        assert a.stuck == b.stuck and a.merged == b.merged and a.seams == b.seams
+
+
+def test_batched_equals_one_at_a_time():
+    meshes = [M.l_shape(), stairs(), square_torus(), M.unit_cube(), G.staircase(6)]
+    opts = dict(maxIters=20, threshold=0.05, width=6, depth=2, tree=SMALL_TREE)
+    d = D.Decomposer(**opts)
+    try:
+        batched = d.decompose_many(meshes, batched=True)
+        plain = d.decompose_many(meshes, batched=False)
+        alone = [d.decompose(m) for m in meshes]
+    finally:
+        d.destroy()
+    for b, p, a in zip(batched, plain, alone):
+        _same(b, p)
+        _same(b, a)
+
+
+def test_staircase_configuration():
+    # the staircase decomposition's settings: threshold 0.1, width 6,
+    # width2 3, depth 3, maxNCutting 160, 16 concave edges, 2 refinement
+    # rounds, merging on
+    m = G.staircase(8)
+    r = D.decompose(m, threshold=0.1, width=6, width2=3, depth=3, maxNCutting=160, nConcaveEdges=16, refineRounds=2,
+                    mergeHulls=True)
+    assert len(r.parts) >= 2
+    _check_parts(r, M.volume(m), 0.1)
+    assert r.stats["candidates"] > 0 and r.stats["treeRuns"] >= 1
