@@ -179,6 +179,8 @@ class DecomposeOpts(C.Structure):
         ("mergePlaneTol", C.c_float),
         ("profile", C.c_int32),
         ("threads", C.c_int32),
+        ("verbose", C.c_int32),
+        ("reserved", C.c_int32),
         ("tree", TreeConfig),
     ]
 

@@ -14,6 +14,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -130,6 +131,7 @@ class Engine {
 
   ~Engine() {
     if (tree) cuacd_tree_destroy(tree);
+    if (bigTree) cuacd_tree_destroy(bigTree);
   }
 
   [[noreturn]] void cuda_fail(int rc, const char* what) {
@@ -186,14 +188,61 @@ class Engine {
           p.hasHd = true;
         }
       });
-      for (size_t k = 0; k < n && !allowFail; k++)
-        if (std::isnan(out[s + k].hullVol)) {
+      // a hull that failed on the tree's slabs (more faces than its hull
+      // bound allows) is built again on a second tree with room for every
+      // point, where the reference falls back to its CPU hull (decompose.ts:
+      // 183-188, merge.ts:371)
+      for (size_t k = 0; k < n; k++) {
+        if (!std::isnan(out[s + k].hullVol)) continue;
+        if (!retry_hull(*ms[s + k], withHd, out[s + k]) && !allowFail) {
           char msg[160];
           snprintf(msg, sizeof msg, "GPU hull failed (code %d) for a part with %u vertices", status[k], cm[k].nv);
           throw Failure{CUACD_E_CAPACITY, msg};
         }
+      }
       s += n;
     }
+  }
+
+  // the hull (and Hausdorff distance) of one mesh on a tree whose hull bound
+  // covers all of its points; false when that hull fails too
+  void* bigTree = nullptr;
+  uint32_t bigTreeVerts = 0;
+  bool retry_hull(const Mesh& m, bool withHd, Part& p) {
+    const uint32_t need = (uint32_t)m.nv();
+    if (need <= (uint32_t)o.tree.hullMaxVerts) {
+      // the bound already covered the points: a larger one does not help
+      if (bigTree == nullptr || need > bigTreeVerts) return false;
+    }
+    if (bigTree == nullptr || bigTreeVerts < need) {
+      if (bigTree) cuacd_tree_destroy(bigTree);
+      cuacd_tree_config cfg = o.tree;
+      cfg.hullMaxVerts = (int32_t)std::max<uint32_t>(need, 2 * (uint32_t)o.tree.hullMaxVerts);
+      cfg.hullBudgetBytes = std::max<uint64_t>(cfg.hullBudgetBytes, (uint64_t)cfg.hullMaxVerts * 4096);
+      int rc = 0;
+      bigTree = cuacd_tree_create(&cfg, &rc);
+      if (!bigTree) cuda_fail(rc, "hull retry tree");
+      bigTreeVerts = (uint32_t)cfg.hullMaxVerts;
+    }
+    const cuacd_mesh cm{m.v.data(), m.t.data(), need, (uint32_t)m.nt()};
+    const uint32_t stride = 6 * need;
+    std::vector<uint32_t> tris((size_t)stride + 1);
+    float vol = 0, hd = 0;
+    uint32_t ntri = 0;
+    int32_t status = 0;
+    const auto t0 = Clock::now();
+    const int rc = withHd ? cuacd_tree_hulls_with_hausdorff(bigTree, &cm, 1, tris.data(), stride, &vol, &ntri, &hd, &status)
+                          : cuacd_tree_hull_meshes(bigTree, &cm, 1, 0, tris.data(), stride, &vol, &ntri, &status);
+    gpuMs += ms_since(t0);
+    if (rc != CUACD_OK) cuda_fail(rc, "hull retry");
+    if (status != 0) return false;
+    p.hull = host::compact_hull(m.v.data(), tris.data(), ntri, nullptr);
+    p.hullVol = vol;
+    if (withHd && std::isfinite(hd)) {
+      p.hd = hd;
+      p.hasHd = true;
+    }
+    return true;
   }
 
   // Hausdorff distances of pairs (a_k, b_k); batches of up to 1024, halved
@@ -414,6 +463,13 @@ class Engine {
     std::vector<Part> made;
     hulls(halves, true, made);
     hullMs += ms_since(th);
+    if (o.verbose) {
+      size_t nParts = 0, nTris = 0;
+      for (Job* j : jobs) nParts += j->parts.size();
+      for (const Mesh* m : halves) nTris += m->nt();
+      fprintf(stderr, "[iter %d] cutting %zu parts, %zu cuts applied, %zu half triangles, %zu parts; tree %.1f ms, hull %.1f ms\n",
+              iter, seeds.size(), which.size(), nTris, nParts + which.size(), treeMs, hullMs);
+    }
     // per job, in cutting order: the positive half replaces the part, the
     // negative half is appended
     for (size_t q = 0; q < which.size(); q++) {
@@ -624,6 +680,9 @@ class Engine {
       std::vector<double> hd;
       hausdorff(ha, hb, hd);
       hdMs += ms_since(thd);
+      if (o.verbose)
+        fprintf(stderr, "[merge %d] %zu new pairs hulled, %zu Hausdorff pairs; hull %.1f ms, hausdorff %.1f ms\n", round,
+                todo.size(), ha.size(), hullMs, hdMs);
       for (size_t q = 0; q < hk.size(); q++) {
         PairEval& ev = evals[base + hk[q]];
         ev.hd = hd[q];

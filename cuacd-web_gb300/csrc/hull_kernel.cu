@@ -58,7 +58,10 @@ struct HullSm {
   uint32_t seed[80];
   uint32_t nf, nalive, fail, compacted;
   uint32_t ncand, ok, nvis;
-  uint32_t nfRef;  // register hull: the slot count the slot-array form would have
+  uint32_t nfRef;    // register hull: the slot count the slot-array form would have
+  uint32_t remapN;   // candidates cand[0, remapN) whose owner slots a compaction renumbers
+  uint32_t newBase;  // first slot of the faces the last insertion created
+  uint32_t pad[2];
 };
 
 // Register hull (one warp, up to TINY_FACES faces, face k in lane k): the
@@ -264,6 +267,12 @@ __device__ __noinline__ uint32_t hull_compact(const HullCtx& h, HullSm& hs, GrpS
   }
   Grp<G>::sync();
   auto rank = [&](uint32_t f) { return h.wp[f >> 5] + __popc(h.bm[f >> 5] & ((1u << (f & 31)) - 1u)); };
+  // the candidates' owners (alive faces) move with their faces
+  for (uint32_t k = lid; k < hs.remapN; k += G) {
+    const uint32_t i = h.cand[k];
+    const uint32_t o = h.owner[i];
+    if (o < nf && bm_test(h.bm, o)) h.owner[i] = rank(o);
+  }
   for (uint32_t c = 0; c * G < nf; c++) {
     const uint32_t f = c * G + lid;
     uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0, w2 = w0, w3 = w0, nb = w0;
@@ -416,6 +425,7 @@ __device__ __noinline__ void hull_insert(const HullCtx& h, HullSm& hs, GrpSmem& 
   }
   for (uint32_t vi = lid; vi < nvis; vi += G) h.F[16 * (size_t)h.vis[vi]] &= 0x7fffffffu;
   if (lid == 0) {
+    hs.newBase = nf;
     hs.nf = nf + nnew;
     hs.nalive = nalive + nnew - nvis;
     hs.nvis = nvis;
@@ -641,6 +651,70 @@ __device__ __noinline__ uint32_t hull_tiny_grow(const HullCtx& h, HullSm& hs, Ti
   return nIns;
 }
 
+// Reassignment of candidate i over every face [0, nf1), as the reference
+// does after a compaction (shaders.ts:1090-1101), without scanning every
+// face: the faces visible from a point form one edge-connected patch, so the
+// patch is walked from one visible face and the most visible face of the
+// patch (first slot on ties) is the most visible face of all. The walk
+// starts at the point's owner when it survived the insertion (an alive face
+// keeps its record, so it still sees the point), else at the first new face
+// that sees the point; a point outside a dead owner and outside the new hull
+// is outside one of the new faces (the cone faces cover what the dead faces
+// saw), so when no new face sees it the point is inside. A patch larger than
+// PATCH_CAP falls back to the scan.
+#define PATCH_CAP 64u
+__device__ __noinline__ void reassign_patch(const HullCtx& h, uint32_t i, uint32_t own, bool dead, uint32_t nb0,
+                                            uint32_t nf1) {
+  const f3 pt = h.qvert(i);
+  uint32_t q[PATCH_CAP];
+  uint32_t n = 0;
+  uint32_t bestF = CUACD_NONE;
+  float bestD = 0.0f;
+  if (!dead) {
+    const float v = h.face_eval(own, pt, i);
+    if (!(v > 0.0f)) {
+      h.assign(i, 0, nf1);
+      return;
+    }
+    q[n++] = own;
+    bestF = own;
+    bestD = v;
+  } else {
+    for (uint32_t f = nb0; f < nf1; f++) {
+      const float v = h.face_eval(f, pt, i);
+      if (v > 0.0f) {
+        q[n++] = f;
+        bestF = f;
+        bestD = v;
+        break;
+      }
+    }
+  }
+  for (uint32_t head = 0; head < n; head++) {
+    const uint32_t f = q[head];
+    for (int k = 0; k < 3; k++) {
+      const uint32_t g = h.nbr[4 * (size_t)f + k];
+      if (g >= nf1) continue;
+      bool seen = false;
+      for (uint32_t j = 0; j < n; j++) seen |= q[j] == g;
+      if (seen) continue;
+      const float v = h.face_eval(g, pt, i);
+      if (!(v > 0.0f)) continue;
+      if (n == PATCH_CAP) {
+        h.assign(i, 0, nf1);
+        return;
+      }
+      q[n++] = g;
+      if (v > bestD || (v == bestD && g < bestF)) {
+        bestD = v;
+        bestF = g;
+      }
+    }
+  }
+  h.owner[i] = bestF;
+  h.dist[i] = bestF != CUACD_NONE ? bestD : 0.0f;
+}
+
 // farthest-first insertion of the candidate list (shaders.ts:1060-1129)
 template <int G>
 __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t nfPrev, uint32_t maxIter) {
@@ -658,22 +732,32 @@ __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem
     grp_argmax_pos<G>(md, mi, sm);
     if (md < 0.0f) break;
     const uint32_t pick = mi;
-    if (lid == 0) hs.compacted = 0;
+    if (lid == 0) {
+      hs.compacted = 0;
+      hs.remapN = ncand;
+    }
     Grp<G>::sync();
     hull_insert<G>(h, hs, sm, pick, h.owner[pick]);
     nIns++;
     if (hs.fail) break;
     const uint32_t nfNow = hs.nf;
     const bool compacted = hs.compacted != 0;
-    if (lid == 0) { h.owner[pick] = CUACD_NONE; h.dist[pick] = 0.0f; }
+    const uint32_t newBase = hs.newBase;
     Grp<G>::sync();
-    // an owner face died in this insertion exactly when it was visible
+    if (lid == 0) { h.owner[pick] = CUACD_NONE; h.dist[pick] = 0.0f; hs.remapN = 0; }
+    Grp<G>::sync();
+    // an owner face died in this insertion exactly when it was visible;
+    // after a compaction every candidate is reassigned over every face
     for (uint32_t k = lid; k < ncand; k += G) {
       uint32_t i = h.cand[k];
       uint32_t own = h.owner[i];
       if (own == CUACD_NONE) continue;
-      if (!compacted && !bm_test(h.bm, own)) continue;
-      h.assign(i, compacted ? 0 : nfPrev, nfNow);
+      if (compacted) {
+        reassign_patch(h, i, own, bm_test(h.bm, own), newBase, nfNow);
+        continue;
+      }
+      if (!bm_test(h.bm, own)) continue;
+      h.assign(i, nfPrev, nfNow);
     }
     Grp<G>::sync();
     for (uint32_t vi = lid; vi < hs.nvis; vi += G) h.bm[h.vis[vi] >> 5] = 0;
@@ -975,6 +1059,7 @@ restart:
       hs.ok = i3 != CUACD_NONE ? 1u : 0u;
       hs.nf = 4;
       hs.nalive = 4;
+      hs.remapN = 0;
     }
   }
   Grp<G>::sync();

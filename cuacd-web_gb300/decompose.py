@@ -43,6 +43,7 @@ DEFAULT_OPTIONS = dict(
     mergePlaneTol=1e-3,
     profile=False,
     threads=0,
+    verbose=0,
 )
 
 STUCK_REASONS = {0: None, 1: "no-plane", 2: "cut-failed", 3: "not-closed", 4: "degenerate"}

@@ -127,3 +127,138 @@ def _orient_outward(m: Mesh) -> Mesh:
     if signed_volume(m) < 0:
         return Mesh(m.verts, m.tris[:, [0, 2, 1]])
     return m
+
+
+# ---------------------------------------------------------------------------
+# Gaussian-blob isosurfaces (marching tetrahedra)
+
+# The six tetrahedra of the Kuhn split of a unit cube: corner offsets along
+# each permutation (a, b, c) of the axes from (0,0,0) to (1,1,1). Neighbouring
+# cubes split their shared faces the same way, so the surface is conforming.
+_KUHN = []
+for _a, _b, _c in ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)):
+    _p = [0, 0, 0]
+    _tet = [tuple(_p)]
+    for _ax in (_a, _b, _c):
+        _p[_ax] = 1
+        _tet.append(tuple(_p))
+    _KUHN.append(_tet)
+
+
+def isosurface(field: np.ndarray, lo, hi, level: float) -> Mesh:
+    """Closed, outward-wound surface {field = level} of a sampled field
+    (inside = field > level) by marching tetrahedra on the Kuhn split of
+    each grid cube. Vertices sit on grid edges and are shared by edge, so the
+    mesh is a closed 2-manifold when the field is below the level on the
+    grid's boundary. Values equal to the level count as outside."""
+    f = np.asarray(field, np.float64)
+    nx, ny, nz = f.shape
+    lo = np.asarray(lo, np.float64)
+    hi = np.asarray(hi, np.float64)
+    step = (hi - lo) / (np.array([nx, ny, nz]) - 1)
+    ins = f > level
+    # cube origins
+    ci, cj, ck = np.meshgrid(np.arange(nx - 1), np.arange(ny - 1), np.arange(nz - 1), indexing="ij")
+    ci, cj, ck = ci.ravel(), cj.ravel(), ck.ravel()
+    # keep cubes whose 8 corners are not all on one side
+    corners = np.stack([ins[ci + dx, cj + dy, ck + dz] for dx in (0, 1) for dy in (0, 1) for dz in (0, 1)], 1)
+    mixed = corners.any(1) & ~corners.all(1)
+    ci, cj, ck = ci[mixed], cj[mixed], ck[mixed]
+
+    def gid(i, j, k):
+        return (i * ny + j) * nz + k
+
+    tets = np.concatenate([np.stack([gid(ci + o[0], cj + o[1], ck + o[2]) for o in tet], 1) for tet in _KUHN])
+    s = ins.ravel()[tets]
+    nin = s.sum(1)
+    fr = f.ravel()
+    tris_e = []  # triangles as (edge a, edge b) pairs of grid ids, shape (n, 3, 2)
+    orient = []  # (inside id, outside id) of each triangle, to wind it outward
+    # one corner alone on its side: one triangle on its three edges
+    for lone_inside in (True, False):
+        sel = nin == (1 if lone_inside else 3)
+        t = tets[sel]
+        st = s[sel] if lone_inside else ~s[sel]
+        k = np.argmax(st, 1)
+        lone = t[np.arange(len(t)), k]
+        others = np.stack([t[np.arange(len(t)), (k + d) % 4] for d in (1, 2, 3)], 1)
+        tris_e.append(np.stack([np.stack([lone, others[:, q]], 1) for q in range(3)], 1))
+        ins_id, out_id = (lone, others[:, 0]) if lone_inside else (others[:, 0], lone)
+        orient.append(np.stack([ins_id, out_id], 1))
+    # two inside, two outside: a quad on the four crossing edges
+    sel = nin == 2
+    t = tets[sel]
+    st = s[sel]
+    order = np.argsort(~st, axis=1, kind="stable")  # inside corners first
+    i1, i2 = t[np.arange(len(t)), order[:, 0]], t[np.arange(len(t)), order[:, 1]]
+    o1, o2 = t[np.arange(len(t)), order[:, 2]], t[np.arange(len(t)), order[:, 3]]
+    q = [np.stack([i1, o1], 1), np.stack([i1, o2], 1), np.stack([i2, o2], 1), np.stack([i2, o1], 1)]
+    tris_e.append(np.stack([q[0], q[1], q[2]], 1))
+    tris_e.append(np.stack([q[0], q[2], q[3]], 1))
+    orient.append(np.stack([i1, o1], 1))
+    orient.append(np.stack([i1, o1], 1))
+    E = np.concatenate(tris_e)  # (n, 3, 2)
+    O = np.concatenate(orient)
+    # weld by grid edge
+    a, b = np.minimum(E[..., 0], E[..., 1]), np.maximum(E[..., 0], E[..., 1])
+    key = a.astype(np.int64) * (nx * ny * nz) + b
+    uk, inv = np.unique(key.ravel(), return_inverse=True)
+    ea, eb = uk // (nx * ny * nz), uk % (nx * ny * nz)
+
+    def pos(g):
+        i, r = np.divmod(g, ny * nz)
+        j, k = np.divmod(r, nz)
+        return lo + np.stack([i, j, k], 1) * step
+
+    fa, fb = fr[ea], fr[eb]
+    tt = (level - fa) / (fb - fa)
+    verts = pos(ea) + tt[:, None] * (pos(eb) - pos(ea))
+    tris = inv.reshape(-1, 3)
+    # wind outward: the normal points from the inside corner to the outside one
+    v0, v1, v2 = verts[tris[:, 0]], verts[tris[:, 1]], verts[tris[:, 2]]
+    nrm = np.cross(v1 - v0, v2 - v0)
+    d = pos(O[:, 1]) - pos(O[:, 0])
+    flip = (nrm * d).sum(1) < 0
+    tris[flip] = tris[flip][:, [0, 2, 1]]
+    return Mesh(verts.astype(np.float32), tris.astype(np.uint32))
+
+
+def blob_field(n_blobs: int, grid: int, seed: int = 0, sigma=(0.15, 0.45)):
+    """Sum of n seeded isotropic Gaussian blobs (centres uniform in [-1, 1]^3,
+    sigma uniform in `sigma`, unit amplitude) sampled on a grid^3 lattice
+    spanning the centres' box plus 3.2 sigma_max on every side."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-1, 1, (n_blobs, 3))
+    sg = rng.uniform(sigma[0], sigma[1], n_blobs)
+    pad = 3.2 * sigma[1]
+    lo, hi = np.full(3, -1 - pad), np.full(3, 1 + pad)
+    ax = np.linspace(lo[0], hi[0], grid)
+    f = np.zeros((grid, grid, grid))
+    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij", sparse=True)
+    for k in range(n_blobs):
+        f += np.exp(-((X - c[k, 0]) ** 2 + (Y - c[k, 1]) ** 2 + (Z - c[k, 2]) ** 2) / (2 * sg[k] ** 2))
+    return f, lo, hi
+
+
+def blob_mesh(n_blobs: int = 24, grid: int = 160, seed: int = 0, level: float = 0.5, sigma=(0.15, 0.45)) -> Mesh:
+    """Isosurface (level 0.5) of a sum of Gaussian blobs, marching tetrahedra."""
+    f, lo, hi = blob_field(n_blobs, grid, seed, sigma)
+    # a sample exactly at the level would put a vertex on a grid point
+    f = np.where(f == level, np.nextafter(level, 0.0), f)
+    return isosurface(f, lo, hi, level)
+
+
+def blob_batch(n_meshes: int = 256, seed: int = 0, tri_range=(500, 60000)):
+    """Uneven batch: blob counts uniform in 2..32, each mesh's grid chosen so
+    the triangle counts are log-uniform in tri_range (the count of a
+    marching-tetrahedra surface grows with the square of the grid size)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_meshes):
+        nb = int(rng.integers(2, 33))
+        target = float(np.exp(rng.uniform(np.log(tri_range[0]), np.log(tri_range[1]))))
+        g0 = 24
+        m0 = blob_mesh(nb, g0, seed=seed * 100003 + k)
+        g = int(np.clip(round(g0 * np.sqrt(target / max(m0.nt, 1))), 8, 400))
+        out.append(blob_mesh(nb, g, seed=seed * 100003 + k))
+    return out

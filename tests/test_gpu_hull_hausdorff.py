@@ -78,6 +78,30 @@ def test_hull_stages_and_large_parts(tree_mod, oracle):
                 assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"]
 
 
+def test_hull_compaction_heavy_sets(tree_mod, oracle):
+    """Point sets whose hulls compact their face slots many times (every
+    point on a sphere; a marching-tetrahedra blob whose vertices share grid
+    lines and planes): after each compaction every candidate is reassigned
+    over every face, which the kernel does by walking each point's visible
+    patch."""
+    cfg = dict(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    g = tree_mod.GpuTree(**cfg)
+    o = oracle.OracleTree(**cfg)
+    rng = np.random.default_rng(11)
+    s = rng.normal(size=(3000, 3))
+    s /= np.linalg.norm(s, axis=1, keepdims=True)
+    inner = rng.uniform(-0.7, 0.7, size=(3000, 3))
+    sets = [M.Mesh(np.concatenate([s, inner]).astype(np.float32), np.zeros((0, 3), np.uint32)),
+            gen.blob_mesh(6, 26, seed=3)]
+    rg, sg = g.hull_meshes(sets)
+    ro, so = o.hull_meshes(sets)
+    assert list(sg) == list(so)
+    for a, b in zip(rg, ro):
+        assert (a is None) == (b is None)
+        if a is not None:
+            assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"]
+
+
 def hd_pairs(oracle):
     t = oracle.OracleTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
     pairs = []
