@@ -324,6 +324,10 @@ def run_engine(args):
         line["cpu_baseline"] = {"value": c / s, "unit": UNIT, "cores": nthr, "kind": "port",
                                 "sample": f"{sample} staircase seeds, one tree run with {REFINE_ROUNDS} refinement "
                                           f"rounds on the oracle's CPU restatement ({c} candidates, {s:.1f} s)"}
+    if world == 1 and not args.no_decompose:
+        # the metric's second half: whole decompositions per second, the
+        # uneven batch decomposed together against one mesh at a time
+        line["decompose"] = decompose_measure(args.meshes)
     print(json.dumps(line), flush=True)
 
 
@@ -395,6 +399,87 @@ def run_secondary(args):
     print(json.dumps(line), flush=True)
 
 
+# The uneven-batch decomposition: blob meshes (2..32 Gaussian blobs, marching
+# tetrahedra, triangle counts log-uniform in 500..60k) at threshold 0.05,
+# width 6, depth 2; the hull bound covers every part, so no GPU hull fails.
+DEC_TREE = dict(vertexCap=64 << 20, triCap=64 << 20, edgeCap=4 << 20, scratchWords=64 << 20,
+                hullBudgetBytes=8 << 30, hullMaxVerts=32768)
+DEC_OPTS = dict(threshold=0.05, width=6, width2=3, depth=2, tree=DEC_TREE)
+# the single large organic mesh: 24 blobs, about 56k triangles, threshold
+# 0.1, width 9, depth 3
+BIG_OPTS = dict(threshold=0.1, width=9, width2=3, depth=3, maxNCutting=160, tree=DEC_TREE)
+
+
+def _parts_equal(ra, rb):
+    if len(ra.parts) != len(rb.parts):
+        return False
+    return all(a.mesh.nv == b.mesh.nv and a.meshVol == b.meshVol and a.hullVol == b.hullVol
+               and a.hausdorff == b.hausdorff for a, b in zip(ra.parts, rb.parts))
+
+
+def decompose_measure(n_meshes, big_steps=2):
+    """meshes/s of the uneven batch decomposed together and one at a time
+    (same decomposer, same parts), and the large mesh's latency."""
+    dec = importlib.import_module("cuacd-web_gb300.decompose")
+    gen = importlib.import_module("cuacd-web_gb300.meshgen")
+    meshes = gen.blob_batch(n_meshes, seed=0)
+    d = dec.Decomposer(**DEC_OPTS)
+    try:
+        small = sorted(meshes, key=lambda m: m.nt)[:2]
+        d.decompose_many(small, batched=True)  # warm-up: tree buffers and graphs
+        t0 = time.perf_counter()
+        rb = d.decompose_many(meshes, batched=True)
+        tb = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        rp = d.decompose_many(meshes, batched=False)
+        tp = time.perf_counter() - t0
+    finally:
+        d.destroy()
+    same = all(_parts_equal(a, b) for a, b in zip(rb, rp))
+    big = gen.blob_mesh(24, 71, seed=0)
+    d = dec.Decomposer(**BIG_OPTS)
+    try:
+        d.decompose(big)
+        ms = []
+        for _ in range(big_steps):
+            t0 = time.perf_counter()
+            rbig = d.decompose(big)
+            ms.append(1000 * (time.perf_counter() - t0))
+    finally:
+        d.destroy()
+    h2d = sum(m.verts.nbytes + m.tris.nbytes for m in meshes)
+    d2h = sum(p.mesh.verts.nbytes + p.mesh.tris.nbytes + p.hull.verts.nbytes + p.hull.tris.nbytes
+              for r in rb for p in r.parts)
+    return {
+        "metric": "meshes decomposed/s, batched vs one at a time",
+        "batched": {"value": n_meshes / tb, "unit": "meshes/s", "seconds": tb},
+        "plain": {"value": n_meshes / tp, "unit": "meshes/s", "seconds": tp},
+        "speedup": tp / tb,
+        "parts_equal": same,
+        "parts": sum(len(r.parts) for r in rb),
+        "stuck": sum(p.stuck for r in rb for p in r.parts),
+        "config": {"workload": f"{n_meshes} blob meshes (2..32 Gaussian blobs, marching tetrahedra, triangles "
+                               f"log-uniform in 500..60k, seed 0)", "tris": sum(m.nt for m in meshes),
+                   "threshold": 0.05, "width": 6, "width2": 3, "depth": 2, "maxNCutting": 16, "nConcaveEdges": 16,
+                   "refineRounds": 2, "mergeHulls": True, "hullMaxVerts": DEC_TREE["hullMaxVerts"]},
+        "e2e_bytes": {"h2d": h2d, "d2h": d2h},
+        "large_mesh": {"tris": big.nt, "ms": statistics.median(ms), "parts": len(rbig.parts),
+                       "iterations": rbig.iterations, "config": "24 blobs, 71^3 grid, threshold 0.1, width 9, depth 3"},
+    }
+
+
+def run_decompose(args):
+    m = decompose_measure(args.meshes, big_steps=max(args.steps, 1))
+    line = {"metric": m["metric"], "value": m["batched"]["value"], "unit": "meshes/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": 1000 * m["batched"]["seconds"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": m["config"],
+            "e2e": {"value": m["batched"]["value"], "unit": "meshes/s", "h2d_bytes_per_step": m["e2e_bytes"]["h2d"],
+                    "d2h_bytes_per_step": m["e2e_bytes"]["d2h"]},
+            "plain": m["plain"], "speedup": m["speedup"], "parts_equal": m["parts_equal"], "parts": m["parts"],
+            "large_mesh": m["large_mesh"]}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -403,11 +488,15 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--seeds", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls"])
+    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls", "decompose"])
     ap.add_argument("--pairs", type=int, default=256)
+    ap.add_argument("--meshes", type=int, default=32, help="meshes of the uneven decomposition batch")
+    ap.add_argument("--no-decompose", action="store_true", help="leave the decomposition summary out of the tree line")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "decompose":
+        run_decompose(args)
     elif args.workload != "tree":
         run_secondary(args)
     else:
