@@ -402,8 +402,8 @@ def run_secondary(args):
 # The uneven-batch decomposition: blob meshes (2..32 Gaussian blobs, marching
 # tetrahedra, triangle counts log-uniform in 500..60k) at threshold 0.05,
 # width 6, depth 2; the hull bound covers every part, so no GPU hull fails.
-DEC_TREE = dict(vertexCap=64 << 20, triCap=64 << 20, edgeCap=4 << 20, scratchWords=64 << 20,
-                hullBudgetBytes=8 << 30, hullMaxVerts=32768)
+DEC_TREE = dict(vertexCap=256 << 20, triCap=256 << 20, edgeCap=16 << 20, scratchWords=256 << 20,
+                hullBudgetBytes=16 << 30, hullMaxVerts=32768)
 DEC_OPTS = dict(threshold=0.05, width=6, width2=3, depth=2, tree=DEC_TREE)
 # the single large organic mesh: 24 blobs, about 56k triangles, threshold
 # 0.1, width 9, depth 3
@@ -468,6 +468,67 @@ def decompose_measure(n_meshes, big_steps=2):
     }
 
 
+def run_serve(args):
+    """Serving: Poisson arrivals of decomposition requests (40% staircases of
+    4..16 steps, 40% blobs of 2k..60k triangles, 20% carved icospheres of
+    level 3..5; thresholds 0.05 or 0.1) into the continuous-batching server
+    for `duration` seconds, then drained. Latency = completion time minus
+    arrival time, queueing included."""
+    import numpy as np
+
+    dec = importlib.import_module("cuacd-web_gb300.decompose")
+    gen = importlib.import_module("cuacd-web_gb300.meshgen")
+    pool = gen.serving_mix(args.pool, seed=0)
+    rng = np.random.default_rng(1)
+    arr = np.cumsum(rng.exponential(1.0 / args.rate, size=int(args.rate * args.duration * 2) + 16))
+    arr = arr[arr < args.duration]
+    pick = rng.integers(0, len(pool), size=len(arr))
+    srv = dec.Server(admit_tris=args.admit_tris, threshold=0.05, width=6, width2=3, depth=2, tree=DEC_TREE)
+    try:
+        # warm-up: the two trees (one per threshold) and their buffers
+        for k, (_, m, thr) in enumerate(sorted(pool, key=lambda x: x[1].nt)[:4]):
+            t = srv.submit(m, thr)
+            while srv.take(t) is None:
+                srv.step()
+        t0 = time.perf_counter()
+        i, out, lat, kinds = 0, {}, [], {}
+        with ClockSampler(0) as clk:
+            while i < len(arr) or srv.pending:
+                now = time.perf_counter() - t0
+                while i < len(arr) and arr[i] <= now:
+                    kind, m, thr = pool[pick[i]]
+                    out[srv.submit(m, thr)] = (arr[i], kind)
+                    i += 1
+                if srv.pending:
+                    srv.step()
+                elif i < len(arr):
+                    time.sleep(max(0.0, arr[i] - (time.perf_counter() - t0)))
+                for t in list(out):
+                    r = srv.take(t)
+                    if r is not None:
+                        a, kind = out.pop(t)
+                        ms = 1000 * (time.perf_counter() - t0 - a)
+                        lat.append(ms)
+                        kinds.setdefault(kind, []).append(ms)
+        wall = time.perf_counter() - t0
+    finally:
+        srv.destroy()
+    lat = np.array(lat)
+    line = {"metric": "decomposition requests served/s", "value": len(lat) / wall, "unit": "requests/s", "n_gpus": 1,
+            "steps": 1, "warmup": 1, "ms_per_step": 1000 * wall, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"Poisson arrivals at {args.rate} req/s for {args.duration} s "
+                                   f"({len(arr)} requests from {args.pool} distinct meshes), then drained",
+                       "mix": "40% staircases 4..16 steps, 40% blobs 2k..60k tris, 20% carved icospheres L3..5",
+                       "thresholds": [0.05, 0.1], "admit_tris": args.admit_tris, "width": 6, "depth": 2},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "max": float(lat.max())},
+            "latency_ms_by_kind": {k: {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)),
+                                       "n": len(v)} for k, v in kinds.items()},
+            "offered_rate": args.rate, "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_decompose(args):
     m = decompose_measure(args.meshes, big_steps=max(args.steps, 1))
     line = {"metric": m["metric"], "value": m["batched"]["value"], "unit": "meshes/s", "n_gpus": 1,
@@ -488,15 +549,21 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--seeds", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls", "decompose"])
+    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls", "decompose", "serve"])
     ap.add_argument("--pairs", type=int, default=256)
     ap.add_argument("--meshes", type=int, default=32, help="meshes of the uneven decomposition batch")
     ap.add_argument("--no-decompose", action="store_true", help="leave the decomposition summary out of the tree line")
+    ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
+    ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
+    ap.add_argument("--pool", type=int, default=48, help="serving: distinct request meshes")
+    ap.add_argument("--admit-tris", type=int, default=1 << 20, help="serving: triangles admitted at once")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "decompose":
         run_decompose(args)
+    elif args.workload == "serve":
+        run_serve(args)
     elif args.workload != "tree":
         run_secondary(args)
     else:

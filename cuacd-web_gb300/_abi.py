@@ -26,7 +26,7 @@ class TreeConfig(C.Structure):
         ("scratchWords", C.c_uint64),
         ("hullBudgetBytes", C.c_uint64),
         ("pruneLastLevel", C.c_int32),
-        ("reserved", C.c_int32),
+        ("warpMaxNv", C.c_int32),
     ]
 
 
@@ -102,6 +102,7 @@ DEFAULT_TREE_CONFIG = dict(
     scratchWords=48 << 20,
     hullBudgetBytes=256 << 20,
     pruneLastLevel=1,
+    warpMaxNv=0,
 )
 
 

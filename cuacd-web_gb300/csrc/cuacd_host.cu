@@ -215,7 +215,7 @@ struct Tree {
     P.minEdgeDist = cfg.minEdgeDist;
     P.hullSlabWords = slabWords;
     P.slabStride = slabStride;
-    P.smallNv = SMALL_NV;
+    P.smallNv = cfg.warpMaxNv > 0 ? (uint32_t)cfg.warpMaxNv : SMALL_NV;
     return P;
   }
   // hull launches of one level; work counter `slot` must be zero beforehand

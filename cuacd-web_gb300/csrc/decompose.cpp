@@ -97,6 +97,7 @@ struct Job {
   bool normalized = false;
   std::vector<Part> parts;
   bool cutting_done = false;
+  int iter = 0;  // iterations started
   bool merging = false;
   cuacd_decompose_stats st{};
   // merge state
@@ -177,6 +178,16 @@ class Engine {
         const Mesh& m = *ms[s + k];
         p.mesh = m;
         p.meshVol = host::volume(m);
+        if (status[k] == 8) {
+          // fewer than 4 hull faces: the points are flat (or fewer than 4),
+          // the hull is the set itself with no volume, and a flat part is its
+          // own hull (distance 0)
+          p.hull = m;
+          p.hullVol = 0.0;
+          p.hd = 0.0;
+          p.hasHd = true;
+          return;
+        }
         if (status[k] != 0) {
           p.hullVol = NAN;
           return;
@@ -311,8 +322,12 @@ class Engine {
 
   // ---- one decomposition iteration over all active jobs ------------------
 
-  // returns false when no job had a part to cut
-  bool iterate(std::vector<Job*>& jobs, int iter) {
+  // One iteration (decompose.ts:258-358) of every job whose cutting is not
+  // done; each job counts its own iterations, so jobs may join between
+  // calls. Returns false when no job had a part to cut.
+  bool iterate(std::vector<Job*>& jobs) {
+    for (Job* j : jobs)
+      if (!j->cutting_done && j->iter >= o.maxIters) j->cutting_done = true;
     // Hausdorff of the parts that lack it
     {
       std::vector<Part*> ps;
@@ -326,8 +341,11 @@ class Engine {
       size_t part;
     };
     std::vector<Seed> seeds;
+    int iterShown = 0;
     for (Job* j : jobs) {
       if (j->cutting_done) continue;
+      const int iter = j->iter++;
+      iterShown = std::max(iterShown, iter);
       j->st.iterations = iter + 1;
       // ascending by cost; the last maxNCutting above the threshold
       std::vector<std::pair<double, size_t>> order;
@@ -351,6 +369,7 @@ class Engine {
     const auto tc = Clock::now();
     std::vector<std::vector<float>> planes(seeds.size());
     parallel_for(seeds.size(), threads, [&](size_t k) {
+      const int iter = seeds[k].job->iter - 1;
       if (iter < o.concaveIters && o.nConcaveEdges > 0)
         planes[k] = host::concave_edge_planes(seeds[k].job->parts[seeds[k].part].mesh, o.nConcaveEdges, o.concaveEps,
                                               o.concaveThreshold, (uint32_t)(iter * 7919 + (int)seeds[k].part));
@@ -468,7 +487,7 @@ class Engine {
       for (Job* j : jobs) nParts += j->parts.size();
       for (const Mesh* m : halves) nTris += m->nt();
       fprintf(stderr, "[iter %d] cutting %zu parts, %zu cuts applied, %zu half triangles, %zu parts; tree %.1f ms, hull %.1f ms\n",
-              iter, seeds.size(), which.size(), nTris, nParts + which.size(), treeMs, hullMs);
+              iterShown, seeds.size(), which.size(), nTris, nParts + which.size(), treeMs, hullMs);
     }
     // per job, in cutting order: the positive half replaces the part, the
     // negative half is appended
@@ -754,7 +773,9 @@ class Engine {
 
   // ---- the whole decomposition of a set of jobs ---------------------------
 
-  void run(std::vector<Job*>& jobs) {
+  // checks, normalisation and the first part (the whole mesh with its hull
+  // and Hausdorff distance) of new jobs (decompose.ts:213-253)
+  void begin(std::vector<Job*>& jobs) {
     for (Job* j : jobs) {
       if (o.requireClosed && !host::is_closed(j->input))
         throw Failure{CUACD_E_INVALID,
@@ -767,21 +788,22 @@ class Engine {
         j->mesh = j->input;
       }
     }
-    // the first part of every job: the whole mesh with its hull
-    {
-      std::vector<const Mesh*> ms;
-      for (Job* j : jobs) ms.push_back(&j->mesh);
-      std::vector<Part> made;
-      const auto th = Clock::now();
-      hulls(ms, true, made);
-      hullMs += ms_since(th);
-      for (size_t k = 0; k < jobs.size(); k++) {
-        made[k].id = nextId++;
-        jobs[k]->parts.push_back(std::move(made[k]));
-      }
+    std::vector<const Mesh*> ms;
+    for (Job* j : jobs) ms.push_back(&j->mesh);
+    std::vector<Part> made;
+    const auto th = Clock::now();
+    hulls(ms, true, made);
+    hullMs += ms_since(th);
+    for (size_t k = 0; k < jobs.size(); k++) {
+      made[k].id = nextId++;
+      jobs[k]->parts.push_back(std::move(made[k]));
     }
-    for (int iter = 0; iter < o.maxIters; iter++)
-      if (!iterate(jobs, iter)) break;
+  }
+
+  // jobs whose cutting is done: the last Hausdorff distances, the merge pass
+  // and the parts back in input units (decompose.ts:360-392)
+  void finish(std::vector<Job*>& jobs) {
+    evals.clear();  // pair evaluations live for one merge pass
     {
       std::vector<Part*> ps;
       for (Job* j : jobs)
@@ -797,6 +819,158 @@ class Engine {
         for (Plane& s : p.seams) s = host::denormalize_plane(s, j->norm);
       }
     }
+  }
+
+  void run(std::vector<Job*>& jobs) {
+    begin(jobs);
+    while (iterate(jobs)) {
+    }
+    finish(jobs);
+  }
+};
+
+// An Engine with its tree built from the options (decompose.ts:128-149).
+Engine* make_engine(const cuacd_decompose_opts& o, int* err) {
+  if (o.width % 3 != 0 || o.width2 % 3 != 0) {
+    *err = set_error(CUACD_E_INVALID, "width and width2 must be multiples of 3");
+    return nullptr;
+  }
+  if (!(o.threshold > 0) || o.maxNCutting < 1 || o.maxIters < 0 || o.mergeRounds < 0) {
+    *err = set_error(CUACD_E_INVALID, "decomposer: invalid option");
+    return nullptr;
+  }
+  std::unique_ptr<Engine> e(new Engine());
+  e->o = o;
+  cuacd_tree_config cfg = o.tree;
+  cfg.width = o.width;
+  cfg.width2 = o.width2;
+  cfg.depth = o.depth;
+  cfg.nConcaveEdges = o.nConcaveEdges;
+  cfg.minEdgeDist = std::min(o.threshold / 4.0f, 0.015f);
+  int rc = 0;
+  e->tree = cuacd_tree_create(&cfg, &rc);
+  if (!e->tree) {
+    *err = rc ? rc : CUACD_E_INVALID;
+    return nullptr;
+  }
+  e->o.tree = cfg;
+  cuacd_set_profile(e->tree, o.profile);
+  e->planeSlots = cuacd_plane_slots(e->tree);
+  const unsigned hc = std::thread::hardware_concurrency();
+  e->threads = o.threads > 0 ? o.threads : (int)std::max(1u, hc);
+  *err = CUACD_OK;
+  return e.release();
+}
+
+// ---------------------------------------------------------------------------
+// Serving: continuous batching of decompositions. Requests wait in a queue
+// and are admitted in arrival order while the triangles of the admitted
+// meshes stay within a budget (at least one is always admitted). Every step
+// runs one iteration of every admitted decomposition together (one tree
+// launch per threshold), then finishes the ones with nothing left to cut
+// (merge pass included), so a request that arrives while others are on the
+// GPU joins them at the next step. A decomposition's parts do not depend on
+// what else was admitted with it.
+struct Request {
+  uint64_t ticket = 0;
+  std::unique_ptr<Job> job;
+  Clock::time_point submitted;
+  float threshold = 0;
+  uint64_t tris = 0;
+};
+
+class Server {
+ public:
+  cuacd_decompose_opts base{};
+  uint64_t admitTris = 0;
+  std::map<uint32_t, std::unique_ptr<Engine>> engines;  // by threshold bits
+  std::vector<Request> queue;                           // FIFO
+  size_t queueHead = 0;
+  std::vector<Request> active;
+  std::map<uint64_t, std::unique_ptr<Result>> done;
+  std::map<uint64_t, std::pair<int, std::string>> failed;
+  uint64_t nextTicket = 1;
+  uint64_t activeTris = 0;
+
+  Engine* engine_for(float thr) {
+    uint32_t key;
+    std::memcpy(&key, &thr, 4);
+    auto it = engines.find(key);
+    if (it != engines.end()) return it->second.get();
+    cuacd_decompose_opts o = base;
+    o.threshold = thr;
+    int err = 0;
+    Engine* e = make_engine(o, &err);
+    if (!e) throw Failure{err, cuacd_last_error()};
+    engines.emplace(key, std::unique_ptr<Engine>(e));
+    return e;
+  }
+
+  void complete(Request& r) {
+    std::unique_ptr<Result> res(new Result());
+    cuacd_decompose_stats s = r.job->st;
+    s.nParts = (int32_t)r.job->parts.size();
+    s.totalMs = ms_since(r.submitted);
+    res->stats.push_back(s);
+    res->parts.push_back(std::move(r.job->parts));
+    done.emplace(r.ticket, std::move(res));
+  }
+
+  int step(int* completed) {
+    int nDone = 0;
+    // admission
+    std::vector<size_t> admitted;
+    while (queueHead < queue.size()) {
+      Request& q = queue[queueHead];
+      if (!active.empty() && activeTris + q.tris > admitTris) break;
+      activeTris += q.tris;
+      active.push_back(std::move(q));
+      admitted.push_back(active.size() - 1);
+      queueHead++;
+    }
+    if (queueHead == queue.size()) {
+      queue.clear();
+      queueHead = 0;
+    }
+    // new jobs: a mesh that is not closed fails alone
+    std::map<Engine*, std::vector<Job*>> fresh;
+    for (size_t k : admitted) {
+      Request& r = active[k];
+      if (base.requireClosed && !host::is_closed(r.job->input)) {
+        failed[r.ticket] = {CUACD_E_INVALID, "input mesh is not closed (open or non-manifold edges)"};
+        r.job.reset();
+        continue;
+      }
+      fresh[engine_for(r.threshold)].push_back(r.job.get());
+    }
+    for (auto& kv : fresh) kv.first->begin(kv.second);
+    // one iteration of every admitted decomposition, per threshold
+    std::map<Engine*, std::vector<Job*>> groups;
+    for (Request& r : active)
+      if (r.job) groups[engine_for(r.threshold)].push_back(r.job.get());
+    for (auto& kv : groups) kv.first->iterate(kv.second);
+    // decompositions with nothing left to cut finish together
+    std::map<Engine*, std::vector<Job*>> fin;
+    for (Request& r : active)
+      if (r.job && r.job->cutting_done) fin[engine_for(r.threshold)].push_back(r.job.get());
+    for (auto& kv : fin) kv.first->finish(kv.second);
+    std::vector<Request> keep;
+    for (Request& r : active) {
+      if (!r.job) {
+        activeTris -= r.tris;
+        continue;
+      }
+      if (r.job->cutting_done) {
+        activeTris -= r.tris;
+        complete(r);
+        nDone++;
+      } else {
+        keep.push_back(std::move(r));
+      }
+    }
+    active.swap(keep);
+    if (completed) *completed = nDone;
+    return CUACD_OK;
   }
 };
 
@@ -842,35 +1016,10 @@ void* cuacd_decomposer_create(const cuacd_decompose_opts* o, int* err) {
     setErr(set_error(CUACD_E_INVALID, "cuacd_decomposer_create: null options"));
     return nullptr;
   }
-  if (o->width % 3 != 0 || o->width2 % 3 != 0) {
-    setErr(set_error(CUACD_E_INVALID, "width and width2 must be multiples of 3"));
-    return nullptr;
-  }
-  if (!(o->threshold > 0) || o->maxNCutting < 1 || o->maxIters < 0 || o->mergeRounds < 0) {
-    setErr(set_error(CUACD_E_INVALID, "cuacd_decomposer_create: invalid option"));
-    return nullptr;
-  }
-  std::unique_ptr<Engine> e(new Engine());
-  e->o = *o;
-  cuacd_tree_config cfg = o->tree;
-  cfg.width = o->width;
-  cfg.width2 = o->width2;
-  cfg.depth = o->depth;
-  cfg.nConcaveEdges = o->nConcaveEdges;
-  cfg.minEdgeDist = std::min(o->threshold / 4.0f, 0.015f);
   int rc = 0;
-  e->tree = cuacd_tree_create(&cfg, &rc);
-  if (!e->tree) {
-    setErr(rc ? rc : CUACD_E_INVALID);
-    return nullptr;
-  }
-  e->o.tree = cfg;
-  cuacd_set_profile(e->tree, o->profile);
-  e->planeSlots = cuacd_plane_slots(e->tree);
-  const unsigned hc = std::thread::hardware_concurrency();
-  e->threads = o->threads > 0 ? o->threads : (int)std::max(1u, hc);
-  setErr(CUACD_OK);
-  return e.release();
+  Engine* e = make_engine(*o, &rc);
+  setErr(rc);
+  return e;
 }
 
 void cuacd_decomposer_destroy(void* d) { delete static_cast<Engine*>(d); }
@@ -973,6 +1122,82 @@ int cuacd_result_stats(const void* r, int mesh, cuacd_decompose_stats* out) {
 }
 
 void cuacd_result_free(void* r) { delete static_cast<Result*>(r); }
+
+// ---- serving -----------------------------------------------------------
+
+void* cuacd_server_create(const cuacd_decompose_opts* o, uint64_t admitTris, int* err) {
+  if (!o) {
+    if (err) *err = set_error(CUACD_E_INVALID, "cuacd_server_create: null options");
+    return nullptr;
+  }
+  std::unique_ptr<Server> s(new Server());
+  s->base = *o;
+  s->admitTris = admitTris;
+  try {
+    s->engine_for(o->threshold);  // validates the options and builds the first tree
+  } catch (const Failure& f) {
+    if (err) *err = set_error(f.code, f.msg.c_str());
+    return nullptr;
+  }
+  if (err) *err = CUACD_OK;
+  return s.release();
+}
+
+void cuacd_server_destroy(void* s) { delete static_cast<Server*>(s); }
+
+int cuacd_server_submit(void* sv, const cuacd_mesh* m, float threshold, uint64_t* ticket) {
+  Server* s = static_cast<Server*>(sv);
+  if (!s || !m || !ticket || (m->nv && !m->verts) || (m->nt && !m->tris))
+    return set_error(CUACD_E_INVALID, "cuacd_server_submit: invalid argument");
+  Request r;
+  r.ticket = s->nextTicket++;
+  r.job.reset(new Job());
+  r.job->input.v.assign(m->verts, m->verts + 3 * (size_t)m->nv);
+  r.job->input.t.assign(m->tris, m->tris + 3 * (size_t)m->nt);
+  for (uint32_t x : r.job->input.t)
+    if (x >= m->nv) return set_error(CUACD_E_INVALID, "cuacd_server_submit: triangle index out of range");
+  r.submitted = Clock::now();
+  r.threshold = threshold > 0 ? threshold : s->base.threshold;
+  r.tris = m->nt;
+  *ticket = r.ticket;
+  s->queue.push_back(std::move(r));
+  return CUACD_OK;
+}
+
+int cuacd_server_step(void* sv, int* completed) {
+  Server* s = static_cast<Server*>(sv);
+  if (!s) return set_error(CUACD_E_INVALID, "cuacd_server_step: null server");
+  try {
+    return s->step(completed);
+  } catch (const Failure& f) {
+    return set_error(f.code, f.msg.c_str());
+  } catch (const std::bad_alloc&) {
+    return set_error(CUACD_E_CAPACITY, "cuacd_server_step: host memory exhausted");
+  }
+}
+
+int cuacd_server_pending(const void* sv) {
+  const Server* s = static_cast<const Server*>(sv);
+  return s ? (int)(s->queue.size() - s->queueHead + s->active.size()) : 0;
+}
+
+int cuacd_server_take(void* sv, uint64_t ticket, void** result) {
+  Server* s = static_cast<Server*>(sv);
+  if (!s || !result) return set_error(CUACD_E_INVALID, "cuacd_server_take: invalid argument");
+  *result = nullptr;
+  auto f = s->failed.find(ticket);
+  if (f != s->failed.end()) {
+    const int code = f->second.first;
+    const std::string msg = f->second.second;
+    s->failed.erase(f);
+    return set_error(code, msg.c_str());
+  }
+  auto it = s->done.find(ticket);
+  if (it == s->done.end()) return 1;
+  *result = it->second.release();
+  s->done.erase(it);
+  return CUACD_OK;
+}
 
 // ---- host geometry entry points ----------------------------------------
 

@@ -737,7 +737,15 @@ __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem
       hs.remapN = ncand;
     }
     Grp<G>::sync();
-    hull_insert<G>(h, hs, sm, pick, h.owner[pick]);
+    if (G > 32) {
+      // a visible patch is a few faces: the insertion's walk, horizon and
+      // linking run on the first warp with warp-level scans, the block
+      // meets once afterwards instead of at every step
+      if (threadIdx.x < 32) hull_insert<32>(h, hs, sm, pick, h.owner[pick]);
+      Grp<G>::sync();
+    } else {
+      hull_insert<G>(h, hs, sm, pick, h.owner[pick]);
+    }
     nIns++;
     if (hs.fail) break;
     const uint32_t nfNow = hs.nf;

@@ -72,6 +72,13 @@ def _lib():
         L.cuacd_cut_free.argtypes = [C.c_void_p]
         L.cuacd_concave_planes.argtypes = [P(A.MeshRef), C.c_int, C.c_double, C.c_double, C.c_uint32, P(C.c_float),
                                            C.c_int]
+        L.cuacd_server_create.restype = C.c_void_p
+        L.cuacd_server_create.argtypes = [P(A.DecomposeOpts), C.c_uint64, P(C.c_int)]
+        L.cuacd_server_destroy.argtypes = [C.c_void_p]
+        L.cuacd_server_submit.argtypes = [C.c_void_p, P(A.MeshRef), C.c_float, P(C.c_uint64)]
+        L.cuacd_server_step.argtypes = [C.c_void_p, P(C.c_int)]
+        L.cuacd_server_pending.argtypes = [C.c_void_p]
+        L.cuacd_server_take.argtypes = [C.c_void_p, C.c_uint64, P(C.c_void_p)]
         _bound = True
     return L
 
@@ -123,6 +130,33 @@ def _arr(ptr, n, dtype, width):
     return np.ctypeslib.as_array(ptr, shape=(n * width,)).astype(dtype, copy=True).reshape(n, width)
 
 
+def _take_results(res, n) -> list:
+    """Copies n meshes' results out of a result handle and frees it."""
+    L = _lib()
+    try:
+        out = []
+        for k in range(n):
+            parts = []
+            for p in range(L.cuacd_result_parts(res, k)):
+                v = A.PartView()
+                _check(L.cuacd_result_part(res, k, p, C.byref(v)))
+                seams = _arr(v.seams, v.nSeams, np.float64, 4)
+                parts.append(Part(
+                    mesh=Mesh(_arr(v.verts, v.nv, np.float32, 3), _arr(v.tris, v.nt, np.uint32, 3)),
+                    hull=Mesh(_arr(v.hullVerts, v.hullNv, np.float32, 3), _arr(v.hullTris, v.hullNt, np.uint32, 3)),
+                    meshVol=float(v.meshVol), hullVol=float(v.hullVol),
+                    hausdorff=None if math.isnan(v.hausdorff) else float(v.hausdorff),
+                    stuck=bool(v.stuck), stuckReason=STUCK_REASONS.get(v.stuckReason),
+                    seams=[tuple(float(x) for x in s) for s in seams], merged=int(v.merged)))
+            st = A.DecomposeStats()
+            _check(L.cuacd_result_stats(res, k, C.byref(st)))
+            stats = {name: getattr(st, name) for name, _ in A.DecomposeStats._fields_}
+            out.append(DecomposeResult(parts=parts, iterations=int(st.iterations), stats=stats))
+        return out
+    finally:
+        L.cuacd_result_free(res)
+
+
 class Decomposer:
     """Decomposer (decompose.ts:128-392): one GPU tree, reused across calls."""
 
@@ -150,28 +184,7 @@ class Decomposer:
         ma = A.MeshArray([A.as_mesh(m) for m in meshes])
         res = C.c_void_p()
         _check(L.cuacd_decompose(self.h, ma.arr, ma.n, int(batched), C.byref(res)))
-        try:
-            out = []
-            for k in range(ma.n):
-                parts = []
-                for p in range(L.cuacd_result_parts(res, k)):
-                    v = A.PartView()
-                    _check(L.cuacd_result_part(res, k, p, C.byref(v)))
-                    seams = _arr(v.seams, v.nSeams, np.float64, 4)
-                    parts.append(Part(
-                        mesh=Mesh(_arr(v.verts, v.nv, np.float32, 3), _arr(v.tris, v.nt, np.uint32, 3)),
-                        hull=Mesh(_arr(v.hullVerts, v.hullNv, np.float32, 3), _arr(v.hullTris, v.hullNt, np.uint32, 3)),
-                        meshVol=float(v.meshVol), hullVol=float(v.hullVol),
-                        hausdorff=None if math.isnan(v.hausdorff) else float(v.hausdorff),
-                        stuck=bool(v.stuck), stuckReason=STUCK_REASONS.get(v.stuckReason),
-                        seams=[tuple(float(x) for x in s) for s in seams], merged=int(v.merged)))
-                st = A.DecomposeStats()
-                _check(L.cuacd_result_stats(res, k, C.byref(st)))
-                stats = {name: getattr(st, name) for name, _ in A.DecomposeStats._fields_}
-                out.append(DecomposeResult(parts=parts, iterations=int(st.iterations), stats=stats))
-            return out
-        finally:
-            L.cuacd_result_free(res)
+        return _take_results(res, ma.n)
 
     def decompose(self, mesh) -> DecomposeResult:
         return self.decompose_many([mesh], batched=False)[0]
@@ -193,6 +206,57 @@ def decompose_batch(meshes, batched: bool = True, **options) -> list:
         return d.decompose_many(meshes, batched=batched)
     finally:
         d.destroy()
+
+
+class Server:
+    """Continuous batching of decompositions (cuacd_server_*): submit
+    meshes at any time, step the server, take finished results. Each step
+    runs one iteration of every admitted decomposition together; requests
+    are admitted in arrival order while the admitted triangles stay within
+    admit_tris."""
+
+    def __init__(self, admit_tris: int = 8 << 20, **options):
+        L = _lib()
+        self.opts = _opts(dict(options))
+        err = C.c_int(0)
+        self.h = L.cuacd_server_create(C.byref(self.opts), C.c_uint64(int(admit_tris)), C.byref(err))
+        if not self.h:
+            raise CuacdError(err.value, L.cuacd_last_error().decode())
+
+    def destroy(self):
+        if getattr(self, "h", None):
+            _lib().cuacd_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    def submit(self, mesh, threshold: float = 0.0) -> int:
+        ma = A.MeshArray([A.as_mesh(mesh)])
+        t = C.c_uint64()
+        _check(_lib().cuacd_server_submit(self.h, ma.arr, C.c_float(threshold), C.byref(t)))
+        return int(t.value)
+
+    def step(self) -> int:
+        n = C.c_int(0)
+        _check(_lib().cuacd_server_step(self.h, C.byref(n)))
+        return int(n.value)
+
+    @property
+    def pending(self) -> int:
+        return int(_lib().cuacd_server_pending(self.h))
+
+    def take(self, ticket: int):
+        """The DecomposeResult of a finished request, or None while it runs."""
+        res = C.c_void_p()
+        rc = _lib().cuacd_server_take(self.h, C.c_uint64(ticket), C.byref(res))
+        if rc == 1:
+            return None
+        _check(rc)
+        return _take_results(res, 1)[0]
 
 
 def plane_cut(mesh, plane):

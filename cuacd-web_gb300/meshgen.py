@@ -262,3 +262,53 @@ def blob_batch(n_meshes: int = 256, seed: int = 0, tri_range=(500, 60000)):
         g = int(np.clip(round(g0 * np.sqrt(target / max(m0.nt, 1))), 8, 400))
         out.append(blob_mesh(nb, g, seed=seed * 100003 + k))
     return out
+
+
+def carved_sphere(level: int = 4, n_holes: int = 3, seed: int = 0) -> Mesh:
+    """A unit sphere minus n_holes seeded spheres (centres near the surface,
+    radii 0.2..0.6), meshed from its signed distance by marching tetrahedra
+    on a grid sized so the triangle count is near an icosphere of `level`
+    (20 * 4^level)."""
+    rng = np.random.default_rng(seed)
+    d = rng.normal(size=(n_holes, 3))
+    c = d / np.linalg.norm(d, axis=1, keepdims=True) * rng.uniform(0.6, 1.1, (n_holes, 1))
+    r = rng.uniform(0.2, 0.6, n_holes)
+
+    def field(g):
+        ax = np.linspace(-1.25, 1.25, g)
+        X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij", sparse=True)
+        sd = np.sqrt(X * X + Y * Y + Z * Z) - 1.0
+        for k in range(n_holes):
+            hole = np.sqrt((X - c[k, 0]) ** 2 + (Y - c[k, 1]) ** 2 + (Z - c[k, 2]) ** 2) - r[k]
+            sd = np.maximum(sd, -hole)
+        f = -sd
+        return np.where(f == 0.0, -1e-12, f)
+
+    target = 20 * 4 ** level
+    g0 = 24
+    m0 = isosurface(field(g0), (-1.25,) * 3, (1.25,) * 3, 0.0)
+    g = int(np.clip(round(g0 * np.sqrt(target / max(m0.nt, 1))), 8, 400))
+    return isosurface(field(g), (-1.25,) * 3, (1.25,) * 3, 0.0)
+
+
+def serving_mix(n: int, seed: int = 0):
+    """The serving workload's request mix: 40% staircases of 4..16 steps,
+    40% Gaussian-blob isosurfaces of 2k..60k triangles, 20% icospheres of
+    level 3..5 carved by 1..6 spheres; thresholds drawn from {0.05, 0.1}.
+    Returns (kind, mesh, threshold) triples."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        u = rng.uniform()
+        thr = float(rng.choice([0.05, 0.1]))
+        if u < 0.4:
+            out.append(("staircase", staircase(int(rng.integers(4, 17))), thr))
+        elif u < 0.8:
+            nb = int(rng.integers(2, 33))
+            target = float(np.exp(rng.uniform(np.log(2000), np.log(60000))))
+            m0 = blob_mesh(nb, 24, seed=seed * 7919 + k)
+            g = int(np.clip(round(24 * np.sqrt(target / max(m0.nt, 1))), 8, 400))
+            out.append(("blob", blob_mesh(nb, g, seed=seed * 7919 + k), thr))
+        else:
+            out.append(("carved", carved_sphere(int(rng.integers(3, 6)), int(rng.integers(1, 7)), seed=seed * 7919 + k), thr))
+    return out

@@ -58,7 +58,9 @@ typedef struct {
   uint64_t scratchWords;
   uint64_t hullBudgetBytes; /* bytes of hull scratch slabs in flight */
   int32_t pruneLastLevel;   /* last-level branch and bound (tree.ts:29-30) */
-  int32_t reserved;
+  int32_t warpMaxNv;        /* hulls of parts up to this many points run on one
+                               warp each, larger ones on a 256-thread block
+                               (0: 1024); the results do not depend on it */
 } cuacd_tree_config;
 
 /* Mesh (mesh.ts:7-10): nv vertices (3 floats each), nt triangles (3 u32). */
@@ -294,6 +296,26 @@ int cuacd_result_parts(const void* result, int mesh);
 int cuacd_result_part(const void* result, int mesh, int part, cuacd_part_view* out);
 int cuacd_result_stats(const void* result, int mesh, cuacd_decompose_stats* out);
 void cuacd_result_free(void* result);
+
+/* Serving (no counterpart in the reference, whose decompose serves one mesh
+ * per call): continuous batching of decompositions. Requests queue in
+ * arrival order and are admitted while the admitted meshes' triangles stay
+ * within admitTris (one is always admitted). Each cuacd_server_step runs one
+ * iteration of every admitted decomposition together, one tree launch per
+ * threshold, and finishes (merge pass included) the decompositions with
+ * nothing left to cut; a request submitted between steps joins at the next
+ * one. A decomposition's parts are the same as cuacd_decompose gives it.
+ * threshold <= 0 takes the options' threshold; other values get a tree of
+ * their own (minEdgeDist follows the threshold). cuacd_server_take returns
+ * CUACD_OK with a one-mesh result handle (cuacd_result_* accessors; stats
+ * totalMs = time from submission to completion) once the request finished,
+ * 1 while it is queued or running, or the request's error. */
+void* cuacd_server_create(const cuacd_decompose_opts* o, uint64_t admitTris, int* err);
+void cuacd_server_destroy(void* server);
+int cuacd_server_submit(void* server, const cuacd_mesh* mesh, float threshold, uint64_t* ticket);
+int cuacd_server_step(void* server, int* completed);
+int cuacd_server_pending(const void* server);
+int cuacd_server_take(void* server, uint64_t ticket, void** result);
 
 /* planeCut with caps (src/cpu/cut.ts:33-315) on the host, for callers that
  * apply a cut themselves. plane = a, b, c, d (a x + b y + c z + d = 0). On

@@ -82,6 +82,32 @@ def test_batched_equals_one_at_a_time():
         _same(b, a)
 
 
+def test_server_same_alone_and_in_the_mix():
+    """Continuous batching: requests arrive while others run, with two
+    thresholds; every result equals the mesh decomposed alone."""
+    opts = dict(maxIters=20, threshold=0.05, width=6, depth=2, tree=SMALL_TREE)
+    meshes = [M.l_shape(), stairs(), square_torus(), G.staircase(6), G.noisy_icosphere(2, seed=4), M.unit_cube()]
+    thresholds = [0.05, 0.1, 0.05, 0.1, 0.05, 0.05]
+    s = D.Server(admit_tris=200, **opts)
+    try:
+        tickets = {}
+        arrivals = {0: [0, 1], 1: [2], 2: [3, 4], 4: [5]}
+        step = 0
+        while step < 200 and (len(tickets) < len(meshes) or s.pending):
+            for k in arrivals.get(step, []):
+                tickets[k] = s.submit(meshes[k], thresholds[k])
+            s.step()
+            step += 1
+        got = {k: s.take(t) for k, t in tickets.items()}
+    finally:
+        s.destroy()
+    assert all(r is not None for r in got.values())
+    for k, m in enumerate(meshes):
+        alone = D.decompose(m, **dict(opts, threshold=thresholds[k]))
+        _same(got[k], alone)
+        assert got[k].stats["totalMs"] > 0
+
+
 def test_staircase_configuration():
     # the staircase decomposition's settings: threshold 0.1, width 6,
     # width2 3, depth 3, maxNCutting 160, 16 concave edges, 2 refinement
