@@ -187,7 +187,7 @@ def run_reference(args):
     if rank != 0:
         return
     n = host_threads()
-    sample = max(n, 32)
+    sample = 8 * n  # each step about half a second of work on all host threads
     seeds, planes, refine = workload(sample)
     for _ in range(args.warmup):
         cpu_tree_rate(seeds[:n], planes[:n], refine, n)
@@ -294,8 +294,10 @@ def run_engine(args):
     # ---- roofline of the dominant kernel ----
     dom = max((k for k in kms if k in ("plan", "emit", "hull", "scan", "record")), key=lambda k: kms[k])
     depth, stages = TREE["depth"], 1 + REFINE_ROUNDS
+    # a level's hull step is two launches (warp and 256-thread groups), timed
+    # together; on the staircase only the warp launch has parts
     launches_per_step = {"plan": depth * stages, "scan": depth * stages, "emit": depth * stages,
-                         "hull": 2 * depth * stages, "record": depth * stages}
+                         "hull": depth * stages, "record": depth * stages}
     byte_idx = {"plan": 0, "emit": 1, "hull": 2}
     peak, peak_kind = peaks()
     roof = None
@@ -314,11 +316,13 @@ def run_engine(args):
             "e2e": {"value": world * e2e_c / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1000 * e2e_s / args.steps},
             "roofline": roof, "clocks": clk.summary(),
-            "gpu_launches": args.steps * stages * (depth * 6 + 1),
+            # per level: plan, scan sums, scan, emit, two hull widths,
+            # record; per stage one evaluate
+            "gpu_launches": args.steps * stages * (depth * 7 + 1),
             "candidates_per_step": cands / args.steps}
     if world == 1 and not args.no_cpu_baseline:
         nthr = host_threads()
-        sample = 2 * nthr
+        sample = 64 * nthr  # several seconds of CPU work on the host's cores
         s2, p2, r2 = workload(sample)
         c, s = cpu_tree_rate(s2, p2, r2, nthr)
         line["cpu_baseline"] = {"value": c / s, "unit": UNIT, "cores": nthr, "kind": "port",

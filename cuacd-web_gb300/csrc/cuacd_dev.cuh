@@ -83,7 +83,8 @@ struct Level {
   uint32_t exportBase, exportStride;  // hull face export into T (u32 offsets)
   uint32_t lastLevel, hullStage, nSeeds;
   uint32_t hdDescBase;      // != 0: write a Hausdorff descriptor at part + hdDescBase
-  uint32_t workSlot;        // hull work counter of this launch (D.work)
+  uint32_t workSlot;        // hull work counters of this launch: D.work[slot] (warp
+                            // groups) and D.work[16 + slot] (256-thread groups)
   uint32_t maxNvHint;       // largest part the host knows of, or 0: read D.work[32 + workSlot]
 };
 

@@ -26,9 +26,9 @@ void launch_emit(const Level& P, const Dev& D, bool big, cudaStream_t s);
 void launch_record(const Level& P, const Dev& D, cudaStream_t s);
 void launch_evaluate(uint32_t stateBase, uint32_t headerOff, uint32_t mode, uint32_t nSeeds, uint32_t jobBase,
                      uint32_t edgePlaneBase, uint32_t edgeStride, const Dev& D, cudaStream_t s);
-void launch_hull(const Level& P, const Dev& D, bool warps, cudaStream_t s);
+void launch_hull(const Level& P, const Dev& D, int width, cudaStream_t s);
 void launch_hd(const HdArgs& A, const Dev& D, cudaStream_t s);
-int hull_blocks_per_sm(bool warps);
+int hull_blocks_per_sm(int width);
 }  // namespace cuacd
 
 using namespace cuacd;
@@ -52,7 +52,9 @@ int set_error(int code, const char* msg) { return fail(code, msg); }
   } while (0)
 
 static const uint32_t VIS_MAX = CUACD_VIS_MAX;
-// parts with at most this many points get a warp per hull, larger ones a block
+// parts with at most SMALL_NV points get a warp per hull, larger ones a
+// 256-thread block (narrower blocks for mid-sized parts measured slower: the
+// passes over all points and candidates need the width)
 static const uint32_t SMALL_NV = 1024;
 // parents with more points than this get a block per plan / emit job
 static const uint32_t BIG_JOB_NV = 2048;
@@ -218,13 +220,14 @@ struct Tree {
     P.smallNv = cfg.warpMaxNv > 0 ? (uint32_t)cfg.warpMaxNv : SMALL_NV;
     return P;
   }
-  // hull launches of one level; work counter `slot` must be zero beforehand
+  // hull launches of one level, warp groups then 256-thread groups; work
+  // counters `slot` and 16 + slot must be zero beforehand
   void hullLaunch(Level P, uint32_t slot) {
     P.workSlot = slot;
     P.nSlabs = nSlabsSmall;
-    launch_hull(P, D, true, stream);
+    launch_hull(P, D, 32, stream);
     P.nSlabs = nSlabsBig;
-    launch_hull(P, D, false, stream);
+    launch_hull(P, D, 256, stream);
   }
   // upload meshes at the start of the pools and write their part descriptors
   // (tree.ts:233-278); returns the host-side descriptors in parts
@@ -552,7 +555,7 @@ struct Tree {
     P.exportBase = tTop; P.exportStride = stride; P.hullStage = (uint32_t)hullStage;
     P.hdDescBase = withHd ? (uint32_t)n : 0;
     P.maxNvHint = std::max(maxNv, 1u);
-    CK(cudaMemsetAsync(D.work, 0, 4, stream));
+    CK(cudaMemsetAsync(D.work, 0, 64 * 4, stream));
     CK(cudaEventRecord(ev0, stream));
     hullLaunch(P, 0);
     if (withHd) {
@@ -722,8 +725,8 @@ void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
   t->edgeStride = (uint32_t)std::max(4 * c->nConcaveEdges, 32);
   cudaGetDevice(&t->device);
   cudaDeviceGetAttribute(&t->nSM, cudaDevAttrMultiProcessorCount, t->device);
-  t->bpsSmall = hull_blocks_per_sm(true);
-  t->bpsBig = hull_blocks_per_sm(false);
+  t->bpsSmall = hull_blocks_per_sm(32);
+  t->bpsBig = hull_blocks_per_sm(256);
   int rc = 0;
   if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&t->ev0) != cudaSuccess || cudaEventCreate(&t->ev1) != cudaSuccess) {

@@ -1236,8 +1236,11 @@ restart:
   }
 }
 
-// Persistent groups: group s owns slab s and walks parts s, s + nSlabs, ...
-// Warp groups take parts with nv <= smallNv, block groups the others.
+// Persistent groups: group s owns slab s and takes the launch's parts from a
+// counter, so parts of uneven size balance across the GPU. Warps take parts
+// with nv <= smallNv, 256-thread blocks the others: an insertion touches a
+// few faces and runs on one warp either way, the block's width serves the
+// passes over all points and candidates, which grow with nv.
 template <int G>
 __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
   __shared__ GrpSmem gsm[Grp<G>::PER_BLOCK];
@@ -1248,13 +1251,25 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
   const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
   if (s >= P.nSlabs) return;
   if (G != 32) {
-    // block groups only serve parts above smallNv: leave at once when the
-    // level has none (the scan recorded its largest child)
+    // leave at once when the level has no part above smallNv (the scan
+    // recorded its largest child)
     const uint32_t mx = P.maxNvHint ? P.maxNvHint : D.work[32 + P.workSlot];
     if (mx <= P.smallNv) return;
   }
   uint32_t* slab = D.slab + (size_t)s * P.slabStride;
-  if (G == 32) {
+  if (G != 32) {
+    for (;;) {
+      uint32_t idx = 0;
+      if (threadIdx.x == 0) idx = atomicAdd(D.work + 16 + P.workSlot, 1u);
+      idx = grp_bcast_u<G>(idx, gsm[0]);
+      if (idx >= P.nChildParts) break;
+      if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr);
+      Grp<G>::sync();
+    }
+    return;
+  }
+  {
     // warp groups take the next part from the launch's counter, so parts of
     // uneven size balance across the GPU
     const int lane = threadIdx.x & 31;
@@ -1267,25 +1282,21 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
       hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], qcs + gi * 3 * QC_MAX, tsm + gi);
       Grp<G>::sync();
     }
-  } else {
-    for (uint32_t idx = s; idx < P.nChildParts; idx += P.nSlabs) {
-      if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr);
-      Grp<G>::sync();
-    }
   }
 }
 
-int hull_blocks_per_sm(bool warps) {
+// resident blocks per SM of the hull kernel of group width 32 or 256
+int hull_blocks_per_sm(int width) {
   int n = 0;
-  if (warps) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<32>, 256, 0);
+  if (width == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<32>, 256, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<256>, 256, 0);
   return n > 0 ? n : 1;
 }
 
-void launch_hull(const Level& P, const Dev& D, bool warps, cudaStream_t s) {
+// hull launch of one group width (32 or 256) over P.nSlabs groups
+void launch_hull(const Level& P, const Dev& D, int width, cudaStream_t s) {
   if (P.nChildParts == 0 || P.nSlabs == 0) return;
-  if (warps) k_hull<32><<<(P.nSlabs + 7) / 8, 256, 0, s>>>(P, D);
+  if (width == 32) k_hull<32><<<(P.nSlabs + 7) / 8, 256, 0, s>>>(P, D);
   else k_hull<256><<<P.nSlabs, 256, 0, s>>>(P, D);
 }
 
