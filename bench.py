@@ -317,8 +317,8 @@ def run_engine(args):
                     "ms_per_step": 1000 * e2e_s / args.steps},
             "roofline": roof, "clocks": clk.summary(),
             # per level: plan, scan sums, scan, emit, two hull widths,
-            # record; per stage one evaluate
-            "gpu_launches": args.steps * stages * (depth * 7 + 1),
+            # record; per stage the last level's seed bound and one evaluate
+            "gpu_launches": args.steps * stages * (depth * 7 + 2),
             "candidates_per_step": cands / args.steps}
     if world == 1 and not args.no_cpu_baseline:
         nthr = host_threads()

@@ -66,6 +66,7 @@ struct Dev {
   uint32_t* ctr;
   unsigned long long* scanTmp;  // scan bases and per-block sums (3 + 3 * blocks)
   uint32_t* work;               // hull work counters, one per hull launch of a run
+  float* ub;                    // per seed: the last level's pruning upper bound
   uint64_t vCap, tCap, eCap, sCap;
 };
 

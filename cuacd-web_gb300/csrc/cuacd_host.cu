@@ -24,6 +24,7 @@ void launch_plan(const Level& P, const Dev& D, bool big, cudaStream_t s);
 void launch_scan(const Level& P, const Dev& D, cudaStream_t s);
 void launch_emit(const Level& P, const Dev& D, bool big, cudaStream_t s);
 void launch_record(const Level& P, const Dev& D, cudaStream_t s);
+void launch_seed_bound(const Level& P, const Dev& D, cudaStream_t s);
 void launch_evaluate(uint32_t stateBase, uint32_t headerOff, uint32_t mode, uint32_t nSeeds, uint32_t jobBase,
                      uint32_t edgePlaneBase, uint32_t edgeStride, const Dev& D, cudaStream_t s);
 void launch_hull(const Level& P, const Dev& D, int width, cudaStream_t s);
@@ -126,7 +127,7 @@ struct Tree {
     pcls.push_back(cls);
   }
   Dev D{};
-  DevBuf bV, bT, bE, bS, bCtr, bSlab, bParts, bItems, bJobs, bPlanes, bSnap, bHd, bScan, bWork;
+  DevBuf bV, bT, bE, bS, bCtr, bSlab, bParts, bItems, bJobs, bPlanes, bSnap, bHd, bScan, bWork, bUb;
   uint32_t workSlots = 0;  // hull launches of the prepared run
   HostBuf hStage, hRead, hSnap, hMeta;
   uint32_t capSeeds = 0, capJobs = 0, capItems = 0, capParts = 0, capPlanes = 0;
@@ -146,7 +147,7 @@ struct Tree {
 
   ~Tree() {
     if (gexec) cudaGraphExecDestroy(gexec);
-    for (DevBuf* b : {&bV, &bT, &bE, &bS, &bCtr, &bSlab, &bParts, &bItems, &bJobs, &bPlanes, &bSnap, &bHd, &bScan, &bWork}) b->release();
+    for (DevBuf* b : {&bV, &bT, &bE, &bS, &bCtr, &bSlab, &bParts, &bItems, &bJobs, &bPlanes, &bSnap, &bHd, &bScan, &bWork, &bUb}) b->release();
     for (HostBuf* b : {&hStage, &hRead, &hSnap, &hMeta}) b->release();
     for (cudaEvent_t e : pev) cudaEventDestroy(e);
     if (ev0) cudaEventDestroy(ev0);
@@ -157,7 +158,7 @@ struct Tree {
     D.V = (float*)bV.p; D.T = (uint32_t*)bT.p; D.E = (uint32_t*)bE.p; D.S = (uint32_t*)bS.p;
     D.slab = (uint32_t*)bSlab.p; D.parts = (PartDesc*)bParts.p; D.items = (ItemDesc*)bItems.p;
     D.jobs = (Job*)bJobs.p; D.planes = (float4*)bPlanes.p; D.ctr = (uint32_t*)bCtr.p;
-    D.scanTmp = (unsigned long long*)bScan.p; D.work = (uint32_t*)bWork.p;
+    D.scanTmp = (unsigned long long*)bScan.p; D.work = (uint32_t*)bWork.p; D.ub = (float*)bUb.p;
     D.vCap = cfg.vertexCap; D.tCap = cfg.triCap; D.eCap = cfg.edgeCap; D.sCap = cfg.scratchWords;
   }
   // tree.ts:191-213
@@ -178,6 +179,7 @@ struct Tree {
     if ((rc = bItems.ensure(nItems * sizeof(ItemDesc)))) return rc;
     if ((rc = bJobs.ensure(std::max<uint64_t>(totalJobs, 1) * sizeof(Job)))) return rc;
     if ((rc = bPlanes.ensure(std::max<uint64_t>(nPlanes, 1) * 16))) return rc;
+    if ((rc = bUb.ensure((size_t)n * 4))) return rc;
     capSeeds = n; capJobs = (uint32_t)totalJobs; capItems = (uint32_t)nItems; capParts = (uint32_t)nParts;
     capPlanes = (uint32_t)nPlanes;
     gvalid = false;
@@ -404,6 +406,9 @@ struct Tree {
         mark(2);
         launch_emit(P, D, big, stream);
         mark(3);
+        // the last level's pruning bound, once per seed (the parent level's
+        // items are final once its record ran)
+        if (P.lastLevel && P.level > 0 && P.nSeeds > 0 && P.nItemsIn > 0) launch_seed_bound(P, D, stream);
         hullLaunch(P, l);
         mark(4);
         launch_record(P, D, stream);

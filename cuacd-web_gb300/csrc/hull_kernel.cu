@@ -1133,19 +1133,8 @@ restart:
     const ItemDesc* pit = D.items + P.itemsInBase + jb->parentItem;
     float ssum = 0.0f;
     for (uint32_t l = 0; l < pit->nLevels; l++) ssum += pit->levelCosts[l];
-    const uint32_t perSeed = P.nItemsIn / P.nSeeds;
-    const uint32_t srcPart = pit->srcPart;
-    float ubMin = 1e30f;
-    for (uint32_t i = lid; i < perSeed; i += G) {
-      const ItemDesc* it = D.items + P.itemsInBase + srcPart * perSeed + i;
-      if (it->flags == 1 && it->nLevels > 0) {
-        float ps = 0.0f;
-        for (uint32_t l = 0; l < it->nLevels; l++) ps += it->levelCosts[l];
-        float u = ps + it->levelCosts[it->nLevels - 1] * (float)(P.totalLevels - it->nLevels);
-        ubMin = fminf(ubMin, u);
-      }
-    }
-    const float ub = grp_min_f<G>(ubMin, sm);
+    // the seed's best completed-path upper bound (k_seed_bound)
+    const float ub = D.ub[pit->srcPart];
     const float vRough = (float)(hull_volume_grid<G>(h, hs, sm) * (double)volScale);
     const float bound = ssum + rv_cost(meshVol, vRough);
     if (bound > ub) {

@@ -612,6 +612,33 @@ __global__ void __launch_bounds__(256) k_emit(const Level P, const Dev D) {
   }
 }
 
+// ============ last-level pruning bound per seed (shaders.ts:1300-1315) ============
+// The reference's hull kernel computes, for every part of the last level, the
+// best completed-path upper bound over its seed's parent-level items; the
+// bound is the same for every part of a seed, so one warp per seed computes
+// it once (same operations, same float32 rounding) and the hulls read it.
+__global__ void __launch_bounds__(256) k_seed_bound(const Level P, const Dev D) {
+  const uint32_t s = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const uint32_t lane = threadIdx.x & 31;
+  if (s >= P.nSeeds) return;
+  const uint32_t perSeed = P.nItemsIn / P.nSeeds;
+  float ubMin = 1e30f;
+  for (uint32_t i = lane; i < perSeed; i += 32) {
+    const ItemDesc* it = D.items + P.itemsInBase + s * perSeed + i;
+    if (it->flags == 1 && it->nLevels > 0) {
+      float ps = 0.0f;
+      for (uint32_t l = 0; l < it->nLevels; l++) ps += it->levelCosts[l];
+      const float u = ps + it->levelCosts[it->nLevels - 1] * (float)(P.totalLevels - it->nLevels);
+      ubMin = fminf(ubMin, u);
+    }
+  }
+  ubMin = warp_min_f(ubMin);
+  if (lane == 0) D.ub[s] = ubMin;
+}
+void launch_seed_bound(const Level& P, const Dev& D, cudaStream_t s) {
+  k_seed_bound<<<(P.nSeeds + 7) / 8, 256, 0, s>>>(P, D);
+}
+
 // ======================= record (shaders.ts:1519-1544) =======================
 __global__ void __launch_bounds__(256) k_record(const Level P, const Dev D) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
