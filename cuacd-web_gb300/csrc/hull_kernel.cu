@@ -854,7 +854,7 @@ __device__ __noinline__ uint32_t hull_assign_all(const HullCtx& h, GrpSmem& sm, 
 
 // exact volume of the alive faces, in grid units
 template <int G>
-__device__ double hull_volume_grid(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
+__device__ __noinline__ double hull_volume_grid(const HullCtx& h, HullSm& hs, GrpSmem& sm) {
   const int lid = Grp<G>::lid();
   uint32_t a0, b0, c0;
   h.abc(0, a0, b0, c0);
@@ -1136,8 +1136,20 @@ restart:
     // the seed's best completed-path upper bound (k_seed_bound)
     const float ub = D.ub[pit->srcPart];
     const float vRough = (float)(hull_volume_grid<G>(h, hs, sm) * (double)volScale);
-    const float bound = ssum + rv_cost(meshVol, vRough);
-    if (bound > ub) {
+    // bound = ssum + rv_cost(meshVol, vRough) > ub, decided with a float32
+    // cube root when it clears the comparison by more than its error (cbrtf
+    // and the products are within 1e-6 relative of rv_cost's double form,
+    // so a margin of 1e-5 of the operands is safe); the double form, which
+    // is slow on this GPU, only runs near the boundary
+    const float gapf = fmaxf(vRough - meshVol, 0.0f);
+    const float rvf = 0.3f * cbrtf(0.2387324f * gapf);
+    const float boundf = ssum + rvf;
+    const float margin = 1e-5f * (fabsf(ssum) + rvf + fabsf(meshVol) + fabsf(vRough)) + 1e-30f;
+    bool prune;
+    if (boundf > ub + margin) prune = true;
+    else if (boundf < ub - margin) prune = false;
+    else prune = ssum + rv_cost(meshVol, vRough) > ub;
+    if (prune) {
       if (lid == 0) {
         pdp->hullVol = vRough;
         pdp->flags = pdp->flags | 4u;
