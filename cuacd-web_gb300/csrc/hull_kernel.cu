@@ -514,8 +514,10 @@ __device__ __forceinline__ uint4 shfl4(uint4 v, uint32_t src) {
 // Returns the number of insertions, or CUACD_NONE when the hull outgrows
 // the warp (the caller then builds it again in the slot-array form). A
 // face-slot failure sets hs.fail = 2 as hull_insert does.
+// Candidates on lanes below nInit start without an owner and are assigned
+// over every face first (the seed phase's assignment over the simplex).
 __device__ __noinline__ uint32_t hull_tiny_grow(const HullCtx& h, HullSm& hs, TinySm& ts, uint32_t maxIter,
-                                                uint32_t ci, uint32_t co, float cd) {
+                                                uint32_t ci, uint32_t co, float cd, uint32_t nInit) {
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t lt = lanemask_lt();
   uint32_t nalive = hs.nalive, nfRef = hs.nfRef;
@@ -530,7 +532,28 @@ __device__ __noinline__ uint32_t hull_tiny_grow(const HullCtx& h, HullSm& hs, Ti
   }
   uint32_t nIns = 0;
   bool outgrown = false;
-  for (uint32_t iter = 0; iter < maxIter; iter++) {
+  // candidates waiting for a (re)assignment over faces [lo, nalive)
+  uint32_t R = __ballot_sync(FULLMASK, lane < nInit);
+  uint32_t lo = 0;
+  for (uint32_t iter = 0;; iter++) {
+    // reassign the candidates whose owner died in the last insertion (all of
+    // them after a compaction) over its new faces (every face after a
+    // compaction); a face ranks first in slot order on ties
+    while (R) {
+      const uint32_t r = __ffs(R) - 1;
+      R &= R - 1;
+      const uint32_t pr = __shfl_sync(FULLMASK, ci, r);
+      float v = -1.0f;
+      if (lane >= lo && lane < nalive) v = tiny_eval(h, F, h.qvert(pr), pr);
+      const uint32_t vk = v > 0.0f ? __float_as_uint(v) : 0u;
+      const uint32_t best = __reduce_max_sync(FULLMASK, vk);
+      const unsigned at = __ballot_sync(FULLMASK, best != 0u && vk == best);
+      if (lane == r) {
+        co = best != 0u ? (uint32_t)(__ffs(at) - 1) : CUACD_NONE;
+        cd = best != 0u ? __uint_as_float(best) : 0.0f;
+      }
+    }
+    if (iter == maxIter) break;
     // the farthest candidate, lowest point index on ties
     const uint32_t key = co != CUACD_NONE ? __float_as_uint(cd) : 0u;
     const uint32_t mk = __reduce_max_sync(FULLMASK, key);
@@ -606,32 +629,17 @@ __device__ __noinline__ uint32_t hull_tiny_grow(const HullCtx& h, HullSm& hs, Ti
       F.nb2 = ts.hB[a];
     }
     __syncwarp();
-    const uint32_t nNow = nS + nnew;
-    // reassign the candidates whose owner died (all of them after a
-    // compaction) over the new faces (every face after a compaction)
+    // owners that survived move down with their faces; the others wait for
+    // the reassignment at the top of the next pass
     if (ci == pick) co = CUACD_NONE;
     bool need = false;
     if (co != CUACD_NONE) {
       if (compacted || ((C >> co) & 1u)) need = true;
       else co = __popc(S & ((1u << co) - 1u));
     }
-    uint32_t R = __ballot_sync(FULLMASK, need);
-    const uint32_t lo = compacted ? 0u : nS;
-    while (R) {
-      const uint32_t r = __ffs(R) - 1;
-      R &= R - 1;
-      const uint32_t pr = __shfl_sync(FULLMASK, ci, r);
-      float v = -1.0f;
-      if (lane >= lo && lane < nNow) v = tiny_eval(h, F, h.qvert(pr), pr);
-      const uint32_t vk = v > 0.0f ? __float_as_uint(v) : 0u;
-      const uint32_t best = __reduce_max_sync(FULLMASK, vk);
-      const unsigned at = __ballot_sync(FULLMASK, best != 0u && vk == best);
-      if (lane == r) {
-        co = best != 0u ? (uint32_t)(__ffs(at) - 1) : CUACD_NONE;
-        cd = best != 0u ? __uint_as_float(best) : 0.0f;
-      }
-    }
-    nalive = nNow;
+    R = __ballot_sync(FULLMASK, need);
+    lo = compacted ? 0u : nS;
+    nalive = nS + nnew;
     nfRef += nnew;
   }
   __syncwarp();
@@ -798,7 +806,7 @@ __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem
 // with an owner, in index order. Each thread holds up to ASSIGN_K points in
 // registers and the slots are read once per ASSIGN_K * G points, the next
 // slot's record loading while the current one is evaluated.
-#define ASSIGN_K 4
+#define ASSIGN_K 2
 template <int G>
 __device__ __noinline__ uint32_t hull_assign_all(const HullCtx& h, GrpSmem& sm, uint32_t nf) {
   const int lid = Grp<G>::lid();
@@ -1097,15 +1105,10 @@ restart:
   uint32_t nIns;
   bool tinyUsed = false;
   if (tiny && nuniq <= TINY_SEEDS) {
-    uint32_t ci = 0, co = CUACD_NONE;
-    float cd = 0.0f;
-    if ((uint32_t)lid < nuniq) {
-      ci = h.cand[lid];
-      h.best_face(ci, 0, 4, co, cd);
-    }
+    const uint32_t ci = (uint32_t)lid < nuniq ? h.cand[lid] : 0u;
     if (lid == 0) hs.nfRef = 4;
     __syncwarp();
-    nIns = hull_tiny_grow(h, hs, *ts, 80, ci, co, cd);
+    nIns = hull_tiny_grow(h, hs, *ts, 80, ci, CUACD_NONE, 0.0f, nuniq);
     if (nIns == CUACD_NONE) {
       tiny = false;
       goto restart;
@@ -1178,7 +1181,7 @@ restart:
       co = h.owner[ci];
       cd = h.dist[ci];
     }
-    const uint32_t n2 = hull_tiny_grow(h, hs, *ts, maxIter, ci, co, cd);
+    const uint32_t n2 = hull_tiny_grow(h, hs, *ts, maxIter, ci, co, cd, 0u);
     if (n2 == CUACD_NONE) {
       tiny = false;
       goto restart;
