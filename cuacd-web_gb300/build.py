@@ -32,6 +32,7 @@ UNITS = {
     "host_mesh.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "plane_cut.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "decompose.cpp": ["-Xcompiler", "-ffp-contract=off"],
+    "cpu_hull.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 HEADERS = ["cuacd_dev.cuh", "host_mesh.h"]
 

@@ -98,6 +98,9 @@ struct Job {
   std::vector<Part> parts;
   bool cutting_done = false;
   int iter = 0;  // iterations started
+  // output-hull cleanup epsilon (decompose.ts:231-236): above a few float32
+  // ulps of the input's largest coordinate relative to its extent
+  double hullEps = 2e-5;
   bool merging = false;
   cuacd_decompose_stats st{};
   // merge state
@@ -145,7 +148,8 @@ class Engine {
   // chunks of at most 256 (decompose.ts:180), halved when a chunk's hull
   // export does not fit the triangle pool. A failed hull is an error unless
   // allowFail, when the part gets a NaN hull volume.
-  void hulls(const std::vector<const Mesh*>& ms, bool withHd, std::vector<Part>& out, bool allowFail = false) {
+  void hulls(const std::vector<const Mesh*>& ms, const std::vector<double>& eps, bool withHd, std::vector<Part>& out,
+             bool allowFail = false) {
     out.resize(ms.size());
     size_t chunk = 256;
     for (size_t s = 0; s < ms.size();) {
@@ -192,7 +196,11 @@ class Engine {
           p.hullVol = NAN;
           return;
         }
-        p.hull = host::compact_hull(m.v.data(), tris.data() + (size_t)k * stride, ntri[k], nullptr);
+        // output faces cleaned (decompose.ts:189, merge.ts:213); the kernel's
+        // volume stays the part's hull volume
+        const std::vector<uint32_t> ct =
+            host::clean_hull_faces(m.v.data(), m.nv(), tris.data() + (size_t)k * stride, 3 * (size_t)ntri[k], eps[s + k]);
+        p.hull = host::compact_hull(m.v.data(), ct.data(), ct.size() / 3, nullptr);
         p.hullVol = vol[k];
         if (withHd && std::isfinite(hd[k])) {
           p.hd = hd[k];
@@ -205,7 +213,7 @@ class Engine {
       // 183-188, merge.ts:371)
       for (size_t k = 0; k < n; k++) {
         if (!std::isnan(out[s + k].hullVol)) continue;
-        if (!retry_hull(*ms[s + k], withHd, out[s + k]) && !allowFail) {
+        if (!retry_hull(*ms[s + k], eps[s + k], withHd, out[s + k]) && !allowFail) {
           char msg[160];
           snprintf(msg, sizeof msg, "GPU hull failed (code %d) for a part with %u vertices", status[k], cm[k].nv);
           throw Failure{CUACD_E_CAPACITY, msg};
@@ -219,7 +227,7 @@ class Engine {
   // covers all of its points; false when that hull fails too
   void* bigTree = nullptr;
   uint32_t bigTreeVerts = 0;
-  bool retry_hull(const Mesh& m, bool withHd, Part& p) {
+  bool retry_hull(const Mesh& m, double eps, bool withHd, Part& p) {
     const uint32_t need = (uint32_t)m.nv();
     if (need <= (uint32_t)o.tree.hullMaxVerts) {
       // the bound already covered the points: a larger one does not help
@@ -247,7 +255,8 @@ class Engine {
     gpuMs += ms_since(t0);
     if (rc != CUACD_OK) cuda_fail(rc, "hull retry");
     if (status != 0) return false;
-    p.hull = host::compact_hull(m.v.data(), tris.data(), ntri, nullptr);
+    const std::vector<uint32_t> ct = host::clean_hull_faces(m.v.data(), m.nv(), tris.data(), 3 * (size_t)ntri, eps);
+    p.hull = host::compact_hull(m.v.data(), ct.data(), ct.size() / 3, nullptr);
     p.hullVol = vol;
     if (withHd && std::isfinite(hd)) {
       p.hd = hd;
@@ -471,16 +480,18 @@ class Engine {
     cutMs += ms_since(ta);
     // hulls and Hausdorff distances of every new half in one submission
     std::vector<const Mesh*> halves;
+    std::vector<double> heps;
     std::vector<size_t> which;
     for (size_t k = 0; k < seeds.size(); k++)
       if (cuts[k].ok) {
         halves.push_back(&cuts[k].pos);
         halves.push_back(&cuts[k].neg);
+        heps.insert(heps.end(), 2, seeds[k].job->hullEps);
         which.push_back(k);
       }
     const auto th = Clock::now();
     std::vector<Part> made;
-    hulls(halves, true, made);
+    hulls(halves, heps, true, made);
     hullMs += ms_since(th);
     if (o.verbose) {
       size_t nParts = 0, nTris = 0;
@@ -649,8 +660,12 @@ class Engine {
       std::vector<Part> hp;
       {
         std::vector<const Mesh*> ptr(todo.size());
-        for (size_t k = 0; k < todo.size(); k++) ptr[k] = &pts[k];
-        hulls(ptr, false, hp, true);
+        std::vector<double> peps(todo.size());
+        for (size_t k = 0; k < todo.size(); k++) {
+          ptr[k] = &pts[k];
+          peps[k] = todo[k].job->hullEps;
+        }
+        hulls(ptr, peps, false, hp, true);
       }
       hullMs += ms_since(th);
       const size_t base = evals.size();
@@ -787,12 +802,25 @@ class Engine {
       } else {
         j->mesh = j->input;
       }
+      float lo[3], hi[3];
+      host::bbox(j->input, lo, hi);
+      double maxAbs = 0, extent = 0;
+      for (int a = 0; a < 3; a++) {
+        maxAbs = std::max({maxAbs, std::fabs((double)lo[a]), std::fabs((double)hi[a])});
+        extent = std::max(extent, (double)hi[a] - (double)lo[a]);
+      }
+      if (!(extent > 0)) extent = 1;
+      j->hullEps = std::max(2e-5, 64 * 6e-8 * (maxAbs / extent));
     }
     std::vector<const Mesh*> ms;
-    for (Job* j : jobs) ms.push_back(&j->mesh);
+    std::vector<double> meps;
+    for (Job* j : jobs) {
+      ms.push_back(&j->mesh);
+      meps.push_back(j->hullEps);
+    }
     std::vector<Part> made;
     const auto th = Clock::now();
-    hulls(ms, true, made);
+    hulls(ms, meps, true, made);
     hullMs += ms_since(th);
     for (size_t k = 0; k < jobs.size(); k++) {
       made[k].id = nextId++;
@@ -1253,6 +1281,34 @@ int cuacd_concave_planes(const cuacd_mesh* mesh, int nConcaveEdges, double conca
   const std::vector<float> p = host::concave_edge_planes(m, nConcaveEdges, concaveEps, concaveThreshold, seed);
   const int n = (int)(p.size() / 4);
   std::copy(p.begin(), p.begin() + 4 * (size_t)std::min(n, cap), out);
+  return n;
+}
+
+int cuacd_quickhull(const double* pts, int n, double eps, double* vOut, int vCap, uint32_t* tOut, int tCap,
+                    int* nvOut) {
+  if (n < 0 || (n > 0 && !pts) || vCap < 0 || tCap < 0 || (vCap > 0 && !vOut) || (tCap > 0 && !tOut) || !nvOut)
+    return set_error(CUACD_E_INVALID, "cuacd_quickhull: invalid argument");
+  std::vector<double> hv;
+  std::vector<uint32_t> ht;
+  host::quickhull(pts, (size_t)n, eps, hv, ht);
+  const int nv = (int)(hv.size() / 3), nt = (int)(ht.size() / 3);
+  *nvOut = nv;
+  if (nv > vCap || nt > tCap) return set_error(CUACD_E_CAPACITY, "cuacd_quickhull: output buffers too small");
+  std::copy(hv.begin(), hv.end(), vOut);
+  std::copy(ht.begin(), ht.end(), tOut);
+  return nt;
+}
+
+int cuacd_clean_hull_faces(const cuacd_mesh* mesh, const uint32_t* tris, uint32_t nt, double eps, uint32_t* out,
+                           int cap) {
+  if (!mesh || (mesh->nv && !mesh->verts) || (nt && !tris) || cap < 0 || (cap > 0 && !out))
+    return set_error(CUACD_E_INVALID, "cuacd_clean_hull_faces: invalid argument");
+  for (size_t i = 0; i < 3 * (size_t)nt; i++)
+    if (tris[i] >= mesh->nv) return set_error(CUACD_E_INVALID, "cuacd_clean_hull_faces: triangle index out of range");
+  const std::vector<uint32_t> c = host::clean_hull_faces(mesh->verts, mesh->nv, tris, 3 * (size_t)nt, eps);
+  const int n = (int)(c.size() / 3);
+  if (n > cap) return set_error(CUACD_E_CAPACITY, "cuacd_clean_hull_faces: output buffer too small");
+  std::copy(c.begin(), c.end(), out);
   return n;
 }
 

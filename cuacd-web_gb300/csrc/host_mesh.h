@@ -89,5 +89,21 @@ Mesh compact_hull(const float* pts, const uint32_t* tris, size_t ntris, double* 
 // (src/cpu/hausdorff.ts): the larger directed distance, exhaustive search
 double hausdorff_cpu(const Mesh& a, const Mesh& b);
 
+// The reference's CPU hull (wasm/quickhull/QuickHull.cpp via wasm/qh.cpp):
+// double-precision quickhull of n points with epsilon relative to the
+// largest extreme coordinate; vOut = hull vertices by first appearance,
+// tOut = triangles (counter-clockwise seen from outside).
+void quickhull(const double* pts, size_t n, double eps, std::vector<double>& vOut, std::vector<uint32_t>& tOut);
+
+// cleanHullFaces (src/cpu/hull.ts:87-155): the hull faces T (indices into
+// V, nv vertices) rebuilt by quickhull from their own vertices, dropping
+// vertices of thin faces, accepted only when closed, of the same volume
+// and containing every vertex; otherwise T itself.
+std::vector<uint32_t> clean_hull_faces(const float* V, size_t nv, const uint32_t* T, size_t nIdx, double eps);
+
+// convexHull (src/cpu/hull.ts:64-73): quickhull at epsilon 1e-7, compacted
+// and wound outward
+Mesh convex_hull_cpu(const float* pts, size_t n, double* volumeOut);
+
 }  // namespace host
 }  // namespace cuacd

@@ -79,6 +79,10 @@ def _lib():
         L.cuacd_server_step.argtypes = [C.c_void_p, P(C.c_int)]
         L.cuacd_server_pending.argtypes = [C.c_void_p]
         L.cuacd_server_take.argtypes = [C.c_void_p, C.c_uint64, P(C.c_void_p)]
+        L.cuacd_quickhull.argtypes = [P(C.c_double), C.c_int, C.c_double, P(C.c_double), C.c_int, P(C.c_uint32),
+                                      C.c_int, P(C.c_int)]
+        L.cuacd_clean_hull_faces.argtypes = [P(A.MeshRef), P(C.c_uint32), C.c_uint32, C.c_double, P(C.c_uint32),
+                                             C.c_int]
         _bound = True
     return L
 
@@ -294,3 +298,39 @@ def concave_planes(mesh, n_concave_edges=16, concave_eps=0.005, concave_threshol
     if n < 0:
         _check(n)
     return out[: 4 * min(n, cap)].reshape(-1, 4).copy()
+
+
+def quickhull(points, eps: float = 1e-7):
+    """The reference's CPU hull, qh_compute (wasm/qh.cpp:16-25): returns
+    (vertices (m, 3) float64, triangles (k, 3) uint32), vertices in first
+    appearance order, triangles counter-clockwise seen from outside."""
+    L = _lib()
+    p = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, 3))
+    n = p.shape[0]
+    vcap, tcap = max(n, 4), max(2 * n, 4)
+    v = np.zeros(3 * vcap, np.float64)
+    t = np.zeros(3 * tcap, np.uint32)
+    nv = C.c_int(0)
+    dp = C.POINTER(C.c_double)
+    k = L.cuacd_quickhull(p.ctypes.data_as(dp), n, float(eps), v.ctypes.data_as(dp), vcap,
+                          t.ctypes.data_as(C.POINTER(C.c_uint32)), tcap, C.byref(nv))
+    if k < 0:
+        _check(k)
+    return v[: 3 * nv.value].reshape(-1, 3).copy(), t[: 3 * k].reshape(-1, 3).copy()
+
+
+def clean_hull_faces(verts, tris, eps: float = 2e-5) -> np.ndarray:
+    """cleanHullFaces (src/cpu/hull.ts:87-155): hull triangles (indices into
+    verts) rebuilt for output; the input triangles when the rebuild is not
+    accepted."""
+    L = _lib()
+    v = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, 3))
+    t = np.ascontiguousarray(np.asarray(tris, np.uint32).reshape(-1, 3))
+    ma = A.MeshArray([Mesh(v, np.zeros((0, 3), np.uint32))])
+    cap = max(2 * v.shape[0], t.shape[0], 1)
+    out = np.zeros(3 * cap, np.uint32)
+    up = C.POINTER(C.c_uint32)
+    k = L.cuacd_clean_hull_faces(ma.arr, t.ctypes.data_as(up), t.shape[0], float(eps), out.ctypes.data_as(up), cap)
+    if k < 0:
+        _check(k)
+    return out[: 3 * k].reshape(-1, 3).copy()

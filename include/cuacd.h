@@ -333,6 +333,23 @@ void cuacd_cut_free(void* halves);
 int cuacd_concave_planes(const cuacd_mesh* mesh, int nConcaveEdges, double concaveEps, double concaveThreshold,
                          uint32_t seed, float* out, int cap);
 
+/* The reference's CPU hull, qh_compute (wasm/qh.cpp:16-25 over
+ * wasm/quickhull/QuickHull.cpp): double-precision quickhull of n points,
+ * eps relative to the largest extreme coordinate. Writes the hull vertices
+ * (3 doubles each, at most vCap) and triangles (3 indices each, at most
+ * tCap, counter-clockwise seen from outside); returns the triangle count and
+ * sets *nvOut, or CUACD_E_CAPACITY when an output does not fit. */
+int cuacd_quickhull(const double* pts, int n, double eps, double* vOut, int vCap, uint32_t* tOut, int tCap,
+                    int* nvOut);
+
+/* cleanHullFaces (src/cpu/hull.ts:87-155): the faces of an exact grid hull
+ * (nt triangles indexing mesh->verts; mesh->tris is not read) rebuilt for
+ * output from their own vertices; returns the count of triangles written to
+ * out (at most cap) or an error. The decomposer applies it to every output
+ * hull with eps = max(2e-5, 64 * 6e-8 * maxAbs / extent) of the input. */
+int cuacd_clean_hull_faces(const cuacd_mesh* mesh, const uint32_t* tris, uint32_t nt, double eps, uint32_t* out,
+                           int cap);
+
 /* Message of the last failure on the calling thread. */
 const char* cuacd_last_error(void);
 

@@ -267,3 +267,135 @@ def eval_candidates(m, planes, threads=1, with_hd=True, use_ref=True):
     lib().orc_eval_candidates(ma.arr, pl.ctypes.data_as(C.POINTER(C.c_double)), len(pl), threads, int(with_hd),
                               int(use_ref), out.ctypes.data_as(C.POINTER(C.c_double)))
     return out
+
+
+# ---- the reference's own CPU hull (oracle/_ref/libqh_ref.so) ----------------
+
+_qh = None
+
+
+def qh_ref():
+    """ctypes handle of the reference's quickhull compiled from its sources
+    (None when oracle/_ref was not built: it needs the reference tree)."""
+    global _qh
+    if _qh is None:
+        path = os.path.join(ORACLE_DIR, "_ref", "libqh_ref.so")
+        if not os.path.exists(path):
+            return None
+        L = C.CDLL(path)
+        P = C.POINTER
+        L.qhref_compute.argtypes = [P(C.c_double), C.c_int, C.c_double, P(C.c_double), C.c_int, P(C.c_uint32),
+                                    C.c_int, P(C.c_int)]
+        _qh = L
+    return _qh
+
+
+def quickhull_ref(points, eps=1e-7):
+    """qh_compute (wasm/qh.cpp:16-25) on the reference's quickhull:
+    (vertices (m, 3) float64, triangles (k, 3) uint32)."""
+    L = qh_ref()
+    p = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, 3))
+    n = p.shape[0]
+    vcap, tcap = max(n, 4), max(2 * n, 4)
+    v = np.zeros(3 * vcap, np.float64)
+    t = np.zeros(3 * tcap, np.uint32)
+    nv = C.c_int(0)
+    dp = C.POINTER(C.c_double)
+    k = L.qhref_compute(p.ctypes.data_as(dp), n, float(eps), v.ctypes.data_as(dp), vcap,
+                        t.ctypes.data_as(C.POINTER(C.c_uint32)), tcap, C.byref(nv))
+    assert k >= 0
+    return v[: 3 * nv.value].reshape(-1, 3).copy(), t[: 3 * k].reshape(-1, 3).copy()
+
+
+def _signed_volume_js(V, T):
+    # src/mesh.ts:59-72, anchored at vertex 0 of V, in double
+    if len(T) == 0:
+        return 0.0
+    o = V[0].astype(np.float64)
+    s = 0.0
+    for a, b, c in T:
+        A = V[a].astype(np.float64) - o
+        B = V[b].astype(np.float64) - o
+        Cc = V[c].astype(np.float64) - o
+        s += A[0] * (B[1] * Cc[2] - B[2] * Cc[1]) + A[1] * (B[2] * Cc[0] - B[0] * Cc[2]) + A[2] * (B[0] * Cc[1] - B[1] * Cc[0])
+    return s / 6
+
+
+def _closed_js(T, nv):
+    # src/mesh.ts:104-119: every directed edge once, its reverse once
+    cnt = {}
+    for t in T:
+        for e in range(3):
+            a, b = int(t[e]), int(t[(e + 1) % 3])
+            if a >= nv or b >= nv:
+                return False
+            cnt[(a, b)] = cnt.get((a, b), 0) + 1
+    return all(c == 1 and cnt.get((b, a)) == 1 for (a, b), c in cnt.items())
+
+
+def clean_hull_faces_ref(V, T, eps=2e-5):
+    """cleanHullFaces (src/cpu/hull.ts:87-155) restated in Python over the
+    reference's quickhull. V (n, 3) float32, T (k, 3) indices."""
+    import math
+    V = np.asarray(V, np.float32).reshape(-1, 3)
+    T = np.asarray(T, np.uint32).reshape(-1, 3)
+    if T.size < 12:
+        return T
+    cand, seen = [], set()
+    for x in T.reshape(-1):
+        if int(x) not in seen:
+            seen.add(int(x))
+            cand.append(int(x))
+    vraw = abs(_signed_volume_js(V, T))
+    vals = [float(V[c][a]) for c in cand for a in range(3)]
+    extent = max(max(vals) - min(vals), 1e-30)
+    tol = 5 * eps * extent
+    for _ in range(6):
+        n = len(cand)
+        if n < 4:
+            return T
+        pts = np.array([[float(x) for x in V[c]] for c in cand], np.float64)
+        by_key = {}
+        for k, c in enumerate(cand):
+            by_key[tuple(pts[k])] = c
+        hv, ht = quickhull_ref(pts, eps)
+        out = []
+        for tri in ht:
+            row = []
+            for i in tri:
+                key = tuple(hv[i])
+                if key not in by_key:
+                    return T
+                row.append(by_key[key])
+            out.append(row)
+        out = np.array(out, np.uint32).reshape(-1, 3)
+        if not _closed_js(out, V.shape[0]):
+            return T
+        sv = _signed_volume_js(V, out)
+        if sv < 0:
+            out = out[:, [0, 2, 1]]
+        if not (abs(abs(sv) - vraw) <= 10 * eps * vraw + 1e-30):
+            return T
+        drop = []
+        for ia, ib, ic in out:
+            a, b, c = (V[i].astype(np.float64) for i in (ia, ib, ic))
+            u, w = b - a, c - a
+            nx, ny, nz = u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]
+            l = math.hypot(nx, ny, nz)
+            lab, lac, lbc = math.hypot(*u), math.hypot(*w), math.hypot(*(c - b))
+            longest = max(lab, lac, lbc)
+            if not (l > eps * extent * longest):
+                d = ia if (lbc >= lab and lbc >= lac) else (ib if lac >= lab else ic)
+                if int(d) not in drop:
+                    drop.append(int(d))
+                continue
+            nx, ny, nz = nx / l, ny / l, nz / l
+            d = nx * a[0] + ny * a[1] + nz * a[2]
+            for q in cand:
+                p = V[q].astype(np.float64)
+                if nx * p[0] + ny * p[1] + nz * p[2] - d > tol:
+                    return T
+        if not drop:
+            return out
+        cand = [c for c in cand if c not in drop]
+    return T

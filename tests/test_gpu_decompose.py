@@ -118,3 +118,42 @@ def test_staircase_configuration():
     assert len(r.parts) >= 2
     _check_parts(r, M.volume(m), 0.1)
     assert r.stats["candidates"] > 0 and r.stats["treeRuns"] >= 1
+
+
+def _hull_issues(h, pts):
+    # hull_output.test.ts:13-38: closed, outward, no degenerate face, every
+    # point of the part inside within 1e-4 of its extent
+    V = h.verts.astype(np.float64)
+    T = h.tris
+    if not M.is_closed(h):
+        return "not closed"
+    if not M.signed_volume(h) > 0:
+        return "not outward"
+    P = pts.verts.astype(np.float64)
+    ext = P.max() - P.min()
+    bad, max_out = 0, 0.0
+    for a, b, c in T:
+        u, w = V[b] - V[a], V[c] - V[a]
+        n = np.cross(u, w)
+        l = np.linalg.norm(n)
+        if not l > 1e-6 * np.linalg.norm(u) * np.linalg.norm(w):
+            bad += 1
+            continue
+        n /= l
+        max_out = max(max_out, float((P @ n - n @ V[a]).max()))
+    if bad:
+        return f"{bad} degenerate faces"
+    if max_out > 1e-4 * ext:
+        return f"points outside by {max_out / ext:.2e} of the extent"
+    return None
+
+
+@pytest.mark.parametrize("merge", [False, True])
+def test_output_hulls_are_clean(merge):
+    # every output hull (cleaned by cleanHullFaces) is a clean closed convex
+    # mesh around its part, with and without merging (hull_output.test.ts)
+    for name, m in (("stairs", stairs()), ("blob", G.blob_mesh(6, 28, 5))):
+        r = D.decompose(m, maxIters=100, threshold=0.05, mergeHulls=merge, tree=dict(SMALL_TREE, hullMaxVerts=4096))
+        bad = [(i, _hull_issues(p.hull, p.mesh)) for i, p in enumerate(r.parts)]
+        bad = [b for b in bad if b[1]]
+        assert not bad, (name, merge, len(r.parts), bad[:5])
