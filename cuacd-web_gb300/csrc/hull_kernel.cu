@@ -20,6 +20,8 @@
 //
 // Compiled with --fmad=false: face ranking values match the CPU oracle bit
 // for bit, and with them the insertion order and the face sets.
+#include <type_traits>
+
 #include "cuacd_dev.cuh"
 
 namespace cuacd {
@@ -135,7 +137,12 @@ struct HullCtx {
   // component is below 2^43 and splits into a low word and a 16-bit high part.
   __device__ __forceinline__ void face_make(uint32_t a, uint32_t b, uint32_t c, uint4& w0, uint4& w1, uint4& w2,
                                             uint4& w3) const {
-    f3 pa = qvert(a), pb = qvert(b), pc = qvert(c);
+    face_make_q(a, b, c, qvert(c), w0, w1, w2, w3);
+  }
+  // face_make with the grid point of corner c given
+  __device__ __forceinline__ void face_make_q(uint32_t a, uint32_t b, uint32_t c, f3 pc, uint4& w0, uint4& w1,
+                                              uint4& w2, uint4& w3) const {
+    f3 pa = qvert(a), pb = qvert(b);
     f3 e1 = pb - pa, e2 = pc - pa;
     f3 n = cross(e1, e2);
     const float kb = 1e-6f * (l1(e1) * l1(e2));
@@ -244,7 +251,8 @@ __device__ __forceinline__ bool bm_test(const uint32_t* bm, uint32_t f) { return
 // prefix plus the bits below f in its word. Neighbour slots are renumbered
 // the same way. Returns the new slot of `track`.
 template <int G>
-__device__ __noinline__ uint32_t hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t track) {
+__device__ __noinline__ uint32_t hull_compact(const HullCtx& h, HullSm& hs, GrpSmem& sm, uint32_t track,
+                                              uint32_t* slotOwn = nullptr, uint32_t nSlots = 0) {
   const int lid = Grp<G>::lid();
   const uint32_t nf = hs.nf;
   const uint32_t nw = (nf + 31) / 32;
@@ -272,6 +280,11 @@ __device__ __noinline__ uint32_t hull_compact(const HullCtx& h, HullSm& hs, GrpS
     const uint32_t i = h.cand[k];
     const uint32_t o = h.owner[i];
     if (o < nf && bm_test(h.bm, o)) h.owner[i] = rank(o);
+  }
+  // owners kept per candidate slot (the block path)
+  for (uint32_t k = lid; k < nSlots; k += G) {
+    const uint32_t o = slotOwn[k];
+    if (o < nf && bm_test(h.bm, o)) slotOwn[k] = rank(o);
   }
   for (uint32_t c = 0; c * G < nf; c++) {
     const uint32_t f = c * G + lid;
@@ -671,8 +684,8 @@ __device__ __noinline__ uint32_t hull_tiny_grow(const HullCtx& h, HullSm& hs, Ti
 // saw), so when no new face sees it the point is inside. A patch larger than
 // PATCH_CAP falls back to the scan.
 #define PATCH_CAP 64u
-__device__ __noinline__ void reassign_patch(const HullCtx& h, uint32_t i, uint32_t own, bool dead, uint32_t nb0,
-                                            uint32_t nf1) {
+__device__ __noinline__ void patch_best(const HullCtx& h, uint32_t i, uint32_t own, bool dead, uint32_t nb0,
+                                        uint32_t nf1, uint32_t& outF, float& outD) {
   const f3 pt = h.qvert(i);
   uint32_t q[PATCH_CAP];
   uint32_t n = 0;
@@ -681,7 +694,7 @@ __device__ __noinline__ void reassign_patch(const HullCtx& h, uint32_t i, uint32
   if (!dead) {
     const float v = h.face_eval(own, pt, i);
     if (!(v > 0.0f)) {
-      h.assign(i, 0, nf1);
+      h.best_face(i, 0, nf1, outF, outD);
       return;
     }
     q[n++] = own;
@@ -709,7 +722,7 @@ __device__ __noinline__ void reassign_patch(const HullCtx& h, uint32_t i, uint32
       const float v = h.face_eval(g, pt, i);
       if (!(v > 0.0f)) continue;
       if (n == PATCH_CAP) {
-        h.assign(i, 0, nf1);
+        h.best_face(i, 0, nf1, outF, outD);
         return;
       }
       q[n++] = g;
@@ -719,8 +732,16 @@ __device__ __noinline__ void reassign_patch(const HullCtx& h, uint32_t i, uint32
       }
     }
   }
-  h.owner[i] = bestF;
-  h.dist[i] = bestF != CUACD_NONE ? bestD : 0.0f;
+  outF = bestF;
+  outD = bestF != CUACD_NONE ? bestD : 0.0f;
+}
+__device__ __forceinline__ void reassign_patch(const HullCtx& h, uint32_t i, uint32_t own, bool dead, uint32_t nb0,
+                                               uint32_t nf1) {
+  uint32_t f;
+  float d;
+  patch_best(h, i, own, dead, nb0, nf1, f, d);
+  h.owner[i] = f;
+  h.dist[i] = d;
 }
 
 // farthest-first insertion of the candidate list (shaders.ts:1060-1129)
@@ -798,6 +819,468 @@ __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem
   }
   if (lid == 0) hs.ncand = ncand;
   Grp<G>::sync();
+  return nIns;
+}
+
+// ---------------------------------------------------------------------------
+// Block path (parts above smallNv points, 256 threads). The same insertion
+// sequence and face slots as hull_grow + hull_insert, laid out for latency:
+//   * the insertion (warp 0) keeps the visible patch in shared memory: a
+//     hash set of its faces, their corners and the faces across their
+//     edges, read once during the walk; the slot order is a rank sort of the
+//     patch and the horizon loop is matched in shared memory. A patch of more
+//     than BIG_VIS faces falls back to hull_insert (nothing global has been
+//     written by then).
+//   * the candidates are kept per candidate slot k (point cand[k], owner
+//     and distance in the owner and dist words at k), so one coalesced pass
+//     after each insertion drops the inserted point, reassigns the points of
+//     dead faces and finds the next pick (largest distance, lowest point
+//     index); dead slots are squeezed out when they reach a quarter.
+#ifndef BIG_VIS
+#define BIG_VIS 128u
+#endif
+#define BIG_HASH 256u
+#define BIG_NREC 32u
+struct BigSm {
+  uint32_t key[BIG_HASH];     // patch face + 1; 0 = empty
+  uint32_t f[BIG_VIS];        // patch faces in walk order
+  uint32_t nb[BIG_VIS][3];    // faces across their edges
+  uint32_t vabc[BIG_VIS][3];  // their corners
+  uint32_t ord[BIG_VIS];      // walk index of the patch's k-th face in slot order
+  uint32_t hzA[3 * BIG_VIS];  // new face j: start and end of its horizon edge
+  uint32_t hzB[3 * BIG_VIS];
+  uint4 nrec[BIG_NREC][4];    // records of the first new faces, for the reassignment
+  unsigned long long red[8];
+  uint32_t redN[8];
+  uint32_t fast, pickSlot, pickStart, ntodo;
+};
+
+__device__ __forceinline__ uint32_t big_hash(uint32_t f) { return (f * 2654435761u) >> 24; }
+__device__ __forceinline__ bool big_has(const BigSm& bs, uint32_t f) {
+  uint32_t s = big_hash(f);
+  for (uint32_t n = 0; n < BIG_HASH; n++) {
+    const uint32_t k = *reinterpret_cast<const volatile uint32_t*>(bs.key + s);
+    if (k == f + 1) return true;
+    if (k == 0) return false;
+    s = (s + 1) & (BIG_HASH - 1);
+  }
+  return false;
+}
+// 1: inserted, 0: already present, 2: table full
+__device__ __forceinline__ uint32_t big_add(BigSm& bs, uint32_t f) {
+  uint32_t s = big_hash(f);
+  for (uint32_t n = 0; n < BIG_HASH; n++) {
+    const uint32_t old = atomicCAS(bs.key + s, 0u, f + 1);
+    if (old == 0) return 1;
+    if (old == f + 1) return 0;
+    s = (s + 1) & (BIG_HASH - 1);
+  }
+  return 2;
+}
+
+// hull_insert for warp 0 with the patch in shared memory; false when the
+// patch exceeds BIG_VIS faces (nothing changed: the caller runs hull_insert)
+__device__ __noinline__ bool big_insert(const HullCtx& h, HullSm& hs, BigSm& bs, uint32_t pIdx, uint32_t start) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lt = lanemask_lt();
+  const f3 p = h.qvert(pIdx);
+  const uint32_t nf = hs.nf, nalive = hs.nalive;
+  for (uint32_t j = lane; j < BIG_HASH; j += 32) bs.key[j] = 0;
+  __syncwarp();
+  if (lane == 0) {
+    big_add(bs, start);
+    bs.f[0] = start;
+    const uint4 w0 = h.rec(start)[0];
+    const uint4 nb = *reinterpret_cast<const uint4*>(h.nbr + 4 * (size_t)start);
+    bs.vabc[0][0] = w0.x & 0x7fffffffu; bs.vabc[0][1] = w0.y; bs.vabc[0][2] = w0.z;
+    bs.nb[0][0] = nb.x; bs.nb[0][1] = nb.y; bs.nb[0][2] = nb.z;
+  }
+  __syncwarp();
+  // breadth-first walk over visible neighbours; a face's record and its
+  // neighbours are read together, once
+  uint32_t head = 0, qn = 1;
+  for (;;) {
+    const uint32_t tasks = 3 * (qn - head);
+    uint32_t added = 0;
+    bool over = false;
+    for (uint32_t t0 = 0; t0 < tasks; t0 += 32) {
+      const uint32_t t = t0 + lane;
+      bool claimed = false;
+      uint32_t g = 0;
+      uint4 w0 = make_uint4(0, 0, 0, 0), nb = w0;
+      if (t < tasks) {
+        g = bs.nb[head + t / 3][t % 3];
+        if (g < nf && !big_has(bs, g)) {
+          const uint4* r = h.rec(g);
+          w0 = r[0];
+          const uint4 w1 = r[1], w2 = r[2];
+          nb = *reinterpret_cast<const uint4*>(h.nbr + 4 * (size_t)g);
+          if (w0.x & ALIVE) {
+            const float v = h.face_filter(w0, w1, w2, p, pIdx);
+            if (v > 0.0f || (v == 0.0f && h.face_exact(w2, r[3], p))) {
+              const uint32_t rr = big_add(bs, g);
+              claimed = rr == 1;
+              over = rr == 2;
+            }
+          }
+        }
+      }
+      const unsigned m = __ballot_sync(FULLMASK, claimed);
+      const uint32_t at = qn + added + __popc(m & lt);
+      if (claimed && at < BIG_VIS) {
+        bs.f[at] = g;
+        bs.vabc[at][0] = w0.x & 0x7fffffffu; bs.vabc[at][1] = w0.y; bs.vabc[at][2] = w0.z;
+        bs.nb[at][0] = nb.x; bs.nb[at][1] = nb.y; bs.nb[at][2] = nb.z;
+      }
+      added += __popc(m);
+    }
+    __syncwarp();
+    head = qn;
+    qn += added;
+    if (__any_sync(FULLMASK, over) || qn > BIG_VIS) return false;
+    if (head == qn) break;
+  }
+  const uint32_t n = qn;
+  if (nf + 3 * n > h.fmax) {
+    // face slots exhausted (hull_insert's code 2)
+    if (lane == 0) hs.fail = 2u;
+    __syncwarp();
+    return true;
+  }
+  // the patch in slot order
+  for (uint32_t i = lane; i < n; i += 32) {
+    const uint32_t fi = bs.f[i];
+    uint32_t r = 0;
+    for (uint32_t j = 0; j < n; j++) r += bs.f[j] < fi ? 1u : 0u;
+    bs.ord[r] = i;
+  }
+  __syncwarp();
+  // horizon edges in order e = 3 * listPos + k become new faces (a, b, p)
+  uint32_t nnew = 0;
+  for (uint32_t c = 0; c * 32 < 3 * n; c++) {
+    const uint32_t e = c * 32 + lane;
+    bool isNew = false;
+    uint32_t a = 0, b = 0, f = 0, twin = 0;
+    if (e < 3 * n) {
+      const uint32_t vi = bs.ord[e / 3], k = e % 3;
+      f = bs.f[vi];
+      twin = bs.nb[vi][k];
+      if (twin >= nf || !big_has(bs, twin)) {
+        isNew = true;
+        a = bs.vabc[vi][k];
+        b = bs.vabc[vi][k == 2 ? 0 : k + 1];
+      }
+    }
+    const unsigned m = __ballot_sync(FULLMASK, isNew);
+    if (isNew) {
+      const uint32_t j = nnew + __popc(m & lt);
+      const uint32_t s = nf + j;
+      // the twin's neighbours are read before the new record is stored
+      uint4 tn = make_uint4(0, 0, 0, 0);
+      if (twin < nf) tn = *reinterpret_cast<const uint4*>(h.nbr + 4 * (size_t)twin);
+      uint4 w0, w1, w2, w3;
+      h.face_make_q(a, b, pIdx, p, w0, w1, w2, w3);
+      uint4* w = h.rec(s);
+      w[0] = w0; w[1] = w1; w[2] = w2; w[3] = w3;
+      if (j < BIG_NREC) {
+        bs.nrec[j][0] = w0; bs.nrec[j][1] = w1; bs.nrec[j][2] = w2; bs.nrec[j][3] = w3;
+      }
+      h.nbr[4 * (size_t)s] = twin;
+      if (twin < nf) {
+        uint32_t* tq = h.nbr + 4 * (size_t)twin;
+        if (tn.x == f) tq[0] = s;
+        if (tn.y == f) tq[1] = s;
+        if (tn.z == f) tq[2] = s;
+      }
+      bs.hzA[j] = a;
+      bs.hzB[j] = b;
+    }
+    nnew += __popc(m);
+  }
+  __syncwarp();
+  // around the horizon loop: (b, p) borders the new face starting at b,
+  // (p, a) the new face ending at a
+  for (uint32_t j = lane; j < nnew; j += 32) {
+    const uint32_t a = bs.hzA[j], b = bs.hzB[j];
+    uint32_t j1 = 0, j2 = 0;
+    for (uint32_t q = 0; q < nnew; q++) {
+      if (bs.hzA[q] == b) j1 = q;
+      if (bs.hzB[q] == a) j2 = q;
+    }
+    h.nbr[4 * (size_t)(nf + j) + 1] = nf + j1;
+    h.nbr[4 * (size_t)(nf + j) + 2] = nf + j2;
+  }
+  for (uint32_t i = lane; i < n; i += 32) h.F[16 * (size_t)bs.f[i]] &= 0x7fffffffu;
+  if (lane == 0) {
+    hs.newBase = nf;
+    hs.nf = nf + nnew;
+    hs.nalive = nalive + nnew - n;
+    hs.nvis = n;
+  }
+  __syncwarp();
+  return true;
+}
+
+// a candidate's new owner: over every face after a compaction (patch walk),
+// else over the new faces when its owner died
+// (best_face over the new faces, the first BIG_NREC read from shared memory
+// when nrec is given)
+__device__ __noinline__ void slot_reassign(const HullCtx& h, uint32_t i, uint32_t own, bool gone, bool compacted,
+                                           uint32_t newBase, uint32_t nfNow, const uint4 (*nrec)[4], uint32_t& outF,
+                                           float& outD) {
+  if (compacted) {
+    patch_best(h, i, own, gone, newBase, nfNow, outF, outD);
+    return;
+  }
+  const f3 pt = h.qvert(i);
+  uint32_t bestF = CUACD_NONE;
+  float bestD = 0.0f;
+  for (uint32_t f = newBase; f < nfNow; f++) {
+    const uint32_t j = f - newBase;
+    const bool sh = nrec != nullptr && j < BIG_NREC;
+    const uint4* w = sh ? nrec[j] : h.rec(f);
+    const uint4 w0 = w[0];
+    if ((w0.x & ALIVE) == 0) continue;
+    const uint4 w2 = w[2];
+    const float dd = h.face_filter(w0, w[1], w2, pt, i);
+    if (dd > bestD) { bestD = dd; bestF = f; }
+    if (dd == 0.0f && bestF == CUACD_NONE && h.face_exact(w2, w[3], pt)) { bestD = 1e-30f; bestF = f; }
+  }
+  outF = bestF;
+  outD = bestD;
+}
+
+__device__ __forceinline__ unsigned long long cand_key(float d, uint32_t i) {
+  return ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)(0xffffffffu - i);
+}
+// block maximum of the candidates' keys and sum of the dead-slot counts;
+// the thread holding the maximum records its slot and owner
+__device__ __forceinline__ unsigned long long big_reduce(BigSm& bs, unsigned long long key, uint32_t slot, uint32_t own,
+                                                         uint32_t& dead) {
+  unsigned long long m = key;
+  uint32_t dn = dead;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long m2 = __shfl_xor_sync(FULLMASK, m, o);
+    m = m2 > m ? m2 : m;
+    dn += __shfl_xor_sync(FULLMASK, dn, o);
+  }
+  const uint32_t w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    bs.red[w] = m;
+    bs.redN[w] = dn;
+  }
+  __syncthreads();
+  m = bs.red[0];
+  dn = bs.redN[0];
+#pragma unroll
+  for (int k = 1; k < 8; k++) {
+    m = bs.red[k] > m ? bs.red[k] : m;
+    dn += bs.redN[k];
+  }
+  if (m != 0 && key == m) {
+    bs.pickSlot = slot;
+    bs.pickStart = own;
+  }
+  __syncthreads();
+  dead = dn;
+  return m;
+}
+
+__device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, GrpSmem& sm, BigSm& bs,
+                                               uint32_t maxIter) {
+  constexpr int G = 256;
+  const uint32_t lid = threadIdx.x;
+  uint32_t ncand = hs.ncand;
+  uint32_t* cown = h.owner;
+  float* cdist = h.dist;
+  // owner and distance to candidate-slot order, in place: each chunk is read
+  // before it is written, and a later chunk reads only points cand[k] >= k
+  // (the assignment pass lists points in index order; the seed list fits
+  // one chunk)
+  unsigned long long best = 0;
+  uint32_t bestSlot = 0, bestOwn = CUACD_NONE, dead = 0;
+  for (uint32_t c = 0; c * G < ncand; c++) {
+    const uint32_t k = c * G + lid;
+    uint32_t o = CUACD_NONE, i = 0;
+    float d = 0.0f;
+    if (k < ncand) {
+      i = h.cand[k];
+      o = h.owner[i];
+      d = h.dist[i];
+    }
+    __syncthreads();
+    if (k < ncand) {
+      cown[k] = o;
+      cdist[k] = d;
+      if (o != CUACD_NONE) {
+        const unsigned long long key = cand_key(d, i);
+        if (key > best) { best = key; bestSlot = k; bestOwn = o; }
+      } else {
+        dead++;
+      }
+    }
+    __syncthreads();
+  }
+  uint32_t nIns = 0;
+  for (uint32_t iter = 0; iter < maxIter; iter++) {
+    best = big_reduce(bs, best, bestSlot, bestOwn, dead);
+    // squeeze dead slots out when they reach a quarter of the list
+    if (4 * dead > ncand) {
+      uint32_t nc = 0;
+      best = 0;
+      bestOwn = CUACD_NONE;
+      for (uint32_t c = 0; c * G < ncand; c++) {
+        const uint32_t k = c * G + lid;
+        uint32_t o = CUACD_NONE, i = 0;
+        float d = 0.0f;
+        if (k < ncand) {
+          o = cown[k];
+          i = h.cand[k];
+          d = cdist[k];
+        }
+        uint32_t tot;
+        const uint32_t pre = grp_scan_bit<G>(o != CUACD_NONE, &tot, sm);
+        __syncthreads();
+        if (o != CUACD_NONE) {
+          const uint32_t at = nc + pre;
+          h.cand[at] = i;
+          cown[at] = o;
+          cdist[at] = d;
+          const unsigned long long key = cand_key(d, i);
+          if (key > best) { best = key; bestSlot = at; bestOwn = o; }
+        }
+        nc += tot;
+        __syncthreads();
+      }
+      ncand = nc;
+      dead = 0;
+      best = big_reduce(bs, best, bestSlot, bestOwn, dead);
+    }
+    if (best == 0) break;
+    const uint32_t pick = 0xffffffffu - (uint32_t)(best & 0xffffffffu);
+    const uint32_t pickSlot = bs.pickSlot;
+    uint32_t start = bs.pickStart;
+    if (lid == 0) {
+      hs.compacted = 0;
+      hs.remapN = 0;
+      bs.ntodo = 0;
+    }
+    __syncthreads();
+    // hull_insert's compaction, by the whole block
+    if (hs.nf + 3 * HULL_VIS_MAX > h.fmax || hs.nf > 2 * hs.nalive + 512) {
+      start = hull_compact<G>(h, hs, sm, start, cown, ncand);
+    }
+    if (threadIdx.x < 32) {
+      const bool fast = big_insert(h, hs, bs, pick, start);
+      if (!fast) hull_insert<32>(h, hs, sm, pick, start);
+      if (threadIdx.x == 0) bs.fast = fast ? 1u : 0u;
+    }
+    __syncthreads();
+    nIns++;
+    if (hs.fail) break;
+    const uint32_t nfNow = hs.nf, newBase = hs.newBase;
+    const bool compacted = hs.compacted != 0, fast = bs.fast != 0;
+    // the inserted point leaves; points of dead faces (all points after a
+    // compaction) are reassigned; the next pick
+    best = 0;
+    bestOwn = CUACD_NONE;
+    dead = 0;
+    bool sweep = compacted;
+    if (!compacted) {
+      // scan, four slots per thread in flight; the slots whose owner died
+      // are listed (in the walk queue's words, free after an insertion) and
+      // reassigned by the whole block afterwards
+      uint32_t* todo = h.q;
+      for (uint32_t k0 = lid; k0 < ncand; k0 += 4 * G) {
+        uint32_t ow[4], ci[4];
+        float cd[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const uint32_t k = k0 + u * G;
+          const bool in = k < ncand;
+          ow[u] = in ? cown[k] : CUACD_NONE;
+          ci[u] = in ? h.cand[k] : 0u;
+          cd[u] = in ? cdist[k] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const uint32_t k = k0 + u * G;
+          if (k >= ncand) break;
+          const uint32_t own = ow[u];
+          if (own == CUACD_NONE) {
+            dead++;
+            continue;
+          }
+          if (k == pickSlot) {
+            cown[k] = CUACD_NONE;
+            dead++;
+            continue;
+          }
+          if (fast ? big_has(bs, own) : bm_test(h.bm, own)) {
+            const uint32_t t = atomicAdd(&bs.ntodo, 1u);
+            if (t < HULL_VIS_MAX) todo[t] = k;
+            continue;
+          }
+          const unsigned long long key = cand_key(cd[u], ci[u]);
+          if (key > best) { best = key; bestSlot = k; bestOwn = own; }
+        }
+      }
+      __syncthreads();
+      const uint32_t nt = bs.ntodo;
+      for (uint32_t t = lid; t < min(nt, HULL_VIS_MAX); t += G) {
+        const uint32_t k = todo[t], i = h.cand[k];
+        uint32_t own;
+        float d;
+        slot_reassign(h, i, cown[k], true, false, newBase, nfNow, fast ? bs.nrec : nullptr, own, d);
+        cown[k] = own;
+        cdist[k] = d;
+        if (own == CUACD_NONE) {
+          dead++;
+        } else {
+          const unsigned long long key = cand_key(d, i);
+          if (key > best) { best = key; bestSlot = k; bestOwn = own; }
+        }
+      }
+      // more than the list holds: the rest is found by a sweep
+      sweep = nt > HULL_VIS_MAX;
+      __syncthreads();
+    }
+    if (sweep) {
+      for (uint32_t k = lid; k < ncand; k += G) {
+        uint32_t own = cown[k];
+        if (own == CUACD_NONE) {
+          if (compacted) dead++;
+          continue;
+        }
+        if (compacted && k == pickSlot) {
+          cown[k] = CUACD_NONE;
+          dead++;
+          continue;
+        }
+        const bool gone = fast ? big_has(bs, own) : bm_test(h.bm, own);
+        if (!compacted && !gone) continue;
+        const uint32_t i = h.cand[k];
+        float d;
+        slot_reassign(h, i, own, gone, compacted, newBase, nfNow, fast ? bs.nrec : nullptr, own, d);
+        cown[k] = own;
+        cdist[k] = d;
+        if (own == CUACD_NONE) {
+          dead++;
+        } else {
+          const unsigned long long key = cand_key(d, i);
+          if (key > best) { best = key; bestSlot = k; bestOwn = own; }
+        }
+      }
+    }
+    __syncthreads();
+    if (!fast) {
+      for (uint32_t vi = lid; vi < hs.nvis; vi += G) h.bm[h.vis[vi] >> 5] = 0;
+      __syncthreads();
+    }
+  }
+  if (lid == 0) hs.ncand = ncand;
+  __syncthreads();
   return nIns;
 }
 
@@ -911,7 +1394,7 @@ __device__ __noinline__ double hull_volume_grid(const HullCtx& h, HullSm& hs, Gr
 
 template <int G>
 __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* slab, HullSm& hs, GrpSmem& sm,
-                         float* qcache, TinySm* ts) {
+                         float* qcache, TinySm* ts, BigSm* bs) {
   const int lid = Grp<G>::lid();
   const uint32_t partIdx = P.partBase + idx;
   PartDesc* pdp = D.parts + partIdx;
@@ -1126,7 +1609,8 @@ restart:
     for (uint32_t k = lid; k < nuniq; k += G) h.assign(h.cand[k], 0, 4);
     if (lid == 0) hs.ncand = nuniq;
     Grp<G>::sync();
-    nIns = hull_grow<G>(h, hs, sm, 4, 80);
+    if constexpr (G == 256) nIns = hull_grow_big(h, hs, sm, *bs, 80);
+    else nIns = hull_grow<G>(h, hs, sm, 4, 80);
   }
   const uint32_t fail0 = hs.fail;
   const uint32_t nfPrev = hs.nf;
@@ -1197,7 +1681,8 @@ restart:
     }
     nIns += hull_grow_lanes(h, hs, sm, nfPrev, maxIter, ci, co, cd);
   } else {
-    nIns += hull_grow<G>(h, hs, sm, nfPrev, maxIter);
+    if constexpr (G == 256) nIns += hull_grow_big(h, hs, sm, *bs, maxIter);
+    else nIns += hull_grow<G>(h, hs, sm, nfPrev, maxIter);
   }
   if (hs.fail) {
     if (lid == 0) {
@@ -1251,6 +1736,7 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
   __shared__ HullSm hsm[Grp<G>::PER_BLOCK];
   __shared__ float qcs[G == 32 ? 8 * 3 * QC_MAX : 1];
   __shared__ TinySm tsm[G == 32 ? 8 : 1];
+  __shared__ typename std::conditional<G == 256, BigSm, char>::type bsm;
   const int gi = Grp<G>::gid();
   const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
   if (s >= P.nSlabs) return;
@@ -1268,7 +1754,7 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
       idx = grp_bcast_u<G>(idx, gsm[0]);
       if (idx >= P.nChildParts) break;
       if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr);
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr, reinterpret_cast<BigSm*>(&bsm));
       Grp<G>::sync();
     }
     return;
@@ -1283,7 +1769,7 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
       idx = __shfl_sync(FULLMASK, idx, 0);
       if (idx >= P.nChildParts) break;
       if (D.parts[P.partBase + idx].nv > P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], qcs + gi * 3 * QC_MAX, tsm + gi);
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], qcs + gi * 3 * QC_MAX, tsm + gi, nullptr);
       Grp<G>::sync();
     }
   }

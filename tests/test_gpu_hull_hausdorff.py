@@ -102,6 +102,28 @@ def test_hull_compaction_heavy_sets(tree_mod, oracle):
             assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"]
 
 
+def test_hull_large_cut_parts(tree_mod, oracle):
+    """Block-path hulls of large cut halves: a planar cap of many exactly
+    coplanar points (axis-aligned cuts) on a curved surface whose vertices
+    share grid lines, the shape of the large-mesh workload's parts."""
+    D = importlib.import_module("cuacd-web_gb300.decompose")
+    cfg = dict(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=16384)
+    g = tree_mod.GpuTree(**cfg)
+    o = oracle.OracleTree(**cfg)
+    blob = M.normalize(gen.blob_mesh(12, 44, seed=4))[0]
+    sets = []
+    for pl in ([1, 0, 0, 0.1], [0, 1, 0, -0.05], [0.3, 0.5, -0.8, 0.05]):
+        sets += list(D.plane_cut(blob, pl))
+    assert max(m.nv for m in sets) > 2000
+    rg, sg = g.hull_meshes(sets)
+    ro, so = o.hull_meshes(sets)
+    assert list(sg) == list(so)
+    for i, (a, b) in enumerate(zip(rg, ro)):
+        assert (a is None) == (b is None), i
+        if a is not None:
+            assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"], i
+
+
 def hd_pairs(oracle):
     t = oracle.OracleTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
     pairs = []
