@@ -393,13 +393,39 @@ def run_secondary(args):
     line = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "dtype": "f32", "data": "synthetic", "config": cfg}
     if args.workload == "hausdorff":
+        # the tensor-core screen: sample-triangle pairs screened (one K = 16
+        # bf16 MMA column each, 2 x 16 flops) and exact distances left
+        st = g.hd_stats()
+        secs = ms / args.steps / 1000.0
+        tflops = 2 * 16 * st["screened"] / secs / 1e12
+        bf16_peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"] \
+            if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 1900.0
+        line["screen"] = {"screened_pairs": st["screened"], "exact_distances": st["exact"],
+                          "exact_fraction": st["exact"] / max(st["screened"], 1), "timeout": st["timeout"],
+                          "tensor_tflops": tflops, "bf16_peak_tflops": bf16_peak, "tensor_frac": tflops / bf16_peak}
+        # the same batch through the exhaustive search alone
+        g2 = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096,
+                              hullBudgetBytes=6 << 30, scratchWords=256 << 20, hdScreenMinTris=-1)
+        a = g.hausdorff(pairs)
+        for _ in range(args.warmup):
+            b = g2.hausdorff(pairs)
+        ms2 = 0.0
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            b = g2.hausdorff(pairs)
+            ms2 += g2.last_gpu_ms
+        line["exhaustive"] = {"value": units * args.steps / (ms2 / 1000.0), "unit": unit,
+                              "ms_per_step": ms2 / args.steps,
+                              "same_results": bool((a.view(np.uint32) == b.view(np.uint32)).all())}
         # float32 operations counted from hd_tri_sq's source: 67 on the face
         # interior branch, 150 through the three edge tests; nominal FP32 peak
         # 152 SMs x 128 lanes x 2 x 2.07 GHz
         peak = 152 * 128 * 2 * 2.07e9 / 1e12
+        ex_value = line["exhaustive"]["value"]
         for c, name in ((67, "flops_face_interior"), (150, "flops_edge_tests")):
-            line.setdefault("fp32", {})[name] = c * value / 1e12
-        line["fp32"]["peak_tflops_nominal"] = peak
+            line.setdefault("fp32_exhaustive", {})[name] = c * ex_value / 1e12
+        line["fp32_exhaustive"]["peak_tflops_nominal"] = peak
     print(json.dumps(line), flush=True)
 
 

@@ -27,6 +27,8 @@ class TreeConfig(C.Structure):
         ("hullBudgetBytes", C.c_uint64),
         ("pruneLastLevel", C.c_int32),
         ("warpMaxNv", C.c_int32),
+        ("hdScreenMinTris", C.c_int32),
+        ("reserved", C.c_int32),
     ]
 
 
@@ -103,6 +105,8 @@ DEFAULT_TREE_CONFIG = dict(
     hullBudgetBytes=256 << 20,
     pruneLastLevel=1,
     warpMaxNv=0,
+    hdScreenMinTris=0,
+    reserved=0,
 )
 
 

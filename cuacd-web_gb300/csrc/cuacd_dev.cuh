@@ -20,8 +20,11 @@ enum { CTR_V = 0, CTR_T = 1, CTR_E = 2, CTR_S = 3, CTR_OVERFLOW = 4, CTR_HULLFAI
 // algorithmic bytes of plan, emit and hull as 64-bit counters (a candidate
 // reads its parent once, writes its children once and each child's points
 // are read once by its hull), then Hausdorff results
+// and the Hausdorff screen's statistics: exact point-triangle distances
+// (64-bit), screened pairs (64-bit) and a flag for a tensor-core wait that
+// timed out
 enum { CTR_VALID_LO = 8, CTR_VALID_HI = 9, CTR_BYTES_PLAN = 10, CTR_BYTES_EMIT = 12, CTR_BYTES_HULL = 14, CTR_HD = 16,
-       CTR_WORDS = 16 + 1024 };
+       CTR_HD_EXACT = 16 + 1024, CTR_HD_SCREENED = 16 + 1026, CTR_HD_ERR = 16 + 1028, CTR_WORDS = 16 + 1032 };
 __device__ __forceinline__ void add_bytes(uint32_t* ctr, int slot, unsigned long long b) {
   atomicAdd(reinterpret_cast<unsigned long long*>(ctr + slot), b);
 }
@@ -100,6 +103,10 @@ struct HdArgs {
   uint32_t* ns;              // per mesh: sample count
   uint32_t partBase;
   uint32_t maxSide;          // largest per-side capacity
+  uint32_t screenMin;        // targets with at least this many triangles are screened
+  const uint32_t* triOff;    // per mesh: first triangle of its screen data
+  uint4* triB;               // per triangle: tensor-core operand row (16 bf16)
+  float4* triG;              // per triangle: corners; w = radius, |c|_1, |c|^2
 };
 
 // Physical words of one hull slab whose reference size (which fixes the face

@@ -564,7 +564,12 @@ struct Tree {
     CK(cudaEventRecord(ev0, stream));
     hullLaunch(P, 0);
     if (withHd) {
-      if ((rc = runHd((uint32_t)n, 0, capOff, capN, totalCap, maxSide))) return rc;
+      std::vector<uint32_t> triCap(2 * n);
+      for (int k = 0; k < n; k++) {
+        triCap[k] = m[k].nt;
+        triCap[n + k] = stride / 3;
+      }
+      if ((rc = runHd((uint32_t)n, 0, capOff, capN, totalCap, maxSide, triCap))) return rc;
     }
     CK(cudaEventRecord(ev1, stream));
     CK(cudaGetLastError());
@@ -612,30 +617,59 @@ struct Tree {
     }
     return area;
   }
+  // triCap: per mesh, an upper bound on its triangles (the screen's data)
   int runHd(uint32_t nPairs, uint32_t partBase, const std::vector<uint32_t>& capOff, const std::vector<uint32_t>& capN,
-            uint64_t totalCap, uint32_t maxSide) {
-    size_t metaBytes = (size_t)(3 * 2 * nPairs) * 4;
-    size_t need = metaBytes + 256 + (size_t)totalCap * 16;
-    int rc = bHd.ensure(need);
-    if (rc) return rc;
-    uint32_t* meta = (uint32_t*)bHd.p;
-    float4* samples = (float4*)((uint8_t*)bHd.p + ((metaBytes + 255) & ~(size_t)255));
-    std::vector<uint32_t> hm(4 * nPairs);
+            uint64_t totalCap, uint32_t maxSide, const std::vector<uint32_t>& triCap) {
+    const size_t metaBytes = (size_t)(4 * 2 * nPairs) * 4;
+    std::vector<uint32_t> hm(8 * nPairs, 0u);
     std::memcpy(hm.data(), capOff.data(), 4ull * 2 * nPairs);
     std::memcpy(hm.data() + 2 * nPairs, capN.data(), 4ull * 2 * nPairs);
+    uint64_t nTri = 0;
+    for (uint32_t m = 0; m < 2 * nPairs; m++) {
+      hm[6 * nPairs + m] = (uint32_t)nTri;
+      nTri += triCap[m];
+    }
+    if (nTri > 0xffffffffull) return fail(CUACD_E_CAPACITY, "hausdorff batch: too many triangles");
+    const size_t sampOff = (metaBytes + 255) & ~(size_t)255;
+    const size_t triBOff = (sampOff + (size_t)totalCap * 16 + 255) & ~(size_t)255;
+    const size_t triGOff = triBOff + (size_t)nTri * 32;
+    int rc = bHd.ensure(triGOff + (size_t)nTri * 48 + 16);
+    if (rc) return rc;
+    uint32_t* meta = (uint32_t*)bHd.p;
     if ((rc = hMeta.ensure(hm.size() * 4))) return rc;
     std::memcpy(hMeta.p, hm.data(), hm.size() * 4);
     CK(cudaMemcpyAsync(meta, hMeta.p, hm.size() * 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaMemsetAsync(D.ctr + CTR_HD_EXACT, 0, 8 * 4, stream));
     HdArgs A;
     A.nPairs = nPairs;
     A.nMeshes = 2 * nPairs;
     A.capOff = meta;
     A.capN = meta + 2 * nPairs;
     A.ns = meta + 4 * nPairs;
-    A.samples = samples;
+    A.triOff = meta + 6 * nPairs;
+    A.samples = (float4*)((uint8_t*)bHd.p + sampOff);
+    A.triB = (uint4*)((uint8_t*)bHd.p + triBOff);
+    A.triG = (float4*)((uint8_t*)bHd.p + triGOff);
     A.partBase = partBase;
     A.maxSide = maxSide;
+    A.screenMin = cfg.hdScreenMinTris == 0 ? 256u : (cfg.hdScreenMinTris < 0 ? 0xffffffffu : (uint32_t)cfg.hdScreenMinTris);
     launch_hd(A, D, stream);
+    hdStatsPending = true;
+    return 0;
+  }
+  // statistics of the last Hausdorff batch's screen: exact distances,
+  // screened sample-triangle pairs, timeout flag
+  bool hdStatsPending = false;
+  uint64_t hdStats[3] = {0, 0, 0};
+  int readHdStats() {
+    if (!hdStatsPending) return 0;
+    uint32_t w[6];
+    CK(cudaStreamSynchronize(stream));
+    CK(cudaMemcpy(w, D.ctr + CTR_HD_EXACT, sizeof w, cudaMemcpyDeviceToHost));
+    hdStats[0] = (uint64_t)w[0] | ((uint64_t)w[1] << 32);
+    hdStats[1] = (uint64_t)w[2] | ((uint64_t)w[3] << 32);
+    hdStats[2] = w[4];
+    hdStatsPending = false;
     return 0;
   }
   // GpuTree.hausdorff (tree.ts:318-372)
@@ -670,7 +704,9 @@ struct Tree {
     CK(cudaMemcpyAsync(D.parts, parts.data(), 2ull * n * sizeof(PartDesc), cudaMemcpyHostToDevice, stream));
     CK(cudaMemsetAsync(D.ctr + CTR_HD, 0, 4ull * n, stream));
     CK(cudaEventRecord(ev0, stream));
-    if ((rc = runHd((uint32_t)n, 0, capOff, capN, off, maxSide))) return rc;
+    std::vector<uint32_t> triCap(2 * n);
+    for (int k = 0; k < 2 * n; k++) triCap[k] = all[k].nt;
+    if ((rc = runHd((uint32_t)n, 0, capOff, capN, off, maxSide, triCap))) return rc;
     CK(cudaEventRecord(ev1, stream));
     CK(cudaGetLastError());
     if ((rc = hRead.ensure(4ull * n))) return rc;
@@ -779,6 +815,14 @@ float cuacd_tree_last_gpu_ms(void* t) {
     return 0.0f;
   }
   return ms;
+}
+int cuacd_tree_hd_stats(void* t, uint64_t* out3) {
+  if (!t || !out3) return fail(CUACD_E_INVALID, "cuacd_tree_hd_stats: invalid argument");
+  Tree* tr = (Tree*)t;
+  int rc = tr->readHdStats();
+  if (rc) return rc;
+  std::memcpy(out3, tr->hdStats, sizeof(uint64_t) * 3);
+  return 0;
 }
 int cuacd_tree_kernel_bytes(void* t, uint64_t* bytes3) {
   if (!t) return fail(CUACD_E_INVALID, "null tree");

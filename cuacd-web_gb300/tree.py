@@ -55,6 +55,7 @@ def load_library():
     L.cuacd_set_profile.argtypes = [C.c_void_p, C.c_int]
     L.cuacd_tree_kernel_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.cuacd_tree_kernel_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
+    L.cuacd_tree_hd_stats.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
     L.cuacd_tree_last_gpu_ms.restype = C.c_float
     L.cuacd_tree_last_gpu_ms.argtypes = [C.c_void_p]
     run_args = [C.c_void_p, P(A.MeshRef), C.c_int, P(C.c_float), C.c_int, P(A.RunOpts)]
@@ -130,6 +131,13 @@ class GpuTree:
         return [int(x) for x in b]
 
     KERNELS = ("reset", "plan", "scan", "emit", "hull", "record", "evaluate")
+
+    def hd_stats(self) -> dict:
+        """The last Hausdorff batch's tensor-core screen: exact distances,
+        screened pairs and whether a tensor-core wait timed out."""
+        b = (C.c_uint64 * 3)()
+        _check(load_library().cuacd_tree_hd_stats(self.h, b))
+        return dict(exact=int(b[0]), screened=int(b[1]), timeout=bool(b[2]))
 
     def kernel_ms(self) -> dict:
         """Per-kernel device time of the last profiled run (stats.kernelMs)."""

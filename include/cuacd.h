@@ -61,6 +61,11 @@ typedef struct {
   int32_t warpMaxNv;        /* hulls of parts up to this many points run on one
                                warp each, larger ones on a 256-thread block
                                (0: 1024); the results do not depend on it */
+  int32_t hdScreenMinTris;  /* Hausdorff target meshes with at least this many
+                               triangles go through the tensor-core screen
+                               (0: 256, < 0: never); the results do not
+                               depend on it */
+  int32_t reserved;
 } cuacd_tree_config;
 
 /* Mesh (mesh.ts:7-10): nv vertices (3 floats each), nt triangles (3 u32). */
@@ -137,6 +142,12 @@ int cuacd_tree_kernel_ms(void* tree, float* ms7);
  * candidate reads its parent once (12 nv + 12 nt + 32 ne), writes its
  * children once, and each child's points are read once by its hull. */
 int cuacd_tree_kernel_bytes(void* tree, uint64_t* bytes3);
+
+/* Hausdorff tensor-core screen of the last Hausdorff batch on this handle
+ * (no reference counterpart): [0] exact point-triangle distances computed,
+ * [1] sample-triangle pairs screened, [2] 1 when a tensor-core wait timed out
+ * (the batch's distances are then incomplete). */
+int cuacd_tree_hd_stats(void* tree, uint64_t* out3);
 
 /* GpuTree.lastHullGpuMs (tree.ts:380): device time of the last completed
  * call on this handle (tree run, hull batch or Hausdorff batch), in ms. */

@@ -51,7 +51,7 @@ def test_config_default_matches_reference(lib):
 
 def test_struct_layouts():
     A = pkg("_abi")
-    assert C.sizeof(A.TreeConfig) == 72
+    assert C.sizeof(A.TreeConfig) == 80
     assert C.sizeof(A.MeshRef) == 24
     assert C.sizeof(A.RunOpts) == 32
     assert C.sizeof(A.SeedResult) == 32

@@ -162,6 +162,37 @@ def test_hulls_with_hausdorff(tree_mod, oracle):
     assert rg[0]["hausdorff"] < 1e-6
 
 
+def test_hausdorff_screen_matches_exhaustive(tree_mod, oracle):
+    """Target meshes of 256 triangles or more go through the tensor-core
+    screen, which skips only triangles that cannot hold a sample's nearest
+    point: its distances are the exhaustive search's bit for bit, on meshes
+    against their hulls (samples on shared faces, distance 0 to many
+    triangles) and on two different surfaces."""
+    cfg = dict(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    on = tree_mod.GpuTree(**cfg)
+    off = tree_mod.GpuTree(**cfg, hdScreenMinTris=-1)
+    pairs = []
+    for seed, (nb, grid) in enumerate([(4, 20), (8, 28), (12, 36)]):
+        m = gen.blob_mesh(nb, grid, seed=seed)
+        h = on.hull_meshes([m])[0][0]
+        pairs.append((m, M.Mesh(m.verts, h["tris"])))
+    pairs.append((gen.noisy_icosphere(4, seed=1), gen.noisy_icosphere(4, seed=2)))
+    pairs.append((gen.noisy_icosphere(3, seed=3), M.unit_cube()))
+    a = on.hausdorff(pairs)
+    st = on.hd_stats()
+    b = off.hausdorff(pairs)
+    assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (a, b)
+    assert st["screened"] > 0 and 0 < st["exact"] < st["screened"] and not st["timeout"], st
+    assert off.hd_stats()["screened"] == 0
+    # the fused hull + Hausdorff batch
+    meshes = [p[0] for p in pairs[:3]]
+    ra = on.hulls_with_hausdorff(meshes)
+    rb = off.hulls_with_hausdorff(meshes)
+    for x, y in zip(ra, rb):
+        assert np.float32(x["hausdorff"]).view(np.uint32) == np.float32(y["hausdorff"]).view(np.uint32)
+        assert np.array_equal(x["tris"], y["tris"])
+
+
 def test_hausdorff_scratch_error(tree_mod):
     g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, scratchWords=1000)
     with pytest.raises(tree_mod.ScratchError) as e:
