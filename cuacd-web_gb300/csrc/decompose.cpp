@@ -504,6 +504,13 @@ class Engine {
     // negative half is appended
     for (size_t q = 0; q < which.size(); q++) {
       const Seed& sd = seeds[which[q]];
+      if (o.verbose >= 2) {
+        // every applied cut, enough to replay the loop on the host
+        const cuacd_seed_result& r = best[which[q]];
+        fprintf(stderr, "[cut] iter %d part %zu nt %zu plane %.9g %.9g %.9g %.9g -> %zu + %zu\n", sd.job->iter,
+                sd.part, sd.job->parts[sd.part].mesh.nt(), r.plane[0], r.plane[1], r.plane[2], r.plane[3],
+                made[2 * q].mesh.nt(), made[2 * q + 1].mesh.nt());
+      }
       made[2 * q].id = nextId++;
       made[2 * q + 1].id = nextId++;
       sd.job->parts[sd.part] = std::move(made[2 * q]);

@@ -252,7 +252,8 @@ typedef struct {
   float mergePlaneTol;
   int32_t profile;
   int32_t threads; /* host threads for cuts and merge geometry, 0 = all cores */
-  int32_t verbose; /* 1: one line per iteration and merge round on stderr */
+  int32_t verbose; /* 1: one line per iteration and merge round on stderr;
+                      2: also every applied cut (part, plane, half sizes) */
   int32_t reserved;
   cuacd_tree_config tree;
 } cuacd_decompose_opts;
