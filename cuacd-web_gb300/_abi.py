@@ -185,7 +185,7 @@ class DecomposeOpts(C.Structure):
         ("profile", C.c_int32),
         ("threads", C.c_int32),
         ("verbose", C.c_int32),
-        ("reserved", C.c_int32),
+        ("streams", C.c_int32),
         ("tree", TreeConfig),
     ]
 

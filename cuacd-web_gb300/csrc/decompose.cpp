@@ -862,7 +862,73 @@ class Engine {
     }
     finish(jobs);
   }
+
+  // engines for concurrent groups of a batch (streams > 1), made on demand
+  std::vector<std::unique_ptr<Engine>> peers;
+  void reset_timers() {
+    evals.clear();
+    treeMs = cutMs = concaveMs = hullMs = hdMs = mergeMs = gpuMs = 0;
+  }
+  // The batch split over `streams` engines by triangle count (largest mesh
+  // to the least loaded group), each group run on its own host thread; each
+  // job records the engine that ran it.
+  void run_groups(std::vector<Job*>& jobs, std::vector<Engine*>& ranBy);
 };
+
+Engine* make_engine(const cuacd_decompose_opts& o, int* err);
+
+void Engine::run_groups(std::vector<Job*>& jobs, std::vector<Engine*>& ranBy) {
+  const int G = (int)std::min<size_t>((size_t)std::max(o.streams, 1), jobs.size());
+  ranBy.assign(jobs.size(), this);
+  if (G <= 1) {
+    reset_timers();
+    run(jobs);
+    return;
+  }
+  while ((int)peers.size() < G - 1) {
+    int err = 0;
+    Engine* p = make_engine(o, &err);
+    if (!p) throw Failure{err ? err : CUACD_E_INVALID, std::string("stream engine: ") + cuacd_last_error()};
+    peers.emplace_back(p);
+  }
+  std::vector<size_t> order(jobs.size());
+  for (size_t k = 0; k < order.size(); k++) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return jobs[a]->input.nt() > jobs[b]->input.nt(); });
+  std::vector<std::vector<Job*>> groups(G);
+  std::vector<uint64_t> load(G, 0);
+  for (size_t k : order) {
+    const int g = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    groups[g].push_back(jobs[k]);
+    load[g] += jobs[k]->input.nt() + 1;
+    ranBy[k] = g == 0 ? this : peers[g - 1].get();
+  }
+  // the host threads of the cut and merge geometry are shared out
+  const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
+  const int per = std::max(2, (int)(hc / (unsigned)G));
+  std::vector<Failure> errs(G);
+  std::vector<int> bad(G, 0);
+  std::vector<std::thread> th;
+  for (int g = 0; g < G; g++) {
+    Engine* en = g == 0 ? this : peers[g - 1].get();
+    en->threads = o.threads > 0 ? o.threads : per;
+    th.emplace_back([&, g, en]() {
+      try {
+        en->reset_timers();
+        en->run(groups[g]);
+      } catch (const Failure& f) {
+        bad[g] = 1;
+        errs[g] = f;
+      } catch (const std::bad_alloc&) {
+        bad[g] = 1;
+        errs[g] = Failure{CUACD_E_CAPACITY, "host memory exhausted"};
+      }
+    });
+  }
+  for (std::thread& t : th) t.join();
+  threads = o.threads > 0 ? o.threads : (int)hc;
+  for (int g = 0; g < G; g++)
+    if (bad[g]) throw errs[g];
+}
 
 // An Engine with its tree built from the options (decompose.ts:128-149).
 Engine* make_engine(const cuacd_decompose_opts& o, int* err) {
@@ -1040,6 +1106,8 @@ void cuacd_decompose_opts_default(cuacd_decompose_opts* o) {
   o->mergePlaneTol = 1e-3f;
   o->profile = 0;
   o->threads = 0;
+  o->verbose = 0;
+  o->streams = 1;
   cuacd_tree_config_default(&o->tree);
 }
 
@@ -1074,13 +1142,13 @@ int cuacd_decompose(void* d, const cuacd_mesh* meshes, int n, int batched, void*
   }
   std::unique_ptr<Result> res(new Result());
   try {
-    e->evals.clear();
-    e->treeMs = e->cutMs = e->concaveMs = e->hullMs = e->hdMs = e->mergeMs = e->gpuMs = 0;
+    e->reset_timers();
     const auto t0 = Clock::now();
+    std::vector<Engine*> ranBy(jobs.size(), e);
     if (batched) {
       std::vector<Job*> all;
       for (auto& j : jobs) all.push_back(j.get());
-      e->run(all);
+      e->run_groups(all, ranBy);
     } else {
       for (auto& j : jobs) {
         std::vector<Job*> one{j.get()};
@@ -1089,17 +1157,19 @@ int cuacd_decompose(void* d, const cuacd_mesh* meshes, int n, int batched, void*
       }
     }
     const double total = ms_since(t0);
-    for (auto& j : jobs) {
+    for (size_t k = 0; k < jobs.size(); k++) {
+      Job* j = jobs[k].get();
+      const Engine* en = ranBy[k];
       cuacd_decompose_stats s = j->st;
       s.nParts = (int32_t)j->parts.size();
       s.totalMs = total;
-      s.treeMs = e->treeMs;
-      s.cutMs = e->cutMs;
-      s.concaveMs = e->concaveMs;
-      s.hullMs = e->hullMs;
-      s.hausdorffMs = e->hdMs;
-      s.mergeMs = e->mergeMs;
-      s.gpuMs = e->gpuMs;
+      s.treeMs = en->treeMs;
+      s.cutMs = en->cutMs;
+      s.concaveMs = en->concaveMs;
+      s.hullMs = en->hullMs;
+      s.hausdorffMs = en->hdMs;
+      s.mergeMs = en->mergeMs;
+      s.gpuMs = en->gpuMs;
       res->stats.push_back(s);
       res->parts.push_back(std::move(j->parts));
     }

@@ -44,6 +44,7 @@ DEFAULT_OPTIONS = dict(
     profile=False,
     threads=0,
     verbose=0,
+    streams=1,
 )
 
 STUCK_REASONS = {0: None, 1: "no-plane", 2: "cut-failed", 3: "not-closed", 4: "degenerate"}

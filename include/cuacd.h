@@ -254,7 +254,11 @@ typedef struct {
   int32_t threads; /* host threads for cuts and merge geometry, 0 = all cores */
   int32_t verbose; /* 1: one line per iteration and merge round on stderr;
                       2: also every applied cut (part, plane, half sizes) */
-  int32_t reserved;
+  int32_t streams; /* batched decompositions: meshes are split (by triangle
+                      count) over this many engines, each with its own tree,
+                      CUDA stream and host thread, so one group's latency-bound
+                      levels overlap another's; 0 or 1 = one engine. The
+                      parts do not depend on it. */
   cuacd_tree_config tree;
 } cuacd_decompose_opts;
 

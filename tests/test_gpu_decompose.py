@@ -80,6 +80,15 @@ def test_batched_equals_one_at_a_time():
     for b, p, a in zip(batched, plain, alone):
         _same(b, p)
         _same(b, a)
+    # the batch split over three engines (streams), each on its own host
+    # thread and CUDA stream: the same parts
+    d = D.Decomposer(**opts, streams=3)
+    try:
+        grouped = d.decompose_many(meshes, batched=True)
+    finally:
+        d.destroy()
+    for g, a in zip(grouped, alone):
+        _same(g, a)
 
 
 def test_server_same_alone_and_in_the_mix():
