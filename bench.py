@@ -76,6 +76,8 @@ class ClockSampler:
         self.lines = []
 
     def __enter__(self):
+        if self.gpu is None:  # no sampling
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -498,22 +500,18 @@ def decompose_measure(n_meshes, big_steps=2):
     }
 
 
-def run_serve(args):
-    """Serving: Poisson arrivals of decomposition requests (40% staircases of
-    4..16 steps, 40% blobs of 2k..60k triangles, 20% carved icospheres of
-    level 3..5; thresholds 0.05 or 0.1) into the continuous-batching server
-    for `duration` seconds, then drained. Latency = completion time minus
-    arrival time, queueing included."""
+def serve_session(dec, pool, rate, duration, admit_tris, seed=1, clocks=False):
+    """One serving session: Poisson arrivals at `rate` for `duration`
+    seconds into a fresh server, then drained. Returns (latencies in ms,
+    per-kind latencies, wall seconds, requests, clock summary)."""
     import numpy as np
 
-    dec = importlib.import_module("cuacd-web_gb300.decompose")
-    gen = importlib.import_module("cuacd-web_gb300.meshgen")
-    pool = gen.serving_mix(args.pool, seed=0)
-    rng = np.random.default_rng(1)
-    arr = np.cumsum(rng.exponential(1.0 / args.rate, size=int(args.rate * args.duration * 2) + 16))
-    arr = arr[arr < args.duration]
+    rng = np.random.default_rng(seed)
+    arr = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 2) + 16))
+    arr = arr[arr < duration]
     pick = rng.integers(0, len(pool), size=len(arr))
-    srv = dec.Server(admit_tris=args.admit_tris, threshold=0.05, width=6, width2=3, depth=2, tree=DEC_TREE)
+    srv = dec.Server(admit_tris=admit_tris, threshold=0.05, width=6, width2=3, depth=2, tree=DEC_TREE)
+    clk_summary = None
     try:
         # warm-up: the two trees (one per threshold) and their buffers
         for k, (_, m, thr) in enumerate(sorted(pool, key=lambda x: x[1].nt)[:4]):
@@ -522,7 +520,7 @@ def run_serve(args):
                 srv.step()
         t0 = time.perf_counter()
         i, out, lat, kinds = 0, {}, [], {}
-        with ClockSampler(0) as clk:
+        with ClockSampler(0 if clocks else None) as clk:
             while i < len(arr) or srv.pending:
                 now = time.perf_counter() - t0
                 while i < len(arr) and arr[i] <= now:
@@ -541,21 +539,46 @@ def run_serve(args):
                         lat.append(ms)
                         kinds.setdefault(kind, []).append(ms)
         wall = time.perf_counter() - t0
+        if clocks:
+            clk_summary = clk.summary()
     finally:
         srv.destroy()
-    lat = np.array(lat)
+    return np.array(lat), kinds, wall, len(arr), clk_summary
+
+
+def _lat_summary(lat, kinds):
+    import numpy as np
+
+    return ({"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)), "max": float(lat.max())},
+            {k: {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)), "n": len(v)}
+             for k, v in kinds.items()})
+
+
+def run_serve(args):
+    """Serving: Poisson arrivals of decomposition requests (40% staircases of
+    4..16 steps, 40% blobs of 2k..60k triangles, 20% carved icospheres of
+    level 3..5; thresholds 0.05 or 0.1) into the continuous-batching server
+    for `duration` seconds, then drained. Latency = completion time minus
+    arrival time, queueing included. A second session at 2 req/s (below the
+    server's capacity) reports the latency without a growing queue."""
+    dec = importlib.import_module("cuacd-web_gb300.decompose")
+    gen = importlib.import_module("cuacd-web_gb300.meshgen")
+    pool = gen.serving_mix(args.pool, seed=0)
+    lat, kinds, wall, n, clk = serve_session(dec, pool, args.rate, args.duration, args.admit_tris, clocks=True)
+    p, pk = _lat_summary(lat, kinds)
     line = {"metric": "decomposition requests served/s", "value": len(lat) / wall, "unit": "requests/s", "n_gpus": 1,
             "steps": 1, "warmup": 1, "ms_per_step": 1000 * wall, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"Poisson arrivals at {args.rate} req/s for {args.duration} s "
-                                   f"({len(arr)} requests from {args.pool} distinct meshes), then drained",
+                                   f"({n} requests from {args.pool} distinct meshes), then drained",
                        "mix": "40% staircases 4..16 steps, 40% blobs 2k..60k tris, 20% carved icospheres L3..5",
                        "thresholds": [0.05, 0.1], "admit_tris": args.admit_tris, "width": 6, "depth": 2},
-            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                           "max": float(lat.max())},
-            "latency_ms_by_kind": {k: {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)),
-                                       "n": len(v)} for k, v in kinds.items()},
-            "offered_rate": args.rate, "clocks": clk.summary()}
+            "latency_ms": p, "latency_ms_by_kind": pk, "offered_rate": args.rate, "clocks": clk}
+    if args.rate > 2.0:
+        lat2, kinds2, wall2, n2, _ = serve_session(dec, pool, 2.0, 15.0, args.admit_tris, seed=2)
+        p2, pk2 = _lat_summary(lat2, kinds2)
+        line["below_capacity"] = {"offered_rate": 2.0, "duration_s": 15.0, "requests": n2,
+                                  "served_per_s": len(lat2) / wall2, "latency_ms": p2, "latency_ms_by_kind": pk2}
     print(json.dumps(line), flush=True)
 
 
