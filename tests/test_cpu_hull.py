@@ -10,8 +10,6 @@ duplicated and grid point sets; cleanHullFaces' triangles are identical to
 a Python restatement of hull.ts:87-155 running on that reference quickhull
 (the one tolerance: Math.hypot, which no C library reproduces bit for bit,
 only decides comparisons against thresholds)."""
-import zlib
-
 import numpy as np
 import pytest
 
@@ -170,3 +168,17 @@ def test_clean_hull_faces_rejects_and_small():
     # a clean hull stays a closed 12-triangle hull of the same corners
     got = D.clean_hull_faces(cube.verts, cube.tris)
     assert got.shape == (12, 3) and D_closed(got, 8) and set(got.reshape(-1)) == set(range(8))
+
+
+def test_quickhull_and_cleanup_edges():
+    # no points, one point: no triangles and no error
+    v, t = D.quickhull(np.zeros((0, 3)))
+    assert v.shape == (0, 3) and t.shape == (0, 3)
+    v, t = D.quickhull(np.array([[1.0, 2.0, 3.0]]))
+    assert t.shape[0] == 4  # the reference's degenerate tetrahedron of repeated indices
+    # an out-of-range triangle index is an error, not a read past the array
+    cube = M.unit_cube()
+    with pytest.raises(Exception):
+        D.clean_hull_faces(cube.verts, np.array([[0, 1, 99]], np.uint32))
+    # no triangles: nothing to clean
+    assert D.clean_hull_faces(cube.verts, np.zeros((0, 3), np.uint32)).shape == (0, 3)
