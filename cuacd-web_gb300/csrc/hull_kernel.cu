@@ -1288,10 +1288,12 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
 // the first slot of largest positive ranking value, candidates = the points
 // with an owner, in index order. Each thread holds up to ASSIGN_K points in
 // registers and the slots are read once per ASSIGN_K * G points, the next
-// slot's record loading while the current one is evaluated.
-#define ASSIGN_K 2
+// slot's record loading while the current one is evaluated. Warp groups
+// hold one point per thread: their kernel is limited by instruction fetch,
+// and the smaller loop measured 4 % faster on the staircase tree than two.
 template <int G>
 __device__ __noinline__ uint32_t hull_assign_all(const HullCtx& h, GrpSmem& sm, uint32_t nf) {
+  constexpr int ASSIGN_K = G == 32 ? 1 : 2;
   const int lid = Grp<G>::lid();
   const uint32_t nv = h.nv;
   uint32_t ncand = 0;
