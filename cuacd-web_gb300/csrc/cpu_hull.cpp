@@ -19,9 +19,10 @@
 #include <cmath>
 #include <cstdint>
 #include <deque>
+#include <cstring>
 #include <map>
 #include <thread>
-#include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "host_mesh.h"
@@ -495,19 +496,44 @@ double signed_volume_ptr(const float* V, const uint32_t* T, size_t nIdx) {
 
 // every directed edge of T once and its reverse once (src/mesh.ts:104-119)
 bool closed_ptr(const uint32_t* T, size_t nIdx, size_t nv) {
-  std::map<std::pair<uint32_t, uint32_t>, int> cnt;
+  std::vector<uint64_t> e;
+  e.reserve(nIdx);
   for (size_t t = 0; t + 2 < nIdx; t += 3)
-    for (int e = 0; e < 3; e++) {
-      const uint32_t a = T[t + e], b = T[t + (e + 1) % 3];
+    for (int k = 0; k < 3; k++) {
+      const uint32_t a = T[t + k], b = T[t + (k + 1) % 3];
       if (a >= nv || b >= nv) return false;
-      cnt[{a, b}]++;
+      e.push_back(((uint64_t)a << 32) | b);
     }
-  for (const auto& kv : cnt) {
-    if (kv.second != 1) return false;
-    auto it = cnt.find({kv.first.second, kv.first.first});
-    if (it == cnt.end() || it->second != 1) return false;
+  std::sort(e.begin(), e.end());
+  for (size_t i = 0; i < e.size(); i++) {
+    if (i + 1 < e.size() && e[i + 1] == e[i]) return false;  // a directed edge twice
+    const uint64_t r = (e[i] << 32) | (e[i] >> 32);
+    if (!std::binary_search(e.begin(), e.end(), r)) return false;
   }
   return true;
+}
+
+// a point's coordinates as a key; -0 and 0 are one key, as the reference's
+// printed-number key makes them
+struct PtKey {
+  uint64_t x, y, z;
+  bool operator==(const PtKey& o) const { return x == o.x && y == o.y && z == o.z; }
+};
+struct PtKeyHash {
+  size_t operator()(const PtKey& k) const {
+    uint64_t h = k.x * 0x9E3779B97F4A7C15ull;
+    h ^= (k.y + 0x632BE59BD9B4E019ull + (h << 6) + (h >> 2));
+    h ^= (k.z + 0x85157AF5ull + (h << 6) + (h >> 2));
+    return (size_t)h;
+  }
+};
+inline PtKey pt_key(double x, double y, double z) {
+  PtKey k;
+  const double a = x + 0.0, b = y + 0.0, c = z + 0.0;
+  std::memcpy(&k.x, &a, 8);
+  std::memcpy(&k.y, &b, 8);
+  std::memcpy(&k.z, &c, 8);
+  return k;
 }
 
 double hyp3(double x, double y, double z) { return std::hypot(x, y, z); }
@@ -532,7 +558,7 @@ bool all_inside(const std::vector<double>& planes, const float* V, const std::ve
     }
   };
   const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
-  const size_t nt = (double)nf * (double)n > 4e6 ? std::min<size_t>(hc, 16) : 1;
+  const size_t nt = (double)nf * (double)n > 1e6 ? std::min<size_t>(hc, 16) : 1;
   if (nt <= 1) {
     range(0, nf);
   } else {
@@ -587,19 +613,20 @@ std::vector<uint32_t> clean_hull_faces(const float* V, size_t nv, const uint32_t
     pts.resize(3 * n);
     // hull vertices map back to the candidate with those coordinates (the
     // last one when several share them)
-    std::map<std::tuple<double, double, double>, uint32_t> byKey;
+    std::unordered_map<PtKey, uint32_t, PtKeyHash> byKey;
+    byKey.reserve(2 * n);
     for (size_t k = 0; k < n; k++) {
       const V3 p = vat(V, cand[k]);
       pts[3 * k] = p.x;
       pts[3 * k + 1] = p.y;
       pts[3 * k + 2] = p.z;
-      byKey[std::make_tuple(p.x, p.y, p.z)] = cand[k];
+      byKey[pt_key(p.x, p.y, p.z)] = cand[k];
     }
     quickhull(pts.data(), n, eps, hv, ht);
     std::vector<uint32_t> out(ht.size());
     for (size_t i = 0; i < ht.size(); i++) {
       const size_t h = 3 * (size_t)ht[i];
-      auto it = byKey.find(std::make_tuple(hv[h], hv[h + 1], hv[h + 2]));
+      auto it = byKey.find(pt_key(hv[h], hv[h + 1], hv[h + 2]));
       if (it == byKey.end()) return raw;
       out[i] = it->second;
     }
