@@ -184,6 +184,19 @@ def dist_setup(args):
     return world, rank, local
 
 
+def max_over_ranks(x: float, world: int, device="cuda") -> float:
+    """The largest of every rank's x (each rank runs its own replica; the
+    job's time is the slowest rank's)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_reference(args):
     world, rank, local = dist_setup(args)
     if rank != 0:
@@ -259,11 +272,7 @@ def run_engine(args):
             lib.cuacd_tree_kernel_bytes(g.h, b)
             kbytes += np.array(list(b), np.float64)
     barrier()
-    t_max = dev_ms
-    if world > 1:
-        tt = torch.tensor([dev_ms], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = max_over_ranks(dev_ms, world)
     value = world * cands / (t_max / 1000.0)
 
     # ---- e2e: public C call with host buffers ----
@@ -281,14 +290,11 @@ def run_engine(args):
         e2e_s += time.perf_counter() - t0
         e2e_c += r["validJobs"]
     barrier()
-    if world > 1:
-        tt = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks(e2e_s, world)
     n = len(seeds)
     ps = g.plane_slots
     h2d = sum(s.verts.nbytes + s.tris.nbytes for s in seeds) + n * ps * 16 \
-        + n * 64 + n * 80 + (16 + 1024) * 4 + n * ps * 16 + (16 + 4 * n) * 16
+        + n * 64 + n * 80 + (16 + 1032) * 4 + n * ps * 16 + (16 + 4 * n) * 16
     d2h = (16 + 4 * n) * 16 + 64
 
     if rank != 0:
