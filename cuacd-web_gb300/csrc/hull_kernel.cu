@@ -850,10 +850,107 @@ struct BigSm {
   uint32_t hzA[3 * BIG_VIS];  // new face j: start and end of its horizon edge
   uint32_t hzB[3 * BIG_VIS];
   uint4 nrec[BIG_NREC][4];    // records of the first new faces, for the reassignment
-  unsigned long long red[8];
-  uint32_t redN[8];
-  uint32_t fast, pickSlot, pickStart, ntodo;
+  uint32_t fast, ntodo;
 };
+
+// Batched rounds. A round takes the next picks in key order c_0, c_1, ...,
+// walks their visible patches on the current hull in parallel (one warp
+// each) and inserts the longest prefix whose insertions, one after
+// another, give the hull the single-pick loop gives:
+//   * the patches are disjoint and no face of a later patch borders a face
+//     of an earlier one. A new face of c_i borders only c_i's other new
+//     faces and the faces across c_i's horizon, so c_j's visible faces,
+//     horizon and new faces are the ones found on the current hull, and
+//     c_j's orphans (the points its patch owns) are the current ones;
+//   * c_j still holds the largest key once c_0 .. c_(j-1) are in: the
+//     orphans of each earlier patch get their new keys over that patch's
+//     new faces, and all of them are below c_j's key;
+//   * neither the compaction rule nor the slot limit fires at any of the
+//     steps (a round whose first step would compact runs the single-pick
+//     step).
+// c_j's new faces take the slots the single-pick loop gives them, right
+// after c_(j-1)'s, so face slots, owners and insertion order are the
+// single-pick loop's.
+#define BAT_K 8u        // picks per round, one warp each
+#define BAT_FACES 32u   // faces of a batched patch, one per lane
+#define BAT_NEW 48u     // its horizon edges (a connected patch of n faces has at most n + 2)
+#define BAT_HASH_BITS 6u
+#define UNI_HASH_BITS 10u
+#define UNI_LOAD 640u
+#ifndef TODO_CAP
+#define TODO_CAP (HULL_VIS_MAX / 2)
+#endif
+struct BatWalk {
+  uint32_t key[1u << BAT_HASH_BITS];  // patch face + 1; 0 = empty
+  uint32_t f[BAT_FACES];              // patch faces in walk order
+  uint32_t nb[BAT_FACES][3];          // faces across their edges
+  uint32_t vabc[BAT_FACES][3];        // their corners
+  uint32_t ord[BAT_FACES];            // walk index of the k-th face in slot order
+  uint32_t hA[BAT_NEW], hB[BAT_NEW];  // new face q: its horizon edge (a, b)
+  uint32_t tw[BAT_NEW], df[BAT_NEW];  // the face across that edge and the patch face inside it
+  uint32_t n, nnew, ok, pick;
+};
+struct BatSm {
+  union {
+    BigSm big;  // the single-pick step
+    BatWalk w[BAT_K];
+  } u;
+  // per thread: its two largest candidate keys with their slots and
+  // owners, and its count of dead slots
+  unsigned long long k1[256], k2[256];
+  uint32_t s1[256], o1[256], s2[256], o2[256], dead[256];
+  // the accepted patches' faces (value: patch index) and the faces across
+  // their edges (value 0xff)
+  uint32_t ukey[1u << UNI_HASH_BITS];
+  uint8_t uval[1u << UNI_HASH_BITS];
+  unsigned long long selKey[BAT_K], maxOrph[BAT_K];
+  uint32_t selSlot[BAT_K], selOwn[BAT_K];
+  uint32_t nfj[BAT_K + 1], nalj[BAT_K + 1];  // slot and alive counts before step j
+  uint32_t nsel, ms, ntodo, totDead;
+};
+
+// open-addressing face sets in shared memory (face + 1 stored, 0 = empty)
+template <uint32_t BITS>
+__device__ __forceinline__ uint32_t tab_hash(uint32_t f) { return (f * 2654435761u) >> (32 - BITS); }
+template <uint32_t BITS>
+__device__ __forceinline__ bool tab_has(const uint32_t* key, uint32_t f) {
+  constexpr uint32_t N = 1u << BITS;
+  uint32_t s = tab_hash<BITS>(f);
+  for (uint32_t n = 0; n < N; n++) {
+    const uint32_t k = *reinterpret_cast<const volatile uint32_t*>(key + s);
+    if (k == f + 1) return true;
+    if (k == 0) return false;
+    s = (s + 1) & (N - 1);
+  }
+  return false;
+}
+// the entry of f, or N when absent (the set is not changing)
+template <uint32_t BITS>
+__device__ __forceinline__ uint32_t tab_find(const uint32_t* key, uint32_t f) {
+  constexpr uint32_t N = 1u << BITS;
+  uint32_t s = tab_hash<BITS>(f);
+  for (uint32_t n = 0; n < N; n++) {
+    const uint32_t k = key[s];
+    if (k == f + 1) return s;
+    if (k == 0) return N;
+    s = (s + 1) & (N - 1);
+  }
+  return N;
+}
+// 1: inserted, 0: already present, 2: set full; *at = its entry
+template <uint32_t BITS>
+__device__ __forceinline__ uint32_t tab_add(uint32_t* key, uint32_t f, uint32_t& at) {
+  constexpr uint32_t N = 1u << BITS;
+  uint32_t s = tab_hash<BITS>(f);
+  for (uint32_t n = 0; n < N; n++) {
+    const uint32_t old = atomicCAS(key + s, 0u, f + 1);
+    at = s;
+    if (old == 0) return 1;
+    if (old == f + 1) return 0;
+    s = (s + 1) & (N - 1);
+  }
+  return 2;
+}
 
 __device__ __forceinline__ uint32_t big_hash(uint32_t f) { return (f * 2654435761u) >> 24; }
 __device__ __forceinline__ bool big_has(const BigSm& bs, uint32_t f) {
@@ -1053,121 +1150,293 @@ __device__ __noinline__ void slot_reassign(const HullCtx& h, uint32_t i, uint32_
 __device__ __forceinline__ unsigned long long cand_key(float d, uint32_t i) {
   return ((unsigned long long)__float_as_uint(d) << 32) | (unsigned long long)(0xffffffffu - i);
 }
-// block maximum of the candidates' keys and sum of the dead-slot counts;
-// the thread holding the maximum records its slot and owner
-__device__ __forceinline__ unsigned long long big_reduce(BigSm& bs, unsigned long long key, uint32_t slot, uint32_t own,
-                                                         uint32_t& dead) {
-  unsigned long long m = key;
-  uint32_t dn = dead;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long m2 = __shfl_xor_sync(FULLMASK, m, o);
-    m = m2 > m ? m2 : m;
-    dn += __shfl_xor_sync(FULLMASK, dn, o);
+// a thread's two largest candidate keys (0 = none) with slots and owners
+struct Top2 {
+  unsigned long long k1, k2;
+  uint32_t s1, o1, s2, o2;
+  __device__ __forceinline__ void clear() {
+    k1 = k2 = 0;
+    s1 = o1 = s2 = o2 = 0;
   }
-  const uint32_t w = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) {
-    bs.red[w] = m;
-    bs.redN[w] = dn;
+  __device__ __forceinline__ void add(unsigned long long k, uint32_t s, uint32_t o) {
+    if (k <= k2) return;
+    if (k > k1) {
+      k2 = k1; s2 = s1; o2 = o1;
+      k1 = k; s1 = s; o1 = o;
+    } else {
+      k2 = k; s2 = s; o2 = o;
+    }
   }
-  __syncthreads();
-  m = bs.red[0];
-  dn = bs.redN[0];
-#pragma unroll
-  for (int k = 1; k < 8; k++) {
-    m = bs.red[k] > m ? bs.red[k] : m;
-    dn += bs.redN[k];
-  }
-  if (m != 0 && key == m) {
-    bs.pickSlot = slot;
-    bs.pickStart = own;
-  }
-  __syncthreads();
-  dead = dn;
-  return m;
+};
+__device__ __forceinline__ void top2_publish(BatSm& B, const Top2& t, uint32_t dead) {
+  const uint32_t i = threadIdx.x;
+  B.k1[i] = t.k1; B.k2[i] = t.k2;
+  B.s1[i] = t.s1; B.o1[i] = t.o1; B.s2[i] = t.s2; B.o2[i] = t.o2;
+  B.dead[i] = dead;
 }
 
-__device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, GrpSmem& sm, BigSm& bs,
-                                               uint32_t maxIter) {
+// warp 0: the block's largest keys in descending order for as long as the
+// order is certain (each thread publishes its two largest, so the list ends
+// once a thread's second key is taken: its third could come next), at most
+// kmax; and the total of the dead-slot counts
+__device__ __noinline__ void bat_select(BatSm& B, uint32_t kmax) {
+  const uint32_t lane = threadIdx.x & 31;
+  uint32_t dn = 0;
+  for (uint32_t t = lane; t < 256; t += 32) dn += B.dead[t];
+  dn = warp_sum_u(dn);
+  uint32_t cur = 0;  // keys taken from thread lane + 32 t, 2 bits per t
+  uint32_t n = 0;
+  while (n < kmax) {
+    unsigned long long bk = 0;
+    uint32_t bt = 0;
+#pragma unroll
+    for (uint32_t t = 0; t < 8; t++) {
+      const uint32_t c = (cur >> (2 * t)) & 3u;
+      const uint32_t th = lane + 32 * t;
+      const unsigned long long k = c == 0 ? B.k1[th] : (c == 1 ? B.k2[th] : 0ull);
+      if (k > bk) { bk = k; bt = t; }
+    }
+    unsigned long long m = bk;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long m2 = __shfl_xor_sync(FULLMASK, m, o);
+      m = m2 > m ? m2 : m;
+    }
+    if (m == 0) break;
+    const uint32_t wl = __ffs(__ballot_sync(FULLMASK, bk == m)) - 1;
+    uint32_t second = 0;
+    if (lane == wl) {
+      const uint32_t c = (cur >> (2 * bt)) & 3u;
+      const uint32_t th = lane + 32 * bt;
+      B.selKey[n] = m;
+      B.selSlot[n] = c == 0 ? B.s1[th] : B.s2[th];
+      B.selOwn[n] = c == 0 ? B.o1[th] : B.o2[th];
+      cur += 1u << (2 * bt);
+      second = c;
+    }
+    n++;
+    if (__shfl_sync(FULLMASK, second, wl) != 0) break;
+  }
+  if (lane == 0) {
+    B.nsel = n;
+    B.totDead = dn;
+  }
+  __syncwarp();
+}
+
+// one warp: the visible patch of point pIdx on the current hull, walked
+// from its owner face `start` as big_insert walks it, in slot order, and
+// its horizon edges in the insertion's order (e = 3 * listPos + k). W.ok = 0
+// when the patch has more than BAT_FACES faces.
+__device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatWalk& W, uint32_t pIdx, uint32_t start) {
+  constexpr uint32_t HB = BAT_HASH_BITS;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lt = lanemask_lt();
+  const f3 p = h.qvert(pIdx);
+  for (uint32_t j = lane; j < (1u << HB); j += 32) W.key[j] = 0;
+  __syncwarp();
+  if (lane == 0) {
+    uint32_t at;
+    tab_add<HB>(W.key, start, at);
+    W.f[0] = start;
+    const uint4 w0 = h.rec(start)[0];
+    const uint4 nb = *reinterpret_cast<const uint4*>(h.nbr + 4 * (size_t)start);
+    W.vabc[0][0] = w0.x & 0x7fffffffu; W.vabc[0][1] = w0.y; W.vabc[0][2] = w0.z;
+    W.nb[0][0] = nb.x; W.nb[0][1] = nb.y; W.nb[0][2] = nb.z;
+  }
+  __syncwarp();
+  uint32_t head = 0, qn = 1;
+  bool bad = false;
+  for (;;) {
+    const uint32_t tasks = 3 * (qn - head);
+    uint32_t added = 0;
+    bool over = false;
+    for (uint32_t t0 = 0; t0 < tasks; t0 += 32) {
+      const uint32_t t = t0 + lane;
+      bool claimed = false;
+      uint32_t g = 0;
+      uint4 w0 = make_uint4(0, 0, 0, 0), nb = w0;
+      if (t < tasks) {
+        g = W.nb[head + t / 3][t % 3];
+        if (g < nf && !tab_has<HB>(W.key, g)) {
+          const uint4* r = h.rec(g);
+          w0 = r[0];
+          const uint4 w1 = r[1], w2 = r[2];
+          nb = *reinterpret_cast<const uint4*>(h.nbr + 4 * (size_t)g);
+          if (w0.x & ALIVE) {
+            const float v = h.face_filter(w0, w1, w2, p, pIdx);
+            if (v > 0.0f || (v == 0.0f && h.face_exact(w2, r[3], p))) {
+              uint32_t at;
+              const uint32_t rr = tab_add<HB>(W.key, g, at);
+              claimed = rr == 1;
+              over = rr == 2;
+            }
+          }
+        }
+      }
+      const unsigned m = __ballot_sync(FULLMASK, claimed);
+      const uint32_t at = qn + added + __popc(m & lt);
+      if (claimed && at < BAT_FACES) {
+        W.f[at] = g;
+        W.vabc[at][0] = w0.x & 0x7fffffffu; W.vabc[at][1] = w0.y; W.vabc[at][2] = w0.z;
+        W.nb[at][0] = nb.x; W.nb[at][1] = nb.y; W.nb[at][2] = nb.z;
+      }
+      added += __popc(m);
+    }
+    __syncwarp();
+    head = qn;
+    qn += added;
+    if (__any_sync(FULLMASK, over) || qn > BAT_FACES) {
+      bad = true;
+      break;
+    }
+    if (head == qn) break;
+  }
+  if (bad) {
+    if (lane == 0) W.ok = 0;
+    __syncwarp();
+    return;
+  }
+  const uint32_t n = qn;
+  if (lane < n) {
+    const uint32_t fi = W.f[lane];
+    uint32_t r = 0;
+    for (uint32_t j = 0; j < n; j++) r += W.f[j] < fi ? 1u : 0u;
+    W.ord[r] = lane;
+  }
+  __syncwarp();
+  uint32_t nnew = 0;
+  for (uint32_t c = 0; c * 32 < 3 * n; c++) {
+    const uint32_t e = c * 32 + lane;
+    bool isNew = false;
+    uint32_t a = 0, b = 0, f = 0, twin = 0;
+    if (e < 3 * n) {
+      const uint32_t vi = W.ord[e / 3], k = e % 3;
+      f = W.f[vi];
+      twin = W.nb[vi][k];
+      if (twin >= nf || !tab_has<HB>(W.key, twin)) {
+        isNew = true;
+        a = W.vabc[vi][k];
+        b = W.vabc[vi][k == 2 ? 0 : k + 1];
+      }
+    }
+    const unsigned m = __ballot_sync(FULLMASK, isNew);
+    const uint32_t q = nnew + __popc(m & lt);
+    if (isNew && q < BAT_NEW) {
+      W.hA[q] = a; W.hB[q] = b;
+      W.tw[q] = twin; W.df[q] = f;
+    }
+    nnew += __popc(m);
+  }
+  if (lane == 0) {
+    W.n = n;
+    W.nnew = nnew;
+    W.ok = nnew <= BAT_NEW ? 1u : 0u;
+    W.pick = pIdx;
+  }
+  __syncwarp();
+}
+
+// warp 0: the longest prefix of the K walked picks whose patches are
+// disjoint and not adjacent, with neither the compaction rule (steps after
+// the first) nor the slot limit firing; the slot and alive counts before
+// each accepted step
+__device__ __noinline__ void bat_validate(const HullCtx& h, const HullSm& hs, BatSm& B, uint32_t K) {
+  constexpr uint32_t UB = UNI_HASH_BITS;
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t j = lane; j < (1u << UB); j += 32) B.ukey[j] = 0;
+  __syncwarp();
+  uint32_t nfc = hs.nf, nalc = hs.nalive, used = 0, ms = 0;
+  if (lane == 0) {
+    B.nfj[0] = nfc;
+    B.nalj[0] = nalc;
+  }
+  for (uint32_t j = 0; j < K; j++) {
+    const BatWalk& W = B.u.w[j];
+    if (!W.ok) break;
+    if (j > 0 && (nfc + 3 * HULL_VIS_MAX > h.fmax || nfc > 2 * nalc + 512)) break;
+    const uint32_t n = W.n;
+    if (nfc + 3 * n > h.fmax || used + 4 * n > UNI_LOAD) break;
+    const uint32_t f = lane < n ? W.f[lane] : 0u;
+    if (__any_sync(FULLMASK, lane < n && tab_has<UB>(B.ukey, f))) break;
+    uint32_t at;
+    if (lane < n && tab_add<UB>(B.ukey, f, at) == 1) B.uval[at] = (uint8_t)j;
+    __syncwarp();
+    if (lane < n) {
+      for (int k = 0; k < 3; k++) {
+        if (tab_add<UB>(B.ukey, W.nb[lane][k], at) == 1) B.uval[at] = 0xffu;
+      }
+    }
+    __syncwarp();
+    used += 4 * n;
+    nfc += W.nnew;
+    nalc = nalc + W.nnew - n;
+    ms = j + 1;
+    if (lane == 0) {
+      B.nfj[j + 1] = nfc;
+      B.nalj[j + 1] = nalc;
+    }
+  }
+  if (lane == 0) B.ms = ms;
+  __syncwarp();
+}
+
+// squeeze dead slots out of the candidate list (slot order kept); returns
+// the new count and publishes the threads' keys
+__device__ __noinline__ uint32_t big_squeeze(const HullCtx& h, GrpSmem& sm, BatSm& B, uint32_t ncand) {
   constexpr int G = 256;
   const uint32_t lid = threadIdx.x;
-  uint32_t ncand = hs.ncand;
-  uint32_t* cown = h.owner;
-  float* cdist = h.dist;
-  // owner and distance to candidate-slot order, in place: each chunk is read
-  // before it is written, and a later chunk reads only points cand[k] >= k
-  // (the assignment pass lists points in index order; the seed list fits
-  // one chunk)
-  unsigned long long best = 0;
-  uint32_t bestSlot = 0, bestOwn = CUACD_NONE, dead = 0;
+  uint32_t nc = 0;
+  Top2 t;
+  t.clear();
   for (uint32_t c = 0; c * G < ncand; c++) {
     const uint32_t k = c * G + lid;
     uint32_t o = CUACD_NONE, i = 0;
     float d = 0.0f;
     if (k < ncand) {
+      o = h.owner[k];
       i = h.cand[k];
-      o = h.owner[i];
-      d = h.dist[i];
+      d = h.dist[k];
     }
+    uint32_t tot;
+    const uint32_t pre = grp_scan_bit<G>(o != CUACD_NONE, &tot, sm);
     __syncthreads();
-    if (k < ncand) {
-      cown[k] = o;
-      cdist[k] = d;
-      if (o != CUACD_NONE) {
-        const unsigned long long key = cand_key(d, i);
-        if (key > best) { best = key; bestSlot = k; bestOwn = o; }
-      } else {
-        dead++;
-      }
+    if (o != CUACD_NONE) {
+      const uint32_t at = nc + pre;
+      h.cand[at] = i;
+      h.owner[at] = o;
+      h.dist[at] = d;
+      t.add(cand_key(d, i), at, o);
     }
+    nc += tot;
     __syncthreads();
   }
-  uint32_t nIns = 0;
-  for (uint32_t iter = 0; iter < maxIter; iter++) {
-    best = big_reduce(bs, best, bestSlot, bestOwn, dead);
-    // squeeze dead slots out when they reach a quarter of the list
-    if (4 * dead > ncand) {
-      uint32_t nc = 0;
-      best = 0;
-      bestOwn = CUACD_NONE;
-      for (uint32_t c = 0; c * G < ncand; c++) {
-        const uint32_t k = c * G + lid;
-        uint32_t o = CUACD_NONE, i = 0;
-        float d = 0.0f;
-        if (k < ncand) {
-          o = cown[k];
-          i = h.cand[k];
-          d = cdist[k];
-        }
-        uint32_t tot;
-        const uint32_t pre = grp_scan_bit<G>(o != CUACD_NONE, &tot, sm);
-        __syncthreads();
-        if (o != CUACD_NONE) {
-          const uint32_t at = nc + pre;
-          h.cand[at] = i;
-          cown[at] = o;
-          cdist[at] = d;
-          const unsigned long long key = cand_key(d, i);
-          if (key > best) { best = key; bestSlot = at; bestOwn = o; }
-        }
-        nc += tot;
-        __syncthreads();
-      }
-      ncand = nc;
-      dead = 0;
-      best = big_reduce(bs, best, bestSlot, bestOwn, dead);
-    }
-    if (best == 0) break;
-    const uint32_t pick = 0xffffffffu - (uint32_t)(best & 0xffffffffu);
-    const uint32_t pickSlot = bs.pickSlot;
-    uint32_t start = bs.pickStart;
+  top2_publish(B, t, 0);
+  __syncthreads();
+  return nc;
+}
+
+// the single-pick step for the selection's first pick: hull_insert's
+// compaction by the whole block, big_insert (hull_insert for a patch above
+// BIG_VIS faces) by warp 0, then one pass over the candidate slots: the
+// inserted point leaves, points of dead faces (all points after a
+// compaction) are reassigned, and the threads' keys are published
+__device__ __noinline__ void big_seq_step(const HullCtx& h, HullSm& hs, GrpSmem& sm, BatSm& B, uint32_t ncand) {
+  constexpr int G = 256;
+  BigSm& bs = B.u.big;
+  const uint32_t lid = threadIdx.x;
+  uint32_t* cown = h.owner;
+  float* cdist = h.dist;
+  const uint32_t pick = 0xffffffffu - (uint32_t)(B.selKey[0] & 0xffffffffu);
+  const uint32_t pickSlot = B.selSlot[0];
+  uint32_t start = B.selOwn[0];
+  {
     if (lid == 0) {
       hs.compacted = 0;
       hs.remapN = 0;
       bs.ntodo = 0;
     }
     __syncthreads();
-    // hull_insert's compaction, by the whole block
     if (hs.nf + 3 * HULL_VIS_MAX > h.fmax || hs.nf > 2 * hs.nalive + 512) {
       start = hull_compact<G>(h, hs, sm, start, cown, ncand);
     }
@@ -1177,15 +1446,12 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
       if (threadIdx.x == 0) bs.fast = fast ? 1u : 0u;
     }
     __syncthreads();
-    nIns++;
-    if (hs.fail) break;
+    if (hs.fail) return;
     const uint32_t nfNow = hs.nf, newBase = hs.newBase;
     const bool compacted = hs.compacted != 0, fast = bs.fast != 0;
-    // the inserted point leaves; points of dead faces (all points after a
-    // compaction) are reassigned; the next pick
-    best = 0;
-    bestOwn = CUACD_NONE;
-    dead = 0;
+    Top2 top;
+    top.clear();
+    uint32_t dead = 0;
     bool sweep = compacted;
     if (!compacted) {
       // scan, four slots per thread in flight; the slots whose owner died
@@ -1223,7 +1489,7 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
             continue;
           }
           const unsigned long long key = cand_key(cd[u], ci[u]);
-          if (key > best) { best = key; bestSlot = k; bestOwn = own; }
+          top.add(key, k, own);
         }
       }
       __syncthreads();
@@ -1239,7 +1505,7 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
           dead++;
         } else {
           const unsigned long long key = cand_key(d, i);
-          if (key > best) { best = key; bestSlot = k; bestOwn = own; }
+          top.add(key, k, own);
         }
       }
       // more than the list holds: the rest is found by a sweep
@@ -1269,14 +1535,244 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
           dead++;
         } else {
           const unsigned long long key = cand_key(d, i);
-          if (key > best) { best = key; bestSlot = k; bestOwn = own; }
+          top.add(key, k, own);
         }
       }
     }
     __syncthreads();
     if (!fast) {
       for (uint32_t vi = lid; vi < hs.nvis; vi += G) h.bm[h.vis[vi] >> 5] = 0;
+    }
+    top2_publish(B, top, dead);
+    __syncthreads();
+  }
+}
+
+// A batched round after validation (B.ms >= 1 steps): the new faces of
+// every validated step at their slots, one pass over the candidate slots
+// that lists the orphans of the validated patches (the walk queue's and
+// visible list's words: slot, then new owner, new distance and step), the
+// orphans' new owners over their step's new faces and the largest new key
+// per step, the accepted prefix, then its commit (twin links, dead faces,
+// counts) and the orphans' new owners. Returns the number of insertions.
+__device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B, uint32_t ncand) {
+  constexpr int G = 256;
+  constexpr uint32_t UB = UNI_HASH_BITS;
+  constexpr uint32_t UN = 1u << UB;
+  const uint32_t lid = threadIdx.x, warp = lid >> 5, lane = lid & 31;
+  const uint32_t ms = B.ms, nf0 = hs.nf;
+  // new faces (a, b, pick) and the links among them and to the twins;
+  // records of steps that are not accepted lie above the slot count and
+  // are overwritten later
+  if (warp < ms) {
+    const BatWalk& W = B.u.w[warp];
+    const uint32_t base = B.nfj[warp], nnew = W.nnew, pIdx = W.pick;
+    const f3 p = h.qvert(pIdx);
+    for (uint32_t q = lane; q < nnew; q += 32) {
+      const uint32_t a = W.hA[q], b = W.hB[q], s = base + q;
+      uint4 w0, w1, w2, w3;
+      h.face_make_q(a, b, pIdx, p, w0, w1, w2, w3);
+      uint4* w = h.rec(s);
+      w[0] = w0; w[1] = w1; w[2] = w2; w[3] = w3;
+      // around the horizon loop: (b, p) borders the new face starting at
+      // b, (p, a) the new face ending at a
+      uint32_t j1 = 0, j2 = 0;
+      for (uint32_t r = 0; r < nnew; r++) {
+        if (W.hA[r] == b) j1 = r;
+        if (W.hB[r] == a) j2 = r;
+      }
+      uint32_t* nq = h.nbr + 4 * (size_t)s;
+      nq[0] = W.tw[q];
+      nq[1] = base + j1;
+      nq[2] = base + j2;
+    }
+  }
+  if (lid == 0) B.ntodo = 0;
+  if (lid < BAT_K) B.maxOrph[lid] = 0;
+  __syncthreads();
+  // one pass over the slots, four per thread in flight
+  Top2 top;
+  top.clear();
+  uint32_t dead = 0;
+  for (uint32_t k0 = lid; k0 < ncand; k0 += 4 * G) {
+    uint32_t ow[4], ci[4];
+    float cd[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t k = k0 + u * G;
+      const bool in = k < ncand;
+      ow[u] = in ? h.owner[k] : CUACD_NONE;
+      ci[u] = in ? h.cand[k] : 0u;
+      cd[u] = in ? h.dist[k] : 0.0f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const uint32_t k = k0 + u * G;
+      if (k >= ncand) break;
+      const uint32_t own = ow[u];
+      if (own == CUACD_NONE) {
+        dead++;
+        continue;
+      }
+      const uint32_t at = tab_find<UB>(B.ukey, own);
+      if (at < UN && B.uval[at] < BAT_K) {
+        const uint32_t t = atomicAdd(&B.ntodo, 1u);
+        if (t < TODO_CAP) h.vis[t] = k;
+        continue;
+      }
+      top.add(cand_key(cd[u], ci[u]), k, own);
+    }
+  }
+  __syncthreads();
+  const uint32_t nt = B.ntodo;
+  uint32_t m = 1;
+  if (nt <= TODO_CAP) {
+    for (uint32_t t = lid; t < nt; t += G) {
+      const uint32_t k = h.vis[t], own = h.owner[k];
+      const uint32_t j = B.uval[tab_find<UB>(B.ukey, own)];
+      uint32_t no = CUACD_NONE;
+      float nd = 0.0f;
+      if (k != B.selSlot[j]) {
+        const uint32_t i = h.cand[k];
+        slot_reassign(h, i, own, true, false, B.nfj[j], B.nfj[j + 1], nullptr, no, nd);
+        if (no != CUACD_NONE) atomicMax(&B.maxOrph[j], cand_key(nd, i));
+      }
+      h.vis[TODO_CAP + t] = no;
+      h.q[t] = __float_as_uint(nd);
+      h.q[TODO_CAP + t] = j;
+    }
+    __syncthreads();
+    // pick j is next while every earlier step's orphans stay below its key
+    unsigned long long run = B.maxOrph[0];
+    for (uint32_t j = 1; j < ms; j++) {
+      if (!(run < B.selKey[j])) break;
+      run = B.maxOrph[j] > run ? B.maxOrph[j] : run;
+      m++;
+    }
+  }
+  // commit: the twins link to the new faces, the patches die
+  if (warp < m) {
+    const BatWalk& W = B.u.w[warp];
+    const uint32_t base = B.nfj[warp];
+    for (uint32_t q = lane; q < W.nnew; q += 32) {
+      const uint32_t twin = W.tw[q], f = W.df[q], s = base + q;
+      if (twin < nf0) {
+        uint32_t* tq = h.nbr + 4 * (size_t)twin;
+        const uint4 tn = *reinterpret_cast<const uint4*>(tq);
+        if (tn.x == f) tq[0] = s;
+        if (tn.y == f) tq[1] = s;
+        if (tn.z == f) tq[2] = s;
+      }
+    }
+    for (uint32_t i = lane; i < W.n; i += 32) h.F[16 * (size_t)W.f[i]] &= 0x7fffffffu;
+  }
+  if (lid == 0) {
+    hs.newBase = nf0;
+    hs.nf = B.nfj[m];
+    hs.nalive = B.nalj[m];
+  }
+  if (nt <= TODO_CAP) {
+    // accepted steps' orphans take their new owners (the picks leave);
+    // the others keep theirs
+    for (uint32_t t = lid; t < nt; t += G) {
+      const uint32_t k = h.vis[t], j = h.q[TODO_CAP + t];
+      if (j < m) {
+        const uint32_t no = h.vis[TODO_CAP + t];
+        const float nd = __uint_as_float(h.q[t]);
+        h.owner[k] = no;
+        h.dist[k] = nd;
+        if (no == CUACD_NONE) dead++;
+        else top.add(cand_key(nd, h.cand[k]), k, no);
+      } else {
+        top.add(cand_key(h.dist[k], h.cand[k]), k, h.owner[k]);
+      }
+    }
+  } else {
+    // more orphans than the list holds: the first step alone, its orphans
+    // reassigned by a sweep
+    for (uint32_t k = lid; k < ncand; k += G) {
+      const uint32_t own = h.owner[k];
+      if (own == CUACD_NONE) continue;
+      const uint32_t at = tab_find<UB>(B.ukey, own);
+      if (at >= UN || B.uval[at] >= BAT_K) continue;
+      const uint32_t i = h.cand[k];
+      if (B.uval[at] != 0) {
+        top.add(cand_key(h.dist[k], i), k, own);
+        continue;
+      }
+      uint32_t no = CUACD_NONE;
+      float nd = 0.0f;
+      if (k != B.selSlot[0]) slot_reassign(h, i, own, true, false, B.nfj[0], B.nfj[1], nullptr, no, nd);
+      h.owner[k] = no;
+      h.dist[k] = nd;
+      if (no == CUACD_NONE) dead++;
+      else top.add(cand_key(nd, i), k, no);
+    }
+  }
+  top2_publish(B, top, dead);
+  __syncthreads();
+  return m;
+}
+
+__device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, GrpSmem& sm, BatSm& B,
+                                               uint32_t maxIter) {
+  constexpr int G = 256;
+  const uint32_t lid = threadIdx.x, warp = lid >> 5;
+  uint32_t ncand = hs.ncand;
+  // owner and distance to candidate-slot order, in place: each chunk is read
+  // before it is written, and a later chunk reads only points cand[k] >= k
+  // (the assignment pass lists points in index order; the seed list fits
+  // one chunk)
+  Top2 top;
+  top.clear();
+  uint32_t dead = 0;
+  for (uint32_t c = 0; c * G < ncand; c++) {
+    const uint32_t k = c * G + lid;
+    uint32_t o = CUACD_NONE, i = 0;
+    float d = 0.0f;
+    if (k < ncand) {
+      i = h.cand[k];
+      o = h.owner[i];
+      d = h.dist[i];
+    }
+    __syncthreads();
+    if (k < ncand) {
+      h.owner[k] = o;
+      h.dist[k] = d;
+      if (o != CUACD_NONE) top.add(cand_key(d, i), k, o);
+      else dead++;
+    }
+    __syncthreads();
+  }
+  top2_publish(B, top, dead);
+  __syncthreads();
+  uint32_t nIns = 0;
+  while (nIns < maxIter) {
+    if (warp == 0) bat_select(B, min(BAT_K, maxIter - nIns));
+    __syncthreads();
+    // squeeze dead slots out when they reach a quarter of the list
+    if (4 * B.totDead > ncand) {
+      ncand = big_squeeze(h, sm, B, ncand);
+      continue;
+    }
+    const uint32_t K = B.nsel;
+    if (K == 0) break;
+    bool seq = hs.nf + 3 * HULL_VIS_MAX > h.fmax || hs.nf > 2 * hs.nalive + 512;
+    if (!seq) {
+      if (warp < K) {
+        bat_walk(h, hs.nf, B.u.w[warp], 0xffffffffu - (uint32_t)(B.selKey[warp] & 0xffffffffu), B.selOwn[warp]);
+      }
       __syncthreads();
+      if (warp == 0) bat_validate(h, hs, B, K);
+      __syncthreads();
+      seq = B.ms == 0;
+    }
+    if (seq) {
+      big_seq_step(h, hs, sm, B, ncand);
+      nIns++;
+      if (hs.fail) break;
+    } else {
+      nIns += bat_step(h, hs, B, ncand);
     }
   }
   if (lid == 0) hs.ncand = ncand;
@@ -1396,7 +1892,7 @@ __device__ __noinline__ double hull_volume_grid(const HullCtx& h, HullSm& hs, Gr
 
 template <int G>
 __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* slab, HullSm& hs, GrpSmem& sm,
-                         float* qcache, TinySm* ts, BigSm* bs) {
+                         float* qcache, TinySm* ts, BatSm* bs) {
   const int lid = Grp<G>::lid();
   const uint32_t partIdx = P.partBase + idx;
   PartDesc* pdp = D.parts + partIdx;
@@ -1738,7 +2234,7 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
   __shared__ HullSm hsm[Grp<G>::PER_BLOCK];
   __shared__ float qcs[G == 32 ? 8 * 3 * QC_MAX : 1];
   __shared__ TinySm tsm[G == 32 ? 8 : 1];
-  __shared__ typename std::conditional<G == 256, BigSm, char>::type bsm;
+  __shared__ typename std::conditional<G == 256, BatSm, char>::type bsm;
   const int gi = Grp<G>::gid();
   const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
   if (s >= P.nSlabs) return;
@@ -1756,7 +2252,7 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
       idx = grp_bcast_u<G>(idx, gsm[0]);
       if (idx >= P.nChildParts) break;
       if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr, reinterpret_cast<BigSm*>(&bsm));
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr, reinterpret_cast<BatSm*>(&bsm));
       Grp<G>::sync();
     }
     return;
