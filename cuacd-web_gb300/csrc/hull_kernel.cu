@@ -875,10 +875,12 @@ struct BigSm {
 #define BAT_FACES 32u   // faces of a batched patch, one per lane
 #define BAT_NEW 48u     // its horizon edges (a connected patch of n faces has at most n + 2)
 #define BAT_HASH_BITS 6u
-#define UNI_HASH_BITS 10u
-#define UNI_LOAD 640u
+#define UNI_HASH_BITS 9u  // holds the accepted patches' faces, at most BAT_K * BAT_FACES
+#define BAT_NRC 16u       // new-face records per step kept in shared memory
+// orphans listed per round (six words each in the visible list's and walk
+// queue's words); a round with more inserts its first step alone
 #ifndef TODO_CAP
-#define TODO_CAP (HULL_VIS_MAX / 2)
+#define TODO_CAP (HULL_VIS_MAX / 3)
 #endif
 struct BatWalk {
   uint32_t key[1u << BAT_HASH_BITS];  // patch face + 1; 0 = empty
@@ -899,13 +901,15 @@ struct BatSm {
   // owners, and its count of dead slots
   unsigned long long k1[256], k2[256];
   uint32_t s1[256], o1[256], s2[256], o2[256], dead[256];
-  // the accepted patches' faces (value: patch index) and the faces across
-  // their edges (value 0xff)
+  // the accepted patches' faces (value: step index)
   uint32_t ukey[1u << UNI_HASH_BITS];
   uint8_t uval[1u << UNI_HASH_BITS];
+  // words 0-2 of the first BAT_NRC new faces of each step
+  uint4 nrc[BAT_K][BAT_NRC][3];
   unsigned long long selKey[BAT_K], maxOrph[BAT_K];
   uint32_t selSlot[BAT_K], selOwn[BAT_K];
   uint32_t nfj[BAT_K + 1], nalj[BAT_K + 1];  // slot and alive counts before step j
+  uint32_t cf[BAT_K];                        // patch j meets an earlier patch
   uint32_t nsel, ms, ntodo, totDead;
 };
 
@@ -1181,38 +1185,45 @@ __device__ __forceinline__ void top2_publish(BatSm& B, const Top2& t, uint32_t d
 // kmax; and the total of the dead-slot counts
 __device__ __noinline__ void bat_select(BatSm& B, uint32_t kmax) {
   const uint32_t lane = threadIdx.x & 31;
+  // lane l merges threads l + 32 t: cur[t] is the next key of thread t
+  unsigned long long cur[8];
   uint32_t dn = 0;
-  for (uint32_t t = lane; t < 256; t += 32) dn += B.dead[t];
+#pragma unroll
+  for (uint32_t t = 0; t < 8; t++) {
+    cur[t] = B.k1[lane + 32 * t];
+    dn += B.dead[lane + 32 * t];
+  }
   dn = warp_sum_u(dn);
-  uint32_t cur = 0;  // keys taken from thread lane + 32 t, 2 bits per t
+  uint32_t taken = 0;  // bit t: thread t's first key is taken
   uint32_t n = 0;
   while (n < kmax) {
-    unsigned long long bk = 0;
+    unsigned long long bk = cur[0];
     uint32_t bt = 0;
 #pragma unroll
-    for (uint32_t t = 0; t < 8; t++) {
-      const uint32_t c = (cur >> (2 * t)) & 3u;
-      const uint32_t th = lane + 32 * t;
-      const unsigned long long k = c == 0 ? B.k1[th] : (c == 1 ? B.k2[th] : 0ull);
-      if (k > bk) { bk = k; bt = t; }
+    for (uint32_t t = 1; t < 8; t++) {
+      if (cur[t] > bk) { bk = cur[t]; bt = t; }
     }
-    unsigned long long m = bk;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long m2 = __shfl_xor_sync(FULLMASK, m, o);
-      m = m2 > m ? m2 : m;
-    }
-    if (m == 0) break;
+    // the warp's largest key: high words, then low words among the lanes
+    // holding the largest high word (a live key has a nonzero high word)
+    const uint32_t hi = __reduce_max_sync(FULLMASK, (uint32_t)(bk >> 32));
+    if (hi == 0) break;
+    const uint32_t lo = __reduce_max_sync(FULLMASK, (uint32_t)(bk >> 32) == hi ? (uint32_t)bk : 0u);
+    const unsigned long long m = ((unsigned long long)hi << 32) | lo;
     const uint32_t wl = __ffs(__ballot_sync(FULLMASK, bk == m)) - 1;
     uint32_t second = 0;
     if (lane == wl) {
-      const uint32_t c = (cur >> (2 * bt)) & 3u;
       const uint32_t th = lane + 32 * bt;
+      const bool first = ((taken >> bt) & 1u) == 0;
       B.selKey[n] = m;
-      B.selSlot[n] = c == 0 ? B.s1[th] : B.s2[th];
-      B.selOwn[n] = c == 0 ? B.o1[th] : B.o2[th];
-      cur += 1u << (2 * bt);
-      second = c;
+      B.selSlot[n] = first ? B.s1[th] : B.s2[th];
+      B.selOwn[n] = first ? B.o1[th] : B.o2[th];
+      const unsigned long long nk = first ? B.k2[th] : 0ull;
+#pragma unroll
+      for (uint32_t t = 0; t < 8; t++) {
+        if (t == bt) cur[t] = nk;
+      }
+      taken |= 1u << bt;
+      second = first ? 0u : 1u;
     }
     n++;
     if (__shfl_sync(FULLMASK, second, wl) != 0) break;
@@ -1337,48 +1348,63 @@ __device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatWalk& W,
   __syncwarp();
 }
 
-// warp 0: the longest prefix of the K walked picks whose patches are
-// disjoint and not adjacent, with neither the compaction rule (steps after
-// the first) nor the slot limit firing; the slot and alive counts before
-// each accepted step
-__device__ __noinline__ void bat_validate(const HullCtx& h, const HullSm& hs, BatSm& B, uint32_t K) {
-  constexpr uint32_t UB = UNI_HASH_BITS;
-  const uint32_t lane = threadIdx.x & 31;
-  for (uint32_t j = lane; j < (1u << UB); j += 32) B.ukey[j] = 0;
-  __syncwarp();
-  uint32_t nfc = hs.nf, nalc = hs.nalive, used = 0, ms = 0;
-  if (lane == 0) {
-    B.nfj[0] = nfc;
-    B.nalj[0] = nalc;
+// warp j < K: whether patch j meets an earlier walked patch i (a face of
+// patch j, or a face across one of its edges, lies in patch i); the whole
+// block clears the set of accepted faces
+__device__ __noinline__ void bat_conflicts(BatSm& B, uint32_t K) {
+  constexpr uint32_t HB = BAT_HASH_BITS, HN = 1u << HB;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (uint32_t j = threadIdx.x; j < (1u << UNI_HASH_BITS); j += 256) B.ukey[j] = 0;
+  if (warp >= K) return;
+  const BatWalk& W = B.u.w[warp];
+  bool hit = false;
+  if (W.ok && lane < W.n) {
+    const uint32_t f = W.f[lane], g0 = W.nb[lane][0], g1 = W.nb[lane][1], g2 = W.nb[lane][2];
+    for (uint32_t i = 0; i < warp && !hit; i++) {
+      const BatWalk& V = B.u.w[i];
+      // a later step never runs after a patch whose walk gave up
+      if (!V.ok) break;
+      hit = tab_find<HB>(V.key, f) < HN || tab_find<HB>(V.key, g0) < HN || tab_find<HB>(V.key, g1) < HN ||
+            tab_find<HB>(V.key, g2) < HN;
+    }
   }
+  hit = __any_sync(FULLMASK, hit);
+  if (lane == 0) B.cf[warp] = hit ? 1u : 0u;
+}
+
+// every thread: the number of accepted steps ms, the longest prefix of the
+// walked picks whose patches are whole, disjoint and not adjacent, with
+// neither the compaction rule (steps after the first) nor the slot limit
+// firing; the slot and alive counts before each step; warps j < ms add
+// patch j's faces to the accepted set
+__device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, BatSm& B, uint32_t K) {
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t nfc = hs.nf, nalc = hs.nalive, ms = 0;
   for (uint32_t j = 0; j < K; j++) {
     const BatWalk& W = B.u.w[j];
-    if (!W.ok) break;
+    if (!W.ok || B.cf[j]) break;
     if (j > 0 && (nfc + 3 * HULL_VIS_MAX > h.fmax || nfc > 2 * nalc + 512)) break;
-    const uint32_t n = W.n;
-    if (nfc + 3 * n > h.fmax || used + 4 * n > UNI_LOAD) break;
-    const uint32_t f = lane < n ? W.f[lane] : 0u;
-    if (__any_sync(FULLMASK, lane < n && tab_has<UB>(B.ukey, f))) break;
-    uint32_t at;
-    if (lane < n && tab_add<UB>(B.ukey, f, at) == 1) B.uval[at] = (uint8_t)j;
-    __syncwarp();
-    if (lane < n) {
-      for (int k = 0; k < 3; k++) {
-        if (tab_add<UB>(B.ukey, W.nb[lane][k], at) == 1) B.uval[at] = 0xffu;
-      }
+    if (nfc + 3 * W.n > h.fmax) break;
+    if (threadIdx.x == 0) {
+      B.nfj[j] = nfc;
+      B.nalj[j] = nalc;
     }
-    __syncwarp();
-    used += 4 * n;
     nfc += W.nnew;
-    nalc = nalc + W.nnew - n;
+    nalc = nalc + W.nnew - W.n;
     ms = j + 1;
-    if (lane == 0) {
-      B.nfj[j + 1] = nfc;
-      B.nalj[j + 1] = nalc;
-    }
   }
-  if (lane == 0) B.ms = ms;
-  __syncwarp();
+  if (threadIdx.x == 0) {
+    B.nfj[ms] = nfc;
+    B.nalj[ms] = nalc;
+    B.ms = ms;
+    B.ntodo = 0;
+  }
+  if (threadIdx.x < BAT_K) B.maxOrph[threadIdx.x] = 0;
+  if (warp < ms && lane < B.u.w[warp].n) {
+    uint32_t at;
+    if (tab_add<UNI_HASH_BITS>(B.ukey, B.u.w[warp].f[lane], at) == 1) B.uval[at] = (uint8_t)warp;
+  }
+  return ms;
 }
 
 // squeeze dead slots out of the candidate list (slot order kept); returns
@@ -1548,19 +1574,50 @@ __device__ __noinline__ void big_seq_step(const HullCtx& h, HullSm& hs, GrpSmem&
   }
 }
 
-// A batched round after validation (B.ms >= 1 steps): the new faces of
-// every validated step at their slots, one pass over the candidate slots
-// that lists the orphans of the validated patches (the walk queue's and
-// visible list's words: slot, then new owner, new distance and step), the
-// orphans' new owners over their step's new faces and the largest new key
-// per step, the accepted prefix, then its commit (twin links, dead faces,
-// counts) and the orphans' new owners. Returns the number of insertions.
+// best_face over the new faces [f0, f1) of one step (all alive), the first
+// BAT_NRC records read from shared memory
+__device__ __forceinline__ void bat_best(const HullCtx& h, uint32_t i, uint32_t f0, uint32_t f1, const uint4 (*nrc)[3],
+                                         uint32_t& outF, float& outD) {
+  const f3 pt = h.qvert(i);
+  uint32_t bestF = CUACD_NONE;
+  float bestD = 0.0f;
+  for (uint32_t f = f0; f < f1; f++) {
+    const uint32_t q = f - f0;
+    uint4 w0, w1, w2;
+    if (q < BAT_NRC) {
+      w0 = nrc[q][0]; w1 = nrc[q][1]; w2 = nrc[q][2];
+    } else {
+      const uint4* w = h.rec(f);
+      w0 = w[0]; w1 = w[1]; w2 = w[2];
+    }
+    const float dd = h.face_filter(w0, w1, w2, pt, i);
+    if (dd > bestD) { bestD = dd; bestF = f; }
+    if (dd == 0.0f && bestF == CUACD_NONE && h.face_exact(w2, h.rec(f)[3], pt)) { bestD = 1e-30f; bestF = f; }
+  }
+  outF = bestF;
+  outD = bestD;
+}
+
+// A batched round after validation (ms >= 1 steps): the new faces of every
+// validated step at their slots while one pass over the candidate slots
+// lists the orphans of the validated patches (six words each in the
+// visible list's and walk queue's words: slot, point, owner, then new
+// owner, new distance, step), the orphans' new owners over their step's
+// new faces and the largest new key per step, the accepted prefix, then its
+// commit (twin links, dead faces, counts) and the orphans' new owners.
+// Returns the number of insertions.
 __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B, uint32_t ncand) {
   constexpr int G = 256;
   constexpr uint32_t UB = UNI_HASH_BITS;
   constexpr uint32_t UN = 1u << UB;
   const uint32_t lid = threadIdx.x, warp = lid >> 5, lane = lid & 31;
   const uint32_t ms = B.ms, nf0 = hs.nf;
+  uint32_t* tK = h.vis;
+  uint32_t* tI = h.vis + TODO_CAP;
+  uint32_t* tO = h.vis + 2 * TODO_CAP;
+  uint32_t* tNO = h.q;
+  uint32_t* tND = h.q + TODO_CAP;
+  uint32_t* tJ = h.q + 2 * TODO_CAP;
   // new faces (a, b, pick) and the links among them and to the twins;
   // records of steps that are not accepted lie above the slot count and
   // are overwritten later
@@ -1574,6 +1631,9 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       h.face_make_q(a, b, pIdx, p, w0, w1, w2, w3);
       uint4* w = h.rec(s);
       w[0] = w0; w[1] = w1; w[2] = w2; w[3] = w3;
+      if (q < BAT_NRC) {
+        B.nrc[warp][q][0] = w0; B.nrc[warp][q][1] = w1; B.nrc[warp][q][2] = w2;
+      }
       // around the horizon loop: (b, p) borders the new face starting at
       // b, (p, a) the new face ending at a
       uint32_t j1 = 0, j2 = 0;
@@ -1587,9 +1647,6 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       nq[2] = base + j2;
     }
   }
-  if (lid == 0) B.ntodo = 0;
-  if (lid < BAT_K) B.maxOrph[lid] = 0;
-  __syncthreads();
   // one pass over the slots, four per thread in flight
   Top2 top;
   top.clear();
@@ -1614,10 +1671,13 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
         dead++;
         continue;
       }
-      const uint32_t at = tab_find<UB>(B.ukey, own);
-      if (at < UN && B.uval[at] < BAT_K) {
+      if (tab_find<UB>(B.ukey, own) < UN) {
         const uint32_t t = atomicAdd(&B.ntodo, 1u);
-        if (t < TODO_CAP) h.vis[t] = k;
+        if (t < TODO_CAP) {
+          tK[t] = k;
+          tI[t] = ci[u];
+          tO[t] = own;
+        }
         continue;
       }
       top.add(cand_key(cd[u], ci[u]), k, own);
@@ -1628,18 +1688,17 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
   uint32_t m = 1;
   if (nt <= TODO_CAP) {
     for (uint32_t t = lid; t < nt; t += G) {
-      const uint32_t k = h.vis[t], own = h.owner[k];
+      const uint32_t k = tK[t], i = tI[t], own = tO[t];
       const uint32_t j = B.uval[tab_find<UB>(B.ukey, own)];
       uint32_t no = CUACD_NONE;
       float nd = 0.0f;
       if (k != B.selSlot[j]) {
-        const uint32_t i = h.cand[k];
-        slot_reassign(h, i, own, true, false, B.nfj[j], B.nfj[j + 1], nullptr, no, nd);
+        bat_best(h, i, B.nfj[j], B.nfj[j + 1], B.nrc[j], no, nd);
         if (no != CUACD_NONE) atomicMax(&B.maxOrph[j], cand_key(nd, i));
       }
-      h.vis[TODO_CAP + t] = no;
-      h.q[t] = __float_as_uint(nd);
-      h.q[TODO_CAP + t] = j;
+      tNO[t] = no;
+      tND[t] = __float_as_uint(nd);
+      tJ[t] = j;
     }
     __syncthreads();
     // pick j is next while every earlier step's orphans stay below its key
@@ -1675,16 +1734,16 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
     // accepted steps' orphans take their new owners (the picks leave);
     // the others keep theirs
     for (uint32_t t = lid; t < nt; t += G) {
-      const uint32_t k = h.vis[t], j = h.q[TODO_CAP + t];
+      const uint32_t k = tK[t], i = tI[t], j = tJ[t];
       if (j < m) {
-        const uint32_t no = h.vis[TODO_CAP + t];
-        const float nd = __uint_as_float(h.q[t]);
+        const uint32_t no = tNO[t];
+        const float nd = __uint_as_float(tND[t]);
         h.owner[k] = no;
         h.dist[k] = nd;
         if (no == CUACD_NONE) dead++;
-        else top.add(cand_key(nd, h.cand[k]), k, no);
+        else top.add(cand_key(nd, i), k, no);
       } else {
-        top.add(cand_key(h.dist[k], h.cand[k]), k, h.owner[k]);
+        top.add(cand_key(h.dist[k], i), k, tO[t]);
       }
     }
   } else {
@@ -1694,7 +1753,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       const uint32_t own = h.owner[k];
       if (own == CUACD_NONE) continue;
       const uint32_t at = tab_find<UB>(B.ukey, own);
-      if (at >= UN || B.uval[at] >= BAT_K) continue;
+      if (at >= UN) continue;
       const uint32_t i = h.cand[k];
       if (B.uval[at] != 0) {
         top.add(cand_key(h.dist[k], i), k, own);
@@ -1702,7 +1761,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       }
       uint32_t no = CUACD_NONE;
       float nd = 0.0f;
-      if (k != B.selSlot[0]) slot_reassign(h, i, own, true, false, B.nfj[0], B.nfj[1], nullptr, no, nd);
+      if (k != B.selSlot[0]) bat_best(h, i, B.nfj[0], B.nfj[1], B.nrc[0], no, nd);
       h.owner[k] = no;
       h.dist[k] = nd;
       if (no == CUACD_NONE) dead++;
@@ -1763,9 +1822,10 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
         bat_walk(h, hs.nf, B.u.w[warp], 0xffffffffu - (uint32_t)(B.selKey[warp] & 0xffffffffu), B.selOwn[warp]);
       }
       __syncthreads();
-      if (warp == 0) bat_validate(h, hs, B, K);
+      bat_conflicts(B, K);
       __syncthreads();
-      seq = B.ms == 0;
+      seq = bat_prefix(h, hs, B, K) == 0;
+      __syncthreads();
     }
     if (seq) {
       big_seq_step(h, hs, sm, B, ncand);
