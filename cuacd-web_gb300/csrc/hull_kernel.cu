@@ -875,8 +875,11 @@ struct BigSm {
 #define BAT_FACES 32u   // faces of a batched patch, one per lane
 #define BAT_NEW 48u     // its horizon edges (a connected patch of n faces has at most n + 2)
 #define BAT_HASH_BITS 6u
-#define UNI_HASH_BITS 9u  // holds the accepted patches' faces, at most BAT_K * BAT_FACES
-#define BAT_NRC 16u       // new-face records per step kept in shared memory
+// the faces of every whole walked patch: at most BAT_K * BAT_FACES, so the
+// set is never more than half full
+#define BLK_HASH_BITS 9u
+#define BAT_NRC 16u  // new-face records per step kept in shared memory
+#define BAT_LIST 8u  // keys per warp list
 // orphans listed per round (six words each in the visible list's and walk
 // queue's words); a round with more inserts its first step alone
 #ifndef TODO_CAP
@@ -897,20 +900,22 @@ struct BatSm {
     BigSm big;  // the single-pick step
     BatWalk w[BAT_K];
   } u;
-  // per thread: its two largest candidate keys with their slots and
-  // owners, and its count of dead slots
-  unsigned long long k1[256], k2[256];
-  uint32_t s1[256], o1[256], s2[256], o2[256], dead[256];
-  // the accepted patches' faces (value: step index)
-  uint32_t ukey[1u << UNI_HASH_BITS];
-  uint8_t uval[1u << UNI_HASH_BITS];
+  // per warp: its largest candidate keys in descending order with their
+  // slots and owners, their count, whether keys below the last one may be
+  // missing, and the warp's count of dead slots
+  unsigned long long wk[8][BAT_LIST];
+  uint32_t ws[8][BAT_LIST], wo[8][BAT_LIST];
+  uint32_t wn[8], wt[8], wdead[8];
+  // faces of the whole walked patches (face + 1, 0 = empty) with the bit
+  // mask of the walks (warps) that hold them
+  uint2 btab[1u << BLK_HASH_BITS];
   // words 0-2 of the first BAT_NRC new faces of each step
   uint4 nrc[BAT_K][BAT_NRC][3];
   unsigned long long selKey[BAT_K], maxOrph[BAT_K];
   uint32_t selSlot[BAT_K], selOwn[BAT_K];
   uint32_t nfj[BAT_K + 1], nalj[BAT_K + 1];  // slot and alive counts before step j
   uint32_t cf[BAT_K];                        // patch j meets an earlier patch
-  uint32_t nsel, ms, ntodo, totDead;
+  uint32_t nsel, ntodo, totDead;
 };
 
 // open-addressing face sets in shared memory (face + 1 stored, 0 = empty)
@@ -954,6 +959,33 @@ __device__ __forceinline__ uint32_t tab_add(uint32_t* key, uint32_t f, uint32_t&
     s = (s + 1) & (N - 1);
   }
   return 2;
+}
+
+// the block's set of whole walked patches' faces: add f with a walk's bit
+// (the set never fills: at most half its entries are used)
+__device__ __forceinline__ void btab_add(BatSm& B, uint32_t f, uint32_t bit) {
+  constexpr uint32_t N = 1u << BLK_HASH_BITS;
+  uint32_t s = tab_hash<BLK_HASH_BITS>(f);
+  for (uint32_t n = 0; n < N; n++) {
+    const uint32_t old = atomicCAS(&B.btab[s].x, 0u, f + 1);
+    if (old == 0 || old == f + 1) {
+      atomicOr(&B.btab[s].y, bit);
+      return;
+    }
+    s = (s + 1) & (N - 1);
+  }
+}
+// the mask of the walks holding face f, 0 when none (the set is not changing)
+__device__ __forceinline__ uint32_t btab_mask(const BatSm& B, uint32_t f) {
+  constexpr uint32_t N = 1u << BLK_HASH_BITS;
+  uint32_t s = tab_hash<BLK_HASH_BITS>(f);
+  for (uint32_t n = 0; n < N; n++) {
+    const uint2 e = B.btab[s];
+    if (e.x == f + 1) return e.y;
+    if (e.x == 0) return 0;
+    s = (s + 1) & (N - 1);
+  }
+  return 0;
 }
 
 __device__ __forceinline__ uint32_t big_hash(uint32_t f) { return (f * 2654435761u) >> 24; }
@@ -1172,61 +1204,77 @@ struct Top2 {
     }
   }
 };
+// every thread of the block: the warp's largest keys from its threads' two
+// largest, in descending order, for as long as the order is certain (once a
+// thread's second key is taken its third could come next, and keys below
+// the BAT_LIST-th may be missing: the list is marked truncated), and the
+// warp's count of dead slots
 __device__ __forceinline__ void top2_publish(BatSm& B, const Top2& t, uint32_t dead) {
-  const uint32_t i = threadIdx.x;
-  B.k1[i] = t.k1; B.k2[i] = t.k2;
-  B.s1[i] = t.s1; B.o1[i] = t.o1; B.s2[i] = t.s2; B.o2[i] = t.o2;
-  B.dead[i] = dead;
+  const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  unsigned long long cur = t.k1;
+  bool first = true;
+  uint32_t n = 0, trunc = 1;
+  const uint32_t dn = warp_sum_u(dead);
+  for (; n < BAT_LIST; n++) {
+    // the largest key: high words, then low words among the lanes holding
+    // the largest high word (a live key has a nonzero high word)
+    const uint32_t hi = __reduce_max_sync(FULLMASK, (uint32_t)(cur >> 32));
+    if (hi == 0) {
+      trunc = 0;
+      break;
+    }
+    const uint32_t lo = __reduce_max_sync(FULLMASK, (uint32_t)(cur >> 32) == hi ? (uint32_t)cur : 0u);
+    const unsigned long long m = ((unsigned long long)hi << 32) | lo;
+    bool sec = false;
+    if (cur == m) {
+      B.wk[w][n] = m;
+      B.ws[w][n] = first ? t.s1 : t.s2;
+      B.wo[w][n] = first ? t.o1 : t.o2;
+      sec = !first;
+      cur = first ? t.k2 : 0ull;
+      first = false;
+    }
+    if (__any_sync(FULLMASK, sec)) {
+      n++;
+      break;
+    }
+  }
+  if (lane == 0) {
+    B.wn[w] = n;
+    B.wt[w] = trunc;
+    B.wdead[w] = dn;
+  }
 }
 
-// warp 0: the block's largest keys in descending order for as long as the
-// order is certain (each thread publishes its two largest, so the list ends
-// once a thread's second key is taken: its third could come next), at most
-// kmax; and the total of the dead-slot counts
+// warp 0: the block's largest keys in descending order, at most kmax, by
+// merging the warps' lists (lane w holds list w's next key). Every key of a
+// warp above the last key of its truncated list is in the list, so the
+// merge stops after taking such a last key; and the total of the dead-slot
+// counts
 __device__ __noinline__ void bat_select(BatSm& B, uint32_t kmax) {
   const uint32_t lane = threadIdx.x & 31;
-  // lane l merges threads l + 32 t: cur[t] is the next key of thread t
-  unsigned long long cur[8];
-  uint32_t dn = 0;
-#pragma unroll
-  for (uint32_t t = 0; t < 8; t++) {
-    cur[t] = B.k1[lane + 32 * t];
-    dn += B.dead[lane + 32 * t];
-  }
-  dn = warp_sum_u(dn);
-  uint32_t taken = 0;  // bit t: thread t's first key is taken
+  const uint32_t wn = lane < 8 ? B.wn[lane] : 0u;
+  const bool wt = lane < 8 && B.wt[lane] != 0;
+  const uint32_t dn = warp_sum_u(lane < 8 ? B.wdead[lane] : 0u);
+  uint32_t pos = 0;
+  unsigned long long cur = wn > 0 ? B.wk[lane][0] : 0ull;
   uint32_t n = 0;
   while (n < kmax) {
-    unsigned long long bk = cur[0];
-    uint32_t bt = 0;
-#pragma unroll
-    for (uint32_t t = 1; t < 8; t++) {
-      if (cur[t] > bk) { bk = cur[t]; bt = t; }
-    }
-    // the warp's largest key: high words, then low words among the lanes
-    // holding the largest high word (a live key has a nonzero high word)
-    const uint32_t hi = __reduce_max_sync(FULLMASK, (uint32_t)(bk >> 32));
+    const uint32_t hi = __reduce_max_sync(FULLMASK, (uint32_t)(cur >> 32));
     if (hi == 0) break;
-    const uint32_t lo = __reduce_max_sync(FULLMASK, (uint32_t)(bk >> 32) == hi ? (uint32_t)bk : 0u);
+    const uint32_t lo = __reduce_max_sync(FULLMASK, (uint32_t)(cur >> 32) == hi ? (uint32_t)cur : 0u);
     const unsigned long long m = ((unsigned long long)hi << 32) | lo;
-    const uint32_t wl = __ffs(__ballot_sync(FULLMASK, bk == m)) - 1;
-    uint32_t second = 0;
-    if (lane == wl) {
-      const uint32_t th = lane + 32 * bt;
-      const bool first = ((taken >> bt) & 1u) == 0;
+    bool stop = false;
+    if (cur == m) {
       B.selKey[n] = m;
-      B.selSlot[n] = first ? B.s1[th] : B.s2[th];
-      B.selOwn[n] = first ? B.o1[th] : B.o2[th];
-      const unsigned long long nk = first ? B.k2[th] : 0ull;
-#pragma unroll
-      for (uint32_t t = 0; t < 8; t++) {
-        if (t == bt) cur[t] = nk;
-      }
-      taken |= 1u << bt;
-      second = first ? 0u : 1u;
+      B.selSlot[n] = B.ws[lane][pos];
+      B.selOwn[n] = B.wo[lane][pos];
+      pos++;
+      stop = pos == wn && wt;
+      cur = pos < wn ? B.wk[lane][pos] : 0ull;
     }
     n++;
-    if (__shfl_sync(FULLMASK, second, wl) != 0) break;
+    if (__any_sync(FULLMASK, stop)) break;
   }
   if (lane == 0) {
     B.nsel = n;
@@ -1237,11 +1285,13 @@ __device__ __noinline__ void bat_select(BatSm& B, uint32_t kmax) {
 
 // one warp: the visible patch of point pIdx on the current hull, walked
 // from its owner face `start` as big_insert walks it, in slot order, and
-// its horizon edges in the insertion's order (e = 3 * listPos + k). W.ok = 0
+// its horizon edges in the insertion's order (e = 3 * listPos + k); the
+// patch's faces also go into the block's set with the warp's bit. W.ok = 0
 // when the patch has more than BAT_FACES faces.
-__device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatWalk& W, uint32_t pIdx, uint32_t start) {
+__device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatSm& B, uint32_t pIdx, uint32_t start) {
   constexpr uint32_t HB = BAT_HASH_BITS;
-  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BatWalk& W = B.u.w[warp];
   const uint32_t lt = lanemask_lt();
   const f3 p = h.qvert(pIdx);
   for (uint32_t j = lane; j < (1u << HB); j += 32) W.key[j] = 0;
@@ -1314,6 +1364,7 @@ __device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatWalk& W,
     uint32_t r = 0;
     for (uint32_t j = 0; j < n; j++) r += W.f[j] < fi ? 1u : 0u;
     W.ord[r] = lane;
+    btab_add(B, fi, 1u << warp);
   }
   __syncwarp();
   uint32_t nnew = 0;
@@ -1348,25 +1399,21 @@ __device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatWalk& W,
   __syncwarp();
 }
 
-// warp j < K: whether patch j meets an earlier walked patch i (a face of
-// patch j, or a face across one of its edges, lies in patch i); the whole
-// block clears the set of accepted faces
+// warp j < K: whether patch j meets an earlier walked patch (a face of
+// patch j, or a face across one of its edges, was claimed by a walk i < j);
+// the round's counters are reset
 __device__ __noinline__ void bat_conflicts(BatSm& B, uint32_t K) {
-  constexpr uint32_t HB = BAT_HASH_BITS, HN = 1u << HB;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (uint32_t j = threadIdx.x; j < (1u << UNI_HASH_BITS); j += 256) B.ukey[j] = 0;
+  if (threadIdx.x == 0) B.ntodo = 0;
+  if (threadIdx.x < BAT_K) B.maxOrph[threadIdx.x] = 0;
   if (warp >= K) return;
   const BatWalk& W = B.u.w[warp];
+  const uint32_t below = (1u << warp) - 1u;
   bool hit = false;
   if (W.ok && lane < W.n) {
-    const uint32_t f = W.f[lane], g0 = W.nb[lane][0], g1 = W.nb[lane][1], g2 = W.nb[lane][2];
-    for (uint32_t i = 0; i < warp && !hit; i++) {
-      const BatWalk& V = B.u.w[i];
-      // a later step never runs after a patch whose walk gave up
-      if (!V.ok) break;
-      hit = tab_find<HB>(V.key, f) < HN || tab_find<HB>(V.key, g0) < HN || tab_find<HB>(V.key, g1) < HN ||
-            tab_find<HB>(V.key, g2) < HN;
-    }
+    const uint32_t g[4] = {W.f[lane], W.nb[lane][0], W.nb[lane][1], W.nb[lane][2]};
+#pragma unroll
+    for (int k = 0; k < 4; k++) hit = hit || (btab_mask(B, g[k]) & below) != 0;
   }
   hit = __any_sync(FULLMASK, hit);
   if (lane == 0) B.cf[warp] = hit ? 1u : 0u;
@@ -1375,11 +1422,13 @@ __device__ __noinline__ void bat_conflicts(BatSm& B, uint32_t K) {
 // every thread: the number of accepted steps ms, the longest prefix of the
 // walked picks whose patches are whole, disjoint and not adjacent, with
 // neither the compaction rule (steps after the first) nor the slot limit
-// firing; the slot and alive counts before each step; warps j < ms add
-// patch j's faces to the accepted set
-__device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, BatSm& B, uint32_t K) {
-  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+// firing; *base = the first new-face slot of the thread's warp's step.
+// Thread 0 stores the slot and alive counts before each step.
+__device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, BatSm& B, uint32_t K,
+                                            uint32_t* base) {
+  const uint32_t warp = threadIdx.x >> 5;
   uint32_t nfc = hs.nf, nalc = hs.nalive, ms = 0;
+  *base = nfc;
   for (uint32_t j = 0; j < K; j++) {
     const BatWalk& W = B.u.w[j];
     if (!W.ok || B.cf[j]) break;
@@ -1389,6 +1438,7 @@ __device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, 
       B.nfj[j] = nfc;
       B.nalj[j] = nalc;
     }
+    if (j == warp) *base = nfc;
     nfc += W.nnew;
     nalc = nalc + W.nnew - W.n;
     ms = j + 1;
@@ -1396,13 +1446,6 @@ __device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, 
   if (threadIdx.x == 0) {
     B.nfj[ms] = nfc;
     B.nalj[ms] = nalc;
-    B.ms = ms;
-    B.ntodo = 0;
-  }
-  if (threadIdx.x < BAT_K) B.maxOrph[threadIdx.x] = 0;
-  if (warp < ms && lane < B.u.w[warp].n) {
-    uint32_t at;
-    if (tab_add<UNI_HASH_BITS>(B.ukey, B.u.w[warp].f[lane], at) == 1) B.uval[at] = (uint8_t)warp;
   }
   return ms;
 }
@@ -1606,12 +1649,11 @@ __device__ __forceinline__ void bat_best(const HullCtx& h, uint32_t i, uint32_t 
 // new faces and the largest new key per step, the accepted prefix, then its
 // commit (twin links, dead faces, counts) and the orphans' new owners.
 // Returns the number of insertions.
-__device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B, uint32_t ncand) {
+__device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B, uint32_t ncand, uint32_t ms,
+                                          uint32_t myBase) {
   constexpr int G = 256;
-  constexpr uint32_t UB = UNI_HASH_BITS;
-  constexpr uint32_t UN = 1u << UB;
   const uint32_t lid = threadIdx.x, warp = lid >> 5, lane = lid & 31;
-  const uint32_t ms = B.ms, nf0 = hs.nf;
+  const uint32_t nf0 = hs.nf;
   uint32_t* tK = h.vis;
   uint32_t* tI = h.vis + TODO_CAP;
   uint32_t* tO = h.vis + 2 * TODO_CAP;
@@ -1623,7 +1665,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
   // are overwritten later
   if (warp < ms) {
     const BatWalk& W = B.u.w[warp];
-    const uint32_t base = B.nfj[warp], nnew = W.nnew, pIdx = W.pick;
+    const uint32_t base = myBase, nnew = W.nnew, pIdx = W.pick;
     const f3 p = h.qvert(pIdx);
     for (uint32_t q = lane; q < nnew; q += 32) {
       const uint32_t a = W.hA[q], b = W.hB[q], s = base + q;
@@ -1671,12 +1713,16 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
         dead++;
         continue;
       }
-      if (tab_find<UB>(B.ukey, own) < UN) {
+      // the first walk holding the owner: an earlier step's patch when two
+      // hold it, and then only that step can be accepted
+      const uint32_t j = __ffs(btab_mask(B, own)) - 1u;
+      if (j < ms) {
         const uint32_t t = atomicAdd(&B.ntodo, 1u);
         if (t < TODO_CAP) {
           tK[t] = k;
           tI[t] = ci[u];
           tO[t] = own;
+          tJ[t] = j;
         }
         continue;
       }
@@ -1688,8 +1734,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
   uint32_t m = 1;
   if (nt <= TODO_CAP) {
     for (uint32_t t = lid; t < nt; t += G) {
-      const uint32_t k = tK[t], i = tI[t], own = tO[t];
-      const uint32_t j = B.uval[tab_find<UB>(B.ukey, own)];
+      const uint32_t k = tK[t], i = tI[t], j = tJ[t];
       uint32_t no = CUACD_NONE;
       float nd = 0.0f;
       if (k != B.selSlot[j]) {
@@ -1698,7 +1743,6 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       }
       tNO[t] = no;
       tND[t] = __float_as_uint(nd);
-      tJ[t] = j;
     }
     __syncthreads();
     // pick j is next while every earlier step's orphans stay below its key
@@ -1752,10 +1796,10 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
     for (uint32_t k = lid; k < ncand; k += G) {
       const uint32_t own = h.owner[k];
       if (own == CUACD_NONE) continue;
-      const uint32_t at = tab_find<UB>(B.ukey, own);
-      if (at >= UN) continue;
+      const uint32_t j = __ffs(btab_mask(B, own)) - 1u;
+      if (j >= ms) continue;
       const uint32_t i = h.cand[k];
-      if (B.uval[at] != 0) {
+      if (j != 0) {
         top.add(cand_key(h.dist[k], i), k, own);
         continue;
       }
@@ -1807,6 +1851,7 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
   __syncthreads();
   uint32_t nIns = 0;
   while (nIns < maxIter) {
+    for (uint32_t e = lid; e < (1u << BLK_HASH_BITS); e += G) B.btab[e] = make_uint2(0u, 0u);
     if (warp == 0) bat_select(B, min(BAT_K, maxIter - nIns));
     __syncthreads();
     // squeeze dead slots out when they reach a quarter of the list
@@ -1816,23 +1861,24 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
     }
     const uint32_t K = B.nsel;
     if (K == 0) break;
-    bool seq = hs.nf + 3 * HULL_VIS_MAX > h.fmax || hs.nf > 2 * hs.nalive + 512;
-    if (!seq) {
-      if (warp < K) {
-        bat_walk(h, hs.nf, B.u.w[warp], 0xffffffffu - (uint32_t)(B.selKey[warp] & 0xffffffffu), B.selOwn[warp]);
-      }
+    uint32_t ms = 0, myBase = 0;
+    if (hs.nf + 3 * HULL_VIS_MAX <= h.fmax && hs.nf <= 2 * hs.nalive + 512) {
+      if (warp < K) bat_walk(h, hs.nf, B, 0xffffffffu - (uint32_t)(B.selKey[warp] & 0xffffffffu), B.selOwn[warp]);
       __syncthreads();
       bat_conflicts(B, K);
       __syncthreads();
-      seq = bat_prefix(h, hs, B, K) == 0;
-      __syncthreads();
+      // the same on every thread; the slot pass reads the block's set of
+      // claimed faces, which no thread writes until the next round
+      ms = bat_prefix(h, hs, B, K, &myBase);
     }
-    if (seq) {
+    if (ms == 0) {
+      // the single-pick step's shared words overlay the walks' words
+      __syncthreads();
       big_seq_step(h, hs, sm, B, ncand);
       nIns++;
       if (hs.fail) break;
     } else {
-      nIns += bat_step(h, hs, B, ncand);
+      nIns += bat_step(h, hs, B, ncand, ms, myBase);
     }
   }
   if (lid == 0) hs.ncand = ncand;
