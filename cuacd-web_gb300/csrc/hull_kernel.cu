@@ -880,6 +880,14 @@ struct BigSm {
 #define BLK_HASH_BITS 9u
 #define BAT_NRC 16u  // new-face records per step kept in shared memory
 #define BAT_LIST 8u  // keys per warp list
+// candidate slots per thread in flight in the batched round's slot pass
+#ifndef SCAN_U
+#define SCAN_U 4
+#endif
+// dead candidate slots are squeezed out above 1 / SQZ_DIV of the list
+#ifndef SQZ_DIV
+#define SQZ_DIV 8u
+#endif
 // orphans listed per round (six words each in the visible list's and walk
 // queue's words); a round with more inserts its first step alone
 #ifndef TODO_CAP
@@ -1689,15 +1697,15 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       nq[2] = base + j2;
     }
   }
-  // one pass over the slots, four per thread in flight
+  // one pass over the slots, SCAN_U per thread in flight
   Top2 top;
   top.clear();
   uint32_t dead = 0;
-  for (uint32_t k0 = lid; k0 < ncand; k0 += 4 * G) {
-    uint32_t ow[4], ci[4];
-    float cd[4];
+  for (uint32_t k0 = lid; k0 < ncand; k0 += SCAN_U * G) {
+    uint32_t ow[SCAN_U], ci[SCAN_U];
+    float cd[SCAN_U];
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < SCAN_U; u++) {
       const uint32_t k = k0 + u * G;
       const bool in = k < ncand;
       ow[u] = in ? h.owner[k] : CUACD_NONE;
@@ -1705,7 +1713,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       cd[u] = in ? h.dist[k] : 0.0f;
     }
 #pragma unroll
-    for (int u = 0; u < 4; u++) {
+    for (int u = 0; u < SCAN_U; u++) {
       const uint32_t k = k0 + u * G;
       if (k >= ncand) break;
       const uint32_t own = ow[u];
@@ -1854,8 +1862,8 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
     for (uint32_t e = lid; e < (1u << BLK_HASH_BITS); e += G) B.btab[e] = make_uint2(0u, 0u);
     if (warp == 0) bat_select(B, min(BAT_K, maxIter - nIns));
     __syncthreads();
-    // squeeze dead slots out when they reach a quarter of the list
-    if (4 * B.totDead > ncand) {
+    // squeeze dead slots out when they pass 1 / SQZ_DIV of the list
+    if (SQZ_DIV * B.totDead > ncand) {
       ncand = big_squeeze(h, sm, B, ncand);
       continue;
     }
