@@ -371,13 +371,34 @@ def run_secondary(args):
     tree_mod = importlib.import_module("cuacd-web_gb300.tree")
     gen = importlib.import_module("cuacd-web_gb300.meshgen")
     mesh = importlib.import_module("cuacd-web_gb300.mesh")
-    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096, hullBudgetBytes=6 << 30,
-                         scratchWords=256 << 20)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    n = args.pairs
-    parts = [gen.noisy_icosphere(3, noise=0.15, seed=s) for s in range(n)]
-    hulls, _ = g.hull_meshes(parts)
-    if args.workload == "hausdorff":
+    if args.workload == "bighulls":
+        # the large-part hulls of a decomposition's first cuts: the 56k-triangle
+        # blob mesh (28,152 points) cut by 64 seeded planes through its middle
+        dec = importlib.import_module("cuacd-web_gb300.decompose")
+        big = mesh.normalize(gen.blob_mesh(24, 71, seed=0))[0]
+        rng = np.random.default_rng(0)
+        parts = []
+        for _ in range(64):
+            nrm = rng.normal(size=3)
+            nrm /= np.linalg.norm(nrm)
+            parts += list(dec.plane_cut(big, [nrm[0], nrm[1], nrm[2], rng.uniform(-0.2, 0.2)]))
+        g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=32768,
+                             hullBudgetBytes=16 << 30, scratchWords=64 << 20)
+        n = len(parts)
+        call = lambda: g.hull_meshes(parts, no_export=True)  # noqa: E731
+        metric, unit, units = "convex hulls/s", "hulls/s", n
+        cfg = {"workload": f"hulls of the {n} halves of the 56,300-triangle blob mesh cut by 64 seeded planes "
+                           f"(mean {np.mean([m.nv for m in parts]):.0f} points)", "l2": "flushed between steps"}
+    else:
+        g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096,
+                             hullBudgetBytes=6 << 30, scratchWords=256 << 20)
+        n = args.pairs
+        parts = [gen.noisy_icosphere(3, noise=0.15, seed=s) for s in range(n)]
+        hulls, _ = g.hull_meshes(parts)
+    if args.workload == "bighulls":
+        pass
+    elif args.workload == "hausdorff":
         pairs = [(m, mesh.Mesh(m.verts, h["tris"])) for m, h in zip(parts, hulls)]
         evals = sum(sample_counts(a) * b.nt + sample_counts(b) * a.nt for a, b in pairs)
         call = lambda: g.hausdorff(pairs)  # noqa: E731
@@ -434,6 +455,18 @@ def run_secondary(args):
         for c, name in ((67, "flops_face_interior"), (150, "flops_edge_tests")):
             line.setdefault("fp32_exhaustive", {})[name] = c * ex_value / 1e12
         line["fp32_exhaustive"]["peak_tflops_nominal"] = peak
+    if args.workload == "bighulls":
+        # one hull alone: the whole mesh's point set, its latency
+        one = [big]
+        for _ in range(args.warmup):
+            g.hull_meshes(one, no_export=True)
+        t = []
+        for _ in range(args.steps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            g.hull_meshes(one, no_export=True)
+            t.append(g.last_gpu_ms)
+        line["single"] = {"points": big.nv, "ms": statistics.median(t)}
     print(json.dumps(line), flush=True)
 
 
@@ -608,7 +641,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--seeds", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls", "decompose", "serve"])
+    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls", "bighulls", "decompose", "serve"])
     ap.add_argument("--pairs", type=int, default=256)
     ap.add_argument("--meshes", type=int, default=32, help="meshes of the uneven decomposition batch")
     ap.add_argument("--no-decompose", action="store_true", help="leave the decomposition summary out of the tree line")
