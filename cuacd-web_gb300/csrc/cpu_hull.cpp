@@ -538,27 +538,91 @@ inline PtKey pt_key(double x, double y, double z) {
 
 double hyp3(double x, double y, double z) { return std::hypot(x, y, z); }
 
-// every point within tol of every plane (n . p - d <= tol), the points in
-// SoA arrays so the inner loop vectorises; a large set is split over threads
+// every point within tol of every plane (n . p - d <= tol). The points are
+// grouped, 32 consecutive points in Morton order of their coordinates, each
+// group with a bounding sphere; a plane skips a group whose sphere lies
+// below tol by more than a slack that covers the rounding of the bound and
+// of every per-point value (both at most a few units in the last place of
+// |n| |p| + |d|; the slack is 1e-9 of that), so the answer is the per-point
+// loop's. A large set is split over threads.
 bool all_inside(const std::vector<double>& planes, const float* V, const std::vector<uint32_t>& idx, double tol) {
+  constexpr size_t GS = 32;
   const size_t n = idx.size(), nf = planes.size() / 4;
+  if (n == 0) return true;
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}, maxAbs = 0;
+  for (size_t k = 0; k < n; k++)
+    for (int a = 0; a < 3; a++) {
+      const double c = V[3 * (size_t)idx[k] + a];
+      lo[a] = std::min(lo[a], c);
+      hi[a] = std::max(hi[a], c);
+      maxAbs = std::max(maxAbs, std::fabs(c));
+    }
+  // Morton order on a 1024^3 grid over the bounding box
+  auto spread = [](uint64_t v) {
+    v &= 0x3ff;
+    v = (v | (v << 16)) & 0x30000ffull;
+    v = (v | (v << 8)) & 0x300f00full;
+    v = (v | (v << 4)) & 0x30c30c3ull;
+    v = (v | (v << 2)) & 0x9249249ull;
+    return v;
+  };
+  std::vector<std::pair<uint64_t, uint32_t>> order(n);
+  for (size_t k = 0; k < n; k++) {
+    uint64_t code = 0;
+    for (int a = 0; a < 3; a++) {
+      const double span = hi[a] - lo[a];
+      const double t = span > 0 ? ((double)V[3 * (size_t)idx[k] + a] - lo[a]) / span : 0.0;
+      const uint64_t q = (uint64_t)std::min(1023.0, std::max(0.0, t * 1024.0));
+      code |= spread(q) << a;
+    }
+    order[k] = {code, (uint32_t)k};
+  }
+  std::sort(order.begin(), order.end());
   std::vector<double> px(n), py(n), pz(n);
   for (size_t k = 0; k < n; k++) {
-    px[k] = V[3 * (size_t)idx[k]];
-    py[k] = V[3 * (size_t)idx[k] + 1];
-    pz[k] = V[3 * (size_t)idx[k] + 2];
+    const size_t i = 3 * (size_t)idx[order[k].second];
+    px[k] = V[i];
+    py[k] = V[i + 1];
+    pz[k] = V[i + 2];
+  }
+  const size_t ng = (n + GS - 1) / GS;
+  std::vector<double> gx(ng), gy(ng), gz(ng), gr(ng);
+  for (size_t g = 0; g < ng; g++) {
+    const size_t k0 = g * GS, k1 = std::min(n, k0 + GS);
+    double bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (size_t k = k0; k < k1; k++) {
+      bl[0] = std::min(bl[0], px[k]); bh[0] = std::max(bh[0], px[k]);
+      bl[1] = std::min(bl[1], py[k]); bh[1] = std::max(bh[1], py[k]);
+      bl[2] = std::min(bl[2], pz[k]); bh[2] = std::max(bh[2], pz[k]);
+    }
+    gx[g] = 0.5 * (bl[0] + bh[0]);
+    gy[g] = 0.5 * (bl[1] + bh[1]);
+    gz[g] = 0.5 * (bl[2] + bh[2]);
+    double r = 0;
+    for (size_t k = k0; k < k1; k++) {
+      const double dx = px[k] - gx[g], dy = py[k] - gy[g], dz = pz[k] - gz[g];
+      r = std::max(r, std::sqrt(dx * dx + dy * dy + dz * dz));
+    }
+    gr[g] = r * (1 + 1e-9) + 1e-300;
   }
   std::atomic<bool> outside{false};
   auto range = [&](size_t f0, size_t f1) {
     for (size_t f = f0; f < f1 && !outside.load(std::memory_order_relaxed); f++) {
       const double nx = planes[4 * f], ny = planes[4 * f + 1], nz = planes[4 * f + 2], d = planes[4 * f + 3];
-      double m = -INFINITY;
-      for (size_t k = 0; k < n; k++) m = std::max(m, nx * px[k] + ny * py[k] + nz * pz[k] - d);
-      if (m > tol) outside.store(true, std::memory_order_relaxed);
+      const double nlen = std::sqrt(nx * nx + ny * ny + nz * nz) * (1 + 1e-9);
+      const double cut = tol - 1e-9 * (6 * nlen * maxAbs + std::fabs(d)) - 1e-300;
+      bool out = false;
+      for (size_t g = 0; g < ng && !out; g++) {
+        if (nx * gx[g] + ny * gy[g] + nz * gz[g] - d + gr[g] * nlen <= cut) continue;
+        const size_t k1 = std::min(n, g * GS + GS);
+        for (size_t k = g * GS; k < k1; k++)
+          if (nx * px[k] + ny * py[k] + nz * pz[k] - d > tol) out = true;
+      }
+      if (out) outside.store(true, std::memory_order_relaxed);
     }
   };
   const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
-  const size_t nt = (double)nf * (double)n > 1e6 ? std::min<size_t>(hc, 16) : 1;
+  const size_t nt = (double)nf * (double)ng > 4e6 ? std::min<size_t>(hc, 16) : 1;
   if (nt <= 1) {
     range(0, nf);
   } else {
