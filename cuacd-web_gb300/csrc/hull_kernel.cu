@@ -871,14 +871,17 @@ struct BigSm {
 // c_j's new faces take the slots the single-pick loop gives them, right
 // after c_(j-1)'s, so face slots, owners and insertion order are the
 // single-pick loop's.
-#define BAT_K 8u        // picks per round, one warp each
+// picks per round: one per warp of the block (NW warps)
 #define BAT_FACES 32u   // faces of a batched patch, one per lane
-#define BAT_NEW 48u     // its horizon edges (a connected patch of n faces has at most n + 2)
+#define BAT_NEW 36u     // its horizon edges (a connected patch of n faces has at most n + 2)
 #define BAT_HASH_BITS 6u
-// the faces of every whole walked patch: at most BAT_K * BAT_FACES, so the
-// set is never more than half full
-#define BLK_HASH_BITS 9u
-#define BAT_NRC 16u  // new-face records per step kept in shared memory
+// the faces of every whole walked patch: at most NW * BAT_FACES, so the set
+// is never more than half full
+template <int NW>
+struct BatDims {
+  static constexpr uint32_t BLK_BITS = NW <= 8 ? 9u : 10u;
+  static constexpr uint32_t NRC = NW <= 8 ? 16u : 8u;  // new-face records per step kept in shared memory
+};
 #define BAT_LIST 8u  // keys per warp list
 // candidate slots per thread in flight in the batched round's slot pass
 #ifndef SCAN_U
@@ -903,26 +906,28 @@ struct BatWalk {
   uint32_t tw[BAT_NEW], df[BAT_NEW];  // the face across that edge and the patch face inside it
   uint32_t n, nnew, ok, pick;
 };
+template <int NW>
 struct BatSm {
+  static constexpr uint32_t BLK_BITS = BatDims<NW>::BLK_BITS, NRC = BatDims<NW>::NRC;
   union {
     BigSm big;  // the single-pick step
-    BatWalk w[BAT_K];
+    BatWalk w[NW];
   } u;
   // per warp: its largest candidate keys in descending order with their
   // slots and owners, their count, whether keys below the last one may be
   // missing, and the warp's count of dead slots
-  unsigned long long wk[8][BAT_LIST];
-  uint32_t ws[8][BAT_LIST], wo[8][BAT_LIST];
-  uint32_t wn[8], wt[8], wdead[8];
+  unsigned long long wk[NW][BAT_LIST];
+  uint32_t ws[NW][BAT_LIST], wo[NW][BAT_LIST];
+  uint32_t wn[NW], wt[NW], wdead[NW];
   // faces of the whole walked patches (face + 1, 0 = empty) with the bit
   // mask of the walks (warps) that hold them
-  uint2 btab[1u << BLK_HASH_BITS];
-  // words 0-2 of the first BAT_NRC new faces of each step
-  uint4 nrc[BAT_K][BAT_NRC][3];
-  unsigned long long selKey[BAT_K], maxOrph[BAT_K];
-  uint32_t selSlot[BAT_K], selOwn[BAT_K];
-  uint32_t nfj[BAT_K + 1], nalj[BAT_K + 1];  // slot and alive counts before step j
-  uint32_t cf[BAT_K];                        // patch j meets an earlier patch
+  uint2 btab[1u << BLK_BITS];
+  // words 0-2 of the first NRC new faces of each step
+  uint4 nrc[NW][NRC][3];
+  unsigned long long selKey[NW], maxOrph[NW];
+  uint32_t selSlot[NW], selOwn[NW];
+  uint32_t nfj[NW + 1], nalj[NW + 1];  // slot and alive counts before step j
+  uint32_t cf[NW];                     // patch j meets an earlier patch
   uint32_t nsel, ntodo, totDead;
 };
 
@@ -971,9 +976,10 @@ __device__ __forceinline__ uint32_t tab_add(uint32_t* key, uint32_t f, uint32_t&
 
 // the block's set of whole walked patches' faces: add f with a walk's bit
 // (the set never fills: at most half its entries are used)
-__device__ __forceinline__ void btab_add(BatSm& B, uint32_t f, uint32_t bit) {
-  constexpr uint32_t N = 1u << BLK_HASH_BITS;
-  uint32_t s = tab_hash<BLK_HASH_BITS>(f);
+template <int NW>
+__device__ __forceinline__ void btab_add(BatSm<NW>& B, uint32_t f, uint32_t bit) {
+  constexpr uint32_t N = 1u << BatSm<NW>::BLK_BITS;
+  uint32_t s = tab_hash<BatSm<NW>::BLK_BITS>(f);
   for (uint32_t n = 0; n < N; n++) {
     const uint32_t old = atomicCAS(&B.btab[s].x, 0u, f + 1);
     if (old == 0 || old == f + 1) {
@@ -984,9 +990,10 @@ __device__ __forceinline__ void btab_add(BatSm& B, uint32_t f, uint32_t bit) {
   }
 }
 // the mask of the walks holding face f, 0 when none (the set is not changing)
-__device__ __forceinline__ uint32_t btab_mask(const BatSm& B, uint32_t f) {
-  constexpr uint32_t N = 1u << BLK_HASH_BITS;
-  uint32_t s = tab_hash<BLK_HASH_BITS>(f);
+template <int NW>
+__device__ __forceinline__ uint32_t btab_mask(const BatSm<NW>& B, uint32_t f) {
+  constexpr uint32_t N = 1u << BatSm<NW>::BLK_BITS;
+  uint32_t s = tab_hash<BatSm<NW>::BLK_BITS>(f);
   for (uint32_t n = 0; n < N; n++) {
     const uint2 e = B.btab[s];
     if (e.x == f + 1) return e.y;
@@ -1217,7 +1224,8 @@ struct Top2 {
 // thread's second key is taken its third could come next, and keys below
 // the BAT_LIST-th may be missing: the list is marked truncated), and the
 // warp's count of dead slots
-__device__ __forceinline__ void top2_publish(BatSm& B, const Top2& t, uint32_t dead) {
+template <int NW>
+__device__ __forceinline__ void top2_publish(BatSm<NW>& B, const Top2& t, uint32_t dead) {
   const uint32_t w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned long long cur = t.k1;
   bool first = true;
@@ -1259,11 +1267,12 @@ __device__ __forceinline__ void top2_publish(BatSm& B, const Top2& t, uint32_t d
 // warp above the last key of its truncated list is in the list, so the
 // merge stops after taking such a last key; and the total of the dead-slot
 // counts
-__device__ __noinline__ void bat_select(BatSm& B, uint32_t kmax) {
+template <int NW>
+__device__ __noinline__ void bat_select(BatSm<NW>& B, uint32_t kmax) {
   const uint32_t lane = threadIdx.x & 31;
-  const uint32_t wn = lane < 8 ? B.wn[lane] : 0u;
-  const bool wt = lane < 8 && B.wt[lane] != 0;
-  const uint32_t dn = warp_sum_u(lane < 8 ? B.wdead[lane] : 0u);
+  const uint32_t wn = lane < NW ? B.wn[lane] : 0u;
+  const bool wt = lane < NW && B.wt[lane] != 0;
+  const uint32_t dn = warp_sum_u(lane < NW ? B.wdead[lane] : 0u);
   uint32_t pos = 0;
   unsigned long long cur = wn > 0 ? B.wk[lane][0] : 0ull;
   uint32_t n = 0;
@@ -1296,7 +1305,8 @@ __device__ __noinline__ void bat_select(BatSm& B, uint32_t kmax) {
 // its horizon edges in the insertion's order (e = 3 * listPos + k); the
 // patch's faces also go into the block's set with the warp's bit. W.ok = 0
 // when the patch has more than BAT_FACES faces.
-__device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatSm& B, uint32_t pIdx, uint32_t start) {
+template <int NW>
+__device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatSm<NW>& B, uint32_t pIdx, uint32_t start) {
   constexpr uint32_t HB = BAT_HASH_BITS;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   BatWalk& W = B.u.w[warp];
@@ -1410,10 +1420,11 @@ __device__ __noinline__ void bat_walk(const HullCtx& h, uint32_t nf, BatSm& B, u
 // warp j < K: whether patch j meets an earlier walked patch (a face of
 // patch j, or a face across one of its edges, was claimed by a walk i < j);
 // the round's counters are reset
-__device__ __noinline__ void bat_conflicts(BatSm& B, uint32_t K) {
+template <int NW>
+__device__ __noinline__ void bat_conflicts(BatSm<NW>& B, uint32_t K) {
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) B.ntodo = 0;
-  if (threadIdx.x < BAT_K) B.maxOrph[threadIdx.x] = 0;
+  if (threadIdx.x < NW) B.maxOrph[threadIdx.x] = 0;
   if (warp >= K) return;
   const BatWalk& W = B.u.w[warp];
   const uint32_t below = (1u << warp) - 1u;
@@ -1432,7 +1443,8 @@ __device__ __noinline__ void bat_conflicts(BatSm& B, uint32_t K) {
 // neither the compaction rule (steps after the first) nor the slot limit
 // firing; *base = the first new-face slot of the thread's warp's step.
 // Thread 0 stores the slot and alive counts before each step.
-__device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, BatSm& B, uint32_t K,
+template <int NW>
+__device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, BatSm<NW>& B, uint32_t K,
                                             uint32_t* base) {
   const uint32_t warp = threadIdx.x >> 5;
   uint32_t nfc = hs.nf, nalc = hs.nalive, ms = 0;
@@ -1460,8 +1472,9 @@ __device__ __noinline__ uint32_t bat_prefix(const HullCtx& h, const HullSm& hs, 
 
 // squeeze dead slots out of the candidate list (slot order kept); returns
 // the new count and publishes the threads' keys
-__device__ __noinline__ uint32_t big_squeeze(const HullCtx& h, GrpSmem& sm, BatSm& B, uint32_t ncand) {
-  constexpr int G = 256;
+template <int NW>
+__device__ __noinline__ uint32_t big_squeeze(const HullCtx& h, GrpSmem& sm, BatSm<NW>& B, uint32_t ncand) {
+  constexpr int G = 32 * NW;
   const uint32_t lid = threadIdx.x;
   uint32_t nc = 0;
   Top2 t;
@@ -1498,8 +1511,9 @@ __device__ __noinline__ uint32_t big_squeeze(const HullCtx& h, GrpSmem& sm, BatS
 // BIG_VIS faces) by warp 0, then one pass over the candidate slots: the
 // inserted point leaves, points of dead faces (all points after a
 // compaction) are reassigned, and the threads' keys are published
-__device__ __noinline__ void big_seq_step(const HullCtx& h, HullSm& hs, GrpSmem& sm, BatSm& B, uint32_t ncand) {
-  constexpr int G = 256;
+template <int NW>
+__device__ __noinline__ void big_seq_step(const HullCtx& h, HullSm& hs, GrpSmem& sm, BatSm<NW>& B, uint32_t ncand) {
+  constexpr int G = 32 * NW;
   BigSm& bs = B.u.big;
   const uint32_t lid = threadIdx.x;
   uint32_t* cown = h.owner;
@@ -1626,7 +1640,8 @@ __device__ __noinline__ void big_seq_step(const HullCtx& h, HullSm& hs, GrpSmem&
 }
 
 // best_face over the new faces [f0, f1) of one step (all alive), the first
-// BAT_NRC records read from shared memory
+// NRC records read from shared memory
+template <uint32_t NRC>
 __device__ __forceinline__ void bat_best(const HullCtx& h, uint32_t i, uint32_t f0, uint32_t f1, const uint4 (*nrc)[3],
                                          uint32_t& outF, float& outD) {
   const f3 pt = h.qvert(i);
@@ -1635,7 +1650,7 @@ __device__ __forceinline__ void bat_best(const HullCtx& h, uint32_t i, uint32_t 
   for (uint32_t f = f0; f < f1; f++) {
     const uint32_t q = f - f0;
     uint4 w0, w1, w2;
-    if (q < BAT_NRC) {
+    if (q < NRC) {
       w0 = nrc[q][0]; w1 = nrc[q][1]; w2 = nrc[q][2];
     } else {
       const uint4* w = h.rec(f);
@@ -1657,9 +1672,11 @@ __device__ __forceinline__ void bat_best(const HullCtx& h, uint32_t i, uint32_t 
 // new faces and the largest new key per step, the accepted prefix, then its
 // commit (twin links, dead faces, counts) and the orphans' new owners.
 // Returns the number of insertions.
-__device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B, uint32_t ncand, uint32_t ms,
+template <int NW>
+__device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm<NW>& B, uint32_t ncand, uint32_t ms,
                                           uint32_t myBase) {
-  constexpr int G = 256;
+  constexpr int G = 32 * NW;
+  constexpr uint32_t NRC = BatSm<NW>::NRC;
   const uint32_t lid = threadIdx.x, warp = lid >> 5, lane = lid & 31;
   const uint32_t nf0 = hs.nf;
   uint32_t* tK = h.vis;
@@ -1681,7 +1698,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       h.face_make_q(a, b, pIdx, p, w0, w1, w2, w3);
       uint4* w = h.rec(s);
       w[0] = w0; w[1] = w1; w[2] = w2; w[3] = w3;
-      if (q < BAT_NRC) {
+      if (q < NRC) {
         B.nrc[warp][q][0] = w0; B.nrc[warp][q][1] = w1; B.nrc[warp][q][2] = w2;
       }
       // around the horizon loop: (b, p) borders the new face starting at
@@ -1746,7 +1763,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       uint32_t no = CUACD_NONE;
       float nd = 0.0f;
       if (k != B.selSlot[j]) {
-        bat_best(h, i, B.nfj[j], B.nfj[j + 1], B.nrc[j], no, nd);
+        bat_best<NRC>(h, i, B.nfj[j], B.nfj[j + 1], B.nrc[j], no, nd);
         if (no != CUACD_NONE) atomicMax(&B.maxOrph[j], cand_key(nd, i));
       }
       tNO[t] = no;
@@ -1813,7 +1830,7 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
       }
       uint32_t no = CUACD_NONE;
       float nd = 0.0f;
-      if (k != B.selSlot[0]) bat_best(h, i, B.nfj[0], B.nfj[1], B.nrc[0], no, nd);
+      if (k != B.selSlot[0]) bat_best<NRC>(h, i, B.nfj[0], B.nfj[1], B.nrc[0], no, nd);
       h.owner[k] = no;
       h.dist[k] = nd;
       if (no == CUACD_NONE) dead++;
@@ -1825,9 +1842,10 @@ __device__ __noinline__ uint32_t bat_step(const HullCtx& h, HullSm& hs, BatSm& B
   return m;
 }
 
-__device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, GrpSmem& sm, BatSm& B,
+template <int NW>
+__device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, GrpSmem& sm, BatSm<NW>& B,
                                                uint32_t maxIter) {
-  constexpr int G = 256;
+  constexpr int G = 32 * NW;
   const uint32_t lid = threadIdx.x, warp = lid >> 5;
   uint32_t ncand = hs.ncand;
   // owner and distance to candidate-slot order, in place: each chunk is read
@@ -1859,8 +1877,8 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
   __syncthreads();
   uint32_t nIns = 0;
   while (nIns < maxIter) {
-    for (uint32_t e = lid; e < (1u << BLK_HASH_BITS); e += G) B.btab[e] = make_uint2(0u, 0u);
-    if (warp == 0) bat_select(B, min(BAT_K, maxIter - nIns));
+    for (uint32_t e = lid; e < (1u << BatSm<NW>::BLK_BITS); e += G) B.btab[e] = make_uint2(0u, 0u);
+    if (warp == 0) bat_select(B, min((uint32_t)NW, maxIter - nIns));
     __syncthreads();
     // squeeze dead slots out when they pass 1 / SQZ_DIV of the list
     if (SQZ_DIV * B.totDead > ncand) {
@@ -1989,7 +2007,7 @@ __device__ __noinline__ double hull_volume_grid(const HullCtx& h, HullSm& hs, Gr
   }
   __int128 tot = (__int128)hi << 64 | (__int128)lo;
   if (G > 32) {
-    __shared__ unsigned long long vs[8][2];
+    __shared__ unsigned long long vs[G / 32][2];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     __syncthreads();
     if (lane == 0) { vs[w][0] = lo; vs[w][1] = (unsigned long long)hi; }
@@ -2006,7 +2024,7 @@ __device__ __noinline__ double hull_volume_grid(const HullCtx& h, HullSm& hs, Gr
 
 template <int G>
 __device__ void hull_one(const Level& P, const Dev& D, uint32_t idx, uint32_t* slab, HullSm& hs, GrpSmem& sm,
-                         float* qcache, TinySm* ts, BatSm* bs) {
+                         float* qcache, TinySm* ts, BatSm<(G >= 256 ? G / 32 : 8)>* bs) {
   const int lid = Grp<G>::lid();
   const uint32_t partIdx = P.partBase + idx;
   PartDesc* pdp = D.parts + partIdx;
@@ -2221,7 +2239,7 @@ restart:
     for (uint32_t k = lid; k < nuniq; k += G) h.assign(h.cand[k], 0, 4);
     if (lid == 0) hs.ncand = nuniq;
     Grp<G>::sync();
-    if constexpr (G == 256) nIns = hull_grow_big(h, hs, sm, *bs, 80);
+    if constexpr (G >= 256) nIns = hull_grow_big<G / 32>(h, hs, sm, *bs, 80);
     else nIns = hull_grow<G>(h, hs, sm, 4, 80);
   }
   const uint32_t fail0 = hs.fail;
@@ -2293,7 +2311,7 @@ restart:
     }
     nIns += hull_grow_lanes(h, hs, sm, nfPrev, maxIter, ci, co, cd);
   } else {
-    if constexpr (G == 256) nIns += hull_grow_big(h, hs, sm, *bs, maxIter);
+    if constexpr (G >= 256) nIns += hull_grow_big<G / 32>(h, hs, sm, *bs, maxIter);
     else nIns += hull_grow<G>(h, hs, sm, nfPrev, maxIter);
   }
   if (hs.fail) {
@@ -2343,12 +2361,13 @@ restart:
 // few faces and runs on one warp either way, the block's width serves the
 // passes over all points and candidates, which grow with nv.
 template <int G>
-__global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
+__global__ void __launch_bounds__(G == 512 ? 512 : 256, G == 512 ? 2 : 4) k_hull(const Level P, const Dev D) {
   __shared__ GrpSmem gsm[Grp<G>::PER_BLOCK];
   __shared__ HullSm hsm[Grp<G>::PER_BLOCK];
   __shared__ float qcs[G == 32 ? 8 * 3 * QC_MAX : 1];
   __shared__ TinySm tsm[G == 32 ? 8 : 1];
-  __shared__ typename std::conditional<G == 256, BatSm, char>::type bsm;
+  using BS = BatSm<(G >= 256 ? G / 32 : 8)>;
+  __shared__ typename std::conditional<G >= 256, BS, char>::type bsm;
   const int gi = Grp<G>::gid();
   const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
   if (s >= P.nSlabs) return;
@@ -2366,7 +2385,7 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
       idx = grp_bcast_u<G>(idx, gsm[0]);
       if (idx >= P.nChildParts) break;
       if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr, reinterpret_cast<BatSm*>(&bsm));
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr, reinterpret_cast<BS*>(&bsm));
       Grp<G>::sync();
     }
     return;
@@ -2387,10 +2406,11 @@ __global__ void __launch_bounds__(256, 4) k_hull(const Level P, const Dev D) {
   }
 }
 
-// resident blocks per SM of the hull kernel of group width 32 or 256
+// resident blocks per SM of the hull kernel of group width 32, 256 or 512
 int hull_blocks_per_sm(int width) {
   int n = 0;
   if (width == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<32>, 256, 0);
+  else if (width == 512) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<512>, 512, 0);
   else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<256>, 256, 0);
   return n > 0 ? n : 1;
 }
@@ -2399,6 +2419,7 @@ int hull_blocks_per_sm(int width) {
 void launch_hull(const Level& P, const Dev& D, int width, cudaStream_t s) {
   if (P.nChildParts == 0 || P.nSlabs == 0) return;
   if (width == 32) k_hull<32><<<(P.nSlabs + 7) / 8, 256, 0, s>>>(P, D);
+  else if (width == 512) k_hull<512><<<P.nSlabs, 512, 0, s>>>(P, D);
   else k_hull<256><<<P.nSlabs, 256, 0, s>>>(P, D);
 }
 
