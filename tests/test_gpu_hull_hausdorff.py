@@ -124,6 +124,34 @@ def test_hull_large_cut_parts(tree_mod, oracle):
             assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"], i
 
 
+def test_hull_block_widths(tree_mod, oracle):
+    """Large parts on both block widths: a batch of 320 parts (more than one
+    wave of 512-thread blocks on 152 SMs, so 256-thread blocks with 8 picks
+    per round) and its first 8 parts alone (512-thread blocks, 16 picks per
+    round) give the oracle's faces and volumes."""
+    D = importlib.import_module("cuacd-web_gb300.decompose")
+    cfg = dict(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=16384)
+    g = tree_mod.GpuTree(**cfg)
+    o = oracle.OracleTree(**cfg)
+    blob = M.normalize(gen.blob_mesh(12, 44, seed=4))[0]
+    sets = list(D.plane_cut(blob, [0.3, 0.5, -0.8, 0.05]))
+    rng = np.random.default_rng(21)
+    while len(sets) < 320:
+        n = int(rng.integers(1100, 1500))
+        s = rng.normal(size=(n, 3))
+        s /= np.linalg.norm(s, axis=1, keepdims=True)
+        s *= rng.uniform(0.8, 1.0, size=(n, 1))
+        sets.append(M.Mesh(s.astype(np.float32), np.zeros((0, 3), np.uint32)))
+    ro, so = o.hull_meshes(sets)
+    for subset in (sets, sets[:8]):
+        rg, sg = g.hull_meshes(subset)
+        assert list(sg) == list(so[: len(subset)])
+        for i, (a, b) in enumerate(zip(rg, ro)):
+            assert (a is None) == (b is None), i
+            if a is not None:
+                assert np.array_equal(a["tris"], b["tris"]) and a["volume"] == b["volume"], i
+
+
 def hd_pairs(oracle):
     t = oracle.OracleTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
     pairs = []
