@@ -139,13 +139,19 @@ template <> struct Grp<512> {
   static __device__ __forceinline__ int gid() { return 0; }
   static constexpr int PER_BLOCK = 1;
 };
+template <> struct Grp<1024> {
+  static __device__ __forceinline__ void sync() { __syncthreads(); }
+  static __device__ __forceinline__ int lid() { return threadIdx.x; }
+  static __device__ __forceinline__ int gid() { return 0; }
+  static constexpr int PER_BLOCK = 1;
+};
 
 // Per-group shared scratch for cross-warp reductions (unused by warp groups)
-// (one entry per warp of the widest group, 512 threads)
+// (one entry per warp of the widest group, 1024 threads)
 struct GrpSmem {
-  double d[16];
-  uint32_t u[16][4];
-  float f[16][4];
+  double d[32];
+  uint32_t u[32][4];
+  float f[32][4];
   uint32_t bc[8];
 };
 

@@ -104,7 +104,7 @@ struct HostBuf {
 struct Tree {
   cuacd_tree_config cfg;
   uint32_t edgeStride = 0;
-  int device = 0, nSM = 0, bpsSmall = 1, bpsBig = 1, bpsWide = 1;
+  int device = 0, nSM = 0, bpsSmall = 1, bpsBig = 1, bpsWide = 0, bpsXL = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool profile = false;
@@ -224,17 +224,26 @@ struct Tree {
   }
   // hull launches of one level, warp groups then block groups; work
   // counters `slot` and 16 + slot must be zero beforehand. Parts above
-  // warpMaxNv points take 512-thread blocks when the level's parts fit the
-  // GPU's 512-thread block slots in one wave (the more threads per part, the
-  // shorter each insertion round), else 256-thread blocks (twice as many
-  // parts at once).
+  // warpMaxNv points take the widest blocks (1024, then 512 threads) whose
+  // resident slots hold all the level's parts in one wave (the more threads
+  // per part, the shorter each insertion round), else 256-thread blocks
+  // (the most parts at once).
   void hullLaunch(Level P, uint32_t slot) {
     P.workSlot = slot;
     P.nSlabs = nSlabsSmall;
     launch_hull(P, D, 32, stream);
-    const bool wide = P.nChildParts <= (uint32_t)(nSM * bpsWide);
-    P.nSlabs = wide ? std::min(nSlabsBig, (uint32_t)(nSM * bpsWide)) : nSlabsBig;
-    launch_hull(P, D, wide ? 512 : 256, stream);
+    int width = 256;
+    uint32_t slabs = nSlabsBig;
+    for (const auto& [w, bps] : {std::pair<int, int>{1024, bpsXL}, {512, bpsWide}}) {
+      const uint32_t cap = (uint32_t)(nSM * bps);
+      if (bps > 0 && P.nChildParts <= cap) {
+        width = w;
+        slabs = std::min(nSlabsBig, cap);
+        break;
+      }
+    }
+    P.nSlabs = slabs;
+    launch_hull(P, D, width, stream);
   }
   // upload meshes at the start of the pools and write their part descriptors
   // (tree.ts:233-278); returns the host-side descriptors in parts
@@ -771,9 +780,10 @@ void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
   t->edgeStride = (uint32_t)std::max(4 * c->nConcaveEdges, 32);
   cudaGetDevice(&t->device);
   cudaDeviceGetAttribute(&t->nSM, cudaDevAttrMultiProcessorCount, t->device);
-  t->bpsSmall = hull_blocks_per_sm(32);
-  t->bpsBig = hull_blocks_per_sm(256);
+  t->bpsSmall = std::max(1, hull_blocks_per_sm(32));
+  t->bpsBig = std::max(1, hull_blocks_per_sm(256));
   t->bpsWide = hull_blocks_per_sm(512);
+  t->bpsXL = hull_blocks_per_sm(1024);
   int rc = 0;
   if (cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&t->ev0) != cudaSuccess || cudaEventCreate(&t->ev1) != cudaSuccess) {

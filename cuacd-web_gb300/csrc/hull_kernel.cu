@@ -879,8 +879,11 @@ struct BigSm {
 // is never more than half full
 template <int NW>
 struct BatDims {
-  static constexpr uint32_t BLK_BITS = NW <= 8 ? 9u : 10u;
+  static constexpr uint32_t BLK_BITS = NW <= 8 ? 9u : (NW <= 16 ? 10u : 11u);
   static constexpr uint32_t NRC = NW <= 8 ? 16u : 8u;  // new-face records per step kept in shared memory
+  // picks per round: one per warp, at most 20 (the merge of the warps'
+  // lists is serial in the picks, and later picks rarely pass the checks)
+  static constexpr uint32_t KMAX = NW < 20 ? (uint32_t)NW : 20u;
 };
 #define BAT_LIST 8u  // keys per warp list
 // candidate slots per thread in flight in the batched round's slot pass
@@ -1878,7 +1881,7 @@ __device__ __noinline__ uint32_t hull_grow_big(const HullCtx& h, HullSm& hs, Grp
   uint32_t nIns = 0;
   while (nIns < maxIter) {
     for (uint32_t e = lid; e < (1u << BatSm<NW>::BLK_BITS); e += G) B.btab[e] = make_uint2(0u, 0u);
-    if (warp == 0) bat_select(B, min((uint32_t)NW, maxIter - nIns));
+    if (warp == 0) bat_select(B, min(BatDims<NW>::KMAX, maxIter - nIns));
     __syncthreads();
     // squeeze dead slots out when they pass 1 / SQZ_DIV of the list
     if (SQZ_DIV * B.totDead > ncand) {
@@ -2362,13 +2365,15 @@ restart:
 // per warp per round, and its width serves the passes over all points and
 // candidates, which grow with nv.
 template <int G>
-__global__ void __launch_bounds__(G == 512 ? 512 : 256, G == 512 ? 2 : 4) k_hull(const Level P, const Dev D) {
+__global__ void __launch_bounds__(G >= 512 ? G : 256, G == 1024 ? 1 : (G == 512 ? 2 : 4))
+    k_hull(const Level P, const Dev D) {
   __shared__ GrpSmem gsm[Grp<G>::PER_BLOCK];
   __shared__ HullSm hsm[Grp<G>::PER_BLOCK];
   __shared__ float qcs[G == 32 ? 8 * 3 * QC_MAX : 1];
   __shared__ TinySm tsm[G == 32 ? 8 : 1];
+  // the block path's shared words (BatSm) in the launch's dynamic shared memory
+  extern __shared__ __align__(16) unsigned char hull_dyn[];
   using BS = BatSm<(G >= 256 ? G / 32 : 8)>;
-  __shared__ typename std::conditional<G >= 256, BS, char>::type bsm;
   const int gi = Grp<G>::gid();
   const uint32_t s = blockIdx.x * Grp<G>::PER_BLOCK + gi;
   if (s >= P.nSlabs) return;
@@ -2386,7 +2391,7 @@ __global__ void __launch_bounds__(G == 512 ? 512 : 256, G == 512 ? 2 : 4) k_hull
       idx = grp_bcast_u<G>(idx, gsm[0]);
       if (idx >= P.nChildParts) break;
       if (D.parts[P.partBase + idx].nv <= P.smallNv) continue;
-      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr, reinterpret_cast<BS*>(&bsm));
+      hull_one<G>(P, D, idx, slab, hsm[gi], gsm[gi], nullptr, nullptr, reinterpret_cast<BS*>(hull_dyn));
       Grp<G>::sync();
     }
     return;
@@ -2407,21 +2412,34 @@ __global__ void __launch_bounds__(G == 512 ? 512 : 256, G == 512 ? 2 : 4) k_hull
   }
 }
 
-// resident blocks per SM of the hull kernel of group width 32, 256 or 512
+// resident blocks per SM of the hull kernel of group width 32, 256, 512 or
+// 1024 (0 when a width cannot run)
+// (sets the block kernels' dynamic shared memory limit to their BatSm, for
+// the device current at the call)
+template <int G>
+static int wide_blocks_per_sm() {
+  const size_t dyn = sizeof(BatSm<G / 32>);
+  cudaFuncSetAttribute(k_hull<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  int n = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<G>, G, dyn);
+  return n;
+}
 int hull_blocks_per_sm(int width) {
   int n = 0;
   if (width == 32) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<32>, 256, 0);
-  else if (width == 512) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<512>, 512, 0);
-  else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_hull<256>, 256, 0);
-  return n > 0 ? n : 1;
+  else if (width == 1024) n = wide_blocks_per_sm<1024>();
+  else if (width == 512) n = wide_blocks_per_sm<512>();
+  else n = wide_blocks_per_sm<256>();
+  return n;
 }
 
 // hull launch of one group width (32 or 256) over P.nSlabs groups
 void launch_hull(const Level& P, const Dev& D, int width, cudaStream_t s) {
   if (P.nChildParts == 0 || P.nSlabs == 0) return;
   if (width == 32) k_hull<32><<<(P.nSlabs + 7) / 8, 256, 0, s>>>(P, D);
-  else if (width == 512) k_hull<512><<<P.nSlabs, 512, 0, s>>>(P, D);
-  else k_hull<256><<<P.nSlabs, 256, 0, s>>>(P, D);
+  else if (width == 1024) k_hull<1024><<<P.nSlabs, 1024, sizeof(BatSm<32>), s>>>(P, D);
+  else if (width == 512) k_hull<512><<<P.nSlabs, 512, sizeof(BatSm<16>), s>>>(P, D);
+  else k_hull<256><<<P.nSlabs, 256, sizeof(BatSm<8>), s>>>(P, D);
 }
 
 // ---------------------------------------------------------------------------
@@ -2534,7 +2552,7 @@ extern "C" int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint3
   D.work = scratch + NOALLOC_WORK_OFF;
   k_noalloc_setup<<<1, 64, 0, s>>>(scratch, nv);
   if (nv <= P.smallNv) k_hull<32><<<1, 256, 0, s>>>(P, D);
-  else k_hull<256><<<1, 256, 0, s>>>(P, D);
+  else k_hull<256><<<1, 256, sizeof(BatSm<8>), s>>>(P, D);
   k_noalloc_finish<<<1, 1, 0, s>>>(scratch, volume, ntris, status);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return set_error(-4, cudaGetErrorString(e));
