@@ -268,21 +268,37 @@ struct Cap {
   }
 
   const char* run() {
-    // boundary edges: directed edges without a reverse twin, in first-seen order
-    std::unordered_set<uint64_t> edges;
+    // boundary edges: directed edges without a reverse twin, in first-seen
+    // order, each distinct edge once. The directed edges are grouped by
+    // source vertex (counting sort, each group in edge order), so a repeat
+    // and a twin are found in the short lists of the edge's two vertices.
+    const size_t ne = tris.size();
+    const uint32_t nvx = (uint32_t)(xyz.size() / 3);
+    std::vector<uint32_t> off(nvx + 1, 0), dst(ne), fill;
+    for (size_t i = 0; i < ne; i++) off[tris[i] + 1]++;
+    for (uint32_t v = 0; v < nvx; v++) off[v + 1] += off[v];
+    fill.assign(off.begin(), off.end() - 1);
+    for (size_t i = 0; i < ne; i += 3)
+      for (int e = 0; e < 3; e++) dst[fill[tris[i + e]]++] = tris[i + (e + 1) % 3];
+    std::fill(fill.begin(), fill.end(), 0u);
     std::vector<uint64_t> order;
-    edges.reserve(tris.size() * 2);
-    for (size_t i = 0; i < tris.size(); i += 3)
+    for (size_t i = 0; i < ne; i += 3)
       for (int e = 0; e < 3; e++) {
-        const uint64_t k = ekey(tris[i + e], tris[i + (e + 1) % 3]);
-        if (edges.insert(k).second) order.push_back(k);
+        const uint32_t a = tris[i + e], b = tris[i + (e + 1) % 3];
+        // this edge's place in a's list; an earlier a -> b there is a repeat
+        const uint32_t at = off[a] + fill[a]++;
+        bool seen = false;
+        for (uint32_t k = off[a]; k < at && !seen; k++) seen = dst[k] == b;
+        if (seen) continue;
+        bool twin = false;
+        for (uint32_t k = off[b]; k < off[b + 1] && !twin; k++) twin = dst[k] == a;
+        if (!twin) order.push_back(ekey(a, b));
       }
     std::vector<uint32_t> starts;
     std::unordered_map<uint32_t, std::vector<uint32_t>> next;
     size_t nBoundary = 0;
     for (uint64_t k : order) {
       const uint32_t a = (uint32_t)(k >> 32), b = (uint32_t)k;
-      if (edges.count(ekey(b, a))) continue;
       nBoundary++;
       auto it = next.find(a);
       if (it == next.end()) {
