@@ -15,9 +15,14 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <functional>
+#include <future>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -44,6 +49,9 @@ inline double rv_cost(double meshVol, double hullVol) {
 
 struct Part {
   Mesh mesh, hull;
+  // the output hull while its cleanup still runs on the engine's workers
+  // (hull is set from it before anything reads the hull)
+  std::shared_future<Mesh> hullTask;
   double meshVol = 0, hullVol = 0;
   double hd = 0;
   bool hasHd = false;
@@ -86,6 +94,57 @@ void parallel_for(size_t n, int threads, F&& fn) {
     });
   for (auto& th : pool) th.join();
 }
+
+// workers for host tasks that the decomposition loop does not wait for (the
+// output hulls' cleanup, needed only by the merge pass and the output)
+class TaskPool {
+ public:
+  explicit TaskPool(int n) : n_(std::max(n, 1)) {}
+  ~TaskPool() {
+    {
+      std::lock_guard<std::mutex> l(m_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (std::thread& t : th_) t.join();
+  }
+  std::shared_future<Mesh> submit(std::function<Mesh()> fn) {
+    auto task = std::make_shared<std::packaged_task<Mesh()>>(std::move(fn));
+    std::shared_future<Mesh> f = task->get_future().share();
+    {
+      std::lock_guard<std::mutex> l(m_);
+      q_.push_back([task]() { (*task)(); });
+      if (th_.size() < (size_t)n_ && idle_ == 0) th_.emplace_back([this]() { work(); });
+    }
+    cv_.notify_one();
+    return f;
+  }
+
+ private:
+  void work() {
+    for (;;) {
+      std::function<void()> job;
+      {
+        std::unique_lock<std::mutex> l(m_);
+        idle_++;
+        cv_.wait(l, [&] { return stop_ || !q_.empty(); });
+        idle_--;
+        // the queue drains before the workers stop
+        if (q_.empty()) return;
+        job = std::move(q_.front());
+        q_.pop_front();
+      }
+      job();
+    }
+  }
+  int n_;
+  int idle_ = 0;
+  bool stop_ = false;
+  std::mutex m_;
+  std::condition_variable cv_;
+  std::deque<std::function<void()>> q_;
+  std::vector<std::thread> th_;
+};
 
 // ---------------------------------------------------------------------------
 // one decomposition in flight
@@ -138,6 +197,16 @@ class Engine {
     if (bigTree) cuacd_tree_destroy(bigTree);
   }
 
+  // output-hull cleanups run here while the loop goes on
+  std::unique_ptr<TaskPool> pool;
+  TaskPool& clean_pool() { return *pool; }
+  // the part's output hull, once its cleanup is done
+  static void resolve(Part& p) {
+    if (!p.hullTask.valid()) return;
+    p.hull = p.hullTask.get();
+    p.hullTask = std::shared_future<Mesh>();
+  }
+
   [[noreturn]] void cuda_fail(int rc, const char* what) {
     throw Failure{rc, std::string(what) + ": " + cuacd_last_error()};
   }
@@ -148,9 +217,12 @@ class Engine {
   // chunks of at most 256 (decompose.ts:180), halved when a chunk's hull
   // export does not fit the triangle pool. A failed hull is an error unless
   // allowFail, when the part gets a NaN hull volume.
+  // defer: the output hulls' cleanup goes to the workers (the part's
+  // hullTask) instead of finishing before the call returns
   void hulls(const std::vector<const Mesh*>& ms, const std::vector<double>& eps, bool withHd, std::vector<Part>& out,
-             bool allowFail = false) {
+             bool allowFail = false, bool defer = false) {
     out.resize(ms.size());
+    if (defer && !pool) pool = std::make_unique<TaskPool>(threads);
     size_t chunk = 256;
     for (size_t s = 0; s < ms.size();) {
       const size_t n = std::min(chunk, ms.size() - s);
@@ -198,9 +270,19 @@ class Engine {
         }
         // output faces cleaned (decompose.ts:189, merge.ts:213); the kernel's
         // volume stays the part's hull volume
-        const std::vector<uint32_t> ct =
-            host::clean_hull_faces(m.v.data(), m.nv(), tris.data() + (size_t)k * stride, 3 * (size_t)ntri[k], eps[s + k]);
-        p.hull = host::compact_hull(m.v.data(), ct.data(), ct.size() / 3, nullptr);
+        const uint32_t* raw = tris.data() + (size_t)k * stride;
+        if (defer) {
+          std::vector<uint32_t> rt(raw, raw + 3 * (size_t)ntri[k]);
+          std::vector<float> pv(m.v);
+          const double e = eps[s + k];
+          p.hullTask = clean_pool().submit([pv = std::move(pv), rt = std::move(rt), e]() {
+            const std::vector<uint32_t> ct = host::clean_hull_faces(pv.data(), pv.size() / 3, rt.data(), rt.size(), e);
+            return host::compact_hull(pv.data(), ct.data(), ct.size() / 3, nullptr);
+          });
+        } else {
+          const std::vector<uint32_t> ct = host::clean_hull_faces(m.v.data(), m.nv(), raw, 3 * (size_t)ntri[k], eps[s + k]);
+          p.hull = host::compact_hull(m.v.data(), ct.data(), ct.size() / 3, nullptr);
+        }
         p.hullVol = vol[k];
         if (withHd && std::isfinite(hd[k])) {
           p.hd = hd[k];
@@ -300,6 +382,7 @@ class Engine {
     std::vector<Part*> todo;
     for (Part* p : ps)
       if (!p->hasHd) {
+        resolve(*p);
         todo.push_back(p);
         a.push_back(&p->mesh);
         b.push_back(&p->hull);
@@ -491,7 +574,7 @@ class Engine {
       }
     const auto th = Clock::now();
     std::vector<Part> made;
-    hulls(halves, heps, true, made);
+    hulls(halves, heps, true, made, false, true);
     hullMs += ms_since(th);
     if (o.verbose) {
       size_t nParts = 0, nTris = 0;
@@ -827,7 +910,7 @@ class Engine {
     }
     std::vector<Part> made;
     const auto th = Clock::now();
-    hulls(ms, meps, true, made);
+    hulls(ms, meps, true, made, false, true);
     hullMs += ms_since(th);
     for (size_t k = 0; k < jobs.size(); k++) {
       made[k].id = nextId++;
@@ -839,6 +922,8 @@ class Engine {
   // and the parts back in input units (decompose.ts:360-392)
   void finish(std::vector<Job*>& jobs) {
     evals.clear();  // pair evaluations live for one merge pass
+    for (Job* j : jobs)
+      for (Part& p : j->parts) resolve(p);
     {
       std::vector<Part*> ps;
       for (Job* j : jobs)
