@@ -954,19 +954,6 @@ __device__ __forceinline__ bool tab_has(const uint32_t* key, uint32_t f) {
   }
   return false;
 }
-// the entry of f, or N when absent (the set is not changing)
-template <uint32_t BITS>
-__device__ __forceinline__ uint32_t tab_find(const uint32_t* key, uint32_t f) {
-  constexpr uint32_t N = 1u << BITS;
-  uint32_t s = tab_hash<BITS>(f);
-  for (uint32_t n = 0; n < N; n++) {
-    const uint32_t k = key[s];
-    if (k == f + 1) return s;
-    if (k == 0) return N;
-    s = (s + 1) & (N - 1);
-  }
-  return N;
-}
 // 1: inserted, 0: already present, 2: set full; *at = its entry
 template <uint32_t BITS>
 __device__ __forceinline__ uint32_t tab_add(uint32_t* key, uint32_t f, uint32_t& at) {
@@ -1011,27 +998,13 @@ __device__ __forceinline__ uint32_t btab_mask(const BatSm<NW>& B, uint32_t f) {
   return 0;
 }
 
-__device__ __forceinline__ uint32_t big_hash(uint32_t f) { return (f * 2654435761u) >> 24; }
-__device__ __forceinline__ bool big_has(const BigSm& bs, uint32_t f) {
-  uint32_t s = big_hash(f);
-  for (uint32_t n = 0; n < BIG_HASH; n++) {
-    const uint32_t k = *reinterpret_cast<const volatile uint32_t*>(bs.key + s);
-    if (k == f + 1) return true;
-    if (k == 0) return false;
-    s = (s + 1) & (BIG_HASH - 1);
-  }
-  return false;
-}
+// the single-pick step's patch set (BIG_HASH = 2^8 entries)
+static_assert(BIG_HASH == (1u << 8), "the single-pick patch set has 2^8 entries");
+__device__ __forceinline__ bool big_has(const BigSm& bs, uint32_t f) { return tab_has<8>(bs.key, f); }
 // 1: inserted, 0: already present, 2: table full
 __device__ __forceinline__ uint32_t big_add(BigSm& bs, uint32_t f) {
-  uint32_t s = big_hash(f);
-  for (uint32_t n = 0; n < BIG_HASH; n++) {
-    const uint32_t old = atomicCAS(bs.key + s, 0u, f + 1);
-    if (old == 0) return 1;
-    if (old == f + 1) return 0;
-    s = (s + 1) & (BIG_HASH - 1);
-  }
-  return 2;
+  uint32_t at;
+  return tab_add<8>(bs.key, f, at);
 }
 
 // hull_insert for warp 0 with the patch in shared memory; false when the

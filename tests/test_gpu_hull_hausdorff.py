@@ -125,10 +125,10 @@ def test_hull_large_cut_parts(tree_mod, oracle):
 
 
 def test_hull_block_widths(tree_mod, oracle):
-    """Large parts on both block widths: a batch of 320 parts (more than one
-    wave of 512-thread blocks on 152 SMs, so 256-thread blocks with 8 picks
-    per round) and its first 8 parts alone (512-thread blocks, 16 picks per
-    round) give the oracle's faces and volumes."""
+    """Large parts on every block width: on 152 SMs a batch of 320 parts
+    runs on 256-thread blocks (8 picks per round), its first 200 parts on
+    512-thread blocks (two per SM) and its first 8 on 1024-thread blocks (one
+    per SM, 16 picks per round); all give the oracle's faces and volumes."""
     D = importlib.import_module("cuacd-web_gb300.decompose")
     cfg = dict(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=16384)
     g = tree_mod.GpuTree(**cfg)
@@ -143,7 +143,7 @@ def test_hull_block_widths(tree_mod, oracle):
         s *= rng.uniform(0.8, 1.0, size=(n, 1))
         sets.append(M.Mesh(s.astype(np.float32), np.zeros((0, 3), np.uint32)))
     ro, so = o.hull_meshes(sets)
-    for subset in (sets, sets[:8]):
+    for subset in (sets, sets[:200], sets[:8]):
         rg, sg = g.hull_meshes(subset)
         assert list(sg) == list(so[: len(subset)])
         for i, (a, b) in enumerate(zip(rg, ro)):
