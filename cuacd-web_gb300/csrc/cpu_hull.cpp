@@ -355,7 +355,9 @@ class QuickHull {
       }
     std::vector<uint32_t> horizon, visible, newFaces, newEdges;
     std::vector<std::pair<uint32_t, uint32_t>> walk;  // (face, half edge entered through)
-    std::vector<std::vector<uint32_t>> orphans;
+    // the visible faces' points in visible-face order (their lists keep
+    // their storage for the faces that reuse the slots)
+    std::vector<uint32_t> orphans;
     uint64_t pass = 0;
     while (!queue.empty()) {
       pass++;
@@ -429,10 +431,8 @@ class QuickHull {
         }
         F_[fi].he = QH_NONE;
         freeF_.push_back(fi);
-        if (!F_[fi].pts.empty()) {
-          orphans.push_back(std::move(F_[fi].pts));
-          F_[fi].pts = std::vector<uint32_t>();
-        }
+        orphans.insert(orphans.end(), F_[fi].pts.begin(), F_[fi].pts.end());
+        F_[fi].pts.clear();
       }
       while (reused < 2 * hc) {
         newEdges.push_back(add_edge());
@@ -459,12 +459,11 @@ class QuickHull {
         E_[BC].opp = newEdges[(2 * (i + 1)) % (2 * hc)];
       }
       // each orphaned point goes to the first new face that sees it
-      for (const std::vector<uint32_t>& list : orphans)
-        for (uint32_t q : list) {
-          if (q == eye) continue;
-          for (size_t j = 0; j < hc; j++)
-            if (add_point(F_[newFaces[j]], q)) break;
-        }
+      for (uint32_t q : orphans) {
+        if (q == eye) continue;
+        for (size_t j = 0; j < hc; j++)
+          if (add_point(F_[newFaces[j]], q)) break;
+      }
       for (uint32_t nf : newFaces)
         if (!F_[nf].pts.empty() && !F_[nf].queued) {
           queue.push_back(nf);
