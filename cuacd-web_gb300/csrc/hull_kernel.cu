@@ -9,8 +9,8 @@
 // otherwise (the reference uses three 32-bit limbs; the sign is the same).
 //
 // GB300 design:
-//   * one group per part: a warp for parts up to smallNv points, a 256- or
-//     512-thread block above; persistent groups walk the level's parts, each
+//   * one group per part: a warp for parts up to smallNv points, a block of
+//     256, 512 or 1024 threads above; persistent groups walk the level's parts, each
 //     with its own scratch slab (owner, dist, candidates, faces, visible list)
 //   * visible faces are listed in slot order and new faces are created in
 //     horizon-edge order with group prefix sums, so the face sets are
@@ -823,7 +823,7 @@ __device__ __noinline__ uint32_t hull_grow(const HullCtx& h, HullSm& hs, GrpSmem
 }
 
 // ---------------------------------------------------------------------------
-// Block path (parts above smallNv points, 256 or 512 threads). The same insertion
+// Block path (parts above smallNv points, 256, 512 or 1024 threads). The same insertion
 // sequence and face slots as hull_grow + hull_insert, laid out for latency:
 //   * the insertion (warp 0) keeps the visible patch in shared memory: a
 //     hash set of its faces, their corners and the faces across their
@@ -2338,10 +2338,10 @@ restart:
 
 // Persistent groups: group s owns slab s and takes the launch's parts from a
 // counter, so parts of uneven size balance across the GPU. Warps take parts
-// with nv <= smallNv, blocks of 256 or 512 threads the others (512 when the
-// level's parts fit one wave of them): the block inserts up to one point
-// per warp per round, and its width serves the passes over all points and
-// candidates, which grow with nv.
+// with nv <= smallNv, blocks of 256, 512 or 1024 threads the others (the
+// widest whose resident blocks hold the level's parts in one wave): the
+// block inserts up to one point per warp (at most 16) per round, and its
+// width serves the passes over all points and candidates, which grow with nv.
 template <int G>
 __global__ void __launch_bounds__(G >= 512 ? G : 256, G == 1024 ? 1 : (G == 512 ? 2 : 4))
     k_hull(const Level P, const Dev D) {
