@@ -26,7 +26,9 @@ G = pkg("meshgen")
 
 def _meshes():
     out = [("cube", M.unit_cube()), ("l_shape", M.l_shape()), ("torus", square_torus()), ("stairs", stairs()),
-           ("l_prism", l_prism()), ("staircase8", G.staircase(8)), ("ico3", G.noisy_icosphere(3, seed=1))]
+           ("l_prism", l_prism()), ("staircase8", G.staircase(8)), ("ico3", G.noisy_icosphere(3, seed=1)),
+           # marching-tetrahedra surface: vertices on shared grid lines and planes
+           ("blob", M.normalize(G.blob_mesh(6, 26, seed=3))[0])]
     return out
 
 
