@@ -886,8 +886,8 @@ struct BatDims {
   static constexpr uint32_t NRC = NW <= 8 ? 16u : 8u;  // new-face records per step kept in shared memory
   // picks per round: one per warp, at most KMAX_CAP (the merge of the
   // warps' lists is serial in the picks, and later picks rarely pass the
-  // checks: on 28k-point blob hulls 12 and 16 measured the same, 20 2 %
-  // slower, 28 5 % slower)
+  // checks: on 15-28k-point blob hulls 12 and 16 measured the same, 20
+  // 1-2 % slower, 28 4-6 % slower)
   static constexpr uint32_t KMAX = NW < KMAX_CAP ? (uint32_t)NW : KMAX_CAP;
 };
 #define BAT_LIST 8u  // keys per warp list
