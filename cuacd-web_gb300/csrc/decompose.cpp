@@ -1006,6 +1006,10 @@ void Engine::run_groups(std::vector<Job*>& jobs, std::vector<Engine*>& ranBy) {
       } catch (const std::bad_alloc&) {
         bad[g] = 1;
         errs[g] = Failure{CUACD_E_CAPACITY, "host memory exhausted"};
+      } catch (const std::exception& x) {
+        // e.g. a worker thread the system would not start
+        bad[g] = 1;
+        errs[g] = Failure{CUACD_E_CAPACITY, std::string("host error: ") + x.what()};
       }
     });
   }
@@ -1265,6 +1269,9 @@ int cuacd_decompose(void* d, const cuacd_mesh* meshes, int n, int batched, void*
   } catch (const std::bad_alloc&) {
     e->evals.clear();
     return set_error(CUACD_E_CAPACITY, "cuacd_decompose: host memory exhausted");
+  } catch (const std::exception& x) {
+    e->evals.clear();
+    return set_error(CUACD_E_CAPACITY, (std::string("cuacd_decompose: host error: ") + x.what()).c_str());
   }
   *result = res.release();
   return CUACD_OK;
@@ -1363,6 +1370,8 @@ int cuacd_server_step(void* sv, int* completed) {
     return set_error(f.code, f.msg.c_str());
   } catch (const std::bad_alloc&) {
     return set_error(CUACD_E_CAPACITY, "cuacd_server_step: host memory exhausted");
+  } catch (const std::exception& x) {
+    return set_error(CUACD_E_CAPACITY, (std::string("cuacd_server_step: host error: ") + x.what()).c_str());
   }
 }
 
