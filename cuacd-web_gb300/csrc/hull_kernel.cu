@@ -2481,31 +2481,89 @@ __global__ void k_noalloc_finish(const uint32_t* scratch, float* volume, uint32_
 using namespace cuacd;
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
+
+// The scratch array's device address in the calling thread's current
+// context. In host code the array's name is only a stand-in, so the address
+// is looked up with cudaGetSymbolAddress, once per context: the cache is keyed
+// on the context's id (cuCtxGetId, reached through the runtime's driver entry
+// points so the library needs no link against libcuda), which changes when a
+// device's primary context is re-created (after cudaDeviceReset), when the
+// module and with it the array may move.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+
+static int noalloc_scratch_address(uint32_t** out) {
+  static std::mutex mu;
+  static CtxGetCurrentFn getCurrent = nullptr;
+  static CtxGetIdFn getId = nullptr;
+  static bool resolved = false;
+  struct Entry { unsigned long long ctx; uint32_t* addr; };
+  static Entry cache[64];
+  static int nCache = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!resolved) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+      return set_error(-4, "cuacd_hull_points_noalloc: driver entry points cuCtxGetCurrent / cuCtxGetId unavailable");
+    getCurrent = (CtxGetCurrentFn)f1;
+    getId = (CtxGetIdFn)f2;
+    resolved = true;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  void* p = nullptr;
+  if (getCurrent(&ctx) != 0) return set_error(-4, "cuacd_hull_points_noalloc: no usable CUDA device");
+  if (ctx != nullptr) {
+    if (getId(ctx, &id) != 0) return set_error(-4, "cuacd_hull_points_noalloc: cannot read the context id");
+    for (int i = 0; i < nCache; i++)
+      if (cache[i].ctx == id) {
+        *out = cache[i].addr;
+        return 0;
+      }
+  }
+  // not seen yet (or no context is current: the runtime makes the current
+  // device's primary context current on this call)
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess) return set_error(-4, cudaGetErrorString(e));
+  if (ctx == nullptr) {
+    if (getCurrent(&ctx) != 0 || ctx == nullptr || getId(ctx, &id) != 0)
+      return set_error(-4, "cuacd_hull_points_noalloc: no current CUDA context");
+  }
+  Entry ent{id, (uint32_t*)p};
+  if (nCache < 64) cache[nCache++] = ent;
+  else {  // more contexts than slots over the process's life: reuse the oldest
+    std::memmove(cache, cache + 1, sizeof(Entry) * 63);
+    cache[63] = ent;
+  }
+  *out = (uint32_t*)p;
+  return 0;
+}
 
 extern "C" int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint32_t* tris, uint32_t trisCap,
                                          float* volume, uint32_t* ntris, int32_t* status, void* stream) {
   if (!points || !tris || !volume || !ntris || !status) return set_error(-1, "cuacd_hull_points_noalloc: null buffer");
   if (nv > NOALLOC_MAX_POINTS)
     return set_error(-2, "cuacd_hull_points_noalloc: at most 4096 points (the fixed scratch holds one 4096-point slab)");
-  if (trisCap < 12) return set_error(-1, "cuacd_hull_points_noalloc: trisCap must hold at least 4 triangles (12 u32)");
-  // the scratch array's device address, looked up once per device with that
-  // device current (in host code its name is only a stand-in)
-  static std::mutex mu;
-  static uint32_t* addr[64] = {nullptr};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return set_error(-4, "cuacd_hull_points_noalloc: no current device");
-  {
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess) return set_error(-4, cudaGetErrorString(e));
-      addr[dev] = (uint32_t*)p;
-    }
+  // a hull of nv points is a closed triangulated surface over at most nv
+  // vertices, so it has at most 2 nv - 4 triangles; a smaller buffer could
+  // not take every face, and the call is refused before any work is queued
+  const uint64_t need = 3ull * std::max<uint64_t>(nv >= 4 ? 2ull * nv - 4 : 0, 4);
+  if (trisCap < need) {
+    char msg[160];
+    snprintf(msg, sizeof(msg),
+             "cuacd_hull_points_noalloc: trisCap %u u32 is below the %llu a hull of %u points may need (3 * (2 nv - 4), "
+             "at least 12)", trisCap, (unsigned long long)need, nv);
+    return set_error(-2, msg);
   }
-  uint32_t* scratch = addr[dev];
+  uint32_t* scratch = nullptr;
+  if (int rc = noalloc_scratch_address(&scratch)) return rc;
   cudaStream_t s = (cudaStream_t)stream;
   const uint32_t maxNv = std::max(nv, 1u);
   const uint32_t fmax = 2 * std::min(4096u, maxNv) + 3 * HULL_VIS_MAX + 1024;

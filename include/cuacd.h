@@ -209,18 +209,23 @@ int cuacd_tree_read_plane(void* tree, uint32_t index, float* out4);
  * the moment they need a hull (a host application whose own arena or
  * caching allocator owns the device memory, or an interactive loop that
  * must not stall running work on cudaMalloc / cudaFree). The caller passes
- * device buffers it owns: points (nv * 3 floats), tris (trisCap u32, at
- * least 12), and one float, one u32 and one i32 for the volume, the
- * triangle count and the status (as cuacd_tree_hull_meshes: 0 or the
- * failure code). The kernel's scratch is a fixed array of about 1.7 MiB inside
- * the library, which every GPU that loads the library keeps until exit; it
- * holds at most 4096 points, and larger sets are rejected with
- * CUACD_E_CAPACITY. Work is queued on `stream` (a cudaStream_t, NULL for
- * the default stream); results are valid once that stream has completed.
- * The first call on a device looks up the array's device address (with
- * that device current), so make the first call before any stream capture.
- * All calls share the one array: calls that overlap on the GPU (different
- * streams, or different host threads) race and must be serialised. */
+ * device buffers it owns: points (nv * 3 floats), tris (trisCap u32), and
+ * one float, one u32 and one i32 for the volume, the triangle count and the
+ * status (as cuacd_tree_hull_meshes: 0, or the failure code, 8 for fewer
+ * than 4 points or a flat set). A hull of nv points has at most 2 nv - 4
+ * triangles, so trisCap must be at least 3 * max(2 nv - 4, 4) u32; a smaller
+ * buffer is refused with CUACD_E_CAPACITY before any work is queued (no
+ * hull is ever cut short). The kernel's scratch is a fixed array of about
+ * 1.7 MiB inside the library, which every GPU that loads the library keeps
+ * until exit; it holds at most 4096 points, and larger sets are rejected
+ * with CUACD_E_CAPACITY. Work is queued on `stream` (a cudaStream_t of the
+ * current device, NULL for the default stream); results are valid once that
+ * stream has completed. The first call in a CUDA context (the first on a
+ * device, and the first after its context was re-created) looks up the
+ * array's device address in that context, so make it before any stream
+ * capture. All calls share the one array and each leaves its contents
+ * behind: calls that overlap on the GPU (different streams, or different
+ * host threads) race and must be serialised. */
 int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint32_t* tris, uint32_t trisCap, float* volume,
                               uint32_t* ntris, int32_t* status, void* stream);
 
