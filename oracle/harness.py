@@ -24,10 +24,14 @@ Mesh = importlib.import_module("cuacd-web_gb300.mesh").Mesh
 _lib = None
 
 
+def reference_dir():
+    """The reference checkout, where present (CUACD_REFERENCE_DIR)."""
+    return os.environ.get("CUACD_REFERENCE_DIR", "/root/reference")
+
+
 def build_oracle():
     subprocess.run(["make", "-s", "-C", ORACLE_DIR, "liboracle.so"], check=True)
-    ref_src = "/root/reference/wasm/quickhull/QuickHull.cpp"
-    if os.path.exists(ref_src):
+    if os.path.exists(os.path.join(reference_dir(), "wasm/quickhull/QuickHull.cpp")):
         subprocess.run(["make", "-s", "-C", ORACLE_DIR, "ref"], check=True)
 
 

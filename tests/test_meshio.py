@@ -81,11 +81,9 @@ def test_js_number_printing(x, s):
 
 
 def test_reference_stl_fixture_loads():
-    # the reference's own test mesh (tests/data/49160.stl), where the
-    # reference tree is present: closed after welding (decompose.test.ts:52-55)
-    path = "/root/reference/tests/data/49160.stl"
-    if not os.path.exists(path):
-        pytest.skip("reference tree not present")
+    # the reference's own test mesh (its tests/data/49160.stl, committed as a
+    # fixture): closed after welding (decompose.test.ts:52-55)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "49160.stl")
     with open(path, "rb") as f:
         m = IO.parse_stl(f.read())
     assert m.tris.shape[0] > 0
