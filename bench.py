@@ -2,8 +2,9 @@
 """Cut candidates evaluated per second by the lookahead tree on GB300.
 
 Workload (the staircase configuration): the closed union of 8 boxes (1.0 x
-0.25 x k * 0.125, k = 1..8, 96 triangles in this triangulation), normalised
-to a largest extent of 2 as decompose() does, cut with width 6, width2 3,
+0.25 x k * 0.125, k = 1..8), welded without T-junctions, its side-wall
+triangles split at their centroids: 188 triangles over 96 vertices,
+normalised to a largest extent of 2 as decompose() does, cut with width 6, width2 3,
 depth 3, 16 concave edges (64 plane slots), threshold 0.1 (minEdgeDist
 0.015) and 2 refinement rounds of 8 probes. One step is one GpuTree.run over
 a batch of maxNCutting = 160 such seeds: the tree, its evaluate kernel and
@@ -17,7 +18,7 @@ e2e: the same metric through the public C call cuacd_tree_run with host
   buffers: seed upload, the run and the result readback in the timed region.
 
 --impl reference: the CPU restatement of the same path (the oracle port of
-the reference's kernels) on all host threads, timed on bounded samples.
+the reference's kernels) on all host threads, on the same 160-seed batch.
 """
 from __future__ import annotations
 
@@ -48,7 +49,7 @@ def workload(n_seeds):
     gen = importlib.import_module("cuacd-web_gb300.meshgen")
     mesh = importlib.import_module("cuacd-web_gb300.mesh")
     conc = importlib.import_module("cuacd-web_gb300.concave")
-    seed, _, _ = mesh.normalize(gen.staircase(8))
+    seed, _, _ = mesh.normalize(gen.staircase(8, wall_centroids=True))
     planes = conc.concave_edge_planes(seed, TREE["nConcaveEdges"])
     spacing = conc.refine_spacing([seed], THRESHOLD, TREE["width"])[0]
     seeds = [seed] * n_seeds
@@ -57,7 +58,7 @@ def workload(n_seeds):
 
 
 def config_dict(n_seeds):
-    return {"workload": f"staircase-8 lookahead tree, {n_seeds} seeds per step", "mesh": "staircase-8 (96 tris, 50 verts)",
+    return {"workload": f"staircase-8 lookahead tree, {n_seeds} seeds per step", "mesh": "staircase-8 (188 tris, 96 verts: side-wall triangles split at their centroids)",
             "seeds": n_seeds, "width": TREE["width"], "width2": TREE["width2"], "depth": TREE["depth"],
             "nConcaveEdges": TREE["nConcaveEdges"], "threshold": THRESHOLD, "refineRounds": REFINE_ROUNDS,
             "refineProbes": REFINE_PROBES, "l2": "flushed between timed steps (256 MiB write)"}
@@ -127,15 +128,22 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel):
-    """dram bytes per launch of a kernel from the committed ncu summary."""
+def profile_figures(kernel):
+    """Figures of a kernel at this workload from its committed ncu summary
+    (lines `name: value`): traffic_bytes_per_launch (dram read + write per
+    launch), issue_active_pct, warps_active_pct."""
     p = os.path.join(ROOT, "profiles", f"{kernel}_staircase160.md")
+    out = {}
     if not os.path.exists(p):
-        return None
+        return out
     for line in open(p):
-        if line.startswith("traffic_bytes_per_launch:"):
-            return float(line.split(":")[1])
-    return None
+        k, sep, v = line.partition(":")
+        if sep and k.strip() in ("traffic_bytes_per_launch", "issue_active_pct", "warps_active_pct"):
+            try:
+                out[k.strip()] = float(v)
+            except ValueError:
+                pass
+    return out
 
 
 def cpu_tree_rate(seeds, planes, refine, threads):
@@ -202,7 +210,7 @@ def run_reference(args):
     if rank != 0:
         return
     n = host_threads()
-    sample = 8 * n  # each step about half a second of work on all host threads
+    sample = args.seeds  # the engine arm's batch: 160 seeds per step
     seeds, planes, refine = workload(sample)
     for _ in range(args.warmup):
         cpu_tree_rate(seeds[:n], planes[:n], refine, n)
@@ -308,16 +316,35 @@ def run_engine(args):
                          "hull": depth * stages, "record": depth * stages}
     byte_idx = {"plan": 0, "emit": 1, "hull": 2}
     peak, peak_kind = peaks()
+
+    def kernel_roof(k):
+        """HBM fraction of kernel class k from its algorithmic bytes (counted
+        by the kernels) over its average launch time in the timed steps, with
+        the issue figures of its committed ncu summary at this workload."""
+        nl = launches_per_step[k] * args.steps
+        per_launch = kbytes[byte_idx[k]] / nl
+        avg_s = kms[k] / 1000.0 / nl
+        achieved = per_launch / avg_s / 1e9
+        prof = profile_figures(f"k_{k}")
+        r = {"achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+             "algorithmic_bytes_per_launch": per_launch, "avg_launch_us": avg_s * 1e6,
+             "traffic": prof.get("traffic_bytes_per_launch")}
+        if "issue_active_pct" in prof:
+            r["issue_active"] = prof["issue_active_pct"] / 100.0
+        if "warps_active_pct" in prof:
+            r["warps_active"] = prof["warps_active_pct"] / 100.0
+        return r
+
     roof = None
     if dom in byte_idx:
-        nl = launches_per_step[dom] * args.steps
-        per_launch = kbytes[byte_idx[dom]] / nl
-        avg_s = kms[dom] / 1000.0 / nl
-        achieved = per_launch / avg_s / 1e9
-        roof = {"bound": "hbm", "kernel": f"k_{dom}", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch,
-                "avg_launch_us": avg_s * 1e6, "traffic": ncu_traffic(f"k_{dom}"),
-                "kernel_ms_per_step": {k: v / args.steps for k, v in kms.items()}}
+        # the hull is bound by instruction issue and latency (integer
+        # predicates, shared memory, dependent L2 round trips): its bound is
+        # issue, reported as the issue-active fraction beside its HBM fraction
+        roof = dict(bound="issue" if dom == "hull" else "hbm", kernel=f"k_{dom}", **kernel_roof(dom))
+        if dom == "hull" and "issue_active" in roof:
+            roof["issue_frac"] = roof["issue_active"]
+        roof["kernels"] = {f"k_{k}": kernel_roof(k) for k in byte_idx if k != dom}
+        roof["kernel_ms_per_step"] = {k: v / args.steps for k, v in kms.items()}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_dict(args.seeds),

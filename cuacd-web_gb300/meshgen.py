@@ -67,7 +67,8 @@ def random_planes(m: Mesh, n: int, seed: int = 0) -> np.ndarray:
     return np.concatenate([nrm, -off[:, None]], axis=1).astype(np.float32)
 
 
-def staircase(n_steps: int = 8, width: float = 1.0, depth: float = 0.25, rise: float = 0.125) -> Mesh:
+def staircase(n_steps: int = 8, width: float = 1.0, depth: float = 0.25, rise: float = 0.125,
+              wall_centroids: bool = False) -> Mesh:
     """Union of n_steps boxes [0, width] x [(k-1) depth, k depth] x [0, k rise],
     k = 1..n_steps, as one closed manifold without T-junctions.
 
@@ -75,7 +76,13 @@ def staircase(n_steps: int = 8, width: float = 1.0, depth: float = 0.25, rise: f
     column: a quad for the first column and a pentagon (the previous
     column's top corner on its left edge) for the others, fanned from the
     bottom-left corner. Treads, risers, the back wall and the bottom are one
-    quad per box. For n_steps = 8 this is 96 triangles.
+    quad per box. For n_steps = 8 this is 96 triangles over 50 vertices.
+
+    wall_centroids: every side-wall triangle is split at its centroid into
+    three, so the two large walls carry interior vertices. For n_steps = 8
+    that adds 46 vertices: 188 triangles over 96 vertices (a closed genus-0
+    triangulation has 2 V - 4 triangles), the staircase configuration's
+    triangle count. The solid, and so every hull, is the same.
     """
     ys = [k * depth for k in range(n_steps + 1)]
     hs = [k * rise for k in range(n_steps + 1)]
@@ -105,7 +112,14 @@ def staircase(n_steps: int = 8, width: float = 1.0, depth: float = 0.25, rise: f
             # is counter-clockwise seen from +x, so wall 0 is reversed
             for i in range(1, len(ids) - 1):
                 t = (ids[0], ids[i], ids[i + 1])
-                tris.append(t if side == 1 else (t[0], t[2], t[1]))
+                t = t if side == 1 else (t[0], t[2], t[1])
+                if wall_centroids:
+                    p = [verts[j] for j in t]
+                    c = len(verts)
+                    verts.append(tuple(sum(q[a] for q in p) / 3.0 for a in range(3)))
+                    tris.extend([(t[0], t[1], c), (t[1], t[2], c), (t[2], t[0], c)])
+                else:
+                    tris.append(t)
     for k in range(1, n_steps + 1):
         y0, y1, h = ys[k - 1], ys[k], hs[k]
         # tread (+z)
