@@ -27,6 +27,8 @@ UNITS = {
     "hull_kernel.cu": ["--fmad=false"],
     "hausdorff_kernels.cu": [],
     "cuacd_host.cu": [],
+    # the GPU capped cut rounds every double operation as the host cut does
+    "cut_kernels.cu": ["--fmad=false"],
     # host geometry of the decomposition loop: double arithmetic rounded as
     # the reference's JavaScript rounds it, so no contraction into FMA
     "host_mesh.cpp": ["-Xcompiler", "-ffp-contract=off"],
@@ -34,7 +36,7 @@ UNITS = {
     "decompose.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "cpu_hull.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["cuacd_dev.cuh", "host_mesh.h"]
+HEADERS = ["cuacd_dev.cuh", "host_mesh.h", "cut_engine.h"]
 
 
 def nvcc() -> str:

@@ -18,6 +18,8 @@
 
 #include "../../include/cuacd.h"
 #include "cuacd_dev.cuh"
+#include "cut_engine.h"
+#include "host_mesh.h"
 
 namespace cuacd {
 void launch_plan(const Level& P, const Dev& D, bool big, cudaStream_t s);
@@ -145,7 +147,10 @@ struct Tree {
   std::vector<uint64_t> gsig;
   bool gvalid = false;
 
+  cut::Engine* cutter = nullptr;  // the GPU capped cut, created on first use
+
   ~Tree() {
+    if (cutter) cut::engine_destroy(cutter);
     if (gexec) cudaGraphExecDestroy(gexec);
     for (DevBuf* b : {&bV, &bT, &bE, &bS, &bCtr, &bSlab, &bParts, &bItems, &bJobs, &bPlanes, &bSnap, &bHd, &bScan, &bWork, &bUb}) b->release();
     for (HostBuf* b : {&hStage, &hRead, &hSnap, &hMeta}) b->release();
@@ -808,6 +813,53 @@ void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
 }
 
 void cuacd_tree_destroy(void* t) { delete (Tree*)t; }
+
+int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, const int32_t* meshOfCut,
+                          const double* planes, int nCuts, void** halves) {
+  Tree* t = (Tree*)tree;
+  if (!t || !halves || nCuts < 0 || (nCuts > 0 && (!meshOfCut || !planes || !meshes)))
+    return fail(CUACD_E_INVALID, "cuacd_tree_plane_cuts: invalid argument");
+  *halves = nullptr;
+  if (!t->cutter && !(t->cutter = cut::engine_create())) return fail(CUACD_E_CUDA, "cut engine creation failed");
+  std::vector<cut::CutSpec> cs((size_t)nCuts);
+  for (int k = 0; k < nCuts; k++) {
+    const double* p = planes + 4 * (size_t)k;
+    const host::PlaneFrame f = host::plane_frame(host::Plane{p[0], p[1], p[2], p[3]});
+    cs[k].mesh = meshOfCut[k];
+    for (int a = 0; a < 3; a++) {
+      cs[k].n[a] = f.n[a];
+      cs[k].u[a] = f.u[a];
+      cs[k].v[a] = f.v[a];
+    }
+    cs[k].d = f.d;
+  }
+  cut::Halves* h = new cut::Halves();
+  const int rc = cut::engine_run(t->cutter, t->stream, meshes, nMeshes, cs.data(), nCuts, h);
+  if (rc != CUACD_OK) {
+    delete h;
+    return rc;
+  }
+  *halves = h;
+  return CUACD_OK;
+}
+
+int cuacd_cuts_half(const void* halves, int cut, int side, const float** verts, uint32_t* nv, const uint32_t** tris,
+                    uint32_t* nt) {
+  const cut::Halves* h = (const cut::Halves*)halves;
+  if (!h || cut < 0 || (size_t)cut >= h->status.size() || side < 0 || side > 1)
+    return fail(CUACD_E_INVALID, "cuacd_cuts_half: invalid argument");
+  const size_t k = 2 * (size_t)cut + side;
+  const int st = h->status[cut];
+  if (verts) *verts = st == 0 ? h->V + 3 * h->vOff[k] : nullptr;
+  if (tris) *tris = st == 0 ? h->T + 3 * h->tOff[k] : nullptr;
+  if (nv) *nv = st == 0 ? h->nv[k] : 0;
+  if (nt) *nt = st == 0 ? h->nt[k] : 0;
+  return st;
+}
+
+float cuacd_cuts_gpu_ms(const void* halves) { return halves ? ((const cut::Halves*)halves)->gpuMs : 0.0f; }
+
+void cuacd_cuts_free(void* halves) { delete (cut::Halves*)halves; }
 int cuacd_plane_slots(const void* t) { return (int)((const Tree*)t)->edgeStride; }
 int cuacd_vis_max(void) { return CUACD_VIS_MAX; }
 void cuacd_set_profile(void* t, int on) {

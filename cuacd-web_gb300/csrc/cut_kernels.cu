@@ -1,0 +1,1534 @@
+// cut_kernels.cu — the capped plane cut of the decomposition loop
+// (src/cpu/cut.ts:33-315) on the GPU, for a batch of (mesh, plane) cuts.
+//
+// The result of every cut is bit for bit the host cut's (csrc/plane_cut.cpp):
+// the same half meshes, vertices in the same order (numbered by first use in
+// each half's triangle list), the same triangles in the same order, the same
+// cap triangulation and the same failures. The steps:
+//
+//   classify   one thread per vertex: signed distance in double, the
+//              three-state side (on the plane within 1e-6), whether the
+//              plane splits the mesh at all;
+//   count      one thread per triangle: how many triangles each half gets
+//              (Sutherland-Hodgman on one triangle gives at most a quad) and
+//              whether a half's triangles there can hold a cap boundary edge
+//              (two vertices on the plane); a device-wide scan turns the
+//              counts into each triangle's output positions;
+//   surface    one thread per triangle: writes the halves' surface
+//              triangles in input order, intersection vertices shared per
+//              edge through a hash table keyed on the edge (its coordinates
+//              depend only on the edge's lower and higher vertex);
+//   cap        one warp per (cut, half): the half's boundary edges in
+//              first-seen order, their loops, the loops' classification
+//              (outer or hole by signed area, parent by the hole centroid's
+//              crossing number) and the caps (ear clipping with holes
+//              bridged in, or centroid fans). The sequential steps run on
+//              every lane of the warp with identical data (warp-uniform
+//              code: identical stores, no divergence); the ear test, the
+//              edge gathering and the twin search split their loops over
+//              the lanes;
+//   compact    one thread per triangle corner: first use of every vertex
+//              (atomicMin), a scan of the first uses numbers the vertices,
+//              then the halves are written to the output pools.
+//
+// The host computes the per-cut constants that involve library functions
+// (the normal's length and the cap basis, both from std::hypot), so the
+// device only adds, multiplies, divides and compares doubles; this unit
+// compiles with --fmad=false and the host cut without contraction, so both
+// round every operation the same way.
+//
+// Boundary edges are looked for among edges with both ends on the plane:
+// for a closed input mesh every boundary edge of a half lies there (an edge
+// with an end off the plane keeps its reverse in the same half).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cut_engine.h"
+
+#define CUT_FULL 0xffffffffu
+#define CUT_NONE 0xffffffffu
+
+namespace cuacd {
+int set_error(int code, const char* msg);
+
+namespace cut {
+
+// ---------------------------------------------------------------------------
+// records
+
+struct CutDesc {
+  double n[3], d;         // unit normal and offset of the plane
+  double u[3], w[3];      // orthonormal basis of the plane for the caps
+  uint32_t vOff, nv;      // input mesh: first vertex and count in the vertex pool
+  uint32_t tOff, nt;      // first triangle and count in the triangle pool
+  uint32_t vBase, tBase;  // this cut's range in the per-vertex / per-triangle scratch
+  uint32_t pad[2];
+};
+static_assert(sizeof(CutDesc) == 112, "CutDesc layout");
+
+// written by the count step
+struct CutSizes {
+  uint32_t anyPos, anyNeg, straddle, pad;
+  uint32_t surf[2];  // surface triangles of each half
+  uint32_t cand[2];  // input triangles whose half triangles may hold a boundary edge
+};
+
+// set by the host from the sizes
+struct CutLayout {
+  uint32_t hashOff, hashSize;      // intersection hash (keys, coordinates)
+  uint32_t surfOff[2], surfCnt[2];  // surface triangles (vertex ids before compaction)
+  uint32_t candOff[2], candCnt[2];  // candidate entries (first half triangle, count)
+  uint32_t preOff[2];              // first-use array over the half's vertex ids
+  uint32_t capMax[2];              // cap triangles the cap scratch holds
+  uint32_t capWord[2], capDbl[2];  // the cap step's scratch in the word and double arenas
+  uint32_t mEdge[2];               // bound on the half's plane edges (6 per candidate)
+  uint32_t active, pad;
+};
+
+// written by the cap and compact steps
+struct CutOut {
+  int32_t fail[2];   // per half: 0 or a CUT_* failure
+  uint32_t cap[2];   // cap triangles of each half
+  uint32_t cent[2];  // centroid vertices of each half
+  uint32_t nvOut[2];
+};
+
+enum { CUT_OK = 0, CUT_NO_SPLIT = 1, CUT_OPEN_CHAIN = 2, CUT_DEAD_END = 3, CUT_CYCLE = 4, CUT_SCRATCH = 5 };
+
+constexpr double ON_PLANE_EPS = 1e-6;  // the host cut's default eps
+constexpr unsigned long long EMPTY_KEY = ~0ull;
+
+// the cap step's scratch of one half, carved from m = its plane-edge bound
+struct CapCarve {
+  uint32_t eA, eB;          // plane edges (m each)
+  uint32_t eh, ehKey, ehVal;  // edge hash: entries, keys (2 words each), first index
+  uint32_t bSrc, bDst, bNext, bUsed;  // boundary edges (m each)
+  uint32_t sh, shKey, shHead, shTail;  // source-vertex hash
+  uint32_t starts;          // source vertices in first-seen order (m)
+  uint32_t loopV, loopS;    // loop vertices (m), loop starts (m + 1)
+  uint32_t depth, parent;   // per loop (m)
+  uint32_t nd;              // ear-clip node capacity (3 m + 4)
+  uint32_t ndI, ndPrev, ndNext, ndAlive;
+  uint32_t gId;             // a group's ring: vertex ids (m)
+  uint32_t holeL;           // a group's holes: leftmost node (m)
+  uint32_t capT;            // cap triangles, 3 words each (capMax)
+  uint32_t words;
+  uint32_t l2, area, ndX, ndY, gXY, holeX, cent;  // double arena
+  uint32_t dbls;
+};
+
+__host__ __device__ inline uint32_t pow2_at_least(uint32_t x) {
+  uint32_t p = 16;
+  while (p < x) p <<= 1;
+  return p;
+}
+
+__host__ __device__ inline CapCarve carve(uint32_t m, uint32_t capMax) {
+  CapCarve c;
+  uint32_t o = 0;
+  c.eh = pow2_at_least(2 * m);
+  c.ehKey = o; o += 2 * c.eh;  // first: 8-byte aligned keys
+  c.ehVal = o; o += c.eh;
+  c.eA = o; o += m;
+  c.eB = o; o += m;
+  c.bSrc = o; o += m;
+  c.bDst = o; o += m;
+  c.bNext = o; o += m;
+  c.bUsed = o; o += m;
+  c.sh = pow2_at_least(2 * m);
+  c.shKey = o; o += c.sh;
+  c.shHead = o; o += c.sh;
+  c.shTail = o; o += c.sh;
+  c.starts = o; o += m;
+  c.loopV = o; o += m;
+  c.loopS = o; o += m + 1;
+  c.depth = o; o += m;
+  c.parent = o; o += m;
+  c.nd = 3 * m + 4;
+  c.ndI = o; o += c.nd;
+  c.ndPrev = o; o += c.nd;
+  c.ndNext = o; o += c.nd;
+  c.ndAlive = o; o += c.nd;
+  c.gId = o; o += m;
+  c.holeL = o; o += m;
+  c.capT = o; o += 3 * capMax;
+  c.words = (o + 1) & ~1u;
+  uint32_t d = 0;
+  c.l2 = d; d += 2 * m;
+  c.area = d; d += m;
+  c.ndX = d; d += c.nd;
+  c.ndY = d; d += c.nd;
+  c.gXY = d; d += 2 * m;
+  c.holeX = d; d += m;
+  c.cent = d; d += 3 * m;
+  c.dbls = d;
+  return c;
+}
+
+// ---------------------------------------------------------------------------
+// device-wide exclusive scan of uint32 or uint4 values: out has n + 1
+// entries, out[n] = total
+
+__device__ __forceinline__ uint32_t vadd(uint32_t a, uint32_t b) { return a + b; }
+__device__ __forceinline__ uint4 vadd(uint4 a, uint4 b) { return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ uint32_t vsub(uint32_t a, uint32_t b) { return a - b; }
+__device__ __forceinline__ uint4 vsub(uint4 a, uint4 b) { return make_uint4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+template <typename T>
+__device__ __forceinline__ T vzero();
+template <>
+__device__ __forceinline__ uint32_t vzero<uint32_t>() { return 0u; }
+template <>
+__device__ __forceinline__ uint4 vzero<uint4>() { return make_uint4(0, 0, 0, 0); }
+__device__ __forceinline__ uint32_t vshfl_up(uint32_t v, int d) { return __shfl_up_sync(CUT_FULL, v, d); }
+__device__ __forceinline__ uint4 vshfl_up(uint4 v, int d) {
+  return make_uint4(__shfl_up_sync(CUT_FULL, v.x, d), __shfl_up_sync(CUT_FULL, v.y, d),
+                    __shfl_up_sync(CUT_FULL, v.z, d), __shfl_up_sync(CUT_FULL, v.w, d));
+}
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 4;
+constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// inclusive scan of one value per thread over the block (blockDim.x a
+// multiple of 32, at most 1024); *total = the block's sum
+template <typename T>
+__device__ T block_inclusive(T v, T* warpSums, T* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int d = 1; d < 32; d <<= 1) {
+    T u = vshfl_up(v, d);
+    if (lane >= d) v = vadd(v, u);
+  }
+  if (lane == 31) warpSums[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    T s = lane < nw ? warpSums[lane] : vzero<T>();
+    for (int d = 1; d < 32; d <<= 1) {
+      T u = vshfl_up(s, d);
+      if (lane >= d) s = vadd(s, u);
+    }
+    warpSums[lane] = s;
+  }
+  __syncthreads();
+  if (wid > 0) v = vadd(v, warpSums[wid - 1]);
+  *total = warpSums[nw - 1];
+  __syncthreads();
+  return v;
+}
+
+template <typename T>
+__global__ void k_scan_tiles(const T* __restrict__ in, uint32_t n, T* __restrict__ tileSums) {
+  __shared__ T ws[32];
+  const uint32_t base = blockIdx.x * SCAN_TILE;
+  T s = vzero<T>();
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    const uint32_t i = base + threadIdx.x * SCAN_ITEMS + k;
+    if (i < n) s = vadd(s, in[i]);
+  }
+  T total;
+  block_inclusive(s, ws, &total);
+  if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
+}
+
+// tile sums to exclusive tile starts, in place (one block); total at [nTiles]
+template <typename T>
+__global__ void k_scan_tile_starts(T* __restrict__ tileSums, uint32_t nTiles) {
+  __shared__ T ws[32];
+  T carry = vzero<T>();
+  for (uint32_t c = 0; c < nTiles; c += blockDim.x) {
+    const uint32_t i = c + threadIdx.x;
+    const T v = i < nTiles ? tileSums[i] : vzero<T>();
+    T total;
+    const T inc = block_inclusive(v, ws, &total);
+    if (i < nTiles) tileSums[i] = vadd(carry, vsub(inc, v));
+    carry = vadd(carry, total);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) tileSums[nTiles] = carry;
+}
+
+template <typename T>
+__global__ void k_scan_apply(const T* __restrict__ in, uint32_t n, const T* __restrict__ tileStarts,
+                             uint32_t nTiles, T* __restrict__ out) {
+  __shared__ T ws[32];
+  const uint32_t base = blockIdx.x * SCAN_TILE;
+  T loc[SCAN_ITEMS];
+  T s = vzero<T>();
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    const uint32_t i = base + threadIdx.x * SCAN_ITEMS + k;
+    loc[k] = i < n ? in[i] : vzero<T>();
+    s = vadd(s, loc[k]);
+  }
+  T total;
+  const T inc = block_inclusive(s, ws, &total);
+  T cur = vadd(tileStarts[blockIdx.x], vsub(inc, s));
+  for (int k = 0; k < SCAN_ITEMS; k++) {
+    const uint32_t i = base + threadIdx.x * SCAN_ITEMS + k;
+    if (i < n) out[i] = cur;
+    cur = vadd(cur, loc[k]);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = tileStarts[nTiles];
+}
+
+// ---------------------------------------------------------------------------
+// helpers
+
+// the segment holding element g: the largest c with pre[c] <= g (pre has
+// n + 1 entries, pre[0] = 0, pre[n] > g)
+__device__ __forceinline__ uint32_t find_seg(const uint32_t* __restrict__ pre, uint32_t n, uint32_t g) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (pre[mid] <= g) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__host__ __device__ __forceinline__ uint32_t mix_key(unsigned long long k) {
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdull;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ull;
+  k ^= k >> 33;
+  return (uint32_t)k;
+}
+
+__device__ __forceinline__ int side_of(double v) { return v > ON_PLANE_EPS ? 1 : (v < -ON_PLANE_EPS ? -1 : 0); }
+
+// ---------------------------------------------------------------------------
+// classify: signed distance and side of every vertex
+
+__global__ void k_cut_classify(const CutDesc* __restrict__ D, const uint32_t* __restrict__ vPre, uint32_t n,
+                               uint32_t totalV, const float* __restrict__ V, double* __restrict__ dist,
+                               int8_t* __restrict__ sgn, CutSizes* __restrict__ S) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= totalV) return;
+  const uint32_t c = find_seg(vPre, n, g);
+  const CutDesc& d = D[c];
+  const uint32_t i = g - d.vBase;
+  const float* p = V + 3 * ((size_t)d.vOff + i);
+  const double x = p[0], y = p[1], z = p[2];
+  // n.x x + n.y y + n.z z + d, left to right (the host cut's order)
+  double v = d.n[0] * x;
+  v = v + d.n[1] * y;
+  v = v + d.n[2] * z;
+  v = v + d.d;
+  const int s = side_of(v);
+  dist[g] = v;
+  sgn[g] = (int8_t)s;
+  if (s > 0 && S[c].anyPos == 0) atomicOr(&S[c].anyPos, 1u);
+  if (s < 0 && S[c].anyNeg == 0) atomicOr(&S[c].anyNeg, 1u);
+}
+
+// triangles a half gets from one triangle: Sutherland-Hodgman keeps the
+// vertices on the kept side or on the plane and adds one vertex per edge
+// that crosses the plane strictly; the polygon is fanned
+__device__ __forceinline__ uint32_t clip_count(const int s[3], int keep) {
+  int np = 0;
+  for (int k = 0; k < 3; k++) {
+    const int sp = s[k] * keep, sq = s[(k + 1) % 3] * keep;
+    if (sp >= 0) np++;
+    if (s[k] != 0 && s[(k + 1) % 3] != 0 && sp * sq < 0) np++;
+  }
+  return np > 2 ? (uint32_t)(np - 2) : 0u;
+}
+
+// per triangle: (positive half triangles, negative half triangles, positive
+// candidate, negative candidate); a candidate is a triangle whose half
+// triangles have two vertices on the plane (a straddling triangle always,
+// else one with two vertices of side 0)
+__device__ __forceinline__ uint4 tri_counts(const int s[3], bool* straddle) {
+  const bool hasPos = s[0] > 0 || s[1] > 0 || s[2] > 0;
+  const bool hasNeg = s[0] < 0 || s[1] < 0 || s[2] < 0;
+  const int zeros = (s[0] == 0) + (s[1] == 0) + (s[2] == 0);
+  *straddle = hasPos && hasNeg;
+  if (!hasPos && !hasNeg) return make_uint4(0, 0, 0, 0);
+  if (!hasNeg) return make_uint4(1, 0, zeros >= 2 ? 1 : 0, 0);
+  if (!hasPos) return make_uint4(0, 1, 0, zeros >= 2 ? 1 : 0);
+  const uint32_t p = clip_count(s, 1), q = clip_count(s, -1);
+  return make_uint4(p, q, p > 0 ? 1 : 0, q > 0 ? 1 : 0);
+}
+
+__global__ void k_cut_count(const CutDesc* __restrict__ D, const uint32_t* __restrict__ tPre, uint32_t n,
+                            uint32_t totalT, const uint32_t* __restrict__ T, const int8_t* __restrict__ sgn,
+                            uint4* __restrict__ cnt, CutSizes* __restrict__ S) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= totalT) return;
+  const uint32_t c = find_seg(tPre, n, g);
+  const CutDesc& d = D[c];
+  const uint32_t* tri = T + 3 * ((size_t)d.tOff + (g - d.tBase));
+  const int s[3] = {sgn[d.vBase + tri[0]], sgn[d.vBase + tri[1]], sgn[d.vBase + tri[2]]};
+  bool straddle;
+  cnt[g] = tri_counts(s, &straddle);
+  if (straddle) atomicAdd(&S[c].straddle, 1u);
+}
+
+__global__ void k_cut_sizes(const CutDesc* __restrict__ D, uint32_t n, const uint4* __restrict__ pre,
+                            CutSizes* __restrict__ S) {
+  const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  const uint4 a = pre[D[c].tBase], b = pre[D[c].tBase + D[c].nt];
+  S[c].surf[0] = b.x - a.x;
+  S[c].surf[1] = b.y - a.y;
+  S[c].cand[0] = b.z - a.z;
+  S[c].cand[1] = b.w - a.w;
+}
+
+// ---------------------------------------------------------------------------
+// surface: the halves' triangles in input order
+
+// the intersection vertex of edge (lo, hi): its slot in the cut's hash;
+// coordinates p + t (q - p), t = dist[lo] / (dist[lo] - dist[hi])
+__device__ uint32_t isect_slot(unsigned long long* __restrict__ keys, double* __restrict__ xyz, uint32_t hashOff,
+                               uint32_t hashSize, uint32_t lo, uint32_t hi, const double* __restrict__ dist,
+                               const float* __restrict__ V, uint32_t vBase, uint32_t vOff) {
+  const unsigned long long key = ((unsigned long long)lo << 32) | hi;
+  uint32_t h = mix_key(key) & (hashSize - 1);
+  for (uint32_t probe = 0; probe < hashSize; probe++, h = (h + 1) & (hashSize - 1)) {
+    const unsigned long long old = atomicCAS(keys + hashOff + h, EMPTY_KEY, key);
+    if (old == EMPTY_KEY) {
+      const double dl = dist[vBase + lo], dh = dist[vBase + hi];
+      const double t = dl / (dl - dh);
+      const float* P = V + 3 * ((size_t)vOff + lo);
+      const float* Q = V + 3 * ((size_t)vOff + hi);
+      double* o = xyz + 3 * ((size_t)hashOff + h);
+      for (int a = 0; a < 3; a++) {
+        const double pa = P[a], qa = Q[a];
+        o[a] = pa + t * (qa - pa);
+      }
+      return h;
+    }
+    if (old == key) return h;
+  }
+  return CUT_NONE;
+}
+
+__global__ void k_cut_surface(const CutDesc* __restrict__ D, const CutLayout* __restrict__ L,
+                              const uint32_t* __restrict__ tPre, uint32_t n, uint32_t totalT,
+                              const uint32_t* __restrict__ T, const float* __restrict__ V,
+                              const double* __restrict__ dist, const int8_t* __restrict__ sgn,
+                              const uint4* __restrict__ pre, unsigned long long* __restrict__ hashKeys,
+                              double* __restrict__ hashXYZ, uint32_t* __restrict__ surfT, uint2* __restrict__ candE,
+                              CutOut* __restrict__ O) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= totalT) return;
+  const uint32_t c = find_seg(tPre, n, g);
+  const CutLayout& l = L[c];
+  if (!l.active) return;
+  const CutDesc& d = D[c];
+  const uint32_t* tri = T + 3 * ((size_t)d.tOff + (g - d.tBase));
+  const uint32_t ids[3] = {tri[0], tri[1], tri[2]};
+  const int s[3] = {sgn[d.vBase + ids[0]], sgn[d.vBase + ids[1]], sgn[d.vBase + ids[2]]};
+  bool straddle;
+  const uint4 cn = tri_counts(s, &straddle);
+  if (cn.x + cn.y == 0) return;
+  const uint4 P = vsub(pre[g], pre[d.tBase]);  // this triangle's positions within the cut
+  if (!straddle) {
+    const int side = cn.x ? 0 : 1;
+    const uint32_t at = side == 0 ? P.x : P.y;
+    uint32_t* o = surfT + 3 * ((size_t)l.surfOff[side] + at);
+    o[0] = ids[0]; o[1] = ids[1]; o[2] = ids[2];
+    if (side == 0 && cn.z) candE[l.candOff[0] + P.z] = make_uint2(at, 1);
+    if (side == 1 && cn.w) candE[l.candOff[1] + P.w] = make_uint2(at, 1);
+    return;
+  }
+  uint32_t ix[3] = {CUT_NONE, CUT_NONE, CUT_NONE};
+  for (int k = 0; k < 3; k++) {
+    const int k1 = (k + 1) % 3;
+    if (s[k] != 0 && s[k1] != 0 && s[k] * s[k1] < 0) {
+      const uint32_t lo = min(ids[k], ids[k1]), hi = max(ids[k], ids[k1]);
+      const uint32_t h = isect_slot(hashKeys, hashXYZ, l.hashOff, l.hashSize, lo, hi, dist, V, d.vBase, d.vOff);
+      if (h == CUT_NONE) {
+        O[c].fail[0] = CUT_SCRATCH;
+        return;
+      }
+      ix[k] = d.nv + h;
+    }
+  }
+  for (int side = 0; side < 2; side++) {
+    const int keep = side == 0 ? 1 : -1;
+    uint32_t poly[4];
+    int np = 0;
+    for (int k = 0; k < 3; k++) {
+      const int sp = s[k] * keep;
+      if (sp >= 0) poly[np++] = ids[k];
+      if (ix[k] != CUT_NONE) poly[np++] = ix[k];
+    }
+    const uint32_t at = side == 0 ? P.x : P.y;
+    uint32_t* o = surfT + 3 * ((size_t)l.surfOff[side] + at);
+    for (int k = 1; k + 1 < np; k++) {
+      o[3 * (k - 1)] = poly[0];
+      o[3 * (k - 1) + 1] = poly[k];
+      o[3 * (k - 1) + 2] = poly[k + 1];
+    }
+    if (np > 2) candE[l.candOff[side] + (side == 0 ? P.z : P.w)] = make_uint2(at, (uint32_t)(np - 2));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// cap: one warp per (cut, half)
+
+struct CapCtx {
+  const CutDesc* d;
+  uint32_t hashSize, hashOff, nv;
+  const double* hashXYZ;
+  const float* V;
+  // a vertex's coordinates before compaction (an input vertex or an
+  // intersection; centroids are never looked up here)
+  __device__ void pos(uint32_t q, double& x, double& y, double& z) const {
+    if (q < nv) {
+      const float* p = V + 3 * ((size_t)d->vOff + q);
+      x = p[0];
+      y = p[1];
+      z = p[2];
+    } else {
+      const double* p = hashXYZ + 3 * ((size_t)hashOff + (q - nv));
+      x = p[0];
+      y = p[1];
+      z = p[2];
+    }
+  }
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ double orient2(double ax, double ay, double bx, double by, double cx, double cy) {
+  return (bx - ax) * (cy - ay) - (by - ay) * (cx - ax);
+}
+
+__device__ __forceinline__ int dsgn(double x) { return x > 0 ? 1 : (x < 0 ? -1 : 0); }
+
+// hash of 64-bit keys in the word arena: slot of key, inserting it when
+// `insert` (atomic, for the lanes' parallel inserts); CUT_NONE when absent
+__device__ uint32_t kh_find(unsigned long long* keys, uint32_t size, unsigned long long key, bool insert) {
+  uint32_t h = mix_key(key) & (size - 1);
+  for (uint32_t probe = 0; probe < size; probe++, h = (h + 1) & (size - 1)) {
+    unsigned long long k = keys[h];
+    if (k == key) return h;
+    if (k == EMPTY_KEY) {
+      if (!insert) return CUT_NONE;
+      const unsigned long long old = atomicCAS(keys + h, EMPTY_KEY, key);
+      if (old == EMPTY_KEY || old == key) return h;
+    }
+  }
+  return CUT_NONE;
+}
+
+// warp-uniform hash of 32-bit keys (every lane performs the same stores)
+__device__ uint32_t uh_find(uint32_t* keys, uint32_t size, uint32_t key, bool insert, bool* inserted) {
+  uint32_t h = mix_key(key) & (size - 1);
+  *inserted = false;
+  for (uint32_t probe = 0; probe < size; probe++, h = (h + 1) & (size - 1)) {
+    const uint32_t k = keys[h];
+    if (k == key) return h;
+    if (k == CUT_NONE) {
+      if (!insert) return CUT_NONE;
+      keys[h] = key;
+      *inserted = true;
+      return h;
+    }
+  }
+  return CUT_NONE;
+}
+
+struct Ring {  // ear-clip node arrays of one half (warp-uniform)
+  uint32_t *I, *prev, *next, *alive;
+  double *X, *Y;
+  uint32_t n, cap;
+  __device__ int32_t add(uint32_t i, double x, double y, int32_t last) {
+    const uint32_t k = n++;
+    I[k] = i;
+    X[k] = x;
+    Y[k] = y;
+    alive[k] = 1;
+    if (last < 0) {
+      prev[k] = next[k] = k;
+    } else {
+      next[k] = next[last];
+      prev[k] = (uint32_t)last;
+      prev[next[last]] = k;
+      next[last] = k;
+    }
+    return (int32_t)k;
+  }
+  // ring vertices [s, e) of the group, counter-clockwise (ccw) or clockwise
+  __device__ int32_t ring(const uint32_t* gid, const double* gxy, uint32_t s, uint32_t e, bool ccw) {
+    double a = 0;
+    for (uint32_t k = s; k < e; k++) {
+      const uint32_t j = k + 1 < e ? k + 1 : s;
+      a += gxy[2 * k] * gxy[2 * j + 1] - gxy[2 * j] * gxy[2 * k + 1];
+    }
+    int32_t last = -1;
+    if ((a > 0) == ccw) {
+      for (uint32_t k = s; k < e; k++) last = add(k, gxy[2 * k], gxy[2 * k + 1], last);
+    } else {
+      for (uint32_t k = e; k-- > s;) last = add(k, gxy[2 * k], gxy[2 * k + 1], last);
+    }
+    (void)gid;
+    return last;
+  }
+  __device__ void bridge(uint32_t a, uint32_t b) {
+    const uint32_t a2 = n++;
+    I[a2] = I[a]; X[a2] = X[a]; Y[a2] = Y[a]; alive[a2] = 1;
+    const uint32_t b2 = n++;
+    I[b2] = I[b]; X[b2] = X[b]; Y[b2] = Y[b]; alive[b2] = 1;
+    const uint32_t an = next[a], bp = prev[b];
+    next[a] = b;
+    prev[b] = a;
+    next[a2] = an;
+    prev[an] = a2;
+    next[b2] = a2;
+    prev[a2] = b2;
+    next[bp] = b2;
+    prev[b2] = bp;
+  }
+  __device__ bool reflex(uint32_t k) const {
+    return orient2(X[prev[k]], Y[prev[k]], X[k], Y[k], X[next[k]], Y[next[k]]) < 0;
+  }
+};
+
+// an outer vertex visible from hole vertex h (leftmost of its loop), as the
+// host clipper's find_bridge: the nearest crossing of the leftward ray with
+// a downward edge of the counter-clockwise outer loop, its endpoint of larger
+// x, replaced by the reflex vertex of smallest angle inside the triangle
+__device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
+  const double hx = P.X[h], hy = P.Y[h];
+  double qx = -INFINITY;
+  int32_t m = -1;
+  uint32_t p = outer;
+  do {
+    const uint32_t an = P.next[p];
+    const double ax = P.X[p], ay = P.Y[p], bx = P.X[an], by = P.Y[an];
+    if (hy <= ay && hy >= by && by != ay) {
+      const double x = ax + (hy - ay) * (bx - ax) / (by - ay);
+      if (x <= hx && x > qx) {
+        qx = x;
+        if (x == hx) {
+          if (hy == ay) return (int32_t)p;
+          if (hy == by) return (int32_t)an;
+        }
+        m = ax < bx ? (int32_t)an : (int32_t)p;
+      }
+    }
+    p = an;
+  } while (p != outer);
+  if (m < 0) return -1;
+  if (hx == qx) return m;
+  const uint32_t stop = (uint32_t)m;
+  const double mx = P.X[m], my = P.Y[m];
+  double tanMin = INFINITY;
+  p = (uint32_t)m;
+  do {
+    const double cx = P.X[p], cy = P.Y[p];
+    if (hx >= cx && cx >= mx && hx != cx) {
+      const double d1 = orient2(hx, hy, qx, hy, cx, cy), d2 = orient2(qx, hy, mx, my, cx, cy),
+                   d3 = orient2(mx, my, hx, hy, cx, cy);
+      const bool inTri = (d1 >= 0 && d2 >= 0 && d3 >= 0) || (d1 <= 0 && d2 <= 0 && d3 <= 0);
+      if (inTri && P.reflex(p)) {
+        const double tn = fabs(hy - cy) / (hx - cx);
+        if (tn < tanMin || (tn == tanMin && cx > P.X[m])) {
+          m = (int32_t)p;
+          tanMin = tn;
+        }
+      }
+    }
+    p = P.next[p];
+  } while (p != stop);
+  return m;
+}
+
+// no other live node inside (or on) the triangle of ear k; the lanes split
+// the nodes and vote
+__device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
+  const uint32_t a = P.prev[k], b = k, c = P.next[k];
+  const double ax = P.X[a], ay = P.Y[a], bx = P.X[b], by = P.Y[b], cx = P.X[c], cy = P.Y[c];
+  const double ar = orient2(ax, ay, bx, by, cx, cy);
+  if (ar < 0 || (ar == 0 && !allowFlat)) return false;
+  const double lx = fmin(ax, cx), hx = fmax(ax, cx), ly = fmin(ay, cy), hy = fmax(ay, cy);
+  bool hit = false;
+  for (uint32_t q = lane; q < P.n; q += 32) {
+    if (!P.alive[q] || q == a || q == b || q == c) continue;
+    const double qx = P.X[q], qy = P.Y[q];
+    if ((qx == ax && qy == ay) || (qx == bx && qy == by) || (qx == cx && qy == cy)) continue;
+    if (orient2(ax, ay, bx, by, qx, qy) >= 0 && orient2(bx, by, cx, cy, qx, qy) >= 0 &&
+        orient2(cx, cy, ax, ay, qx, qy) >= 0 && (ar > 0 || (qx >= lx && qx <= hx && qy >= ly && qy <= hy)))
+      hit = true;
+  }
+  return !__any_sync(CUT_FULL, hit);
+}
+
+// ear clipping of the group's ring (outer loop [0, outerEnd), holes from
+// holeStart); writes ring-index triples to out; returns the triangle count
+// (fewer than n + 2 h - 2 when the polygon could not be clipped)
+__device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, uint32_t nAll, const uint32_t* hs,
+                             uint32_t nHoles, uint32_t* holeL, double* holeX, uint32_t* out, int lane) {
+  P.n = 0;
+  const uint32_t outerEnd = nHoles == 0 ? nAll : hs[0];
+  if (outerEnd < 3) return 0;
+  const uint32_t outer = (uint32_t)P.ring(gid, gxy, 0, outerEnd, true);
+  uint32_t nh = 0;
+  for (uint32_t k = 0; k < nHoles; k++) {
+    const uint32_t s = hs[k], e = k + 1 < nHoles ? hs[k + 1] : nAll;
+    if (e <= s) continue;
+    const uint32_t h = (uint32_t)P.ring(gid, gxy, s, e, false);
+    uint32_t left = h, p = h;
+    do {
+      if (P.X[p] < P.X[left] || (P.X[p] == P.X[left] && P.Y[p] < P.Y[left])) left = p;
+      p = P.next[p];
+    } while (p != h);
+    // stable insertion by leftmost x
+    uint32_t j = nh;
+    while (j > 0 && holeX[j - 1] > P.X[left]) {
+      holeX[j] = holeX[j - 1];
+      holeL[j] = holeL[j - 1];
+      j--;
+    }
+    holeX[j] = P.X[left];
+    holeL[j] = left;
+    nh++;
+  }
+  for (uint32_t k = 0; k < nh; k++) {
+    const int32_t m = find_bridge(P, holeL[k], outer);
+    if (m < 0) return 0;
+    P.bridge((uint32_t)m, holeL[k]);
+  }
+  uint32_t count = 0;
+  {
+    uint32_t p = outer;
+    do {
+      count++;
+      p = P.next[p];
+    } while (p != outer);
+  }
+  uint32_t nOut = 0;
+  uint32_t ear = outer, stop = outer;
+  bool flat = false;
+  while (count > 3) {
+    if (is_ear(P, ear, flat, lane)) {
+      const uint32_t a = P.prev[ear], c = P.next[ear];
+      out[3 * nOut] = P.I[a];
+      out[3 * nOut + 1] = P.I[ear];
+      out[3 * nOut + 2] = P.I[c];
+      nOut++;
+      P.next[a] = c;
+      P.prev[c] = a;
+      P.alive[ear] = 0;
+      count--;
+      ear = c;
+      stop = c;
+      flat = false;
+      __syncwarp();
+      continue;
+    }
+    ear = P.next[ear];
+    if (ear == stop) {
+      if (flat) return nOut;
+      flat = true;
+    }
+  }
+  const uint32_t a = P.prev[ear], c = P.next[ear];
+  out[3 * nOut] = P.I[a];
+  out[3 * nOut + 1] = P.I[ear];
+  out[3 * nOut + 2] = P.I[c];
+  return nOut + 1;
+}
+
+__global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __restrict__ L, CutOut* __restrict__ O,
+                          uint32_t n, const uint32_t* __restrict__ surfT, const uint2* __restrict__ candE,
+                          const int8_t* __restrict__ sgn, const double* __restrict__ hashXYZ,
+                          const float* __restrict__ V, uint32_t* __restrict__ W, double* __restrict__ X) {
+  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw >= 2 * n) return;
+  const uint32_t c = gw >> 1, side = gw & 1;
+  const CutLayout& l = L[c];
+  if (!l.active || O[c].fail[0] != 0) return;
+  const CutDesc& d = D[c];
+  const uint32_t nCand = l.candCnt[side];
+  if (nCand == 0) return;
+  const uint32_t m = l.mEdge[side], capMax = l.capMax[side];
+  const CapCarve cv = carve(m, capMax);
+  uint32_t* w = W + l.capWord[side];
+  double* x = X + l.capDbl[side];
+  const uint32_t* st = surfT + 3 * (size_t)l.surfOff[side];
+  const uint32_t nv = d.nv;
+  CapCtx ctx{&d, l.hashSize, l.hashOff, nv, hashXYZ, V};
+  const double dir = side == 0 ? -1.0 : 1.0;
+  auto onPlane = [&](uint32_t v) { return v >= nv || sgn[d.vBase + v] == 0; };
+  auto failWith = [&](int code) {
+    if (lane == 0) O[c].fail[side] = code;
+  };
+
+  // 1. the plane edges of the half's candidate triangles, in first-seen
+  // order (candidate order, then triangle, then edge)
+  uint32_t* eA = w + cv.eA;
+  uint32_t* eB = w + cv.eB;
+  uint32_t E = 0;
+  for (uint32_t base = 0; base < nCand; base += 32) {
+    const uint32_t i = base + lane;
+    uint32_t ea[6], eb[6];
+    uint32_t k = 0;
+    if (i < nCand) {
+      const uint2 ce = candE[l.candOff[side] + i];
+      for (uint32_t tt = 0; tt < ce.y && tt < 2; tt++) {
+        const uint32_t* tri = st + 3 * (size_t)(ce.x + tt);
+        for (int e = 0; e < 3; e++) {
+          const uint32_t a = tri[e], b = tri[(e + 1) % 3];
+          if (onPlane(a) && onPlane(b)) {
+            ea[k] = a;
+            eb[k] = b;
+            k++;
+          }
+        }
+      }
+    }
+    uint32_t inc = k;
+    for (int dd = 1; dd < 32; dd <<= 1) {
+      const uint32_t u = __shfl_up_sync(CUT_FULL, inc, dd);
+      if (lane >= dd) inc += u;
+    }
+    const uint32_t tot = __shfl_sync(CUT_FULL, inc, 31);
+    const uint32_t at = E + inc - k;
+    for (uint32_t j = 0; j < k; j++) {
+      if (at + j < m) {
+        eA[at + j] = ea[j];
+        eB[at + j] = eb[j];
+      }
+    }
+    E += tot;
+  }
+  if (E > m) {
+    failWith(CUT_SCRATCH);
+    return;
+  }
+  __syncwarp();
+  // 2. first occurrence of every directed edge and its reverse
+  unsigned long long* ehKey = reinterpret_cast<unsigned long long*>(w + cv.ehKey);
+  uint32_t* ehVal = w + cv.ehVal;
+  for (uint32_t i = lane; i < E; i += 32) {
+    const unsigned long long key = ((unsigned long long)eA[i] << 32) | eB[i];
+    const uint32_t h = kh_find(ehKey, cv.eh, key, true);
+    if (h != CUT_NONE) atomicMin(ehVal + h, i);
+  }
+  __syncwarp();
+  uint32_t* bSrc = w + cv.bSrc;
+  uint32_t* bDst = w + cv.bDst;
+  uint32_t B = 0;
+  for (uint32_t base = 0; base < E; base += 32) {
+    const uint32_t i = base + lane;
+    bool f = false;
+    uint32_t a = 0, b = 0;
+    if (i < E) {
+      a = eA[i];
+      b = eB[i];
+      const uint32_t h = kh_find(ehKey, cv.eh, ((unsigned long long)a << 32) | b, false);
+      const bool first = h != CUT_NONE && ehVal[h] == i;
+      const bool twin = kh_find(ehKey, cv.eh, ((unsigned long long)b << 32) | a, false) != CUT_NONE;
+      f = first && !twin;
+    }
+    const uint32_t bal = __ballot_sync(CUT_FULL, f);
+    if (f) {
+      const uint32_t at = B + __popc(bal & lanemask_lt());
+      bSrc[at] = a;
+      bDst[at] = b;
+    }
+    B += __popc(bal);
+  }
+  __syncwarp();
+  if (B == 0) return;
+
+  // ---- from here on warp-uniform: every lane runs the same sequential
+  // steps on the same data (stores are identical), lanes split only the ear
+  // test and the per-loop work
+
+  // 3. boundary edges grouped by source vertex, in first-seen order
+  uint32_t* bNext = w + cv.bNext;
+  uint32_t* bUsed = w + cv.bUsed;
+  uint32_t* shKey = w + cv.shKey;
+  uint32_t* shHead = w + cv.shHead;
+  uint32_t* shTail = w + cv.shTail;
+  uint32_t* starts = w + cv.starts;
+  uint32_t nStarts = 0;
+  for (uint32_t i = 0; i < B; i++) {
+    bool ins;
+    const uint32_t h = uh_find(shKey, cv.sh, bSrc[i], true, &ins);
+    if (h == CUT_NONE) {
+      failWith(CUT_SCRATCH);
+      return;
+    }
+    bNext[i] = CUT_NONE;
+    bUsed[i] = 0;
+    if (ins) {
+      shHead[h] = i;
+      shTail[h] = i;
+      starts[nStarts++] = bSrc[i];
+    } else {
+      bNext[shTail[h]] = i;
+      shTail[h] = i;
+    }
+  }
+  __syncwarp();
+  // 4. boundary loops: from each start, each unused out-edge in order, then
+  // the first unused out-edge at every vertex
+  uint32_t* loopV = w + cv.loopV;
+  uint32_t* loopS = w + cv.loopS;
+  uint32_t nLoops = 0, nLV = 0;
+  loopS[0] = 0;
+  for (uint32_t si = 0; si < nStarts; si++) {
+    const uint32_t start = starts[si];
+    bool ins;
+    const uint32_t hs = uh_find(shKey, cv.sh, start, false, &ins);
+    for (uint32_t e = shHead[hs]; e != CUT_NONE; e = bNext[e]) {
+      if (bUsed[e]) continue;
+      if (nLV >= m) {
+        failWith(CUT_SCRATCH);
+        return;
+      }
+      const uint32_t lvStart = nLV;
+      loopV[nLV++] = start;
+      bUsed[e] = 1;
+      uint32_t cur = bDst[e];
+      uint32_t guard = 0;
+      while (cur != start) {
+        if (nLV >= m) {
+          failWith(CUT_SCRATCH);
+          return;
+        }
+        loopV[nLV++] = cur;
+        const uint32_t hc = uh_find(shKey, cv.sh, cur, false, &ins);
+        if (hc == CUT_NONE) {
+          failWith(CUT_OPEN_CHAIN);
+          return;
+        }
+        uint32_t nx = CUT_NONE;
+        for (uint32_t e2 = shHead[hc]; e2 != CUT_NONE; e2 = bNext[e2])
+          if (!bUsed[e2]) {
+            nx = e2;
+            break;
+          }
+        if (nx == CUT_NONE) {
+          failWith(CUT_DEAD_END);
+          return;
+        }
+        bUsed[nx] = 1;
+        cur = bDst[nx];
+        if (++guard > B + 1) {
+          failWith(CUT_CYCLE);
+          return;
+        }
+      }
+      if (nLV - lvStart >= 3) loopS[++nLoops] = nLV;
+      else nLV = lvStart;
+    }
+  }
+  __syncwarp();
+  if (nLoops == 0) return;
+  // 5. loop coordinates in the plane's basis and signed areas (a lane per loop)
+  double* l2 = x + cv.l2;
+  double* area = x + cv.area;
+  for (uint32_t li = lane; li < nLoops; li += 32) {
+    const uint32_t s0 = loopS[li], e0 = loopS[li + 1];
+    for (uint32_t k = s0; k < e0; k++) {
+      double px, py, pz;
+      ctx.pos(loopV[k], px, py, pz);
+      double a = px * d.u[0];
+      a = a + py * d.u[1];
+      a = a + pz * d.u[2];
+      double b = px * d.w[0];
+      b = b + py * d.w[1];
+      b = b + pz * d.w[2];
+      l2[2 * k] = a;
+      l2[2 * k + 1] = b;
+    }
+    double s = 0;
+    for (uint32_t k = s0; k < e0; k++) {
+      const uint32_t j = k + 1 < e0 ? k + 1 : s0;
+      s += l2[2 * k] * l2[2 * j + 1] - l2[2 * j] * l2[2 * k + 1];
+    }
+    area[li] = s / 2;
+  }
+  __syncwarp();
+  // outer loops wind like the largest loop
+  int32_t largest = -1;
+  for (uint32_t i = 0; i < nLoops; i++)
+    if (largest < 0 || fabs(area[i]) > fabs(area[largest])) largest = (int32_t)i;
+  const int outerSign = dsgn(area[largest]);
+  // 6. a hole's parent: the smallest larger outer loop containing the hole's
+  // area centroid (a lane per loop)
+  uint32_t* depth = w + cv.depth;
+  uint32_t* parent = w + cv.parent;
+  for (uint32_t i = lane; i < nLoops; i += 32) {
+    depth[i] = 0;
+    parent[i] = CUT_NONE;
+    if (fabs(area[i]) < 1e-18 || dsgn(area[i]) == outerSign) continue;
+    depth[i] = 1;
+    double cx, cy;
+    {
+      const uint32_t s0 = loopS[i], e0 = loopS[i + 1];
+      double sx = 0, sy = 0;
+      for (uint32_t k = s0; k < e0; k++) {
+        const uint32_t j = k + 1 < e0 ? k + 1 : s0;
+        const double wv = l2[2 * k] * l2[2 * j + 1] - l2[2 * j] * l2[2 * k + 1];
+        sx += (l2[2 * k] + l2[2 * j]) * wv;
+        sy += (l2[2 * k + 1] + l2[2 * j + 1]) * wv;
+      }
+      cx = sx / (6 * area[i]);
+      cy = sy / (6 * area[i]);
+    }
+    double bestArea = INFINITY, fallbackArea = -INFINITY;
+    uint32_t fallback = CUT_NONE, par = CUT_NONE;
+    for (uint32_t j = 0; j < nLoops; j++) {
+      if (i == j || fabs(area[j]) < 1e-18 || dsgn(area[j]) != outerSign) continue;
+      if (fabs(area[j]) > fallbackArea) {
+        fallbackArea = fabs(area[j]);
+        fallback = j;
+      }
+      if (fabs(area[j]) <= fabs(area[i])) continue;
+      bool inside = false;
+      const uint32_t s0 = loopS[j], e0 = loopS[j + 1], mm = e0 - s0;
+      for (uint32_t a = 0, b = mm - 1; a < mm; b = a++) {
+        const double xi = l2[2 * (s0 + a)], yi = l2[2 * (s0 + a) + 1], xj = l2[2 * (s0 + b)], yj = l2[2 * (s0 + b) + 1];
+        if ((yi > cy) != (yj > cy) && cx < (xj - xi) * (cy - yi) / (yj - yi) + xi) inside = !inside;
+      }
+      if (inside && fabs(area[j]) < bestArea) {
+        bestArea = fabs(area[j]);
+        par = j;
+      }
+    }
+    parent[i] = par != CUT_NONE ? par : fallback;
+  }
+  __syncwarp();
+  // 7. caps, in the host cut's order: fans of zero-area loops, then each
+  // outer loop with its holes
+  uint32_t* capT = w + cv.capT;
+  double* cent = x + cv.cent;
+  uint32_t nCap = 0, nCent = 0;
+  const uint32_t centBase = nv + l.hashSize;
+  auto fan = [&](uint32_t li) -> bool {
+    const uint32_t s0 = loopS[li], e0 = loopS[li + 1], len = e0 - s0;
+    if (nCap + len > capMax || nCent >= m) return false;
+    double sx = 0, sy = 0, sz = 0;
+    for (uint32_t k = s0; k < e0; k++) {
+      double px, py, pz;
+      ctx.pos(loopV[k], px, py, pz);
+      sx += px;
+      sy += py;
+      sz += pz;
+    }
+    const double dl = (double)len;
+    cent[3 * nCent] = sx / dl;
+    cent[3 * nCent + 1] = sy / dl;
+    cent[3 * nCent + 2] = sz / dl;
+    const uint32_t cid = centBase + nCent++;
+    for (uint32_t k = 0; k < len; k++) {
+      capT[3 * nCap] = cid;
+      capT[3 * nCap + 1] = loopV[s0 + (k + 1) % len];
+      capT[3 * nCap + 2] = loopV[s0 + k];
+      nCap++;
+    }
+    return true;
+  };
+  for (uint32_t i = 0; i < nLoops; i++)
+    if (fabs(area[i]) < 1e-18 && !fan(i)) {
+      failWith(CUT_SCRATCH);
+      return;
+    }
+  Ring P;
+  P.I = w + cv.ndI;
+  P.prev = w + cv.ndPrev;
+  P.next = w + cv.ndNext;
+  P.alive = w + cv.ndAlive;
+  P.X = x + cv.ndX;
+  P.Y = x + cv.ndY;
+  P.cap = cv.nd;
+  P.n = 0;
+  uint32_t* gid = w + cv.gId;
+  double* gxy = x + cv.gXY;
+  uint32_t* holeL = w + cv.holeL;
+  double* holeX = x + cv.holeX;
+  for (uint32_t i = 0; i < nLoops; i++) {
+    if (fabs(area[i]) < 1e-18 || depth[i] % 2 != 0) continue;
+    // the group's ring: the outer loop, then its holes in loop order; the
+    // hole starts go to the end of the depth array's unused tail is not
+    // needed: holeStart values are kept in `parent`-free scratch (starts)
+    uint32_t nAll = 0, nHoles = 0;
+    uint32_t* hs = starts;  // reused: the loop walk is done
+    auto append = [&](uint32_t li) {
+      for (uint32_t k = loopS[li]; k < loopS[li + 1]; k++) {
+        gid[nAll] = loopV[k];
+        gxy[2 * nAll] = l2[2 * k];
+        gxy[2 * nAll + 1] = l2[2 * k + 1];
+        nAll++;
+      }
+    };
+    append(i);
+    for (uint32_t j = 0; j < nLoops; j++)
+      if (parent[j] == i && depth[j] % 2 == 1 && fabs(area[j]) >= 1e-18) {
+        hs[nHoles++] = nAll;
+        append(j);
+      }
+    const uint32_t expected = nAll + 2 * nHoles - 2;
+    if (nCap + nAll + 2 * nHoles > capMax || nAll + 2 * nHoles > P.cap) {
+      failWith(CUT_SCRATCH);
+      return;
+    }
+    __syncwarp();
+    const uint32_t got = ear_clip(P, gid, gxy, nAll, hs, nHoles, holeL, holeX, capT + 3 * nCap, lane);
+    __syncwarp();
+    if (got != expected) {
+      if (!fan(i)) {
+        failWith(CUT_SCRATCH);
+        return;
+      }
+      for (uint32_t j = 0; j < nLoops; j++)
+        if (parent[j] == i && depth[j] % 2 == 1 && fabs(area[j]) >= 1e-18 && !fan(j)) {
+          failWith(CUT_SCRATCH);
+          return;
+        }
+      continue;
+    }
+    // one flip for the whole cap, decided by its largest triangle
+    double bestAbs = 0, bestDot = 0;
+    for (uint32_t k = 0; k < got; k++) {
+      const uint32_t* t = capT + 3 * (nCap + k);
+      double p0x, p0y, p0z, p1x, p1y, p1z, p2x, p2y, p2z;
+      ctx.pos(gid[t[0]], p0x, p0y, p0z);
+      ctx.pos(gid[t[1]], p1x, p1y, p1z);
+      ctx.pos(gid[t[2]], p2x, p2y, p2z);
+      const double ax = p1x - p0x, ay = p1y - p0y, az = p1z - p0z;
+      const double bx = p2x - p0x, by = p2y - p0y, bz = p2z - p0z;
+      const double qx = ay * bz - az * by, qy = az * bx - ax * bz, qz = ax * by - ay * bx;
+      double dd = qx * d.n[0];
+      dd = dd + qy * d.n[1];
+      dd = dd + qz * d.n[2];
+      if (fabs(dd) > bestAbs) {
+        bestAbs = fabs(dd);
+        bestDot = dd;
+      }
+    }
+    const bool flip = bestDot * dir < 0;
+    __syncwarp();
+    for (uint32_t k = 0; k < got; k++) {
+      uint32_t* t = capT + 3 * (nCap + k);
+      const uint32_t a = gid[t[0]], b = gid[t[1]], cc = gid[t[2]];
+      t[0] = a;
+      t[1] = flip ? cc : b;
+      t[2] = flip ? b : cc;
+    }
+    nCap += got;
+    __syncwarp();
+  }
+  if (lane == 0) {
+    O[c].cap[side] = nCap;
+    O[c].cent[side] = nCent;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// compact: vertices numbered by first use in each half's triangle list
+
+struct SideRef {
+  uint32_t c, side, local, tri;
+};
+
+__device__ __forceinline__ SideRef side_of_corner(const uint32_t* cPre, uint32_t n2, uint32_t j) {
+  const uint32_t k = find_seg(cPre, n2, j);
+  SideRef r;
+  r.c = k >> 1;
+  r.side = k & 1;
+  r.local = j - cPre[k];
+  r.tri = r.local / 3;
+  return r;
+}
+
+// the vertex id at a corner of a half, CUT_NONE past the half's triangles
+__device__ __forceinline__ uint32_t corner_id(const CutLayout& l, const CutOut& o, const SideRef& r,
+                                              const uint32_t* surfT, const uint32_t* W) {
+  if (r.tri < l.surfCnt[r.side]) return surfT[3 * (size_t)l.surfOff[r.side] + r.local];
+  const uint32_t ct = r.tri - l.surfCnt[r.side];
+  if (ct >= o.cap[r.side]) return CUT_NONE;
+  const CapCarve cv = carve(l.mEdge[r.side], l.capMax[r.side]);
+  return W[l.capWord[r.side] + cv.capT + 3 * ct + r.local % 3];
+}
+
+__global__ void k_cut_first_use(const CutLayout* __restrict__ L, const CutOut* __restrict__ O,
+                                const uint32_t* __restrict__ cPre, uint32_t n2, uint32_t total,
+                                const uint32_t* __restrict__ surfT, const uint32_t* __restrict__ W,
+                                uint32_t* __restrict__ firstPos) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total) return;
+  const SideRef r = side_of_corner(cPre, n2, j);
+  const CutLayout& l = L[r.c];
+  const CutOut& o = O[r.c];
+  if (!l.active || o.fail[0] || o.fail[1]) return;
+  const uint32_t v = corner_id(l, o, r, surfT, W);
+  if (v == CUT_NONE) return;
+  atomicMin(firstPos + l.preOff[r.side] + v, r.local);
+}
+
+__global__ void k_cut_first_flags(const CutLayout* __restrict__ L, const CutOut* __restrict__ O,
+                                  const uint32_t* __restrict__ cPre, uint32_t n2, uint32_t total,
+                                  const uint32_t* __restrict__ surfT, const uint32_t* __restrict__ W,
+                                  const uint32_t* __restrict__ firstPos, uint32_t* __restrict__ flag) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total) return;
+  const SideRef r = side_of_corner(cPre, n2, j);
+  const CutLayout& l = L[r.c];
+  const CutOut& o = O[r.c];
+  uint32_t f = 0;
+  if (l.active && !o.fail[0] && !o.fail[1]) {
+    const uint32_t v = corner_id(l, o, r, surfT, W);
+    f = v != CUT_NONE && firstPos[l.preOff[r.side] + v] == r.local;
+  }
+  flag[j] = f;
+}
+
+__global__ void k_cut_counts(uint32_t n, const uint32_t* __restrict__ cPre, const uint32_t* __restrict__ fpre,
+                             CutOut* __restrict__ O) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= 2 * n) return;
+  O[k >> 1].nvOut[k & 1] = fpre[cPre[k + 1]] - fpre[cPre[k]];
+}
+
+__global__ void k_cut_write(const CutDesc* __restrict__ D, const CutLayout* __restrict__ L,
+                            const CutOut* __restrict__ O, const uint32_t* __restrict__ cPre, uint32_t n2,
+                            uint32_t total, const uint32_t* __restrict__ surfT, const uint32_t* __restrict__ W,
+                            const double* __restrict__ X, const uint32_t* __restrict__ firstPos,
+                            const uint32_t* __restrict__ fpre, const double* __restrict__ hashXYZ,
+                            const float* __restrict__ V, const unsigned long long* __restrict__ outVOff,
+                            const unsigned long long* __restrict__ outTOff, float* __restrict__ outV,
+                            uint32_t* __restrict__ outT) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= total) return;
+  const SideRef r = side_of_corner(cPre, n2, j);
+  const CutLayout& l = L[r.c];
+  const CutOut& o = O[r.c];
+  if (!l.active || o.fail[0] || o.fail[1]) return;
+  const uint32_t v = corner_id(l, o, r, surfT, W);
+  if (v == CUT_NONE) return;
+  const uint32_t k = 2 * r.c + r.side;
+  const uint32_t fp = firstPos[l.preOff[r.side] + v];
+  const uint32_t idx = fpre[cPre[k] + fp] - fpre[cPre[k]];
+  outT[outTOff[k] + r.local] = idx;
+  if (fp != r.local) return;
+  const CutDesc& d = D[r.c];
+  float* o3 = outV + 3 * (outVOff[k] + idx);
+  if (v < d.nv) {
+    const float* p = V + 3 * ((size_t)d.vOff + v);
+    o3[0] = p[0];
+    o3[1] = p[1];
+    o3[2] = p[2];
+  } else if (v < d.nv + l.hashSize) {
+    const double* p = hashXYZ + 3 * ((size_t)l.hashOff + (v - d.nv));
+    o3[0] = (float)p[0];
+    o3[1] = (float)p[1];
+    o3[2] = (float)p[2];
+  } else {
+    const CapCarve cv = carve(l.mEdge[r.side], l.capMax[r.side]);
+    const double* p = X + l.capDbl[r.side] + cv.cent + 3 * (size_t)(v - d.nv - l.hashSize);
+    o3[0] = (float)p[0];
+    o3[1] = (float)p[1];
+    o3[2] = (float)p[2];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  int ensure(size_t need) {
+    if (need <= bytes) return 0;
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    need = std::max<size_t>(need, 256);
+    if (cudaMalloc(&p, need) != cudaSuccess) return set_error(CUACD_E_CUDA, "cut: device allocation failed");
+    bytes = need;
+    return 0;
+  }
+  template <typename T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+  ~Buf() {
+    if (p) cudaFree(p);
+  }
+};
+
+struct Engine {
+  Buf inV, inT, desc, vPre, tPre, sizes, layout, out, cPre, dist, sgn, cnt, pre, tiles, hashKeys, hashXYZ, surfT,
+      candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::vector<uint8_t> hostScratch;
+};
+
+Halves::~Halves() {
+  if (pinned) cudaFreeHost(pinned);
+}
+
+Engine* engine_create() {
+  Engine* e = new Engine();
+  if (cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
+    delete e;
+    return nullptr;
+  }
+  return e;
+}
+
+void engine_destroy(Engine* e) {
+  if (!e) return;
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  delete e;
+}
+
+#define CUTCK(x)                                                                             \
+  do {                                                                                       \
+    cudaError_t err_ = (x);                                                                  \
+    if (err_ != cudaSuccess) return set_error(CUACD_E_CUDA, (std::string("cut: ") + #x + ": " + \
+                                                             cudaGetErrorString(err_)).c_str()); \
+  } while (0)
+
+template <typename T>
+static int scan(Engine* e, const T* in, uint32_t n, T* out, cudaStream_t s) {
+  const uint32_t nTiles = std::max<uint32_t>(1, (n + SCAN_TILE - 1) / SCAN_TILE);
+  if (int rc = e->tiles.ensure(sizeof(T) * (nTiles + 1))) return rc;
+  T* tiles = e->tiles.as<T>();
+  k_scan_tiles<T><<<nTiles, SCAN_THREADS, 0, s>>>(in, n, tiles);
+  k_scan_tile_starts<T><<<1, 1024, 0, s>>>(tiles, nTiles);
+  k_scan_apply<T><<<nTiles, SCAN_THREADS, 0, s>>>(in, n, tiles, nTiles, out);
+  return 0;
+}
+
+static inline uint32_t blocks(uint64_t n, uint32_t t) { return (uint32_t)std::max<uint64_t>(1, (n + t - 1) / t); }
+
+int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes, const CutSpec* cuts, int nCuts,
+               Halves* out) {
+  if (!e || !out || nCuts < 0 || nMeshes < 0 || (nCuts > 0 && (!meshes || !cuts)))
+    return set_error(CUACD_E_INVALID, "cut: invalid argument");
+  out->status.assign(nCuts, 0);
+  out->vOff.assign(2 * (size_t)nCuts, 0);
+  out->tOff.assign(2 * (size_t)nCuts, 0);
+  out->nv.assign(2 * (size_t)nCuts, 0);
+  out->nt.assign(2 * (size_t)nCuts, 0);
+  out->gpuMs = 0;
+  if (nCuts == 0) return CUACD_OK;
+  // ---- inputs: every mesh once, cut descriptors
+  std::vector<uint64_t> mv(nMeshes + 1, 0), mt(nMeshes + 1, 0);
+  for (int i = 0; i < nMeshes; i++) {
+    const cuacd_mesh& m = meshes[i];
+    if ((m.nv && !m.verts) || (m.nt && !m.tris)) return set_error(CUACD_E_INVALID, "cut: null mesh buffer");
+    for (uint64_t k = 0; k < 3ull * m.nt; k++)
+      if (m.tris[k] >= m.nv) return set_error(CUACD_E_INVALID, "cut: triangle index out of range");
+    mv[i + 1] = mv[i] + m.nv;
+    mt[i + 1] = mt[i] + m.nt;
+  }
+  const uint32_t n = (uint32_t)nCuts;
+  std::vector<CutDesc> desc(n);
+  std::vector<uint32_t> vPre(n + 1, 0), tPre(n + 1, 0);
+  uint64_t totV = 0, totT = 0;
+  for (uint32_t c = 0; c < n; c++) {
+    const CutSpec& cs = cuts[c];
+    if (cs.mesh < 0 || cs.mesh >= nMeshes) return set_error(CUACD_E_INVALID, "cut: mesh index out of range");
+    CutDesc& d = desc[c];
+    std::memset(&d, 0, sizeof(d));
+    for (int a = 0; a < 3; a++) {
+      d.n[a] = cs.n[a];
+      d.u[a] = cs.u[a];
+      d.w[a] = cs.v[a];
+    }
+    d.d = cs.d;
+    d.vOff = (uint32_t)mv[cs.mesh];
+    d.nv = meshes[cs.mesh].nv;
+    d.tOff = (uint32_t)mt[cs.mesh];
+    d.nt = meshes[cs.mesh].nt;
+    d.vBase = (uint32_t)totV;
+    d.tBase = (uint32_t)totT;
+    totV += d.nv;
+    totT += d.nt;
+    vPre[c + 1] = (uint32_t)totV;
+    tPre[c + 1] = (uint32_t)totT;
+  }
+  if (totV >= (1ull << 31) || totT >= (1ull << 30) || mv[nMeshes] >= (1ull << 31))
+    return set_error(CUACD_E_CAPACITY, "cut: batch too large");
+  int rc;
+  if ((rc = e->inV.ensure(12 * mv[nMeshes])) || (rc = e->inT.ensure(12 * mt[nMeshes])) ||
+      (rc = e->desc.ensure(sizeof(CutDesc) * n)) || (rc = e->vPre.ensure(4 * (n + 1))) ||
+      (rc = e->tPre.ensure(4 * (n + 1))) || (rc = e->sizes.ensure(sizeof(CutSizes) * n)) ||
+      (rc = e->layout.ensure(sizeof(CutLayout) * n)) || (rc = e->out.ensure(sizeof(CutOut) * n)) ||
+      (rc = e->dist.ensure(8 * totV)) || (rc = e->sgn.ensure(totV)) || (rc = e->cnt.ensure(16 * totT)) ||
+      (rc = e->pre.ensure(16 * (totT + 1))))
+    return rc;
+  CUTCK(cudaEventRecord(e->ev0, s));
+  for (int i = 0; i < nMeshes; i++) {
+    const cuacd_mesh& m = meshes[i];
+    if (m.nv) CUTCK(cudaMemcpyAsync(e->inV.as<float>() + 3 * mv[i], m.verts, 12ull * m.nv, cudaMemcpyHostToDevice, s));
+    if (m.nt) CUTCK(cudaMemcpyAsync(e->inT.as<uint32_t>() + 3 * mt[i], m.tris, 12ull * m.nt, cudaMemcpyHostToDevice, s));
+  }
+  CUTCK(cudaMemcpyAsync(e->desc.p, desc.data(), sizeof(CutDesc) * n, cudaMemcpyHostToDevice, s));
+  CUTCK(cudaMemcpyAsync(e->vPre.p, vPre.data(), 4 * (n + 1), cudaMemcpyHostToDevice, s));
+  CUTCK(cudaMemcpyAsync(e->tPre.p, tPre.data(), 4 * (n + 1), cudaMemcpyHostToDevice, s));
+  CUTCK(cudaMemsetAsync(e->sizes.p, 0, sizeof(CutSizes) * n, s));
+  const CutDesc* dD = e->desc.as<CutDesc>();
+  CutSizes* dS = e->sizes.as<CutSizes>();
+  if (totV) k_cut_classify<<<blocks(totV, 256), 256, 0, s>>>(dD, e->vPre.as<uint32_t>(), n, (uint32_t)totV,
+                                                               e->inV.as<float>(), e->dist.as<double>(),
+                                                               e->sgn.as<int8_t>(), dS);
+  if (totT) k_cut_count<<<blocks(totT, 256), 256, 0, s>>>(dD, e->tPre.as<uint32_t>(), n, (uint32_t)totT,
+                                                            e->inT.as<uint32_t>(), e->sgn.as<int8_t>(),
+                                                            e->cnt.as<uint4>(), dS);
+  if ((rc = scan<uint4>(e, e->cnt.as<uint4>(), (uint32_t)totT, e->pre.as<uint4>(), s))) return rc;
+  k_cut_sizes<<<blocks(n, 128), 128, 0, s>>>(dD, n, e->pre.as<uint4>(), dS);
+  std::vector<CutSizes> sz(n);
+  CUTCK(cudaMemcpyAsync(sz.data(), dS, sizeof(CutSizes) * n, cudaMemcpyDeviceToHost, s));
+  CUTCK(cudaStreamSynchronize(s));
+
+  // ---- layout
+  std::vector<CutLayout> lay(n);
+  std::vector<CutOut> outRec(n);
+  std::vector<uint32_t> cPre(2 * n + 1, 0);
+  uint64_t hashTot = 0, surfTot = 0, candTot = 0, preTot = 0, corners = 0, wordTot = 0, dblTot = 0;
+  for (uint32_t c = 0; c < n; c++) {
+    CutLayout& l = lay[c];
+    std::memset(&l, 0, sizeof(l));
+    std::memset(&outRec[c], 0, sizeof(CutOut));
+    const bool split = sz[c].anyPos && sz[c].anyNeg;
+    l.active = split ? 1 : 0;
+    if (!split) {
+      out->status[c] = CUT_NO_SPLIT;
+      outRec[c].fail[0] = CUT_NO_SPLIT;
+      cPre[2 * c + 1] = (uint32_t)corners;
+      cPre[2 * c + 2] = (uint32_t)corners;
+      continue;
+    }
+    l.hashSize = pow2_at_least(std::max<uint32_t>(16, 4 * sz[c].straddle));
+    l.hashOff = (uint32_t)hashTot;
+    hashTot += l.hashSize;
+    for (int sd = 0; sd < 2; sd++) {
+      l.surfOff[sd] = (uint32_t)surfTot;
+      l.surfCnt[sd] = sz[c].surf[sd];
+      surfTot += sz[c].surf[sd];
+      l.candOff[sd] = (uint32_t)candTot;
+      l.candCnt[sd] = sz[c].cand[sd];
+      candTot += sz[c].cand[sd];
+      const uint32_t m = 6 * sz[c].cand[sd] + 6;
+      l.mEdge[sd] = m;
+      l.capMax[sd] = 3 * m;
+      l.preOff[sd] = (uint32_t)preTot;
+      preTot += (uint64_t)desc[c].nv + l.hashSize + m;
+      const CapCarve cv = carve(m, l.capMax[sd]);
+      l.capWord[sd] = (uint32_t)wordTot;
+      wordTot += cv.words;
+      l.capDbl[sd] = (uint32_t)dblTot;
+      dblTot += cv.dbls;
+      corners += 3ull * (l.surfCnt[sd] + l.capMax[sd]);
+      cPre[2 * c + sd + 1] = (uint32_t)corners;
+    }
+  }
+  if (corners >= (1ull << 31) || preTot >= (1ull << 31) || wordTot >= (1ull << 32) || dblTot >= (1ull << 31) ||
+      hashTot >= (1ull << 30))
+    return set_error(CUACD_E_CAPACITY, "cut: batch too large");
+  if ((rc = e->hashKeys.ensure(8 * hashTot)) || (rc = e->hashXYZ.ensure(24 * hashTot)) ||
+      (rc = e->surfT.ensure(12 * surfTot)) || (rc = e->candE.ensure(8 * candTot)) ||
+      (rc = e->firstPos.ensure(4 * preTot)) || (rc = e->flag.ensure(4 * corners)) ||
+      (rc = e->fpre.ensure(4 * (corners + 1))) || (rc = e->words.ensure(4 * wordTot)) ||
+      (rc = e->dbls.ensure(8 * dblTot)) || (rc = e->cPre.ensure(4 * (2 * n + 1))) ||
+      (rc = e->outVOff.ensure(8 * 2 * n)) || (rc = e->outTOff.ensure(8 * 2 * n)))
+    return rc;
+  CUTCK(cudaMemcpyAsync(e->layout.p, lay.data(), sizeof(CutLayout) * n, cudaMemcpyHostToDevice, s));
+  CUTCK(cudaMemcpyAsync(e->out.p, outRec.data(), sizeof(CutOut) * n, cudaMemcpyHostToDevice, s));
+  CUTCK(cudaMemcpyAsync(e->cPre.p, cPre.data(), 4 * (2 * n + 1), cudaMemcpyHostToDevice, s));
+  if (hashTot) CUTCK(cudaMemsetAsync(e->hashKeys.p, 0xff, 8 * hashTot, s));
+  if (preTot) CUTCK(cudaMemsetAsync(e->firstPos.p, 0xff, 4 * preTot, s));
+  if (wordTot) CUTCK(cudaMemsetAsync(e->words.p, 0xff, 4 * wordTot, s));
+  const CutLayout* dL = e->layout.as<CutLayout>();
+  CutOut* dO = e->out.as<CutOut>();
+  if (totT)
+    k_cut_surface<<<blocks(totT, 256), 256, 0, s>>>(dD, dL, e->tPre.as<uint32_t>(), n, (uint32_t)totT,
+                                                      e->inT.as<uint32_t>(), e->inV.as<float>(), e->dist.as<double>(),
+                                                      e->sgn.as<int8_t>(), e->pre.as<uint4>(),
+                                                      e->hashKeys.as<unsigned long long>(), e->hashXYZ.as<double>(),
+                                                      e->surfT.as<uint32_t>(), e->candE.as<uint2>(), dO);
+  k_cut_cap<<<blocks(2ull * n * 32, 128), 128, 0, s>>>(dD, dL, dO, n, e->surfT.as<uint32_t>(), e->candE.as<uint2>(),
+                                                       e->sgn.as<int8_t>(), e->hashXYZ.as<double>(),
+                                                       e->inV.as<float>(), e->words.as<uint32_t>(),
+                                                       e->dbls.as<double>());
+  if (corners) {
+    k_cut_first_use<<<blocks(corners, 256), 256, 0, s>>>(dL, dO, e->cPre.as<uint32_t>(), 2 * n, (uint32_t)corners,
+                                                         e->surfT.as<uint32_t>(), e->words.as<uint32_t>(),
+                                                         e->firstPos.as<uint32_t>());
+    k_cut_first_flags<<<blocks(corners, 256), 256, 0, s>>>(dL, dO, e->cPre.as<uint32_t>(), 2 * n, (uint32_t)corners,
+                                                           e->surfT.as<uint32_t>(), e->words.as<uint32_t>(),
+                                                           e->firstPos.as<uint32_t>(), e->flag.as<uint32_t>());
+  }
+  if ((rc = scan<uint32_t>(e, e->flag.as<uint32_t>(), (uint32_t)corners, e->fpre.as<uint32_t>(), s))) return rc;
+  k_cut_counts<<<blocks(2ull * n, 128), 128, 0, s>>>(n, e->cPre.as<uint32_t>(), e->fpre.as<uint32_t>(), dO);
+  CUTCK(cudaMemcpyAsync(outRec.data(), dO, sizeof(CutOut) * n, cudaMemcpyDeviceToHost, s));
+  CUTCK(cudaStreamSynchronize(s));
+
+  // ---- outputs
+  std::vector<unsigned long long> vo(2 * n, 0), to(2 * n, 0);
+  uint64_t outVTot = 0, outTTot = 0;
+  for (uint32_t c = 0; c < n; c++) {
+    const CutOut& o = outRec[c];
+    int st = out->status[c];
+    if (st == 0) st = o.fail[0] ? o.fail[0] : o.fail[1];
+    out->status[c] = st;
+    for (int sd = 0; sd < 2; sd++) {
+      const size_t k = 2 * (size_t)c + sd;
+      vo[k] = outVTot;
+      to[k] = outTTot;
+      if (st != 0) continue;
+      out->nv[k] = o.nvOut[sd];
+      out->nt[k] = lay[c].surfCnt[sd] + o.cap[sd];
+      out->vOff[k] = outVTot;
+      out->tOff[k] = outTTot;
+      outVTot += out->nv[k];
+      outTTot += out->nt[k];
+    }
+  }
+  if ((rc = e->outV.ensure(12 * outVTot)) || (rc = e->outT.ensure(12 * outTTot))) return rc;
+  for (auto& x : to) x *= 3;  // corner offsets
+  CUTCK(cudaMemcpyAsync(e->outVOff.p, vo.data(), 8 * 2 * n, cudaMemcpyHostToDevice, s));
+  CUTCK(cudaMemcpyAsync(e->outTOff.p, to.data(), 8 * 2 * n, cudaMemcpyHostToDevice, s));
+  if (corners)
+    k_cut_write<<<blocks(corners, 256), 256, 0, s>>>(dD, dL, dO, e->cPre.as<uint32_t>(), 2 * n, (uint32_t)corners,
+                                                     e->surfT.as<uint32_t>(), e->words.as<uint32_t>(),
+                                                     e->dbls.as<double>(), e->firstPos.as<uint32_t>(),
+                                                     e->fpre.as<uint32_t>(), e->hashXYZ.as<double>(),
+                                                     e->inV.as<float>(), e->outVOff.as<unsigned long long>(),
+                                                     e->outTOff.as<unsigned long long>(), e->outV.as<float>(),
+                                                     e->outT.as<uint32_t>());
+  CUTCK(cudaGetLastError());
+  const size_t need = 12 * outVTot + 12 * outTTot + 16;
+  if (out->pinnedBytes < need) {
+    if (out->pinned) cudaFreeHost(out->pinned);
+    out->pinned = nullptr;
+    out->pinnedBytes = 0;
+    CUTCK(cudaMallocHost(&out->pinned, need));
+    out->pinnedBytes = need;
+  }
+  out->V = static_cast<float*>(out->pinned);
+  out->T = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(out->pinned) + 12 * outVTot);
+  if (outVTot) CUTCK(cudaMemcpyAsync(out->V, e->outV.p, 12 * outVTot, cudaMemcpyDeviceToHost, s));
+  if (outTTot) CUTCK(cudaMemcpyAsync(out->T, e->outT.p, 12 * outTTot, cudaMemcpyDeviceToHost, s));
+  CUTCK(cudaEventRecord(e->ev1, s));
+  CUTCK(cudaStreamSynchronize(s));
+  cudaEventElapsedTime(&out->gpuMs, e->ev0, e->ev1);
+  return CUACD_OK;
+}
+
+}  // namespace cut
+}  // namespace cuacd

@@ -70,6 +70,15 @@ struct CutResult {
 };
 CutResult plane_cut(const Mesh& m, const Plane& plane, double eps = 1e-6);
 
+// The cut's unit normal n and offset d (the plane divided by the length of
+// its normal, std::hypot) and the orthonormal basis (u, v) of the plane in
+// which its caps are triangulated. The host cut and the GPU cut both take
+// these from here, so both see the same constants.
+struct PlaneFrame {
+  double n[3], d, u[3], v[3];
+};
+PlaneFrame plane_frame(const Plane& plane);
+
 // Triangulates a polygon with holes given as one coordinate ring (outer
 // first, then each hole from holeStart[k]); returns vertex-index triples into
 // the ring. A complete triangulation has n + 2h - 2 triangles; fewer means

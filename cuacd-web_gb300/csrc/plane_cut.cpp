@@ -180,7 +180,8 @@ std::vector<uint32_t> ear_clip(const std::vector<double>& xy, const std::vector<
     } while (p != h);
     holes.push_back({P.n[left].x, left});
   }
-  std::sort(holes.begin(), holes.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
+  // stable, as JavaScript's Array.prototype.sort that earcut relies on
+  std::stable_sort(holes.begin(), holes.end(), [](const auto& a, const auto& b) { return a.first < b.first; });
   for (const auto& hv : holes) {
     const int32_t m = find_bridge(P, hv.second, outer);
     if (m < 0) return out;  // not clippable: the caller falls back
@@ -237,6 +238,8 @@ struct Cap {
   std::vector<uint32_t>& tris;
   double n[3];
   double dir;
+  const double* basis_u;
+  const double* basis_v;
 
   // centroid fan: cap triangle (c, q, p) twins each loop edge p -> q
   void fan(const std::vector<uint32_t>& loop) {
@@ -339,12 +342,8 @@ struct Cap {
     }
     if (loops.empty()) return nullptr;
     // a 2-D basis of the plane
-    const double ax[3] = {std::fabs(n[0]) < 0.9 ? 1.0 : 0.0, std::fabs(n[0]) < 0.9 ? 0.0 : 1.0, 0.0};
-    double u[3] = {ax[1] * n[2] - ax[2] * n[1], ax[2] * n[0] - ax[0] * n[2], ax[0] * n[1] - ax[1] * n[0]};
-    double ul = std::hypot(u[0], u[1], u[2]);
-    if (ul == 0) ul = 1;
-    for (double& x : u) x /= ul;
-    const double v[3] = {n[1] * u[2] - n[2] * u[1], n[2] * u[0] - n[0] * u[2], n[0] * u[1] - n[1] * u[0]};
+    const double* u = basis_u;
+    const double* v = basis_v;
     const size_t L = loops.size();
     std::vector<std::vector<double>> l2(L);
     std::vector<double> area(L);
@@ -479,13 +478,33 @@ Mesh compact(const std::vector<double>& xyz, const std::vector<uint32_t>& tris) 
 
 }  // namespace
 
+PlaneFrame plane_frame(const Plane& pl) {
+  PlaneFrame f;
+  double nlen = std::hypot(pl.a, pl.b, pl.c);
+  if (!(nlen != 0)) nlen = 1;
+  f.n[0] = pl.a / nlen;
+  f.n[1] = pl.b / nlen;
+  f.n[2] = pl.c / nlen;
+  f.d = pl.d / nlen;
+  const double* n = f.n;
+  const double ax[3] = {std::fabs(n[0]) < 0.9 ? 1.0 : 0.0, std::fabs(n[0]) < 0.9 ? 0.0 : 1.0, 0.0};
+  double u[3] = {ax[1] * n[2] - ax[2] * n[1], ax[2] * n[0] - ax[0] * n[2], ax[0] * n[1] - ax[1] * n[0]};
+  double ul = std::hypot(u[0], u[1], u[2]);
+  if (ul == 0) ul = 1;
+  for (double& x : u) x /= ul;
+  for (int a = 0; a < 3; a++) f.u[a] = u[a];
+  f.v[0] = n[1] * u[2] - n[2] * u[1];
+  f.v[1] = n[2] * u[0] - n[0] * u[2];
+  f.v[2] = n[0] * u[1] - n[1] * u[0];
+  return f;
+}
+
 CutResult plane_cut(const Mesh& m, const Plane& pl, double eps) {
   CutResult r;
   const size_t nv = m.nv(), nt = m.nt();
-  double nlen = std::hypot(pl.a, pl.b, pl.c);
-  if (!(nlen != 0)) nlen = 1;
-  const double n[3] = {pl.a / nlen, pl.b / nlen, pl.c / nlen};
-  const double dd = pl.d / nlen;
+  const PlaneFrame fr = plane_frame(pl);
+  const double* n = fr.n;
+  const double dd = fr.d;
   const float* V = m.v.data();
   std::vector<double> dist(nv);
   std::vector<int8_t> sign(nv);
@@ -550,12 +569,12 @@ CutResult plane_cut(const Mesh& m, const Plane& pl, double eps) {
       clip(neg, -1, ids);
     }
   }
-  Cap cp{xyz, pos, {n[0], n[1], n[2]}, -1.0};
+  Cap cp{xyz, pos, {n[0], n[1], n[2]}, -1.0, fr.u, fr.v};
   if (const char* why = cp.run()) {
     r.reason = why;
     return r;
   }
-  Cap cn{xyz, neg, {n[0], n[1], n[2]}, 1.0};
+  Cap cn{xyz, neg, {n[0], n[1], n[2]}, 1.0, fr.u, fr.v};
   if (const char* why = cn.run()) {
     r.reason = why;
     return r;

@@ -72,6 +72,13 @@ def load_library():
         getattr(L, f).argtypes = [C.c_void_p, C.c_uint32, C.c_uint32, P(C.c_uint32)]
     L.cuacd_tree_read_part_geometry.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float), P(C.c_uint32), P(C.c_uint32)]
     L.cuacd_tree_read_plane.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float)]
+    L.cuacd_tree_plane_cuts.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, P(C.c_int32), P(C.c_double), C.c_int,
+                                        P(C.c_void_p)]
+    L.cuacd_cuts_half.argtypes = [C.c_void_p, C.c_int, C.c_int, P(P(C.c_float)), P(C.c_uint32), P(P(C.c_uint32)),
+                                  P(C.c_uint32)]
+    L.cuacd_cuts_gpu_ms.restype = C.c_float
+    L.cuacd_cuts_gpu_ms.argtypes = [C.c_void_p]
+    L.cuacd_cuts_free.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -256,6 +263,46 @@ class GpuTree:
         return out
 
     # ---- debug readers (tree.ts:764-807) ----
+    def plane_cuts(self, meshes, planes, mesh_of_cut=None):
+        """planeCut (src/cpu/cut.ts:33-315) on the GPU: cut k cuts
+        meshes[mesh_of_cut[k]] (mesh k when None) by planes[k] = (a, b, c, d).
+        Returns one (status, positive half, negative half) per cut; status 0
+        or the cut's failure code (the halves are then None). The halves are
+        the host cut's bit for bit. The device time is last_cut_ms."""
+        L = load_library()
+        pl = np.ascontiguousarray(np.asarray(planes, np.float64).reshape(-1, 4))
+        n = pl.shape[0]
+        idx = np.arange(n, dtype=np.int32) if mesh_of_cut is None else np.ascontiguousarray(mesh_of_cut, np.int32)
+        if idx.shape[0] != n:
+            raise ValueError("one mesh index per plane")
+        ma = A.MeshArray([A.as_mesh(m) for m in meshes])
+        h = C.c_void_p()
+        _check(L.cuacd_tree_plane_cuts(self.h, ma.arr, len(meshes), _int32p(idx),
+                                       pl.ctypes.data_as(C.POINTER(C.c_double)), n, C.byref(h)))
+        out = []
+        try:
+            self.last_cut_ms = float(L.cuacd_cuts_gpu_ms(h))
+            for k in range(n):
+                halves = []
+                st = 0
+                for side in (0, 1):
+                    v = C.POINTER(C.c_float)()
+                    t = C.POINTER(C.c_uint32)()
+                    nv = C.c_uint32()
+                    nt = C.c_uint32()
+                    st = L.cuacd_cuts_half(h, k, side, C.byref(v), C.byref(nv), C.byref(t), C.byref(nt))
+                    if st < 0:
+                        _check(st)
+                    if st != 0:
+                        break
+                    vv = np.ctypeslib.as_array(v, shape=(nv.value * 3,)).copy() if nv.value else np.zeros(0, np.float32)
+                    tt = np.ctypeslib.as_array(t, shape=(nt.value * 3,)).copy() if nt.value else np.zeros(0, np.uint32)
+                    halves.append(Mesh(vv.reshape(-1, 3), tt.reshape(-1, 3)))
+                out.append((st, halves[0], halves[1]) if st == 0 else (st, None, None))
+        finally:
+            L.cuacd_cuts_free(h)
+        return out
+
     def items(self, first, n):
         w = np.zeros(20 * n, np.uint32)
         _check(load_library().cuacd_tree_read_items(self.h, first, n, A.uptr(w)))

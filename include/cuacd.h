@@ -229,6 +229,26 @@ int cuacd_tree_read_plane(void* tree, uint32_t index, float* out4);
 int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint32_t* tris, uint32_t trisCap, float* volume,
                               uint32_t* ntris, int32_t* status, void* stream);
 
+/* planeCut (src/cpu/cut.ts:33-315) of nCuts (mesh, plane) pairs on the GPU,
+ * on the tree handle's stream: cut k cuts meshes[meshOfCut[k]] by planes[4k
+ * .. 4k + 3] (a x + b y + c z + d = 0). The halves are the host cut's
+ * (cuacd_plane_cut) bit for bit: the same vertices in the same order, the
+ * same triangles, caps and failures. The meshes must be closed (every
+ * directed edge once and its reverse once), as the decomposer's parts are.
+ * On success *halves receives a handle read with cuacd_cuts_half. */
+int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, const int32_t* meshOfCut,
+                          const double* planes, int nCuts, void** halves);
+/* Half `side` (0 positive, 1 negative) of cut `cut`: returns 0 with the
+ * half's arrays (valid until cuacd_cuts_free), or the cut's failure: 1 the
+ * plane does not split the mesh, 2 open boundary chain, 3 boundary chain dead
+ * end, 4 boundary chain cycle (the reasons cut.ts throws), 5 an internal
+ * scratch bound was exceeded; or a negative error. */
+int cuacd_cuts_half(const void* halves, int cut, int side, const float** verts, uint32_t* nv, const uint32_t** tris,
+                    uint32_t* nt);
+/* Device time of the batch (uploads, kernels and the readback), in ms. */
+float cuacd_cuts_gpu_ms(const void* halves);
+void cuacd_cuts_free(void* halves);
+
 /* ---- decomposition (src/decompose.ts, src/merge.ts) -------------------- */
 
 /* DecomposeOptions (decompose.ts:26-78) with DEFAULT_OPTIONS (decompose.ts:

@@ -1,0 +1,153 @@
+"""The capped plane cut on the GPU (cuacd_tree_plane_cuts, csrc/cut_kernels.cu)
+against the host cut (cuacd_plane_cut, csrc/plane_cut.cpp) and the oracle's
+restatement of src/cpu/cut.ts.
+
+GPU against host: bit for bit — every half's vertex array (positions and
+order) and triangle array, and every failure (a plane that does not split
+the mesh fails both). GPU against the oracle: the halves' vertices are the
+oracle's (same positions in the same order, up to a cap fan centroid on the
+cut plane that one ear clipper adds where the other clips), volumes agree to
+1e-6 relative, both halves are closed. Cap triangles are not compared with
+the oracle: the reference triangulates caps with earcut@3.0.1, absent here,
+so exact cap triangles are unpinned (closedness, volume and the n + 2h - 2
+count are what the reference pins).
+"""
+import zlib
+
+import numpy as np
+import pytest
+
+from conftest import pkg
+from fixtures import M, l_prism, square_torus, stairs
+
+pytestmark = pytest.mark.gpu
+
+D = pkg("decompose")
+G = pkg("meshgen")
+T = pkg("tree")
+
+
+def _tree():
+    return T.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0)
+
+
+def _planes(m, n, seed):
+    rng = np.random.default_rng(seed)
+    v = m.verts.astype(np.float64)
+    lo, hi = v.min(0), v.max(0)
+    out = [[1, 0, 0, -(lo[0] + hi[0]) / 2], [0, 1, 0, -(lo[1] + hi[1]) / 2], [0, 0, 1, -(lo[2] + hi[2]) / 2]]
+    for _ in range(n):
+        nrm = rng.normal(size=3)
+        nrm /= np.linalg.norm(nrm)
+        p = lo + rng.uniform(0.2, 0.8, 3) * (hi - lo)
+        out.append([nrm[0], nrm[1], nrm[2], -float(nrm @ p)])
+    return out
+
+
+def _meshes():
+    return [("cube", M.unit_cube()), ("l_shape", M.l_shape()), ("torus", square_torus()), ("stairs", stairs()),
+            ("l_prism", l_prism()), ("staircase8", G.staircase(8)),
+            ("staircase8_188", G.staircase(8, wall_centroids=True)), ("ico3", G.noisy_icosphere(3, seed=1)),
+            ("ico4", G.noisy_icosphere(4, seed=0)),
+            # marching-tetrahedra surfaces: vertices on shared grid lines and planes
+            ("blob", M.normalize(G.blob_mesh(6, 26, seed=3))[0]),
+            ("blob_big", M.normalize(G.blob_mesh(12, 48, seed=5))[0]),
+            ("carved", G.carved_sphere(3, 3, seed=2))]
+
+
+def _host_cut(mesh, pl):
+    try:
+        return D.plane_cut(mesh, pl)
+    except T.CuacdError:
+        return None
+
+
+def _same(a, b):
+    return (np.array_equal(a.verts.view(np.uint32), b.verts.view(np.uint32)) and a.tris.shape == b.tris.shape
+            and np.array_equal(a.tris, b.tris))
+
+
+def test_gpu_cut_matches_host_cut_bit_for_bit():
+    g = _tree()
+    meshes = _meshes()
+    planes, idx, names = [], [], []
+    for k, (name, m) in enumerate(meshes):
+        for pl in _planes(m, 10, zlib.crc32(name.encode())):
+            planes.append(pl)
+            idx.append(k)
+            names.append(name)
+        # a plane through vertices (on-plane vertices on both halves), and
+        # planes beside the mesh (no split)
+        v = m.verts.astype(np.float64)
+        planes += [[0, 0, 1, -float(v[0, 2])], [1, 0, 0, -float(v[:, 0].max()) - 1.0],
+                   [0, 1, 0, -float(v[:, 1].min())]]
+        idx += [k, k, k]
+        names += [name] * 3
+    got = g.plane_cuts([m for _, m in meshes], planes, idx)
+    n_ok = n_fail = 0
+    for (st, pos, neg), pl, k, name in zip(got, planes, idx, names):
+        ref = _host_cut(meshes[k][1], pl)
+        assert (ref is None) == (st != 0), (name, pl, st)
+        if ref is None:
+            n_fail += 1
+            continue
+        n_ok += 1
+        assert _same(pos, ref[0]) and _same(neg, ref[1]), (name, pl)
+    assert n_ok > 100 and n_fail >= len(meshes)
+
+
+def test_gpu_cut_config1_icosphere_96_planes(oracle):
+    # the icosphere configuration: level 4 (2,562 vertices, 5,120 triangles),
+    # radial noise, 96 seeded planes, one batch
+    m = G.noisy_icosphere(4, noise=0.15, seed=0)
+    planes = G.random_planes(m, 96, seed=0).astype(np.float64)
+    got = _tree().plane_cuts([m], planes, np.zeros(96, np.int32))
+    for (st, pos, neg), pl in zip(got, planes):
+        ref = _host_cut(m, pl)
+        assert (ref is None) == (st != 0)
+        if ref is None:
+            continue
+        assert _same(pos, ref[0]) and _same(neg, ref[1])
+        orc = oracle.plane_cut(m, pl)
+        for r, h in zip(orc, (pos, neg)):
+            rv = np.asarray(r.verts, np.float32).reshape(-1, 3)
+            n = min(len(rv), len(h.verts))
+            assert np.array_equal(rv[:n], h.verts[:n])
+            assert M.is_closed(h)
+            vr, vg = M.signed_volume(r), M.signed_volume(h)
+            assert abs(vr - vg) <= 1e-6 * abs(vr) + 1e-9
+
+
+@pytest.mark.parametrize("name,mesh", _meshes())
+def test_gpu_cut_matches_oracle(oracle, name, mesh):
+    planes = _planes(mesh, 8, zlib.crc32(name.encode()) + 1)
+    got = _tree().plane_cuts([mesh], planes, np.zeros(len(planes), np.int32))
+    for (st, pos, neg), pl in zip(got, planes):
+        ref = oracle.plane_cut(mesh, pl)
+        assert (ref is None) == (st != 0), (name, pl)
+        if ref is None:
+            continue
+        for r, h in zip(ref, (pos, neg)):
+            rv = np.asarray(r.verts, np.float32).reshape(-1, 3)
+            n = min(len(rv), len(h.verts))
+            assert np.array_equal(rv[:n], h.verts[:n]), (name, pl)
+            extra = np.concatenate([rv[n:], h.verts[n:]]).astype(np.float64)
+            nrm = np.asarray(pl[:3], np.float64)
+            assert np.all(np.abs(extra @ nrm + pl[3]) <= 1e-5 * np.linalg.norm(nrm)), (name, pl)
+            assert M.is_closed(h), (name, pl)
+            vr, vg = M.signed_volume(r), M.signed_volume(h)
+            assert abs(vr - vg) <= 1e-6 * abs(vr) + 1e-9, (name, pl, vr, vg)
+
+
+def test_gpu_cut_reference_cases():
+    # tests/cpu.test.ts:18-56 through the GPU cut: cube halves, the L at its
+    # junction, the torus through its hole (an annulus cap: one hole)
+    g = _tree()
+    cube, ell, tor = M.unit_cube(), M.l_shape(), square_torus()
+    got = g.plane_cuts([cube, ell, tor], [[1, 0, 0, -0.5], [1, 0, 0, -1], [1, 0, 0, -1], [0, 0, 1, 0]], [0, 0, 1, 2])
+    (s0, p0, n0), (s1, _, _), (s2, p2, n2), (s3, p3, n3) = got
+    assert s0 == 0 and abs(M.volume(p0) - 0.5) < 1e-6 and abs(M.volume(n0) - 0.5) < 1e-6
+    assert s1 == 1  # the plane does not split the cube
+    assert s2 == 0 and abs(M.volume(p2) - 0.5) < 1e-6 and abs(M.volume(n2) - 1) < 1e-6
+    assert s3 == 0 and M.is_closed(p3) and M.is_closed(n3)
+    assert abs(M.volume(p3) - 0.75) < 1e-6 and p3.nv == 24 and p3.nt == 32 + 16
