@@ -363,11 +363,69 @@ def run_engine(args):
         line["cpu_baseline"] = {"value": c / s, "unit": UNIT, "cores": nthr, "kind": "port",
                                 "sample": f"{sample} staircase seeds, one tree run with {REFINE_ROUNDS} refinement "
                                           f"rounds on the oracle's CPU restatement ({c} candidates, {s:.1f} s)"}
+    if world == 1 and not args.no_cpu_baseline:
+        # the icosphere configuration against the reference's CPU helpers
+        line["cpu_helpers"] = cut_eval_measure()
     if world == 1 and not args.no_decompose:
         # the metric's second half: whole decompositions per second, the
         # uneven batch decomposed together against one mesh at a time
         line["decompose"] = decompose_measure(args.meshes)
     print(json.dumps(line), flush=True)
+
+
+def cut_eval_measure(steps=5, warmup=2):
+    """The icosphere configuration: a level-4 icosphere (2,562 vertices,
+    5,120 triangles) with radial noise U[-0.15, 0.15] of the radius,
+    normalised to the unit cube, cut by 96 seeded planes; every half gets a
+    capped cut, an exact hull, its volumes and rv cost and its sampled
+    Hausdorff distance to its hull. On the GPU through the public call
+    cuacd_tree_eval_cuts (mesh and planes from host memory, results back to
+    host memory, in the timed region); beside it the oracle's restatement of
+    the reference's CPU helpers on 1 host thread and on every host thread."""
+    import numpy as np
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+
+    gen = importlib.import_module("cuacd-web_gb300.meshgen")
+    tree_mod = importlib.import_module("cuacd-web_gb300.tree")
+    m = gen.noisy_icosphere(4, noise=0.15, seed=0)
+    planes = gen.random_planes(m, 96, seed=0).astype(np.float64)
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096, scratchWords=64 << 20)
+    for _ in range(warmup):
+        g.eval_cuts(m, planes)
+    wall, dev = [], []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        got = g.eval_cuts(m, planes)
+        wall.append(time.perf_counter() - t0)
+        dev.append(g.last_eval_ms / 1000.0)
+    g.destroy()
+    harness.lib()
+    nthr = host_threads()
+    t0 = time.perf_counter()
+    ref = harness.eval_candidates(m, planes, threads=1, with_hd=True, use_ref=False)
+    t1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    harness.eval_candidates(m, planes, threads=nthr, with_hd=True, use_ref=False)
+    tn = time.perf_counter() - t0
+    ok = (got[:, 0] == 1) & (ref[:, 0] == 1)
+    rel = lambda a, b: float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-12))) if a.size else 0.0  # noqa: E731
+    hd_err = np.abs(got[ok, 7] - ref[ok, 7]) / (1e-4 + 1e-3 * ref[ok, 7])
+    n = len(planes)
+    return {"metric": "cut candidates evaluated/s (capped cut, hull, volumes, rv, Hausdorff per half)",
+            "workload": "noisy icosphere L4 (2,562 verts, 5,120 tris) x 96 seeded planes, samples "
+                        "max(1000, floor(2000 area)) per mesh side",
+            "gpu": {"value": n / statistics.median(dev), "unit": "candidates/s", "ms": 1000 * statistics.median(dev)},
+            "gpu_e2e": {"value": n / statistics.median(wall), "unit": "candidates/s",
+                        "ms": 1000 * statistics.median(wall), "h2d_bytes_per_step": m.verts.nbytes + m.tris.nbytes + planes.nbytes,
+                        "d2h_bytes_per_step": got.nbytes},
+            "cpu_1thread": {"value": n / t1, "unit": "candidates/s", "cores": 1, "kind": "port", "ms": 1000 * t1},
+            "cpu_all_threads": {"value": n / tn, "unit": "candidates/s", "cores": nthr, "kind": "port", "ms": 1000 * tn},
+            "match": {"split_equal": bool(np.array_equal(got[:, 0], ref[:, 0])), "splits": int(ok.sum()),
+                      "max_rel_volume": rel(got[ok, 1:3], ref[ok, 1:3]), "max_rel_hull": rel(got[ok, 3:5], ref[ok, 3:5]),
+                      "max_abs_rv": float(np.max(np.abs(got[ok, 5:7] - ref[ok, 5:7]))) if ok.any() else 0.0,
+                      "max_hausdorff_err_over_tolerance": float(hd_err.max()) if ok.any() else 0.0}}
 
 
 def sample_counts(m):

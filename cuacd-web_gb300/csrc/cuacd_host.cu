@@ -148,6 +148,7 @@ struct Tree {
   bool gvalid = false;
 
   cut::Engine* cutter = nullptr;  // the GPU capped cut, created on first use
+  float lastEvalMs = 0.0f;        // device time of the last cuacd_tree_eval_cuts
 
   ~Tree() {
     if (cutter) cut::engine_destroy(cutter);
@@ -856,6 +857,66 @@ int cuacd_cuts_half(const void* halves, int cut, int side, const float** verts, 
   if (nt) *nt = st == 0 ? h->nt[k] : 0;
   return st;
 }
+
+int cuacd_tree_eval_cuts(void* tree, const cuacd_mesh* mesh, const double* planes, int n, double* out8) {
+  Tree* t = (Tree*)tree;
+  if (!t || !mesh || n < 0 || (n > 0 && (!planes || !out8))) return fail(CUACD_E_INVALID, "cuacd_tree_eval_cuts: invalid argument");
+  if (n == 0) return CUACD_OK;
+  std::memset(out8, 0, 8 * sizeof(double) * (size_t)n);
+  std::vector<int32_t> which((size_t)n, 0);
+  void* hv = nullptr;
+  int rc = cuacd_tree_plane_cuts(tree, mesh, 1, which.data(), planes, n, &hv);
+  if (rc != CUACD_OK) return rc;
+  cut::Halves* h = (cut::Halves*)hv;
+  float ms = h->gpuMs;
+  // every half of every cut that split, hulled with its Hausdorff distance
+  std::vector<cuacd_mesh> halves;
+  std::vector<int> owner;
+  for (int k = 0; k < n; k++) {
+    if (h->status[k] != 0) continue;
+    for (int sd = 0; sd < 2; sd++) {
+      const size_t i = 2 * (size_t)k + sd;
+      halves.push_back(cuacd_mesh{h->V + 3 * h->vOff[i], h->T + 3 * h->tOff[i], h->nv[i], h->nt[i]});
+      owner.push_back(2 * k + sd);
+    }
+  }
+  const size_t nh = halves.size();
+  std::vector<float> vol(nh), hd(nh);
+  std::vector<uint32_t> nt(nh);
+  std::vector<int32_t> st(nh);
+  size_t batch = std::min<size_t>(nh, CUACD_HD_MAX_PAIRS);
+  for (size_t s0 = 0; s0 < nh;) {
+    const size_t m = std::min(batch, nh - s0);
+    rc = t->hulls(halves.data() + s0, (int)m, 0, nullptr, 0, vol.data() + s0, nt.data() + s0, st.data() + s0,
+                  hd.data() + s0);
+    if (rc == CUACD_E_SCRATCH && m > 1) {  // halve the batch, as merge.ts:405 does
+      batch = std::max<size_t>(1, m / 2);
+      continue;
+    }
+    if (rc != CUACD_OK) {
+      cuacd_cuts_free(hv);
+      return rc;
+    }
+    ms += cuacd_tree_last_gpu_ms(tree);
+    s0 += m;
+  }
+  for (size_t i = 0; i < nh; i++) {
+    const int k = owner[i] / 2, sd = owner[i] % 2;
+    double* o = out8 + 8 * (size_t)k;
+    const double mv = std::fabs(h->vol[(size_t)owner[i]]);
+    const double hvol = st[i] == 0 ? (double)vol[i] : 0.0;
+    o[0] = 1;
+    o[1 + sd] = mv;
+    o[3 + sd] = hvol;
+    o[5 + sd] = 0.3 * std::cbrt((3.0 / (4.0 * M_PI)) * std::max(hvol - mv, 0.0));
+    if (st[i] == 0) o[7] = std::max(o[7], (double)hd[i]);
+  }
+  t->lastEvalMs = ms;
+  cuacd_cuts_free(hv);
+  return CUACD_OK;
+}
+
+float cuacd_tree_eval_cuts_ms(void* tree) { return tree ? ((Tree*)tree)->lastEvalMs : 0.0f; }
 
 float cuacd_cuts_gpu_ms(const void* halves) { return halves ? ((const cut::Halves*)halves)->gpuMs : 0.0f; }
 

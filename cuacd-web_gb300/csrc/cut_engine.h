@@ -28,6 +28,7 @@ struct Halves {
   std::vector<int32_t> status;
   std::vector<uint64_t> vOff, tOff;
   std::vector<uint32_t> nv, nt;
+  std::vector<double> vol;  // signed volume of each half (a fixed-order parallel sum)
   float* V = nullptr;
   uint32_t* T = nullptr;
   float gpuMs = 0.0f;

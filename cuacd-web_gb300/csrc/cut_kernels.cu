@@ -1242,6 +1242,35 @@ __global__ void k_cut_write(const CutDesc* __restrict__ D, const CutLayout* __re
   }
 }
 
+// signed volume of every half by the divergence theorem anchored at its
+// vertex 0 (mesh.ts:58-72): one warp per half, each lane sums its strided
+// triangles in order, then a fixed-order tree across the lanes (the same
+// value on every run; it differs from a sequential sum in the last bits)
+__global__ void k_cut_volume(uint32_t n2, const unsigned long long* __restrict__ vOff,
+                             const unsigned long long* __restrict__ tOff, const uint32_t* __restrict__ halfNt,
+                             const float* __restrict__ outV, const uint32_t* __restrict__ outT,
+                             double* __restrict__ vol) {
+  const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (k >= n2) return;
+  const uint32_t nt = halfNt[k];
+  const float* v = outV + 3 * vOff[k];
+  const uint32_t* t = outT + tOff[k];
+  double s = 0.0;
+  if (nt > 0) {
+    const double ox = v[0], oy = v[1], oz = v[2];
+    for (uint32_t i = lane; i < nt; i += 32) {
+      const uint32_t a = 3 * t[3 * i], b = 3 * t[3 * i + 1], c = 3 * t[3 * i + 2];
+      const double ax = v[a] - ox, ay = v[a + 1] - oy, az = v[a + 2] - oz;
+      const double bx = v[b] - ox, by = v[b + 1] - oy, bz = v[b + 2] - oz;
+      const double cx = v[c] - ox, cy = v[c + 1] - oy, cz = v[c + 2] - oz;
+      s += ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
+    }
+  }
+  for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(CUT_FULL, s, d);
+  if (lane == 0) vol[k] = s / 6.0;
+}
+
 // ---------------------------------------------------------------------------
 // host side
 
@@ -1269,7 +1298,7 @@ struct Buf {
 
 struct Engine {
   Buf inV, inT, desc, vPre, tPre, sizes, layout, out, cPre, dist, sgn, cnt, pre, tiles, hashKeys, hashXYZ, surfT,
-      candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT;
+      candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT, halfNt, vol;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<uint8_t> hostScratch;
 };
@@ -1499,8 +1528,11 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
       outTTot += out->nt[k];
     }
   }
-  if ((rc = e->outV.ensure(12 * outVTot)) || (rc = e->outT.ensure(12 * outTTot))) return rc;
+  if ((rc = e->outV.ensure(12 * outVTot)) || (rc = e->outT.ensure(12 * outTTot)) ||
+      (rc = e->halfNt.ensure(4 * 2 * n)) || (rc = e->vol.ensure(8 * 2 * n)))
+    return rc;
   for (auto& x : to) x *= 3;  // corner offsets
+  CUTCK(cudaMemcpyAsync(e->halfNt.p, out->nt.data(), 4 * 2 * n, cudaMemcpyHostToDevice, s));
   CUTCK(cudaMemcpyAsync(e->outVOff.p, vo.data(), 8 * 2 * n, cudaMemcpyHostToDevice, s));
   CUTCK(cudaMemcpyAsync(e->outTOff.p, to.data(), 8 * 2 * n, cudaMemcpyHostToDevice, s));
   if (corners)
@@ -1511,7 +1543,13 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
                                                      e->inV.as<float>(), e->outVOff.as<unsigned long long>(),
                                                      e->outTOff.as<unsigned long long>(), e->outV.as<float>(),
                                                      e->outT.as<uint32_t>());
+  k_cut_volume<<<blocks(2ull * n * 32, 128), 128, 0, s>>>(2 * n, e->outVOff.as<unsigned long long>(),
+                                                          e->outTOff.as<unsigned long long>(), e->halfNt.as<uint32_t>(),
+                                                          e->outV.as<float>(), e->outT.as<uint32_t>(),
+                                                          e->vol.as<double>());
   CUTCK(cudaGetLastError());
+  out->vol.assign(2 * (size_t)n, 0.0);
+  CUTCK(cudaMemcpyAsync(out->vol.data(), e->vol.p, 8 * 2 * n, cudaMemcpyDeviceToHost, s));
   const size_t need = 12 * outVTot + 12 * outTTot + 16;
   if (out->pinnedBytes < need) {
     if (out->pinned) cudaFreeHost(out->pinned);

@@ -79,6 +79,9 @@ def load_library():
     L.cuacd_cuts_gpu_ms.restype = C.c_float
     L.cuacd_cuts_gpu_ms.argtypes = [C.c_void_p]
     L.cuacd_cuts_free.argtypes = [C.c_void_p]
+    L.cuacd_tree_eval_cuts.argtypes = [C.c_void_p, P(A.MeshRef), P(C.c_double), C.c_int, P(C.c_double)]
+    L.cuacd_tree_eval_cuts_ms.restype = C.c_float
+    L.cuacd_tree_eval_cuts_ms.argtypes = [C.c_void_p]
     _lib = L
     return L
 
@@ -301,6 +304,20 @@ class GpuTree:
                 out.append((st, halves[0], halves[1]) if st == 0 else (st, None, None))
         finally:
             L.cuacd_cuts_free(h)
+        return out
+
+    def eval_cuts(self, mesh, planes):
+        """The reference's CPU helpers per candidate plane, on the GPU: (n, 8)
+        doubles per plane = split, |vol+|, |vol-|, hull+, hull-, rv+, rv-,
+        max Hausdorff (cuacd_tree_eval_cuts). The device time is
+        last_eval_ms."""
+        L = load_library()
+        pl = np.ascontiguousarray(np.asarray(planes, np.float64).reshape(-1, 4))
+        out = np.zeros((pl.shape[0], 8), np.float64)
+        ma = A.MeshArray([A.as_mesh(mesh)])
+        _check(L.cuacd_tree_eval_cuts(self.h, ma.arr, pl.ctypes.data_as(C.POINTER(C.c_double)), pl.shape[0],
+                                      out.ctypes.data_as(C.POINTER(C.c_double))))
+        self.last_eval_ms = float(L.cuacd_tree_eval_cuts_ms(self.h))
         return out
 
     def items(self, first, n):

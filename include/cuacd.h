@@ -245,6 +245,18 @@ int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, con
  * scratch bound was exceeded; or a negative error. */
 int cuacd_cuts_half(const void* halves, int cut, int side, const float** verts, uint32_t* nv, const uint32_t** tris,
                     uint32_t* nt);
+/* The reference's CPU helpers applied to candidate cuts of one mesh
+ * (planeCut, convexHull, volumes and rv, hausdorff: src/cpu/cut.ts,
+ * src/cpu/hull.ts, src/mesh.ts:58-72, src/part.ts:24-26, src/cpu/
+ * hausdorff.ts), on the GPU: the capped cut of every plane in one batch,
+ * then one hull + Hausdorff batch over all halves. out8 receives 8 doubles
+ * per plane: split (1 or 0), |volume| of the positive and negative half,
+ * their hull volumes, their rv costs, and the larger of the two halves'
+ * Hausdorff distances to their hulls (samples by hausdorff_shader.ts:57-78).
+ * Planes that do not split the mesh leave zeros. */
+int cuacd_tree_eval_cuts(void* tree, const cuacd_mesh* mesh, const double* planes, int n, double* out8);
+/* Device time of the last cuacd_tree_eval_cuts (cut batch + hull batches). */
+float cuacd_tree_eval_cuts_ms(void* tree);
 /* Device time of the batch (uploads, kernels and the readback), in ms. */
 float cuacd_cuts_gpu_ms(const void* halves);
 void cuacd_cuts_free(void* halves);

@@ -151,3 +151,24 @@ def test_gpu_cut_reference_cases():
     assert s2 == 0 and abs(M.volume(p2) - 0.5) < 1e-6 and abs(M.volume(n2) - 1) < 1e-6
     assert s3 == 0 and M.is_closed(p3) and M.is_closed(n3)
     assert abs(M.volume(p3) - 0.75) < 1e-6 and p3.nv == 24 and p3.nt == 32 + 16
+
+
+def test_eval_cuts_matches_cpu_helpers(oracle):
+    """The icosphere configuration through cuacd_tree_eval_cuts (GPU cut, hull
+    and Hausdorff of every half) against the oracle's restatement of the
+    reference's CPU helpers (planeCut, grid hull, volumes, rv and the BVH
+    Hausdorff of src/cpu/hausdorff.ts in double): the same planes split,
+    volumes within 1e-6, hull volumes within 1e-5 relative, rv within 1e-5
+    and Hausdorff within the reference's own 1e-4 + 1e-3 d (cpu.test.ts:97-111)."""
+    m = G.noisy_icosphere(4, noise=0.15, seed=0)
+    planes = G.random_planes(m, 24, seed=0).astype(np.float64)
+    g = T.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096, scratchWords=64 << 20)
+    got = g.eval_cuts(m, planes)
+    ref = oracle.eval_candidates(m, planes, threads=4, with_hd=True, use_ref=False)
+    assert np.array_equal(got[:, 0], ref[:, 0]) and got[:, 0].sum() > 12
+    ok = got[:, 0] == 1
+    assert np.allclose(got[ok, 1:3], ref[ok, 1:3], rtol=1e-6, atol=1e-9)
+    assert np.allclose(got[ok, 3:5], ref[ok, 3:5], rtol=1e-5, atol=1e-7)
+    assert np.allclose(got[ok, 5:7], ref[ok, 5:7], rtol=0, atol=1e-5)
+    d = ref[ok, 7]
+    assert np.all(np.abs(got[ok, 7] - d) <= 1e-4 + 1e-3 * d), np.abs(got[ok, 7] - d).max()
