@@ -235,3 +235,76 @@ class DecomposeStats(C.Structure):
         ("mergeMs", C.c_double),
         ("gpuMs", C.c_double),
     ]
+
+
+class PartIn(C.Structure):
+    """cuacd_part_in — a part handed to the merge pass (part.ts:9-22)."""
+
+    _fields_ = [
+        ("mesh", MeshRef),
+        ("hull", MeshRef),
+        ("meshVol", C.c_double),
+        ("hullVol", C.c_double),
+        ("hausdorff", C.c_double),
+        ("seams", C.POINTER(C.c_double)),
+        ("nSeams", C.c_uint32),
+        ("merged", C.c_int32),
+    ]
+
+
+class MergeOpts(C.Structure):
+    """cuacd_merge_opts — MergeOptions (merge.ts:25-42)."""
+
+    _fields_ = [
+        ("threshold", C.c_float),
+        ("maxRounds", C.c_int32),
+        ("planeTol", C.c_double),
+        ("hullEps", C.c_double),
+        ("verbose", C.c_int32),
+        ("reserved", C.c_int32),
+    ]
+
+
+class MergeStats(C.Structure):
+    """cuacd_merge_stats — MergeStats (merge.ts:54-66)."""
+
+    _fields_ = [
+        ("rounds", C.c_int32),
+        ("merges", C.c_int32),
+        ("pairsHulled", C.c_int32),
+        ("pairsHausdorff", C.c_int32),
+        ("hullFallbacks", C.c_int32),
+        ("reserved", C.c_int32),
+        ("hullMs", C.c_double),
+        ("hausdorffMs", C.c_double),
+        ("totalMs", C.c_double),
+    ]
+
+
+class PartArray:
+    """Keeps numpy arrays alive while a C array of cuacd_part_in points at them."""
+
+    def __init__(self, parts):
+        self.keep = []
+        self.arr = (PartIn * max(1, len(parts)))()
+        for i, p in enumerate(parts):
+            for name in ("mesh", "hull"):
+                m = getattr(p, name)
+                v = np.ascontiguousarray(m.verts, dtype=np.float32)
+                t = np.ascontiguousarray(m.tris, dtype=np.uint32)
+                self.keep += [v, t]
+                ref = getattr(self.arr[i], name)
+                ref.verts = v.ctypes.data_as(C.POINTER(C.c_float))
+                ref.tris = t.ctypes.data_as(C.POINTER(C.c_uint32))
+                ref.nv = v.shape[0]
+                ref.nt = t.shape[0]
+            s = np.ascontiguousarray(np.asarray(getattr(p, "seams", []) or [], np.float64).reshape(-1, 4))
+            self.keep.append(s)
+            self.arr[i].seams = s.ctypes.data_as(C.POINTER(C.c_double))
+            self.arr[i].nSeams = s.shape[0]
+            self.arr[i].meshVol = float(p.meshVol)
+            self.arr[i].hullVol = float(p.hullVol)
+            hd = getattr(p, "hausdorff", None)
+            self.arr[i].hausdorff = float("nan") if hd is None else float(hd)
+            self.arr[i].merged = int(getattr(p, "merged", 1) or 1)
+        self.n = len(parts)

@@ -161,6 +161,7 @@ struct Job {
   // ulps of the input's largest coordinate relative to its extent
   double hullEps = 2e-5;
   bool merging = false;
+  int mergeHullFails = 0;  // merged hulls the GPU could not build (the pair stays apart)
   cuacd_decompose_stats st{};
   // merge state
   std::map<std::pair<uint64_t, uint64_t>, size_t> cache;  // pair -> eval index
@@ -767,6 +768,7 @@ class Engine {
         ev.hullVol = hp[k].hullVol;
         // a merged hull that failed on the GPU leaves the pair unmerged
         ev.cost = std::isnan(ev.hullVol) ? INFINITY : rv_cost(A.meshVol + B.meshVol, ev.hullVol);
+        if (std::isnan(ev.hullVol)) todo[k].job->mergeHullFails++;
         ev.hasHull = ev.cost < o.threshold;
         if (ev.hasHull) ev.hull = std::move(hp[k].hull);
         todo[k].job->st.pairsHulled++;
@@ -1275,6 +1277,137 @@ int cuacd_decompose(void* d, const cuacd_mesh* meshes, int n, int batched, void*
   }
   *result = res.release();
   return CUACD_OK;
+}
+
+void cuacd_merge_opts_default(cuacd_merge_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->threshold = 0.05f;
+  o->maxRounds = 32;
+  o->planeTol = 1e-3;
+  o->hullEps = 2e-5;
+}
+
+static bool part_from(const cuacd_part_in& in, Part& p) {
+  if ((in.mesh.nv && !in.mesh.verts) || (in.mesh.nt && !in.mesh.tris) || (in.hull.nv && !in.hull.verts) ||
+      (in.hull.nt && !in.hull.tris) || (in.nSeams && !in.seams))
+    return false;
+  for (uint64_t k = 0; k < 3ull * in.mesh.nt; k++)
+    if (in.mesh.tris[k] >= in.mesh.nv) return false;
+  for (uint64_t k = 0; k < 3ull * in.hull.nt; k++)
+    if (in.hull.tris[k] >= in.hull.nv) return false;
+  p.mesh.v.assign(in.mesh.verts, in.mesh.verts + 3 * (size_t)in.mesh.nv);
+  p.mesh.t.assign(in.mesh.tris, in.mesh.tris + 3 * (size_t)in.mesh.nt);
+  p.hull.v.assign(in.hull.verts, in.hull.verts + 3 * (size_t)in.hull.nv);
+  p.hull.t.assign(in.hull.tris, in.hull.tris + 3 * (size_t)in.hull.nt);
+  p.meshVol = in.meshVol;
+  p.hullVol = in.hullVol;
+  p.hasHd = !std::isnan(in.hausdorff);
+  p.hd = p.hasHd ? in.hausdorff : 0.0;
+  for (uint32_t k = 0; k < in.nSeams; k++)
+    p.seams.push_back(Plane{in.seams[4 * k], in.seams[4 * k + 1], in.seams[4 * k + 2], in.seams[4 * k + 3]});
+  p.merged = in.merged > 0 ? in.merged : 1;
+  return true;
+}
+
+int cuacd_merge_hulls(void* d, const cuacd_part_in* parts, int n, const cuacd_merge_opts* mo, void** result,
+                      cuacd_merge_stats* stats) {
+  if (!d || !result || n < 0 || (n > 0 && !parts)) return set_error(CUACD_E_INVALID, "cuacd_merge_hulls: invalid argument");
+  Engine* e = static_cast<Engine*>(d);
+  *result = nullptr;
+  cuacd_merge_opts mopt;
+  cuacd_merge_opts_default(&mopt);
+  if (mo) mopt = *mo;
+  if (!(mopt.threshold > 0) || mopt.maxRounds < 0 || !(mopt.planeTol >= 0))
+    return set_error(CUACD_E_INVALID, "cuacd_merge_hulls: invalid options");
+  Job j;
+  j.hullEps = mopt.hullEps;
+  for (int k = 0; k < n; k++) {
+    Part p;
+    if (!part_from(parts[k], p)) return set_error(CUACD_E_INVALID, "cuacd_merge_hulls: bad part arrays");
+    p.id = e->nextId++;
+    j.parts.push_back(std::move(p));
+  }
+  std::unique_ptr<Result> res(new Result());
+  const cuacd_decompose_opts saved = e->o;
+  e->o.threshold = mopt.threshold;
+  e->o.mergeRounds = mopt.maxRounds;
+  e->o.mergePlaneTol = (float)mopt.planeTol;
+  e->o.mergeHulls = 1;
+  e->o.verbose = mopt.verbose;
+  try {
+    e->reset_timers();
+    const auto t0 = Clock::now();
+    std::vector<Job*> jobs{&j};
+    e->merge(jobs);
+    e->evals.clear();
+    cuacd_merge_stats st{};
+    st.rounds = j.st.mergeRounds;
+    st.merges = j.st.merges;
+    st.pairsHulled = j.st.pairsHulled;
+    st.pairsHausdorff = j.st.pairsHausdorff;
+    st.hullFallbacks = j.mergeHullFails;
+    st.hullMs = e->hullMs;
+    st.hausdorffMs = e->hdMs;
+    st.totalMs = ms_since(t0);
+    if (stats) *stats = st;
+    cuacd_decompose_stats ds = j.st;
+    ds.nParts = (int32_t)j.parts.size();
+    ds.totalMs = st.totalMs;
+    ds.mergeMs = e->mergeMs;
+    res->stats.push_back(ds);
+    res->parts.push_back(std::move(j.parts));
+  } catch (const Failure& f) {
+    e->o = saved;
+    e->evals.clear();
+    return set_error(f.code, f.msg.c_str());
+  } catch (const std::bad_alloc&) {
+    e->o = saved;
+    e->evals.clear();
+    return set_error(CUACD_E_CAPACITY, "cuacd_merge_hulls: host memory exhausted");
+  } catch (const std::exception& x) {
+    e->o = saved;
+    e->evals.clear();
+    return set_error(CUACD_E_CAPACITY, (std::string("cuacd_merge_hulls: host error: ") + x.what()).c_str());
+  }
+  e->o = saved;
+  *result = res.release();
+  return CUACD_OK;
+}
+
+int cuacd_seam_plane(const cuacd_part_in* a, const cuacd_part_in* b, double tol, double* out4) {
+  if (!a || !b || !out4) return set_error(CUACD_E_INVALID, "cuacd_seam_plane: invalid argument");
+  Part A, B;
+  if (!part_from(*a, A) || !part_from(*b, B)) return set_error(CUACD_E_INVALID, "cuacd_seam_plane: bad part arrays");
+  Plane p{0, 0, 0, 0};
+  if (!Engine::seam_plane(A, B, tol, p)) return 0;
+  out4[0] = p.a;
+  out4[1] = p.b;
+  out4[2] = p.c;
+  out4[3] = p.d;
+  return 1;
+}
+
+int cuacd_filtered_concat(const cuacd_mesh* a, const cuacd_mesh* b, const double* planes, int nPlanes, double tol,
+                          uint32_t* outTris, int cap) {
+  if (!a || !b || nPlanes < 0 || (nPlanes > 0 && !planes) || cap < 0 || (cap > 0 && !outTris))
+    return set_error(CUACD_E_INVALID, "cuacd_filtered_concat: invalid argument");
+  Mesh ma, mb;
+  ma.v.assign(a->verts, a->verts + 3 * (size_t)a->nv);
+  ma.t.assign(a->tris, a->tris + 3 * (size_t)a->nt);
+  mb.v.assign(b->verts, b->verts + 3 * (size_t)b->nv);
+  mb.t.assign(b->tris, b->tris + 3 * (size_t)b->nt);
+  for (uint32_t x : ma.t)
+    if (x >= a->nv) return set_error(CUACD_E_INVALID, "cuacd_filtered_concat: triangle index out of range");
+  for (uint32_t x : mb.t)
+    if (x >= b->nv) return set_error(CUACD_E_INVALID, "cuacd_filtered_concat: triangle index out of range");
+  std::vector<Plane> pl;
+  for (int k = 0; k < nPlanes; k++) pl.push_back(Plane{planes[4 * k], planes[4 * k + 1], planes[4 * k + 2], planes[4 * k + 3]});
+  const Mesh m = Engine::filtered_concat(ma, mb, pl, tol);
+  const int nt = (int)m.nt();
+  if (nt > cap) return set_error(CUACD_E_CAPACITY, "cuacd_filtered_concat: output buffer too small");
+  std::copy(m.t.begin(), m.t.end(), outTris);
+  return nt;
 }
 
 int cuacd_result_meshes(const void* r) { return r ? (int)static_cast<const Result*>(r)->parts.size() : 0; }

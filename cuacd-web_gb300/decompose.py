@@ -84,6 +84,12 @@ def _lib():
                                       C.c_int, P(C.c_int)]
         L.cuacd_clean_hull_faces.argtypes = [P(A.MeshRef), P(C.c_uint32), C.c_uint32, C.c_double, P(C.c_uint32),
                                              C.c_int]
+        L.cuacd_merge_opts_default.argtypes = [P(A.MergeOpts)]
+        L.cuacd_merge_hulls.argtypes = [C.c_void_p, P(A.PartIn), C.c_int, P(A.MergeOpts), P(C.c_void_p),
+                                        P(A.MergeStats)]
+        L.cuacd_seam_plane.argtypes = [P(A.PartIn), P(A.PartIn), C.c_double, P(C.c_double)]
+        L.cuacd_filtered_concat.argtypes = [P(A.MeshRef), P(A.MeshRef), P(C.c_double), C.c_int, C.c_double,
+                                            P(C.c_uint32), C.c_int]
         _bound = True
     return L
 
@@ -193,6 +199,56 @@ class Decomposer:
 
     def decompose(self, mesh) -> DecomposeResult:
         return self.decompose_many([mesh], batched=False)[0]
+
+
+    def merge_hulls(self, parts, threshold: float = 0.05, max_rounds: int = 32, plane_tol: float = 1e-3,
+                    hull_eps: float = 2e-5, verbose: int = 0):
+        """mergeHulls(tree, parts, opts) (merge.ts:170-303) on this
+        decomposer's GPU tree: returns (merged parts, MergeStats dict)."""
+        L = _lib()
+        mo = A.MergeOpts()
+        L.cuacd_merge_opts_default(C.byref(mo))
+        mo.threshold, mo.maxRounds, mo.planeTol, mo.hullEps, mo.verbose = threshold, max_rounds, plane_tol, hull_eps, verbose
+        pa = A.PartArray(parts)
+        res = C.c_void_p()
+        st = A.MergeStats()
+        _check(L.cuacd_merge_hulls(self.h, pa.arr, pa.n, C.byref(mo), C.byref(res), C.byref(st)))
+        out = _take_results(res, 1)[0]
+        return out.parts, {name: getattr(st, name) for name, _ in A.MergeStats._fields_ if name != "reserved"}
+
+
+def merge_hulls(parts, threshold: float = 0.05, max_rounds: int = 32, plane_tol: float = 1e-3, hull_eps: float = 2e-5,
+                **options):
+    """mergeHulls (merge.ts:170-303): (merged parts, MergeStats dict)."""
+    d = Decomposer(threshold=threshold, **options)
+    try:
+        return d.merge_hulls(parts, threshold, max_rounds, plane_tol, hull_eps)
+    finally:
+        d.destroy()
+
+
+def seam_plane(a, b, tol: float = 1e-3):
+    """seamPlane (merge.ts:114-141): the plane (a, b, c, d) or None."""
+    pa = A.PartArray([a, b])
+    out = (C.c_double * 4)()
+    rc = _lib().cuacd_seam_plane(C.byref(pa.arr[0]), C.byref(pa.arr[1]), float(tol), out)
+    if rc < 0:
+        _check(rc)
+    return tuple(float(x) for x in out) if rc == 1 else None
+
+
+def filtered_concat(a, b, planes, tol: float = 1e-3) -> Mesh:
+    """filteredConcat (merge.ts:144-157): the concatenation of a and b without
+    the triangles lying on any of the planes."""
+    ma = A.MeshArray([A.as_mesh(a), A.as_mesh(b)])
+    pl = np.ascontiguousarray(np.asarray(planes, np.float64).reshape(-1, 4))
+    cap = a.nt + b.nt
+    out = np.zeros(max(3 * cap, 3), np.uint32)
+    n = _lib().cuacd_filtered_concat(C.byref(ma.arr[0]), C.byref(ma.arr[1]), pl.ctypes.data_as(C.POINTER(C.c_double)),
+                                     pl.shape[0], float(tol), A.uptr(out), cap)
+    if n < 0:
+        _check(n)
+    return Mesh(np.concatenate([a.verts, b.verts]).astype(np.float32), out[: 3 * n].reshape(-1, 3).copy())
 
 
 def decompose(mesh, **options) -> DecomposeResult:

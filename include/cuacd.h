@@ -350,6 +350,64 @@ int cuacd_result_part(const void* result, int mesh, int part, cuacd_part_view* o
 int cuacd_result_stats(const void* result, int mesh, cuacd_decompose_stats* out);
 void cuacd_result_free(void* result);
 
+/* ---- the merge pass on its own (src/merge.ts:170-303) ------------------- */
+
+/* A part handed to the merge pass (Part, part.ts:9-22): its mesh, its hull
+ * (vertices and outward triangles), volumes, the Hausdorff distance (NaN when
+ * unknown), the seam planes of earlier merges (4 doubles each) and how many
+ * input parts it already holds. */
+typedef struct {
+  cuacd_mesh mesh;
+  cuacd_mesh hull;
+  double meshVol;
+  double hullVol;
+  double hausdorff;
+  const double* seams;
+  uint32_t nSeams;
+  int32_t merged;
+} cuacd_part_in;
+
+/* MergeOptions (merge.ts:25-42) with DEFAULT_MERGE_OPTIONS (merge.ts:44-52);
+ * hulls and Hausdorff distances always run on the GPU. */
+typedef struct {
+  float threshold;
+  int32_t maxRounds;
+  double planeTol;
+  double hullEps; /* epsilon of the merged hulls' cleanup (cleanHullFaces) */
+  int32_t verbose;
+  int32_t reserved;
+} cuacd_merge_opts;
+
+/* MergeStats (merge.ts:54-66). hullFallbacks counts merged hulls the GPU
+ * could not build (the pair then stays unmerged). */
+typedef struct {
+  int32_t rounds;
+  int32_t merges;
+  int32_t pairsHulled;
+  int32_t pairsHausdorff;
+  int32_t hullFallbacks;
+  int32_t reserved;
+  double hullMs, hausdorffMs, totalMs;
+} cuacd_merge_stats;
+
+void cuacd_merge_opts_default(cuacd_merge_opts* o);
+/* mergeHulls(tree, parts, opts) (merge.ts:170-303) on the decomposer's GPU
+ * tree: rounds of cheap rejections, merged hulls of the surviving pairs,
+ * Hausdorff distances of the seam-filtered unions, greedy min-cost matching.
+ * On success *result receives a one-mesh result handle (cuacd_result_parts /
+ * cuacd_result_part with mesh 0) holding the merged part list, and *stats the
+ * pass's statistics. */
+int cuacd_merge_hulls(void* decomposer, const cuacd_part_in* parts, int n, const cuacd_merge_opts* o, void** result,
+                      cuacd_merge_stats* stats);
+/* seamPlane(a, b, tol) (merge.ts:114-141): writes the plane (4 doubles) and
+ * returns 1, or returns 0 when no separating hull face carries mesh area. */
+int cuacd_seam_plane(const cuacd_part_in* a, const cuacd_part_in* b, double tol, double* out4);
+/* filteredConcat(a, b, planes, tol) (merge.ts:144-157): the concatenation's
+ * vertices are a's then b's; writes the kept triangles (over the
+ * concatenation, at most cap of them) and returns their count. */
+int cuacd_filtered_concat(const cuacd_mesh* a, const cuacd_mesh* b, const double* planes, int nPlanes, double tol,
+                          uint32_t* outTris, int cap);
+
 /* Serving (no counterpart in the reference, whose decompose serves one mesh
  * per call): continuous batching of decompositions. Requests queue in
  * arrival order and are admitted while the admitted meshes' triangles stay

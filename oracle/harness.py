@@ -74,6 +74,11 @@ def lib():
     L.orc_rv_cost.argtypes = [C.c_float, C.c_float]
     L.orc_eval_candidates.argtypes = [P(A.MeshRef), P(C.c_double), C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_double)]
     L.orc_load_qh_ref.argtypes = [C.c_char_p]
+    L.orc_seam_plane.argtypes = [P(A.PartIn), P(A.PartIn), C.c_double, P(C.c_double)]
+    L.orc_filtered_concat.argtypes = [P(A.MeshRef), P(A.MeshRef), P(C.c_double), C.c_int, C.c_double, P(C.c_uint32),
+                                      C.c_int]
+    L.orc_merge_hulls.argtypes = [P(A.PartIn), C.c_int, C.c_double, C.c_int, C.c_double, P(C.c_int), P(C.c_int),
+                                  P(C.c_int), P(C.c_double), P(C.c_double), P(C.c_double), P(C.c_int), P(C.c_int)]
     ref = os.path.join(ORACLE_DIR, "_ref", "libqh_ref.so")
     if os.path.exists(ref):
         try:
@@ -403,3 +408,46 @@ def clean_hull_faces_ref(V, T, eps=2e-5):
             return out
         cand = [c for c in cand if c not in drop]
     return T
+
+
+# ---- the merge pass (merge_oracle.cpp) ----------------------------------------
+
+def seam_plane(a, b, tol=1e-3):
+    """seamPlane (merge.ts:114-141): the plane (a, b, c, d) or None."""
+    pa = A.PartArray([a, b])
+    out = (C.c_double * 4)()
+    ok = lib().orc_seam_plane(C.byref(pa.arr[0]), C.byref(pa.arr[1]), float(tol), out)
+    return tuple(float(x) for x in out) if ok else None
+
+
+def filtered_concat(a, b, planes, tol=1e-3):
+    """filteredConcat (merge.ts:144-157): kept triangles over a's then b's vertices."""
+    ma = A.MeshArray([A.as_mesh(a), A.as_mesh(b)])
+    pl = np.ascontiguousarray(np.asarray(planes, np.float64).reshape(-1, 4))
+    cap = a.nt + b.nt
+    out = np.zeros(max(3 * cap, 3), np.uint32)
+    n = lib().orc_filtered_concat(C.byref(ma.arr[0]), C.byref(ma.arr[1]), pl.ctypes.data_as(C.POINTER(C.c_double)),
+                                  pl.shape[0], float(tol), A.uptr(out), cap)
+    return out[: 3 * n].reshape(-1, 3).copy()
+
+
+def merge_hulls(parts, threshold=0.05, max_rounds=32, plane_tol=1e-3):
+    """mergeHulls (merge.ts:170-303) on the oracle's grid hull and float32
+    Hausdorff: a list of output parts (members = input parts in
+    concatenation order, meshVol, hullVol, hausdorff, nSeams) and the stats
+    (rounds, merges, pairsHulled, pairsHausdorff)."""
+    n = len(parts)
+    pa = A.PartArray(parts)
+    n_out = C.c_int(0)
+    ms = np.zeros(n + 1, np.int32)
+    mem = np.zeros(max(n, 1), np.int32)
+    mv, hv, hd = np.zeros(max(n, 1)), np.zeros(max(n, 1)), np.zeros(max(n, 1))
+    ns = np.zeros(max(n, 1), np.int32)
+    st = np.zeros(4, np.int32)
+    ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))  # noqa: E731
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    lib().orc_merge_hulls(pa.arr, n, float(threshold), int(max_rounds), float(plane_tol), C.byref(n_out), ip(ms),
+                          ip(mem), dp(mv), dp(hv), dp(hd), ip(ns), ip(st))
+    out = [dict(members=mem[ms[k]:ms[k + 1]].tolist(), meshVol=float(mv[k]), hullVol=float(hv[k]),
+                hausdorff=float(hd[k]), nSeams=int(ns[k])) for k in range(n_out.value)]
+    return out, dict(rounds=int(st[0]), merges=int(st[1]), pairsHulled=int(st[2]), pairsHausdorff=int(st[3]))
