@@ -7,9 +7,14 @@ same input parts in the same concatenation order (its mesh is bit for bit
 their concatenation), the same mesh volume, hull volume within 1e-6
 relative, the same seam count, Hausdorff within 1e-4 + 1e-3 d, and the same
 statistics (rounds, merges, pairs hulled, pairs with a Hausdorff distance).
-The merged hull meshes themselves are not compared: the engine cleans them
-with its CPU quickhull as merge.ts:213 does, the oracle keeps the raw grid
-hull faces."""
+The merged hull meshes differ in triangulation: the engine cleans them with
+its CPU quickhull as merge.ts:213 does, the oracle keeps the raw grid hull
+faces, so the two passes sample different points of the same hull surface
+and their Hausdorff distances agree to 1e-4 + 1e-2 d only. Each merged
+part's Hausdorff distance is therefore also recomputed by the oracle on the
+engine's own inputs — the part's mesh without the triangles on its seams
+(filteredConcat) against its merged hull — and must agree to the GPU form's
+1e-5 + 1e-4 d."""
 import numpy as np
 import pytest
 
@@ -95,6 +100,13 @@ def test_merge_matches_oracle(oracle, name):
             assert len(g.seams) == r["nSeams"] and g.merged == len(mem)
             if len(mem) > 1:
                 d = r["hausdorff"]
-                assert abs(g.hausdorff - d) <= 1e-4 + 1e-3 * d, (name, thr, g.hausdorff, d)
+                assert abs(g.hausdorff - d) <= 1e-4 + 1e-2 * d, (name, thr, g.hausdorff, d)
+                empty = M.Mesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+                kept = oracle.filtered_concat(g.mesh, empty, g.seams, 1e-3)
+                if len(kept) == 0:
+                    assert g.hausdorff == 0.0
+                else:
+                    e = float(oracle.hausdorff_gpu_form([(M.Mesh(g.mesh.verts, kept), g.hull)])[0])
+                    assert abs(g.hausdorff - e) <= 1e-5 + 1e-4 * e, (name, thr, g.hausdorff, e)
         for k in ("rounds", "merges", "pairsHulled", "pairsHausdorff"):
             assert st[k] == rst[k], (name, thr, k, st, rst)
