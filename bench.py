@@ -706,6 +706,51 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+# the reference's own meshes at its README's comparison settings (width 30,
+# nConcaveEdges 16, threshold 0.05, merging on; README.md:151-157), with the
+# parts and wall times it reports on an RTX 4090
+REF_MESHES = [("49160.stl", 142, 0.77), ("teapot_vox64.stl.gz", 16, 0.69), ("bunny_vox64.stl.gz", 246, 2.3)]
+
+
+def refmeshes_measure(steps=1):
+    import gzip
+
+    dec = importlib.import_module("cuacd-web_gb300.decompose")
+    io = importlib.import_module("cuacd-web_gb300.meshio")
+    mesh_mod = importlib.import_module("cuacd-web_gb300.mesh")
+    out = {}
+    d = dec.Decomposer(threshold=0.05, width=30, nConcaveEdges=16, mergeHulls=True, tree=DEC_TREE)
+    try:
+        for name, ref_parts, ref_s in REF_MESHES:
+            with open(os.path.join(ROOT, "tests", "golden", name), "rb") as f:
+                buf = f.read()
+            m = io.parse_stl(gzip.decompress(buf) if name.endswith(".gz") else buf)
+            d.decompose(m)  # warm-up
+            ms = []
+            for _ in range(max(steps, 1)):
+                t0 = time.perf_counter()
+                r = d.decompose(m)
+                ms.append(1000 * (time.perf_counter() - t0))
+            vol = sum(mesh_mod.volume(p.mesh) for p in r.parts)
+            out[name] = {"tris": m.nt, "parts": len(r.parts), "ms": statistics.median(ms), "iterations": r.iterations,
+                         "volume_rel_err": abs(vol - mesh_mod.volume(m)) / mesh_mod.volume(m),
+                         "reference_rtx4090": {"parts": ref_parts, "ms": 1000 * ref_s}}
+    finally:
+        d.destroy()
+    return out
+
+
+def run_refmeshes(args):
+    res = refmeshes_measure(args.steps)
+    total = sum(v["ms"] for v in res.values())
+    line = {"metric": "reference meshes decomposed (README settings)", "value": 1000 * len(res) / total,
+            "unit": "meshes/s", "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": total,
+            "higher_is_better": True, "dtype": "f32", "data": "the reference's test meshes",
+            "config": {"workload": "49160.stl, teapot_vox64, bunny_vox64 at width 30, nConcaveEdges 16, threshold 0.05, "
+                                   "merging on"}, "meshes": res}
+    print(json.dumps(line), flush=True)
+
+
 def run_decompose(args):
     m = decompose_measure(args.meshes, big_steps=max(args.steps, 1))
     line = {"metric": m["metric"], "value": m["batched"]["value"], "unit": "meshes/s", "n_gpus": 1,
@@ -726,7 +771,8 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--seeds", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="tree", choices=["tree", "hausdorff", "hulls", "bighulls", "decompose", "serve"])
+    ap.add_argument("--workload", default="tree",
+                    choices=["tree", "hausdorff", "hulls", "bighulls", "decompose", "serve", "refmeshes"])
     ap.add_argument("--pairs", type=int, default=256)
     ap.add_argument("--meshes", type=int, default=32, help="meshes of the uneven decomposition batch")
     ap.add_argument("--no-decompose", action="store_true", help="leave the decomposition summary out of the tree line")
@@ -741,6 +787,8 @@ def main():
         run_decompose(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "refmeshes":
+        run_refmeshes(args)
     elif args.workload != "tree":
         run_secondary(args)
     else:

@@ -29,6 +29,7 @@ UNITS = {
     "cuacd_host.cu": [],
     # the GPU capped cut rounds every double operation as the host cut does
     "cut_kernels.cu": ["--fmad=false"],
+    "concave_kernels.cu": ["--fmad=false"],
     # host geometry of the decomposition loop: double arithmetic rounded as
     # the reference's JavaScript rounds it, so no contraction into FMA
     "host_mesh.cpp": ["-Xcompiler", "-ffp-contract=off"],
@@ -36,7 +37,7 @@ UNITS = {
     "decompose.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "cpu_hull.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["cuacd_dev.cuh", "host_mesh.h", "cut_engine.h"]
+HEADERS = ["cuacd_dev.cuh", "host_mesh.h", "cut_engine.h", "dev_scan.cuh", "concave_engine.h"]
 
 
 def nvcc() -> str:

@@ -18,6 +18,7 @@
 
 #include "../../include/cuacd.h"
 #include "cuacd_dev.cuh"
+#include "concave_engine.h"
 #include "cut_engine.h"
 #include "host_mesh.h"
 
@@ -148,10 +149,13 @@ struct Tree {
   bool gvalid = false;
 
   cut::Engine* cutter = nullptr;  // the GPU capped cut, created on first use
+  conc::Engine* concave = nullptr;  // the GPU concave-edge planes, created on first use
+  float lastConcaveMs = 0.0f;
   float lastEvalMs = 0.0f;        // device time of the last cuacd_tree_eval_cuts
 
   ~Tree() {
     if (cutter) cut::engine_destroy(cutter);
+    if (concave) conc::engine_destroy(concave);
     if (gexec) cudaGraphExecDestroy(gexec);
     for (DevBuf* b : {&bV, &bT, &bE, &bS, &bCtr, &bSlab, &bParts, &bItems, &bJobs, &bPlanes, &bSnap, &bHd, &bScan, &bWork, &bUb}) b->release();
     for (HostBuf* b : {&hStage, &hRead, &hSnap, &hMeta}) b->release();
@@ -917,6 +921,17 @@ int cuacd_tree_eval_cuts(void* tree, const cuacd_mesh* mesh, const double* plane
 }
 
 float cuacd_tree_eval_cuts_ms(void* tree) { return tree ? ((Tree*)tree)->lastEvalMs : 0.0f; }
+
+int cuacd_tree_concave_planes(void* tree, const cuacd_mesh* meshes, int n, int nConcaveEdges, double concaveEps,
+                              double concaveThreshold, const uint32_t* seeds, float* out, int32_t* counts) {
+  Tree* t = (Tree*)tree;
+  if (!t || n < 0) return fail(CUACD_E_INVALID, "cuacd_tree_concave_planes: invalid argument");
+  if (!t->concave && !(t->concave = conc::engine_create())) return fail(CUACD_E_CUDA, "concave engine creation failed");
+  return conc::engine_run(t->concave, t->stream, meshes, n, nConcaveEdges, concaveEps, concaveThreshold, seeds, out,
+                          counts, &t->lastConcaveMs);
+}
+
+float cuacd_tree_concave_ms(void* tree) { return tree ? ((Tree*)tree)->lastConcaveMs : 0.0f; }
 
 float cuacd_cuts_gpu_ms(const void* halves) { return halves ? ((const cut::Halves*)halves)->gpuMs : 0.0f; }
 

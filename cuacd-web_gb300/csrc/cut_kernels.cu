@@ -50,6 +50,7 @@
 #include <vector>
 
 #include "cut_engine.h"
+#include "dev_scan.cuh"
 
 #define CUT_FULL 0xffffffffu
 #define CUT_NONE 0xffffffffu
@@ -169,110 +170,6 @@ __host__ __device__ inline CapCarve carve(uint32_t m, uint32_t capMax) {
   c.cent = d; d += 3 * m;
   c.dbls = d;
   return c;
-}
-
-// ---------------------------------------------------------------------------
-// device-wide exclusive scan of uint32 or uint4 values: out has n + 1
-// entries, out[n] = total
-
-__device__ __forceinline__ uint32_t vadd(uint32_t a, uint32_t b) { return a + b; }
-__device__ __forceinline__ uint4 vadd(uint4 a, uint4 b) { return make_uint4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
-__device__ __forceinline__ uint32_t vsub(uint32_t a, uint32_t b) { return a - b; }
-__device__ __forceinline__ uint4 vsub(uint4 a, uint4 b) { return make_uint4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
-template <typename T>
-__device__ __forceinline__ T vzero();
-template <>
-__device__ __forceinline__ uint32_t vzero<uint32_t>() { return 0u; }
-template <>
-__device__ __forceinline__ uint4 vzero<uint4>() { return make_uint4(0, 0, 0, 0); }
-__device__ __forceinline__ uint32_t vshfl_up(uint32_t v, int d) { return __shfl_up_sync(CUT_FULL, v, d); }
-__device__ __forceinline__ uint4 vshfl_up(uint4 v, int d) {
-  return make_uint4(__shfl_up_sync(CUT_FULL, v.x, d), __shfl_up_sync(CUT_FULL, v.y, d),
-                    __shfl_up_sync(CUT_FULL, v.z, d), __shfl_up_sync(CUT_FULL, v.w, d));
-}
-
-constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 4;
-constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-
-// inclusive scan of one value per thread over the block (blockDim.x a
-// multiple of 32, at most 1024); *total = the block's sum
-template <typename T>
-__device__ T block_inclusive(T v, T* warpSums, T* total) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int d = 1; d < 32; d <<= 1) {
-    T u = vshfl_up(v, d);
-    if (lane >= d) v = vadd(v, u);
-  }
-  if (lane == 31) warpSums[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    T s = lane < nw ? warpSums[lane] : vzero<T>();
-    for (int d = 1; d < 32; d <<= 1) {
-      T u = vshfl_up(s, d);
-      if (lane >= d) s = vadd(s, u);
-    }
-    warpSums[lane] = s;
-  }
-  __syncthreads();
-  if (wid > 0) v = vadd(v, warpSums[wid - 1]);
-  *total = warpSums[nw - 1];
-  __syncthreads();
-  return v;
-}
-
-template <typename T>
-__global__ void k_scan_tiles(const T* __restrict__ in, uint32_t n, T* __restrict__ tileSums) {
-  __shared__ T ws[32];
-  const uint32_t base = blockIdx.x * SCAN_TILE;
-  T s = vzero<T>();
-  for (int k = 0; k < SCAN_ITEMS; k++) {
-    const uint32_t i = base + threadIdx.x * SCAN_ITEMS + k;
-    if (i < n) s = vadd(s, in[i]);
-  }
-  T total;
-  block_inclusive(s, ws, &total);
-  if (threadIdx.x == 0) tileSums[blockIdx.x] = total;
-}
-
-// tile sums to exclusive tile starts, in place (one block); total at [nTiles]
-template <typename T>
-__global__ void k_scan_tile_starts(T* __restrict__ tileSums, uint32_t nTiles) {
-  __shared__ T ws[32];
-  T carry = vzero<T>();
-  for (uint32_t c = 0; c < nTiles; c += blockDim.x) {
-    const uint32_t i = c + threadIdx.x;
-    const T v = i < nTiles ? tileSums[i] : vzero<T>();
-    T total;
-    const T inc = block_inclusive(v, ws, &total);
-    if (i < nTiles) tileSums[i] = vadd(carry, vsub(inc, v));
-    carry = vadd(carry, total);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) tileSums[nTiles] = carry;
-}
-
-template <typename T>
-__global__ void k_scan_apply(const T* __restrict__ in, uint32_t n, const T* __restrict__ tileStarts,
-                             uint32_t nTiles, T* __restrict__ out) {
-  __shared__ T ws[32];
-  const uint32_t base = blockIdx.x * SCAN_TILE;
-  T loc[SCAN_ITEMS];
-  T s = vzero<T>();
-  for (int k = 0; k < SCAN_ITEMS; k++) {
-    const uint32_t i = base + threadIdx.x * SCAN_ITEMS + k;
-    loc[k] = i < n ? in[i] : vzero<T>();
-    s = vadd(s, loc[k]);
-  }
-  T total;
-  const T inc = block_inclusive(s, ws, &total);
-  T cur = vadd(tileStarts[blockIdx.x], vsub(inc, s));
-  for (int k = 0; k < SCAN_ITEMS; k++) {
-    const uint32_t i = base + threadIdx.x * SCAN_ITEMS + k;
-    if (i < n) out[i] = cur;
-    cur = vadd(cur, loc[k]);
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = tileStarts[nTiles];
 }
 
 // ---------------------------------------------------------------------------
@@ -428,7 +325,7 @@ __global__ void k_cut_surface(const CutDesc* __restrict__ D, const CutLayout* __
   bool straddle;
   const uint4 cn = tri_counts(s, &straddle);
   if (cn.x + cn.y == 0) return;
-  const uint4 P = vsub(pre[g], pre[d.tBase]);  // this triangle's positions within the cut
+  const uint4 P = scan::vsub(pre[g], pre[d.tBase]);  // this triangle's positions within the cut
   if (!straddle) {
     const int side = cn.x ? 0 : 1;
     const uint32_t at = side == 0 ? P.x : P.y;
@@ -1332,12 +1229,8 @@ void engine_destroy(Engine* e) {
 
 template <typename T>
 static int scan(Engine* e, const T* in, uint32_t n, T* out, cudaStream_t s) {
-  const uint32_t nTiles = std::max<uint32_t>(1, (n + SCAN_TILE - 1) / SCAN_TILE);
-  if (int rc = e->tiles.ensure(sizeof(T) * (nTiles + 1))) return rc;
-  T* tiles = e->tiles.as<T>();
-  k_scan_tiles<T><<<nTiles, SCAN_THREADS, 0, s>>>(in, n, tiles);
-  k_scan_tile_starts<T><<<1, 1024, 0, s>>>(tiles, nTiles);
-  k_scan_apply<T><<<nTiles, SCAN_THREADS, 0, s>>>(in, n, tiles, nTiles, out);
+  if (int rc = e->tiles.ensure(sizeof(T) * (scan::tiles_for(n) + 1))) return rc;
+  scan::exclusive<T>(in, n, out, e->tiles.as<T>(), s);
   return 0;
 }
 

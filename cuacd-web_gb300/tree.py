@@ -79,6 +79,10 @@ def load_library():
     L.cuacd_cuts_gpu_ms.restype = C.c_float
     L.cuacd_cuts_gpu_ms.argtypes = [C.c_void_p]
     L.cuacd_cuts_free.argtypes = [C.c_void_p]
+    L.cuacd_tree_concave_planes.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, C.c_int, C.c_double, C.c_double,
+                                            P(C.c_uint32), P(C.c_float), P(C.c_int32)]
+    L.cuacd_tree_concave_ms.restype = C.c_float
+    L.cuacd_tree_concave_ms.argtypes = [C.c_void_p]
     L.cuacd_tree_eval_cuts.argtypes = [C.c_void_p, P(A.MeshRef), P(C.c_double), C.c_int, P(C.c_double)]
     L.cuacd_tree_eval_cuts_ms.restype = C.c_float
     L.cuacd_tree_eval_cuts_ms.argtypes = [C.c_void_p]
@@ -305,6 +309,23 @@ class GpuTree:
         finally:
             L.cuacd_cuts_free(h)
         return out
+
+    def concave_planes(self, meshes, n_concave_edges=16, concave_eps=0.005, concave_threshold=3.49, seeds=None):
+        """concaveEdgePlanes (src/cpu/concave.ts:25-92) of every mesh on the
+        GPU: a list of (k, 4) float32 plane arrays (seeds[i] = mesh i's
+        reservoir seed, 12345 when None)."""
+        L = load_library()
+        n = len(meshes)
+        sd = np.full(n, 12345, np.uint32) if seeds is None else np.ascontiguousarray(np.asarray(seeds) & 0xFFFFFFFF,
+                                                                                     np.uint32)
+        ne = max(int(n_concave_edges), 0)
+        out = np.zeros((max(n, 1), 4 * max(ne, 1), 4), np.float32)
+        cnt = np.zeros(max(n, 1), np.int32)
+        ma = A.MeshArray([A.as_mesh(m) for m in meshes])
+        _check(L.cuacd_tree_concave_planes(self.h, ma.arr, n, ne, float(concave_eps), float(concave_threshold),
+                                           A.uptr(sd), A.fptr(out), _int32p(cnt)))
+        self.last_concave_ms = float(L.cuacd_tree_concave_ms(self.h))
+        return [out[k, : cnt[k]].copy() for k in range(n)]
 
     def eval_cuts(self, mesh, planes):
         """The reference's CPU helpers per candidate plane, on the GPU: (n, 8)

@@ -245,6 +245,16 @@ int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, con
  * scratch bound was exceeded; or a negative error. */
 int cuacd_cuts_half(const void* halves, int cut, int side, const float** verts, uint32_t* nv, const uint32_t** tris,
                     uint32_t* nt);
+/* concaveEdgePlanes (src/cpu/concave.ts:25-92) of n meshes on the GPU, on
+ * the tree handle's stream: mesh k's planes (at most 4 * nConcaveEdges, 4
+ * floats each) go to out + 16 * nConcaveEdges * k and their count to
+ * counts[k]; seeds[k] is the mesh's reservoir seed. The planes are
+ * cuacd_concave_planes' bit for bit. */
+int cuacd_tree_concave_planes(void* tree, const cuacd_mesh* meshes, int n, int nConcaveEdges, double concaveEps,
+                              double concaveThreshold, const uint32_t* seeds, float* out, int32_t* counts);
+/* Device time of the last cuacd_tree_concave_planes, in ms. */
+float cuacd_tree_concave_ms(void* tree);
+
 /* The reference's CPU helpers applied to candidate cuts of one mesh
  * (planeCut, convexHull, volumes and rv, hausdorff: src/cpu/cut.ts,
  * src/cpu/hull.ts, src/mesh.ts:58-72, src/part.ts:24-26, src/cpu/
