@@ -820,7 +820,7 @@ void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
 void cuacd_tree_destroy(void* t) { delete (Tree*)t; }
 
 int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, const int32_t* meshOfCut,
-                          const double* planes, int nCuts, void** halves) {
+                          const double* planes, int nCuts, int flags, void** halves) {
   Tree* t = (Tree*)tree;
   if (!t || !halves || nCuts < 0 || (nCuts > 0 && (!meshOfCut || !planes || !meshes)))
     return fail(CUACD_E_INVALID, "cuacd_tree_plane_cuts: invalid argument");
@@ -839,7 +839,8 @@ int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, con
     cs[k].d = f.d;
   }
   cut::Halves* h = new cut::Halves();
-  const int rc = cut::engine_run(t->cutter, t->stream, meshes, nMeshes, cs.data(), nCuts, h);
+  const int rc = cut::engine_run(t->cutter, t->stream, meshes, nMeshes, cs.data(), nCuts,
+                                 (flags & CUACD_CUT_CLOSED) != 0, h);
   if (rc != CUACD_OK) {
     delete h;
     return rc;
@@ -869,7 +870,7 @@ int cuacd_tree_eval_cuts(void* tree, const cuacd_mesh* mesh, const double* plane
   std::memset(out8, 0, 8 * sizeof(double) * (size_t)n);
   std::vector<int32_t> which((size_t)n, 0);
   void* hv = nullptr;
-  int rc = cuacd_tree_plane_cuts(tree, mesh, 1, which.data(), planes, n, &hv);
+  int rc = cuacd_tree_plane_cuts(tree, mesh, 1, which.data(), planes, n, 0, &hv);
   if (rc != CUACD_OK) return rc;
   cut::Halves* h = (cut::Halves*)hv;
   float ms = h->gpuMs;

@@ -41,10 +41,11 @@ struct Engine;
 Engine* engine_create();
 void engine_destroy(Engine* e);
 // Cuts meshes[cuts[k].mesh] by each plane on `stream`. Mesh indices must be
-// in range and the meshes closed (each directed edge once, its reverse
-// once), as the decomposer's parts are. Returns CUACD_OK or an error code.
+// in range. closed = the caller vouches that every mesh is closed (each
+// directed edge has a reverse), as the decomposer's parts are: the pass that
+// finds open input edges is skipped. Returns CUACD_OK or an error code.
 int engine_run(Engine* e, cudaStream_t stream, const cuacd_mesh* meshes, int nMeshes, const CutSpec* cuts, int nCuts,
-               Halves* out);
+               bool closed, Halves* out);
 
 }  // namespace cut
 }  // namespace cuacd

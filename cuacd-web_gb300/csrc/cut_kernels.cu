@@ -238,31 +238,34 @@ __device__ __forceinline__ uint32_t clip_count(const int s[3], int keep) {
 
 // per triangle: (positive half triangles, negative half triangles, positive
 // candidate, negative candidate); a candidate is a triangle whose half
-// triangles have two vertices on the plane (a straddling triangle always,
-// else one with two vertices of side 0)
-__device__ __forceinline__ uint4 tri_counts(const int s[3], bool* straddle) {
+// triangles may hold a boundary edge: two vertices on the plane (a
+// straddling triangle always, else one with two vertices of side 0) or an
+// edge of the input without a reverse (`open`, a bit per edge)
+__device__ __forceinline__ uint4 tri_counts(const int s[3], uint32_t open, bool* straddle) {
   const bool hasPos = s[0] > 0 || s[1] > 0 || s[2] > 0;
   const bool hasNeg = s[0] < 0 || s[1] < 0 || s[2] < 0;
   const int zeros = (s[0] == 0) + (s[1] == 0) + (s[2] == 0);
   *straddle = hasPos && hasNeg;
+  const uint32_t cand = (zeros >= 2 || open != 0) ? 1u : 0u;
   if (!hasPos && !hasNeg) return make_uint4(0, 0, 0, 0);
-  if (!hasNeg) return make_uint4(1, 0, zeros >= 2 ? 1 : 0, 0);
-  if (!hasPos) return make_uint4(0, 1, 0, zeros >= 2 ? 1 : 0);
+  if (!hasNeg) return make_uint4(1, 0, cand, 0);
+  if (!hasPos) return make_uint4(0, 1, 0, cand);
   const uint32_t p = clip_count(s, 1), q = clip_count(s, -1);
   return make_uint4(p, q, p > 0 ? 1 : 0, q > 0 ? 1 : 0);
 }
 
 __global__ void k_cut_count(const CutDesc* __restrict__ D, const uint32_t* __restrict__ tPre, uint32_t n,
                             uint32_t totalT, const uint32_t* __restrict__ T, const int8_t* __restrict__ sgn,
-                            uint4* __restrict__ cnt, CutSizes* __restrict__ S) {
+                            const uint8_t* __restrict__ openBits, uint4* __restrict__ cnt, CutSizes* __restrict__ S) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= totalT) return;
   const uint32_t c = find_seg(tPre, n, g);
   const CutDesc& d = D[c];
-  const uint32_t* tri = T + 3 * ((size_t)d.tOff + (g - d.tBase));
+  const uint32_t t = g - d.tBase;
+  const uint32_t* tri = T + 3 * ((size_t)d.tOff + t);
   const int s[3] = {sgn[d.vBase + tri[0]], sgn[d.vBase + tri[1]], sgn[d.vBase + tri[2]]};
   bool straddle;
-  cnt[g] = tri_counts(s, &straddle);
+  cnt[g] = tri_counts(s, openBits ? openBits[d.tOff + t] : 0u, &straddle);
   if (straddle) atomicAdd(&S[c].straddle, 1u);
 }
 
@@ -312,7 +315,7 @@ __global__ void k_cut_surface(const CutDesc* __restrict__ D, const CutLayout* __
                               const double* __restrict__ dist, const int8_t* __restrict__ sgn,
                               const uint4* __restrict__ pre, unsigned long long* __restrict__ hashKeys,
                               double* __restrict__ hashXYZ, uint32_t* __restrict__ surfT, uint2* __restrict__ candE,
-                              CutOut* __restrict__ O) {
+                              const uint8_t* __restrict__ openBits, CutOut* __restrict__ O) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= totalT) return;
   const uint32_t c = find_seg(tPre, n, g);
@@ -323,16 +326,19 @@ __global__ void k_cut_surface(const CutDesc* __restrict__ D, const CutLayout* __
   const uint32_t ids[3] = {tri[0], tri[1], tri[2]};
   const int s[3] = {sgn[d.vBase + ids[0]], sgn[d.vBase + ids[1]], sgn[d.vBase + ids[2]]};
   bool straddle;
-  const uint4 cn = tri_counts(s, &straddle);
+  const uint32_t t = g - d.tBase;
+  const uint4 cn = tri_counts(s, openBits ? openBits[d.tOff + t] : 0u, &straddle);
   if (cn.x + cn.y == 0) return;
+  // candidate entry: first half triangle, and count | input triangle << 2
+  const uint32_t tagT = t << 2;
   const uint4 P = scan::vsub(pre[g], pre[d.tBase]);  // this triangle's positions within the cut
   if (!straddle) {
     const int side = cn.x ? 0 : 1;
     const uint32_t at = side == 0 ? P.x : P.y;
     uint32_t* o = surfT + 3 * ((size_t)l.surfOff[side] + at);
     o[0] = ids[0]; o[1] = ids[1]; o[2] = ids[2];
-    if (side == 0 && cn.z) candE[l.candOff[0] + P.z] = make_uint2(at, 1);
-    if (side == 1 && cn.w) candE[l.candOff[1] + P.w] = make_uint2(at, 1);
+    if (side == 0 && cn.z) candE[l.candOff[0] + P.z] = make_uint2(at, 1u | tagT);
+    if (side == 1 && cn.w) candE[l.candOff[1] + P.w] = make_uint2(at, 1u | tagT);
     return;
   }
   uint32_t ix[3] = {CUT_NONE, CUT_NONE, CUT_NONE};
@@ -364,7 +370,7 @@ __global__ void k_cut_surface(const CutDesc* __restrict__ D, const CutLayout* __
       o[3 * (k - 1) + 1] = poly[k];
       o[3 * (k - 1) + 2] = poly[k + 1];
     }
-    if (np > 2) candE[l.candOff[side] + (side == 0 ? P.z : P.w)] = make_uint2(at, (uint32_t)(np - 2));
+    if (np > 2) candE[l.candOff[side] + (side == 0 ? P.z : P.w)] = make_uint2(at, (uint32_t)(np - 2) | tagT);
   }
 }
 
@@ -640,10 +646,40 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
   return nOut + 1;
 }
 
+// whether the half edge a -> b of a triangle cut from input triangle tri
+// lies on an input edge without a reverse (open bit k of edge tri[k] ->
+// tri[k + 1]); an intersection vertex is identified by its edge's key
+__device__ __forceinline__ bool on_open_edge(uint32_t a, uint32_t b, const uint32_t* tri, uint32_t bits, uint32_t nv,
+                                             const unsigned long long* keys) {
+  if (bits == 0) return false;
+  uint32_t a0 = a, a1 = a, b0 = b, b1 = b;  // each end's input edge ends
+  if (a >= nv) {
+    const unsigned long long k = keys[a - nv];
+    a0 = (uint32_t)(k >> 32);
+    a1 = (uint32_t)k;
+  }
+  if (b >= nv) {
+    const unsigned long long k = keys[b - nv];
+    b0 = (uint32_t)(k >> 32);
+    b1 = (uint32_t)k;
+  }
+  for (int k = 0; k < 3; k++) {
+    if (!(bits >> k & 1)) continue;
+    const uint32_t p = tri[k], q = tri[(k + 1) % 3];
+    const bool aOn = a < nv ? (a == p || a == q) : ((a0 == p && a1 == q) || (a0 == q && a1 == p));
+    const bool bOn = b < nv ? (b == p || b == q) : ((b0 == p && b1 == q) || (b0 == q && b1 == p));
+    // both ends on the edge, not both the same intersection of it
+    if (aOn && bOn && !(a >= nv && b >= nv)) return true;
+  }
+  return false;
+}
+
 __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __restrict__ L, CutOut* __restrict__ O,
                           uint32_t n, const uint32_t* __restrict__ surfT, const uint2* __restrict__ candE,
                           const int8_t* __restrict__ sgn, const double* __restrict__ hashXYZ,
-                          const float* __restrict__ V, uint32_t* __restrict__ W, double* __restrict__ X) {
+                          const float* __restrict__ V, uint32_t* __restrict__ W, double* __restrict__ X,
+                          const uint32_t* __restrict__ Tin, const uint8_t* __restrict__ openBits,
+                          const unsigned long long* __restrict__ hashKeys) {
   const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (gw >= 2 * n) return;
@@ -677,11 +713,14 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
     uint32_t k = 0;
     if (i < nCand) {
       const uint2 ce = candE[l.candOff[side] + i];
-      for (uint32_t tt = 0; tt < ce.y && tt < 2; tt++) {
+      const uint32_t tIn = ce.y >> 2, nOut = ce.y & 3;
+      const uint32_t bits = openBits ? openBits[d.tOff + tIn] : 0u;
+      const uint32_t* inTri = Tin + 3 * ((size_t)d.tOff + tIn);
+      for (uint32_t tt = 0; tt < nOut && tt < 2; tt++) {
         const uint32_t* tri = st + 3 * (size_t)(ce.x + tt);
         for (int e = 0; e < 3; e++) {
           const uint32_t a = tri[e], b = tri[(e + 1) % 3];
-          if (onPlane(a) && onPlane(b)) {
+          if ((onPlane(a) && onPlane(b)) || on_open_edge(a, b, inTri, bits, nv, hashKeys + l.hashOff)) {
             ea[k] = a;
             eb[k] = b;
             k++;
@@ -1168,6 +1207,57 @@ __global__ void k_cut_volume(uint32_t n2, const unsigned long long* __restrict__
   if (lane == 0) vol[k] = s / 6.0;
 }
 
+// open edges of the input meshes (used when the caller does not vouch for
+// closed meshes): every directed edge in its mesh's hash, then per triangle a
+// bit for each edge whose reverse is absent
+__global__ void k_open_insert(const uint32_t* __restrict__ mPre, uint32_t nMeshes, uint32_t totalE,
+                              const uint32_t* __restrict__ meshTOff, const uint32_t* __restrict__ hOff,
+                              const uint32_t* __restrict__ hSize, const uint32_t* __restrict__ T,
+                              unsigned long long* __restrict__ keys) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= totalE) return;
+  const uint32_t mi = find_seg(mPre, nMeshes, g);
+  const uint32_t e = g - mPre[mi], t = e / 3, k = e % 3;
+  const uint32_t* tri = T + 3 * ((size_t)meshTOff[mi] + t);
+  const unsigned long long key = ((unsigned long long)tri[k] << 32) | tri[(k + 1) % 3];
+  const uint32_t size = hSize[mi];
+  unsigned long long* h = keys + hOff[mi];
+  uint32_t i = mix_key(key) & (size - 1);
+  for (uint32_t probe = 0; probe < size; probe++, i = (i + 1) & (size - 1)) {
+    const unsigned long long old = atomicCAS(h + i, EMPTY_KEY, key);
+    if (old == EMPTY_KEY || old == key) return;
+  }
+}
+
+__global__ void k_open_bits(const uint32_t* __restrict__ mtPre, uint32_t nMeshes, uint32_t totalT,
+                            const uint32_t* __restrict__ meshTOff, const uint32_t* __restrict__ hOff,
+                            const uint32_t* __restrict__ hSize, const uint32_t* __restrict__ T,
+                            const unsigned long long* __restrict__ keys, uint8_t* __restrict__ bits) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= totalT) return;
+  const uint32_t mi = find_seg(mtPre, nMeshes, g);
+  const uint32_t t = g - mtPre[mi];
+  const uint32_t* tri = T + 3 * ((size_t)meshTOff[mi] + t);
+  const uint32_t size = hSize[mi];
+  const unsigned long long* h = keys + hOff[mi];
+  uint32_t b = 0;
+  for (int k = 0; k < 3; k++) {
+    const unsigned long long rev = ((unsigned long long)tri[(k + 1) % 3] << 32) | tri[k];
+    uint32_t i = mix_key(rev) & (size - 1);
+    bool found = false;
+    for (uint32_t probe = 0; probe < size; probe++, i = (i + 1) & (size - 1)) {
+      const unsigned long long kk = h[i];
+      if (kk == rev) {
+        found = true;
+        break;
+      }
+      if (kk == EMPTY_KEY) break;
+    }
+    if (!found) b |= 1u << k;
+  }
+  bits[meshTOff[mi] + t] = (uint8_t)b;
+}
+
 // ---------------------------------------------------------------------------
 // host side
 
@@ -1195,7 +1285,7 @@ struct Buf {
 
 struct Engine {
   Buf inV, inT, desc, vPre, tPre, sizes, layout, out, cPre, dist, sgn, cnt, pre, tiles, hashKeys, hashXYZ, surfT,
-      candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT, halfNt, vol;
+      candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT, halfNt, vol, openBits, openKeys, openMeta;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::vector<uint8_t> hostScratch;
 };
@@ -1237,7 +1327,7 @@ static int scan(Engine* e, const T* in, uint32_t n, T* out, cudaStream_t s) {
 static inline uint32_t blocks(uint64_t n, uint32_t t) { return (uint32_t)std::max<uint64_t>(1, (n + t - 1) / t); }
 
 int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes, const CutSpec* cuts, int nCuts,
-               Halves* out) {
+               bool closed, Halves* out) {
   if (!e || !out || nCuts < 0 || nMeshes < 0 || (nCuts > 0 && (!meshes || !cuts)))
     return set_error(CUACD_E_INVALID, "cut: invalid argument");
   out->status.assign(nCuts, 0);
@@ -1303,13 +1393,55 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   CUTCK(cudaMemcpyAsync(e->vPre.p, vPre.data(), 4 * (n + 1), cudaMemcpyHostToDevice, s));
   CUTCK(cudaMemcpyAsync(e->tPre.p, tPre.data(), 4 * (n + 1), cudaMemcpyHostToDevice, s));
   CUTCK(cudaMemsetAsync(e->sizes.p, 0, sizeof(CutSizes) * n, s));
+  // open input edges, unless the caller vouches for closed meshes
+  const uint8_t* dOpen = nullptr;
+  if (!closed && mt[nMeshes] > 0) {
+    const uint32_t nm = (uint32_t)nMeshes;
+    std::vector<uint32_t> meta(5 * (size_t)nm + 2, 0);  // edge prefix, triangle prefix, tOff, hash offset, size
+    uint32_t* ePreH = meta.data();
+    uint32_t* mtPreH = ePreH + nm + 1;
+    uint32_t* tOffH = mtPreH + nm + 1;
+    uint32_t* hOffH = tOffH + nm;
+    uint32_t* hSizeH = hOffH + nm;
+    (void)hSizeH;
+    std::vector<uint32_t> hs(nm);
+    uint64_t hTot = 0;
+    for (uint32_t i = 0; i < nm; i++) {
+      ePreH[i + 1] = ePreH[i] + 3 * meshes[i].nt;
+      mtPreH[i + 1] = mtPreH[i] + meshes[i].nt;
+      tOffH[i] = (uint32_t)mt[i];
+      hOffH[i] = (uint32_t)hTot;
+      hs[i] = pow2_at_least(std::max<uint32_t>(16, 6 * meshes[i].nt));
+      hTot += hs[i];
+    }
+    std::vector<uint32_t> metaAll(meta.begin(), meta.begin() + 4 * (size_t)nm + 2);
+    metaAll.insert(metaAll.end(), hs.begin(), hs.end());
+    if ((rc = e->openBits.ensure(mt[nMeshes])) || (rc = e->openKeys.ensure(8 * hTot)) ||
+        (rc = e->openMeta.ensure(4 * metaAll.size())))
+      return rc;
+    CUTCK(cudaMemcpyAsync(e->openMeta.p, metaAll.data(), 4 * metaAll.size(), cudaMemcpyHostToDevice, s));
+    CUTCK(cudaMemsetAsync(e->openKeys.p, 0xff, 8 * hTot, s));
+    const uint32_t* dm = e->openMeta.as<uint32_t>();
+    const uint32_t* dePre = dm;
+    const uint32_t* dmtPre = dm + nm + 1;
+    const uint32_t* dtOff = dm + 2 * (nm + 1);
+    const uint32_t* dhOff = dtOff + nm;
+    const uint32_t* dhSize = dhOff + nm;
+    k_open_insert<<<blocks(3 * mt[nMeshes], 256), 256, 0, s>>>(dePre, nm, (uint32_t)(3 * mt[nMeshes]), dtOff, dhOff,
+                                                              dhSize, e->inT.as<uint32_t>(),
+                                                              e->openKeys.as<unsigned long long>());
+    k_open_bits<<<blocks(mt[nMeshes], 256), 256, 0, s>>>(dmtPre, nm, (uint32_t)mt[nMeshes], dtOff, dhOff, dhSize,
+                                                        e->inT.as<uint32_t>(), e->openKeys.as<unsigned long long>(),
+                                                        e->openBits.as<uint8_t>());
+    dOpen = e->openBits.as<uint8_t>();
+  }
   const CutDesc* dD = e->desc.as<CutDesc>();
   CutSizes* dS = e->sizes.as<CutSizes>();
   if (totV) k_cut_classify<<<blocks(totV, 256), 256, 0, s>>>(dD, e->vPre.as<uint32_t>(), n, (uint32_t)totV,
                                                                e->inV.as<float>(), e->dist.as<double>(),
                                                                e->sgn.as<int8_t>(), dS);
   if (totT) k_cut_count<<<blocks(totT, 256), 256, 0, s>>>(dD, e->tPre.as<uint32_t>(), n, (uint32_t)totT,
-                                                            e->inT.as<uint32_t>(), e->sgn.as<int8_t>(),
+                                                            e->inT.as<uint32_t>(), e->sgn.as<int8_t>(), dOpen,
                                                             e->cnt.as<uint4>(), dS);
   if ((rc = scan<uint4>(e, e->cnt.as<uint4>(), (uint32_t)totT, e->pre.as<uint4>(), s))) return rc;
   k_cut_sizes<<<blocks(n, 128), 128, 0, s>>>(dD, n, e->pre.as<uint4>(), dS);
@@ -1382,11 +1514,12 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
                                                       e->inT.as<uint32_t>(), e->inV.as<float>(), e->dist.as<double>(),
                                                       e->sgn.as<int8_t>(), e->pre.as<uint4>(),
                                                       e->hashKeys.as<unsigned long long>(), e->hashXYZ.as<double>(),
-                                                      e->surfT.as<uint32_t>(), e->candE.as<uint2>(), dO);
+                                                      e->surfT.as<uint32_t>(), e->candE.as<uint2>(), dOpen, dO);
   k_cut_cap<<<blocks(2ull * n * 32, 128), 128, 0, s>>>(dD, dL, dO, n, e->surfT.as<uint32_t>(), e->candE.as<uint2>(),
                                                        e->sgn.as<int8_t>(), e->hashXYZ.as<double>(),
                                                        e->inV.as<float>(), e->words.as<uint32_t>(),
-                                                       e->dbls.as<double>());
+                                                       e->dbls.as<double>(), e->inT.as<uint32_t>(), dOpen,
+                                                       e->hashKeys.as<unsigned long long>());
   if (corners) {
     k_cut_first_use<<<blocks(corners, 256), 256, 0, s>>>(dL, dO, e->cPre.as<uint32_t>(), 2 * n, (uint32_t)corners,
                                                          e->surfT.as<uint32_t>(), e->words.as<uint32_t>(),

@@ -458,15 +458,33 @@ class Engine {
       for (size_t k = from; k < above.size(); k++) seeds.push_back(Seed{j, above[k]});
     }
     if (seeds.empty()) return false;
-    // concave-edge planes of every cutting part (decompose.ts:276-281)
+    // concave-edge planes of every cutting part (decompose.ts:276-281), one
+    // GPU batch for all of them
     const auto tc = Clock::now();
     std::vector<std::vector<float>> planes(seeds.size());
-    parallel_for(seeds.size(), threads, [&](size_t k) {
-      const int iter = seeds[k].job->iter - 1;
-      if (iter < o.concaveIters && o.nConcaveEdges > 0)
-        planes[k] = host::concave_edge_planes(seeds[k].job->parts[seeds[k].part].mesh, o.nConcaveEdges, o.concaveEps,
-                                              o.concaveThreshold, (uint32_t)(iter * 7919 + (int)seeds[k].part));
-    });
+    if (o.nConcaveEdges > 0) {
+      std::vector<cuacd_mesh> cm;
+      std::vector<uint32_t> sd;
+      std::vector<size_t> which;
+      for (size_t k = 0; k < seeds.size(); k++) {
+        const int iter = seeds[k].job->iter - 1;
+        if (iter >= o.concaveIters) continue;
+        const Mesh& m = seeds[k].job->parts[seeds[k].part].mesh;
+        cm.push_back(cuacd_mesh{m.v.data(), m.t.data(), (uint32_t)m.nv(), (uint32_t)m.nt()});
+        sd.push_back((uint32_t)(iter * 7919 + (int)seeds[k].part));
+        which.push_back(k);
+      }
+      if (!cm.empty()) {
+        const size_t per = 16 * (size_t)o.nConcaveEdges;
+        std::vector<float> buf(per * cm.size());
+        std::vector<int32_t> cnt(cm.size());
+        const int rc = cuacd_tree_concave_planes(tree, cm.data(), (int)cm.size(), o.nConcaveEdges, o.concaveEps,
+                                                 o.concaveThreshold, sd.data(), buf.data(), cnt.data());
+        if (rc != CUACD_OK) cuda_fail(rc, "concave planes");
+        for (size_t q = 0; q < which.size(); q++)
+          planes[which[q]].assign(buf.begin() + q * per, buf.begin() + q * per + 4 * (size_t)cnt[q]);
+      }
+    }
     concaveMs += ms_since(tc);
     // the tree over all cutting parts, halving the batch on pool overflow
     // (decompose.ts:288-320)
@@ -532,16 +550,54 @@ class Engine {
       Mesh pos, neg;
     };
     std::vector<Cut> cuts(seeds.size());
-    parallel_for(seeds.size(), threads, [&](size_t k) {
+    // every winning cut in one GPU batch (the host cut's halves bit for bit)
+    std::vector<cuacd_mesh> cm;
+    std::vector<int32_t> cutOf;
+    std::vector<double> cutPlanes;
+    std::vector<size_t> cutSeed;
+    for (size_t k = 0; k < seeds.size(); k++) {
       Part& p = seeds[k].job->parts[seeds[k].part];
       const cuacd_seed_result& r = best[k];
       if (!(r.valid & 1)) {
         p.stuck = true;
         p.stuckReason = 1;
-        return;
+        continue;
       }
-      const Plane pl{r.plane[0], r.plane[1], r.plane[2], r.plane[3]};
-      host::CutResult c = host::plane_cut(p.mesh, pl);
+      cutOf.push_back((int32_t)cm.size());
+      cm.push_back(cuacd_mesh{p.mesh.v.data(), p.mesh.t.data(), (uint32_t)p.mesh.nv(), (uint32_t)p.mesh.nt()});
+      for (int a = 0; a < 4; a++) cutPlanes.push_back((double)r.plane[a]);
+      cutSeed.push_back(k);
+    }
+    void* halvesH = nullptr;
+    if (!cm.empty()) {
+      // parts are closed when the input was checked closed and every cut's
+      // halves are validated; otherwise the GPU cut also looks for open edges
+      const int flags = o.requireClosed && o.validateCuts ? CUACD_CUT_CLOSED : 0;
+      const int rc = cuacd_tree_plane_cuts(tree, cm.data(), (int)cm.size(), cutOf.data(), cutPlanes.data(),
+                                           (int)cm.size(), flags, &halvesH);
+      if (rc != CUACD_OK) cuda_fail(rc, "plane cuts");
+    }
+    std::vector<host::CutResult> cutRes(seeds.size());
+    for (size_t q = 0; q < cutSeed.size(); q++) {
+      host::CutResult& c = cutRes[cutSeed[q]];
+      const float* v[2];
+      const uint32_t* t[2];
+      uint32_t nv[2], nt[2];
+      int st = 0;
+      for (int sd = 0; sd < 2 && st == 0; sd++) st = cuacd_cuts_half(halvesH, (int)q, sd, &v[sd], &nv[sd], &t[sd], &nt[sd]);
+      if (st != 0) continue;
+      c.ok = true;
+      c.pos.v.assign(v[0], v[0] + 3 * (size_t)nv[0]);
+      c.pos.t.assign(t[0], t[0] + 3 * (size_t)nt[0]);
+      c.neg.v.assign(v[1], v[1] + 3 * (size_t)nv[1]);
+      c.neg.t.assign(t[1], t[1] + 3 * (size_t)nt[1]);
+    }
+    if (halvesH) cuacd_cuts_free(halvesH);
+    parallel_for(seeds.size(), threads, [&](size_t k) {
+      Part& p = seeds[k].job->parts[seeds[k].part];
+      const cuacd_seed_result& r = best[k];
+      if (!(r.valid & 1)) return;
+      host::CutResult& c = cutRes[k];
       if (!c.ok) {
         p.stuck = true;
         p.stuckReason = 2;

@@ -73,7 +73,7 @@ def load_library():
     L.cuacd_tree_read_part_geometry.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float), P(C.c_uint32), P(C.c_uint32)]
     L.cuacd_tree_read_plane.argtypes = [C.c_void_p, C.c_uint32, P(C.c_float)]
     L.cuacd_tree_plane_cuts.argtypes = [C.c_void_p, P(A.MeshRef), C.c_int, P(C.c_int32), P(C.c_double), C.c_int,
-                                        P(C.c_void_p)]
+                                        C.c_int, P(C.c_void_p)]
     L.cuacd_cuts_half.argtypes = [C.c_void_p, C.c_int, C.c_int, P(P(C.c_float)), P(C.c_uint32), P(P(C.c_uint32)),
                                   P(C.c_uint32)]
     L.cuacd_cuts_gpu_ms.restype = C.c_float
@@ -270,12 +270,14 @@ class GpuTree:
         return out
 
     # ---- debug readers (tree.ts:764-807) ----
-    def plane_cuts(self, meshes, planes, mesh_of_cut=None):
+    def plane_cuts(self, meshes, planes, mesh_of_cut=None, closed=False):
         """planeCut (src/cpu/cut.ts:33-315) on the GPU: cut k cuts
         meshes[mesh_of_cut[k]] (mesh k when None) by planes[k] = (a, b, c, d).
         Returns one (status, positive half, negative half) per cut; status 0
         or the cut's failure code (the halves are then None). The halves are
-        the host cut's bit for bit. The device time is last_cut_ms."""
+        the host cut's bit for bit. closed=True vouches that every mesh is
+        closed (skips the open-edge search). The device time is
+        last_cut_ms."""
         L = load_library()
         pl = np.ascontiguousarray(np.asarray(planes, np.float64).reshape(-1, 4))
         n = pl.shape[0]
@@ -285,7 +287,7 @@ class GpuTree:
         ma = A.MeshArray([A.as_mesh(m) for m in meshes])
         h = C.c_void_p()
         _check(L.cuacd_tree_plane_cuts(self.h, ma.arr, len(meshes), _int32p(idx),
-                                       pl.ctypes.data_as(C.POINTER(C.c_double)), n, C.byref(h)))
+                                       pl.ctypes.data_as(C.POINTER(C.c_double)), n, 1 if closed else 0, C.byref(h)))
         out = []
         try:
             self.last_cut_ms = float(L.cuacd_cuts_gpu_ms(h))

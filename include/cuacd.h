@@ -233,11 +233,14 @@ int cuacd_hull_points_noalloc(const float* points, uint32_t nv, uint32_t* tris, 
  * on the tree handle's stream: cut k cuts meshes[meshOfCut[k]] by planes[4k
  * .. 4k + 3] (a x + b y + c z + d = 0). The halves are the host cut's
  * (cuacd_plane_cut) bit for bit: the same vertices in the same order, the
- * same triangles, caps and failures. The meshes must be closed (every
- * directed edge once and its reverse once), as the decomposer's parts are.
- * On success *halves receives a handle read with cuacd_cuts_half. */
+ * same triangles, caps and failures, for open meshes too. flags:
+ * CUACD_CUT_CLOSED when the caller vouches that every mesh is closed (each
+ * directed edge has a reverse, as the decomposer's parts do), which skips
+ * the search for open input edges. On success *halves receives a handle read
+ * with cuacd_cuts_half. */
+#define CUACD_CUT_CLOSED 1
 int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, const int32_t* meshOfCut,
-                          const double* planes, int nCuts, void** halves);
+                          const double* planes, int nCuts, int flags, void** halves);
 /* Half `side` (0 positive, 1 negative) of cut `cut`: returns 0 with the
  * half's arrays (valid until cuacd_cuts_free), or the cut's failure: 1 the
  * plane does not split the mesh, 2 open boundary chain, 3 boundary chain dead

@@ -172,3 +172,57 @@ def test_eval_cuts_matches_cpu_helpers(oracle):
     assert np.allclose(got[ok, 5:7], ref[ok, 5:7], rtol=0, atol=1e-5)
     d = ref[ok, 7]
     assert np.all(np.abs(got[ok, 7] - d) <= 1e-4 + 1e-3 * d), np.abs(got[ok, 7] - d).max()
+
+
+def _open_meshes():
+    cube = M.unit_cube()
+    ico = G.noisy_icosphere(3, seed=2)
+    blob = M.normalize(G.blob_mesh(6, 26, seed=3))[0]
+    return [("cube_open", M.Mesh(cube.verts, cube.tris[2:])),
+            ("ico_cap_removed", M.Mesh(ico.verts, ico.tris[ico.verts[ico.tris][:, :, 2].mean(1) < 0.8])),
+            ("blob_half_shell", M.Mesh(blob.verts, blob.tris[blob.verts[blob.tris][:, :, 0].mean(1) < 0.1])),
+            ("strip", M.Mesh(np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0.2], [0, 2, 0], [1, 2, 0.4]], np.float32),
+                             np.array([[0, 1, 2], [1, 3, 2], [2, 3, 4], [3, 5, 4]], np.uint32)))]
+
+
+def test_gpu_cut_open_meshes_match_host_cut():
+    # open meshes: boundary edges off the plane (the open rims) join the
+    # boundary loops, so most of these cuts fail as the host cut's do, with
+    # the same reason
+    g = _tree()
+    meshes = _open_meshes()
+    planes, idx = [], []
+    for k, (name, m) in enumerate(meshes):
+        for pl in _planes(m, 6, zlib.crc32(name.encode())):
+            planes.append(pl)
+            idx.append(k)
+    got = g.plane_cuts([m for _, m in meshes], planes, idx)
+    for (st, pos, neg), pl, k in zip(got, planes, idx):
+        name, m = meshes[k]
+        try:
+            ref = D.plane_cut(m, pl)
+            err = None
+        except T.CuacdError as x:
+            ref, err = None, str(x)
+        assert (ref is None) == (st != 0), (name, pl, st, err)
+        if ref is None:
+            reason = {1: "does not split", 2: "open boundary chain", 3: "dead end", 4: "cycle"}.get(st)
+            assert reason is not None and reason in err, (name, st, err)
+            continue
+        assert _same(pos, ref[0]) and _same(neg, ref[1]), (name, pl)
+
+
+def test_gpu_cut_closed_flag_gives_the_same_halves():
+    g = _tree()
+    meshes = [m for _, m in _meshes()]
+    planes, idx = [], []
+    for k, m in enumerate(meshes):
+        for pl in _planes(m, 3, 99 + k):
+            planes.append(pl)
+            idx.append(k)
+    a = g.plane_cuts(meshes, planes, idx, closed=False)
+    b = g.plane_cuts(meshes, planes, idx, closed=True)
+    for x, y in zip(a, b):
+        assert x[0] == y[0]
+        if x[0] == 0:
+            assert _same(x[1], y[1]) and _same(x[2], y[2])
