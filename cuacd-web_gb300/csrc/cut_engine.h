@@ -18,7 +18,7 @@ struct CutSpec {
   double n[3], d, u[3], v[3];
 };
 
-// The halves of a batch of cuts, in pinned host memory. status[k] is 0 or
+// The halves of a batch of cuts, in host memory. status[k] is 0 or
 // the cut's failure (1 the plane does not split the mesh, 2 open boundary
 // chain, 3 boundary chain dead end, 4 boundary chain cycle, 5 internal
 // scratch bound exceeded). For cut k and side s (0 positive, 1 negative)
@@ -29,12 +29,10 @@ struct Halves {
   std::vector<uint64_t> vOff, tOff;
   std::vector<uint32_t> nv, nt;
   std::vector<double> vol;  // signed volume of each half (a fixed-order parallel sum)
-  float* V = nullptr;
-  uint32_t* T = nullptr;
+  float* V = nullptr;     // into host
+  uint32_t* T = nullptr;  // into host
   float gpuMs = 0.0f;
-  void* pinned = nullptr;
-  size_t pinnedBytes = 0;
-  ~Halves();
+  std::vector<uint32_t> host;  // every half's vertices, then every half's triangles
 };
 
 struct Engine;

@@ -1287,12 +1287,12 @@ struct Engine {
   Buf inV, inT, desc, vPre, tPre, sizes, layout, out, cPre, dist, sgn, cnt, pre, tiles, hashKeys, hashXYZ, surfT,
       candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT, halfNt, vol, openBits, openKeys, openMeta;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  std::vector<uint8_t> hostScratch;
+  void* stage = nullptr;  // pinned staging of the halves' readback
+  size_t stageBytes = 0;
+  ~Engine() {
+    if (stage) cudaFreeHost(stage);
+  }
 };
-
-Halves::~Halves() {
-  if (pinned) cudaFreeHost(pinned);
-}
 
 Engine* engine_create() {
   Engine* e = new Engine();
@@ -1576,20 +1576,27 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   CUTCK(cudaGetLastError());
   out->vol.assign(2 * (size_t)n, 0.0);
   CUTCK(cudaMemcpyAsync(out->vol.data(), e->vol.p, 8 * 2 * n, cudaMemcpyDeviceToHost, s));
+  // the halves come back into the engine's pinned staging buffer (grown,
+  // never shrunk) and are copied into the result's own host arrays
   const size_t need = 12 * outVTot + 12 * outTTot + 16;
-  if (out->pinnedBytes < need) {
-    if (out->pinned) cudaFreeHost(out->pinned);
-    out->pinned = nullptr;
-    out->pinnedBytes = 0;
-    CUTCK(cudaMallocHost(&out->pinned, need));
-    out->pinnedBytes = need;
+  if (e->stageBytes < need) {
+    if (e->stage) cudaFreeHost(e->stage);
+    e->stage = nullptr;
+    e->stageBytes = 0;
+    CUTCK(cudaMallocHost(&e->stage, std::max<size_t>(need, 1 << 20)));
+    e->stageBytes = std::max<size_t>(need, 1 << 20);
   }
-  out->V = static_cast<float*>(out->pinned);
-  out->T = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(out->pinned) + 12 * outVTot);
-  if (outVTot) CUTCK(cudaMemcpyAsync(out->V, e->outV.p, 12 * outVTot, cudaMemcpyDeviceToHost, s));
-  if (outTTot) CUTCK(cudaMemcpyAsync(out->T, e->outT.p, 12 * outTTot, cudaMemcpyDeviceToHost, s));
+  out->host.resize((need + 3) / 4);
+  out->V = reinterpret_cast<float*>(out->host.data());
+  out->T = out->host.data() + 3 * outVTot;
+  float* stV = static_cast<float*>(e->stage);
+  uint32_t* stT = reinterpret_cast<uint32_t*>(static_cast<uint8_t*>(e->stage) + 12 * outVTot);
+  if (outVTot) CUTCK(cudaMemcpyAsync(stV, e->outV.p, 12 * outVTot, cudaMemcpyDeviceToHost, s));
+  if (outTTot) CUTCK(cudaMemcpyAsync(stT, e->outT.p, 12 * outTTot, cudaMemcpyDeviceToHost, s));
   CUTCK(cudaEventRecord(e->ev1, s));
   CUTCK(cudaStreamSynchronize(s));
+  std::memcpy(out->V, stV, 12 * outVTot);
+  std::memcpy(out->T, stT, 12 * outTTot);
   cudaEventElapsedTime(&out->gpuMs, e->ev0, e->ev1);
   return CUACD_OK;
 }
