@@ -384,7 +384,22 @@ __global__ void __launch_bounds__(HDS_M) k_hd_screen(const HdArgs A, const Dev D
       for (uint32_t j = 0; j < 32; j++) {
         const uint32_t k = c0 + j;
         if (k < cnt) {
-          // |p - c|^2 as screened, and its error bound 2^-13 (...)
+          // |p - c|^2 as screened, and its error bound e = 2^-13 (|p|^2 +
+          // |c|^2 + 2 |p|_1 |c|_1). Derivation (u = 2^-24, bf16 unit
+          // roundoff 2^-8): the hi/lo split leaves |x - x_hi - x_lo| <=
+          // 2^-16 |x| for every coordinate of p and of -2c and for |c|^2, so
+          // the split products miss at most 2^-14 sum|p_i||c_i| + 2^-16
+          // |c|^2; the bf16 x bf16 products are exact in fp32 and the 16-term
+          // accumulation (at most 15 roundings, each at most 2^-23 relative
+          // even if the tensor core truncates) adds at most 1.8e-6 (2
+          // sum|p_i||c_i| + |c|^2); |p|^2 and |c|^2 themselves are fp32 dot
+          // products (3u) and the final add one more u. In total e_true <=
+          // 6.5e-5 sum|p_i||c_i| + 1.8e-5 |c|^2 + 2.4e-7 |p|^2, which e
+          // exceeds by 3.8x, 7x and 500x (sum|p_i||c_i| <= |p|_1 |c|_1);
+          // the fp32 rounding of e, q2 + e and the square roots below are
+          // covered by the 1e-3 relative margin of the comparison. Far from
+          // the origin |p|^2 and -2 p.c cancel and e grows with them: the
+          // screen then keeps more triangles, never a wrong one.
           const float q2 = p2 + __uint_as_float(v[j]);
           const float e = 1.220703125e-4f * (p2 + sCC[k] + 2.0f * p1 * sC1[k]);
           ub = fminf(ub, q2 + e);

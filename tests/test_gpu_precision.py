@@ -8,7 +8,11 @@ Hausdorff distance by the oracle's restatement of src/cpu/hausdorff.ts (the
 same sampling rule, double arithmetic, exact nearest triangle through a BVH).
 
 The bounds asserted are the stated precision of each quantity:
-  tree child meshVol        1e-6 relative (compensated float32 flux terms)
+  tree child meshVol        1e-7 of the seed's volume absolute (float32
+                            flux terms, compensated sums: the error does
+                            not shrink with the part, so slivers show larger
+                            relative errors), and 1e-5 relative for children
+                            of at least 5 % of the seed's volume
   tree child hullVol        4e-6 relative (the hull's 2^21 integer grid)
   rv from tree volumes      2e-5 absolute
   cut half volume           1e-9 relative (fixed-order double sum)
@@ -67,7 +71,8 @@ def test_tree_volumes_and_rv_against_fp64():
     g.run([seed], [planes])
     n_jobs = 6 + g.plane_slots
     jobs = g.jobs(0, n_jobs)
-    errs = dict(meshVol=0.0, hullVol=0.0, rv=0.0)
+    errs = dict(meshVolAbs=0.0, meshVolRel=0.0, meshVolRelLarge=0.0, hullVol=0.0, rv=0.0)
+    seed_vol = abs(M.signed_volume(seed))
     n = 0
     for j in range(n_jobs):
         if jobs[j, 6] != 1:  # valid after plan
@@ -78,13 +83,18 @@ def test_tree_volumes_and_rv_against_fp64():
                 continue
             v64 = vol64_anchored(kid["mesh"], plane)
             h64 = hull64(kid["mesh"].verts)
-            errs["meshVol"] = max(errs["meshVol"], abs(kid["meshVol"] - v64) / v64)
+            err = abs(kid["meshVol"] - v64)
+            errs["meshVolAbs"] = max(errs["meshVolAbs"], err / seed_vol)
+            errs["meshVolRel"] = max(errs["meshVolRel"], err / v64)
+            if v64 >= 0.05 * seed_vol:
+                errs["meshVolRelLarge"] = max(errs["meshVolRelLarge"], err / v64)
             errs["hullVol"] = max(errs["hullVol"], abs(kid["hullVol"] - h64) / h64)
             errs["rv"] = max(errs["rv"], abs(P.rv_cost(kid["meshVol"], kid["hullVol"]) - P.rv_cost(v64, h64)))
             n += 1
-    print(f"tree level-0 children vs FP64 ({n} parts): {errs}")
+    print(f"tree level-0 children vs FP64 ({n} parts; meshVolAbs relative to the seed's volume): {errs}")
     assert n >= 40
-    assert errs["meshVol"] <= 1e-6 and errs["hullVol"] <= 4e-6 and errs["rv"] <= 2e-5
+    assert errs["meshVolAbs"] <= 1e-7 and errs["meshVolRelLarge"] <= 1e-5
+    assert errs["hullVol"] <= 4e-6 and errs["rv"] <= 2e-5
 
 
 def test_cut_evaluation_against_fp64(oracle):
