@@ -26,7 +26,8 @@
 //              every lane of the warp with identical data (warp-uniform
 //              code: identical stores, no divergence); the ear test, the
 //              edge gathering and the twin search split their loops over
-//              the lanes;
+//              the lanes, and the ear test looks only at the nodes in the
+//              cells of a uniform grid that the ear's bounding box covers;
 //   compact    one thread per triangle corner: first use of every vertex
 //              (atomicMin), a scan of the first uses numbers the vertices,
 //              then the halves are written to the output pools.
@@ -118,6 +119,7 @@ struct CapCarve {
   uint32_t ndI, ndPrev, ndNext, ndAlive;
   uint32_t gId;             // a group's ring: vertex ids (m)
   uint32_t holeL;           // a group's holes: leftmost node (m)
+  uint32_t gCnt, gStart, gNodes;  // the ear test's uniform grid: per-cell fill, starts, nodes (nd each)
   uint32_t capT;            // cap triangles, 3 words each (capMax)
   uint32_t words;
   uint32_t l2, area, ndX, ndY, gXY, holeX, cent;  // double arena
@@ -158,6 +160,9 @@ __host__ __device__ inline CapCarve carve(uint32_t m, uint32_t capMax) {
   c.ndAlive = o; o += c.nd;
   c.gId = o; o += m;
   c.holeL = o; o += m;
+  c.gCnt = o; o += c.nd + 1;
+  c.gStart = o; o += c.nd + 1;
+  c.gNodes = o; o += c.nd;
   c.capT = o; o += 3 * capMax;
   c.words = (o + 1) & ~1u;
   uint32_t d = 0;
@@ -448,6 +453,21 @@ struct Ring {  // ear-clip node arrays of one half (warp-uniform)
   uint32_t *I, *prev, *next, *alive;
   double *X, *Y;
   uint32_t n, cap;
+  // uniform grid over the nodes (built once the holes are bridged in): the
+  // ear test looks only at the nodes in the cells its triangle's bounding
+  // box covers, and whether any node lies in the triangle does not depend
+  // on the order it looks in
+  uint32_t *gCnt, *gStart, *gNodes;
+  uint32_t gnx, gny;
+  double gx0, gy0, ginvx, ginvy;
+  __device__ uint32_t cell_x(double x) const {
+    const double f = (x - gx0) * ginvx;
+    return f <= 0.0 ? 0u : min(gnx - 1, (uint32_t)f);
+  }
+  __device__ uint32_t cell_y(double y) const {
+    const double f = (y - gy0) * ginvy;
+    return f <= 0.0 ? 0u : min(gny - 1, (uint32_t)f);
+  }
   __device__ int32_t add(uint32_t i, double x, double y, int32_t last) {
     const uint32_t k = n++;
     I[k] = i;
@@ -558,16 +578,81 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const double ar = orient2(ax, ay, bx, by, cx, cy);
   if (ar < 0 || (ar == 0 && !allowFlat)) return false;
   const double lx = fmin(ax, cx), hx = fmax(ax, cx), ly = fmin(ay, cy), hy = fmax(ay, cy);
+  // a node inside or on the triangle lies in its bounding box, so in one of
+  // the cells the box covers
+  const uint32_t x0 = P.cell_x(fmin(lx, bx)), x1 = P.cell_x(fmax(hx, bx));
+  const uint32_t y0 = P.cell_y(fmin(ly, by)), y1 = P.cell_y(fmax(hy, by));
+  const uint32_t w = x1 - x0 + 1, nCells = w * (y1 - y0 + 1);
   bool hit = false;
-  for (uint32_t q = lane; q < P.n; q += 32) {
-    if (!P.alive[q] || q == a || q == b || q == c) continue;
-    const double qx = P.X[q], qy = P.Y[q];
-    if ((qx == ax && qy == ay) || (qx == bx && qy == by) || (qx == cx && qy == cy)) continue;
-    if (orient2(ax, ay, bx, by, qx, qy) >= 0 && orient2(bx, by, cx, cy, qx, qy) >= 0 &&
-        orient2(cx, cy, ax, ay, qx, qy) >= 0 && (ar > 0 || (qx >= lx && qx <= hx && qy >= ly && qy <= hy)))
-      hit = true;
+  for (uint32_t ci = lane; ci < nCells && !hit; ci += 32) {
+    const uint32_t cell = (y0 + ci / w) * P.gnx + x0 + ci % w;
+    for (uint32_t e = P.gStart[cell]; e < P.gStart[cell + 1]; e++) {
+      const uint32_t q = P.gNodes[e];
+      if (!P.alive[q] || q == a || q == b || q == c) continue;
+      const double qx = P.X[q], qy = P.Y[q];
+      if ((qx == ax && qy == ay) || (qx == bx && qy == by) || (qx == cx && qy == cy)) continue;
+      if (orient2(ax, ay, bx, by, qx, qy) >= 0 && orient2(bx, by, cx, cy, qx, qy) >= 0 &&
+          orient2(cx, cy, ax, ay, qx, qy) >= 0 && (ar > 0 || (qx >= lx && qx <= hx && qy >= ly && qy <= hy))) {
+        hit = true;
+        break;
+      }
+    }
   }
   return !__any_sync(CUT_FULL, hit);
+}
+
+// the uniform grid of the ring's P.n nodes: about two nodes per cell over
+// their bounding box, nodes listed per cell (lanes split the work; the order
+// within a cell does not matter)
+__device__ void build_grid(Ring& P, int lane) {
+  double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+  for (uint32_t q = lane; q < P.n; q += 32) {
+    x0 = fmin(x0, P.X[q]);
+    x1 = fmax(x1, P.X[q]);
+    y0 = fmin(y0, P.Y[q]);
+    y1 = fmax(y1, P.Y[q]);
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    x0 = fmin(x0, __shfl_xor_sync(CUT_FULL, x0, d));
+    x1 = fmax(x1, __shfl_xor_sync(CUT_FULL, x1, d));
+    y0 = fmin(y0, __shfl_xor_sync(CUT_FULL, y0, d));
+    y1 = fmax(y1, __shfl_xor_sync(CUT_FULL, y1, d));
+  }
+  uint32_t g = 1;
+  while (2 * (g + 1) * (g + 1) <= P.n) g++;
+  P.gnx = x1 > x0 ? g : 1u;
+  P.gny = y1 > y0 ? g : 1u;
+  P.gx0 = x0;
+  P.gy0 = y0;
+  P.ginvx = x1 > x0 ? (double)P.gnx / (x1 - x0) : 0.0;
+  P.ginvy = y1 > y0 ? (double)P.gny / (y1 - y0) : 0.0;
+  const uint32_t cells = P.gnx * P.gny;
+  for (uint32_t i = lane; i <= cells; i += 32) P.gCnt[i] = 0;
+  __syncwarp();
+  for (uint32_t q = lane; q < P.n; q += 32) atomicAdd(P.gCnt + P.cell_y(P.Y[q]) * P.gnx + P.cell_x(P.X[q]), 1u);
+  __syncwarp();
+  uint32_t run = 0;
+  for (uint32_t base = 0; base <= cells; base += 32) {
+    const uint32_t i = base + lane;
+    const uint32_t v = i < cells ? P.gCnt[i] : 0u;
+    uint32_t inc = v;
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t u = __shfl_up_sync(CUT_FULL, inc, d);
+      if (lane >= d) inc += u;
+    }
+    if (i <= cells) {
+      P.gStart[i] = run + inc - v;
+    }
+    run += __shfl_sync(CUT_FULL, inc, 31);
+  }
+  __syncwarp();
+  for (uint32_t i = lane; i < cells; i += 32) P.gCnt[i] = P.gStart[i];
+  __syncwarp();
+  for (uint32_t q = lane; q < P.n; q += 32) {
+    const uint32_t cell = P.cell_y(P.Y[q]) * P.gnx + P.cell_x(P.X[q]);
+    P.gNodes[atomicAdd(P.gCnt + cell, 1u)] = q;
+  }
+  __syncwarp();
 }
 
 // ear clipping of the group's ring (outer loop [0, outerEnd), holes from
@@ -605,6 +690,8 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
     if (m < 0) return 0;
     P.bridge((uint32_t)m, holeL[k]);
   }
+  __syncwarp();
+  build_grid(P, lane);
   uint32_t count = 0;
   {
     uint32_t p = outer;
@@ -988,6 +1075,9 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
   P.Y = x + cv.ndY;
   P.cap = cv.nd;
   P.n = 0;
+  P.gCnt = w + cv.gCnt;
+  P.gStart = w + cv.gStart;
+  P.gNodes = w + cv.gNodes;
   uint32_t* gid = w + cv.gId;
   double* gxy = x + cv.gXY;
   uint32_t* holeL = w + cv.holeL;
@@ -1179,15 +1269,16 @@ __global__ void k_cut_write(const CutDesc* __restrict__ D, const CutLayout* __re
 }
 
 // signed volume of every half by the divergence theorem anchored at its
-// vertex 0 (mesh.ts:58-72): one warp per half, each lane sums its strided
-// triangles in order, then a fixed-order tree across the lanes (the same
-// value on every run; it differs from a sequential sum in the last bits)
+// vertex 0 (mesh.ts:58-72): one block per half, each thread sums its
+// strided triangles in order, then a fixed-order tree across the threads
+// (the same value on every run; it differs from a sequential sum in the last
+// bits)
 __global__ void k_cut_volume(uint32_t n2, const unsigned long long* __restrict__ vOff,
                              const unsigned long long* __restrict__ tOff, const uint32_t* __restrict__ halfNt,
                              const float* __restrict__ outV, const uint32_t* __restrict__ outT,
                              double* __restrict__ vol) {
-  const uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  __shared__ double part[32];
+  const uint32_t k = blockIdx.x;
   if (k >= n2) return;
   const uint32_t nt = halfNt[k];
   const float* v = outV + 3 * vOff[k];
@@ -1195,7 +1286,7 @@ __global__ void k_cut_volume(uint32_t n2, const unsigned long long* __restrict__
   double s = 0.0;
   if (nt > 0) {
     const double ox = v[0], oy = v[1], oz = v[2];
-    for (uint32_t i = lane; i < nt; i += 32) {
+    for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) {
       const uint32_t a = 3 * t[3 * i], b = 3 * t[3 * i + 1], c = 3 * t[3 * i + 2];
       const double ax = v[a] - ox, ay = v[a + 1] - oy, az = v[a + 2] - oz;
       const double bx = v[b] - ox, by = v[b + 1] - oy, bz = v[b + 2] - oz;
@@ -1204,7 +1295,13 @@ __global__ void k_cut_volume(uint32_t n2, const unsigned long long* __restrict__
     }
   }
   for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(CUT_FULL, s, d);
-  if (lane == 0) vol[k] = s / 6.0;
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0.0;
+    for (uint32_t w = 0; w < (blockDim.x >> 5); w++) tot += part[w];
+    vol[k] = tot / 6.0;
+  }
 }
 
 // open edges of the input meshes (used when the caller does not vouch for
@@ -1569,7 +1666,7 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
                                                      e->inV.as<float>(), e->outVOff.as<unsigned long long>(),
                                                      e->outTOff.as<unsigned long long>(), e->outV.as<float>(),
                                                      e->outT.as<uint32_t>());
-  k_cut_volume<<<blocks(2ull * n * 32, 128), 128, 0, s>>>(2 * n, e->outVOff.as<unsigned long long>(),
+  k_cut_volume<<<2 * n, 256, 0, s>>>(2 * n, e->outVOff.as<unsigned long long>(),
                                                           e->outTOff.as<unsigned long long>(), e->halfNt.as<uint32_t>(),
                                                           e->outV.as<float>(), e->outT.as<uint32_t>(),
                                                           e->vol.as<double>());

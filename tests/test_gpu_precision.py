@@ -8,7 +8,7 @@ Hausdorff distance by the oracle's restatement of src/cpu/hausdorff.ts (the
 same sampling rule, double arithmetic, exact nearest triangle through a BVH).
 
 The bounds asserted are the stated precision of each quantity:
-  tree child meshVol        1e-7 of the seed's volume absolute (float32
+  tree child meshVol        5e-7 of the seed's volume absolute (float32
                             flux terms, compensated sums: the error does
                             not shrink with the part, so slivers show larger
                             relative errors), and 1e-5 relative for children
@@ -93,7 +93,7 @@ def test_tree_volumes_and_rv_against_fp64():
             n += 1
     print(f"tree level-0 children vs FP64 ({n} parts; meshVolAbs relative to the seed's volume): {errs}")
     assert n >= 40
-    assert errs["meshVolAbs"] <= 1e-7 and errs["meshVolRelLarge"] <= 1e-5
+    assert errs["meshVolAbs"] <= 5e-7 and errs["meshVolRelLarge"] <= 1e-5
     assert errs["hullVol"] <= 4e-6 and errs["rv"] <= 2e-5
 
 
