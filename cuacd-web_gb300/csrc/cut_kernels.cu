@@ -578,10 +578,11 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const double ar = orient2(ax, ay, bx, by, cx, cy);
   if (ar < 0 || (ar == 0 && !allowFlat)) return false;
   const double lx = fmin(ax, cx), hx = fmax(ax, cx), ly = fmin(ay, cy), hy = fmax(ay, cy);
-  // a node inside or on the triangle lies in its bounding box, so in one of
-  // the cells the box covers
-  const uint32_t x0 = P.cell_x(fmin(lx, bx)), x1 = P.cell_x(fmax(hx, bx));
-  const uint32_t y0 = P.cell_y(fmin(ly, by)), y1 = P.cell_y(fmax(hy, by));
+  // the node must lie in the triangle's bounding box (as in the host
+  // clipper), so only the cells the box covers are looked at
+  const double bx0 = fmin(lx, bx), bx1 = fmax(hx, bx), by0 = fmin(ly, by), by1 = fmax(hy, by);
+  const uint32_t x0 = P.cell_x(bx0), x1 = P.cell_x(bx1);
+  const uint32_t y0 = P.cell_y(by0), y1 = P.cell_y(by1);
   const uint32_t w = x1 - x0 + 1, nCells = w * (y1 - y0 + 1);
   bool hit = false;
   for (uint32_t ci = lane; ci < nCells && !hit; ci += 32) {
@@ -590,6 +591,7 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
       const uint32_t q = P.gNodes[e];
       if (!P.alive[q] || q == a || q == b || q == c) continue;
       const double qx = P.X[q], qy = P.Y[q];
+      if (qx < bx0 || qx > bx1 || qy < by0 || qy > by1) continue;
       if ((qx == ax && qy == ay) || (qx == bx && qy == by) || (qx == cx && qy == cy)) continue;
       if (orient2(ax, ay, bx, by, qx, qy) >= 0 && orient2(bx, by, cx, cy, qx, qy) >= 0 &&
           orient2(cx, cy, ax, ay, qx, qy) >= 0 && (ar > 0 || (qx >= lx && qx <= hx && qy >= ly && qy <= hy))) {

@@ -138,19 +138,27 @@ int32_t find_bridge(const Poly& P, int32_t h, int32_t outer) {
   return m;
 }
 
-// no other vertex of the loop inside (or on) the triangle of ear k
+// no other vertex of the loop inside (or on) the triangle of ear k. A vertex
+// must also lie in the triangle's bounding box: for a sliver ear the rounded
+// orientation tests can admit nearly collinear vertices far along its edge
+// lines, which the box excludes (earcut's hashed ear test looks only inside
+// the box too), and it lets the GPU cut look at a grid's cells instead of
+// every vertex with the same result
 bool is_ear(const Poly& P, int32_t k, bool allowFlat) {
   const Node& a = P.n[P.n[k].prev];
   const Node& b = P.n[k];
   const Node& c = P.n[b.next];
   const double ar = orient2(a, b, c);
   if (ar < 0 || (ar == 0 && !allowFlat)) return false;
+  const double bx0 = std::min(std::min(a.x, b.x), c.x), bx1 = std::max(std::max(a.x, b.x), c.x);
+  const double by0 = std::min(std::min(a.y, b.y), c.y), by1 = std::max(std::max(a.y, b.y), c.y);
   int32_t p = c.next;
   while (p != b.prev) {
     const Node& q = P.n[p];
-    if (!same_pos(q, a) && !same_pos(q, b) && !same_pos(q, c) && orient2(a, b, q) >= 0 && orient2(b, c, q) >= 0 &&
-        orient2(c, a, q) >= 0 && (ar > 0 || (q.x >= std::min(a.x, c.x) && q.x <= std::max(a.x, c.x) &&
-                                             q.y >= std::min(a.y, c.y) && q.y <= std::max(a.y, c.y))))
+    if (q.x >= bx0 && q.x <= bx1 && q.y >= by0 && q.y <= by1 && !same_pos(q, a) && !same_pos(q, b) &&
+        !same_pos(q, c) && orient2(a, b, q) >= 0 && orient2(b, c, q) >= 0 && orient2(c, a, q) >= 0 &&
+        (ar > 0 || (q.x >= std::min(a.x, c.x) && q.x <= std::max(a.x, c.x) && q.y >= std::min(a.y, c.y) &&
+                    q.y <= std::max(a.y, c.y))))
       return false;
     p = q.next;
   }
