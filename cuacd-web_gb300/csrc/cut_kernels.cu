@@ -104,6 +104,10 @@ struct CutOut {
 enum { CUT_OK = 0, CUT_NO_SPLIT = 1, CUT_OPEN_CHAIN = 2, CUT_DEAD_END = 3, CUT_CYCLE = 4, CUT_SCRATCH = 5 };
 
 constexpr double ON_PLANE_EPS = 1e-6;  // the host cut's default eps
+// ear-clip nodes a cap warp keeps in shared memory (X, Y, index, links,
+// alive flag, grid: 36 bytes each plus the cell starts)
+constexpr uint32_t CAP_SM_NODES = 2048;
+constexpr size_t CAP_SM_BYTES = 16 * CAP_SM_NODES + 4 * 5 * CAP_SM_NODES + 4 * 2 * (CAP_SM_NODES / 2 + 2);
 constexpr unsigned long long EMPTY_KEY = ~0ull;
 
 // the cap step's scratch of one half, carved from m = its plane-edge bound
@@ -520,6 +524,37 @@ struct Ring {  // ear-clip node arrays of one half (warp-uniform)
   }
 };
 
+// ring vertices [s, e) of the group as nodes P.n .. P.n + (e - s) - 1,
+// counter-clockwise (ccw) or clockwise, as Ring::ring adds them (nodes in
+// creation order, each linked after the previous): the signed area's terms
+// in parallel and their sum in order, then every node at once; returns the
+// last node
+__device__ uint32_t ring_par(Ring& P, const double* gxy, uint32_t s, uint32_t e, bool ccw, int lane) {
+  const uint32_t base = P.n, len = e - s;
+  double* terms = P.X + base;  // scratch until the nodes are written
+  for (uint32_t i = lane; i < len; i += 32) {
+    const uint32_t k = s + i, j = k + 1 < e ? k + 1 : s;
+    terms[i] = gxy[2 * k] * gxy[2 * j + 1] - gxy[2 * j] * gxy[2 * k + 1];
+  }
+  __syncwarp();
+  double a = 0;
+  for (uint32_t i = 0; i < len; i++) a += terms[i];
+  __syncwarp();
+  const bool fwd = (a > 0) == ccw;
+  for (uint32_t i = lane; i < len; i += 32) {
+    const uint32_t k = fwd ? s + i : e - 1 - i, nd = base + i;
+    P.I[nd] = k;
+    P.X[nd] = gxy[2 * k];
+    P.Y[nd] = gxy[2 * k + 1];
+    P.alive[nd] = 1;
+    P.next[nd] = base + (i + 1 == len ? 0 : i + 1);
+    P.prev[nd] = base + (i == 0 ? len - 1 : i - 1);
+  }
+  __syncwarp();
+  P.n = base + len;
+  return base + len - 1;
+}
+
 // an outer vertex visible from hole vertex h (leftmost of its loop), as the
 // host clipper's find_bridge: the nearest crossing of the leftward ray with
 // a downward edge of the counter-clockwise outer loop, its endpoint of larger
@@ -665,12 +700,12 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
   P.n = 0;
   const uint32_t outerEnd = nHoles == 0 ? nAll : hs[0];
   if (outerEnd < 3) return 0;
-  const uint32_t outer = (uint32_t)P.ring(gid, gxy, 0, outerEnd, true);
+  const uint32_t outer = ring_par(P, gxy, 0, outerEnd, true, lane);
   uint32_t nh = 0;
   for (uint32_t k = 0; k < nHoles; k++) {
     const uint32_t s = hs[k], e = k + 1 < nHoles ? hs[k + 1] : nAll;
     if (e <= s) continue;
-    const uint32_t h = (uint32_t)P.ring(gid, gxy, s, e, false);
+    const uint32_t h = ring_par(P, gxy, s, e, false, lane);
     uint32_t left = h, p = h;
     do {
       if (P.X[p] < P.X[left] || (P.X[p] == P.X[left] && P.Y[p] < P.Y[left])) left = p;
@@ -769,7 +804,8 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
                           const float* __restrict__ V, uint32_t* __restrict__ W, double* __restrict__ X,
                           const uint32_t* __restrict__ Tin, const uint8_t* __restrict__ openBits,
                           const unsigned long long* __restrict__ hashKeys) {
-  const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  extern __shared__ __align__(16) unsigned char capSm[];
+  const uint32_t gw = blockIdx.x;  // one warp per block
   const int lane = threadIdx.x & 31;
   if (gw >= 2 * n) return;
   const uint32_t c = gw >> 1, side = gw & 1;
@@ -958,28 +994,35 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
   }
   __syncwarp();
   if (nLoops == 0) return;
-  // 5. loop coordinates in the plane's basis and signed areas (a lane per loop)
+  // 5. loop coordinates in the plane's basis (every loop vertex at once) and
+  // signed areas: the terms at once, each loop's sum in order by one lane
   double* l2 = x + cv.l2;
   double* area = x + cv.area;
-  for (uint32_t li = lane; li < nLoops; li += 32) {
+  double* terms = x + cv.gXY;  // scratch until the groups are assembled
+  for (uint32_t k = lane; k < nLV; k += 32) {
+    double px, py, pz;
+    ctx.pos(loopV[k], px, py, pz);
+    double a = px * d.u[0];
+    a = a + py * d.u[1];
+    a = a + pz * d.u[2];
+    double b = px * d.w[0];
+    b = b + py * d.w[1];
+    b = b + pz * d.w[2];
+    l2[2 * k] = a;
+    l2[2 * k + 1] = b;
+  }
+  __syncwarp();
+  for (uint32_t li = 0; li < nLoops; li++) {
     const uint32_t s0 = loopS[li], e0 = loopS[li + 1];
-    for (uint32_t k = s0; k < e0; k++) {
-      double px, py, pz;
-      ctx.pos(loopV[k], px, py, pz);
-      double a = px * d.u[0];
-      a = a + py * d.u[1];
-      a = a + pz * d.u[2];
-      double b = px * d.w[0];
-      b = b + py * d.w[1];
-      b = b + pz * d.w[2];
-      l2[2 * k] = a;
-      l2[2 * k + 1] = b;
-    }
-    double s = 0;
-    for (uint32_t k = s0; k < e0; k++) {
+    for (uint32_t k = s0 + lane; k < e0; k += 32) {
       const uint32_t j = k + 1 < e0 ? k + 1 : s0;
-      s += l2[2 * k] * l2[2 * j + 1] - l2[2 * j] * l2[2 * k + 1];
+      terms[k] = l2[2 * k] * l2[2 * j + 1] - l2[2 * j] * l2[2 * k + 1];
     }
+  }
+  __syncwarp();
+  for (uint32_t li = lane; li < nLoops; li += 32) {
+    double s = 0;
+    for (uint32_t k = loopS[li]; k < loopS[li + 1]; k++) s += terms[k];
     area[li] = s / 2;
   }
   __syncwarp();
@@ -1068,36 +1111,55 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
       failWith(CUT_SCRATCH);
       return;
     }
-  Ring P;
-  P.I = w + cv.ndI;
-  P.prev = w + cv.ndPrev;
-  P.next = w + cv.ndNext;
-  P.alive = w + cv.ndAlive;
-  P.X = x + cv.ndX;
-  P.Y = x + cv.ndY;
-  P.cap = cv.nd;
-  P.n = 0;
-  P.gCnt = w + cv.gCnt;
-  P.gStart = w + cv.gStart;
-  P.gNodes = w + cv.gNodes;
+  // the ear clipper's nodes and grid: in shared memory when the group fits
+  // CAP_SM_NODES nodes, else in the global scratch
+  Ring Pg;
+  Pg.I = w + cv.ndI;
+  Pg.prev = w + cv.ndPrev;
+  Pg.next = w + cv.ndNext;
+  Pg.alive = w + cv.ndAlive;
+  Pg.X = x + cv.ndX;
+  Pg.Y = x + cv.ndY;
+  Pg.cap = cv.nd;
+  Pg.n = 0;
+  Pg.gCnt = w + cv.gCnt;
+  Pg.gStart = w + cv.gStart;
+  Pg.gNodes = w + cv.gNodes;
+  Ring Ps;
+  {
+    double* sx = reinterpret_cast<double*>(capSm);
+    Ps.X = sx;
+    Ps.Y = sx + CAP_SM_NODES;
+    uint32_t* su = reinterpret_cast<uint32_t*>(sx + 2 * CAP_SM_NODES);
+    Ps.I = su;
+    Ps.prev = su + CAP_SM_NODES;
+    Ps.next = su + 2 * CAP_SM_NODES;
+    Ps.alive = su + 3 * CAP_SM_NODES;
+    Ps.gNodes = su + 4 * CAP_SM_NODES;
+    Ps.gCnt = su + 5 * CAP_SM_NODES;
+    Ps.gStart = Ps.gCnt + CAP_SM_NODES / 2 + 2;
+    Ps.cap = CAP_SM_NODES;
+    Ps.n = 0;
+  }
   uint32_t* gid = w + cv.gId;
   double* gxy = x + cv.gXY;
   uint32_t* holeL = w + cv.holeL;
   double* holeX = x + cv.holeX;
   for (uint32_t i = 0; i < nLoops; i++) {
     if (fabs(area[i]) < 1e-18 || depth[i] % 2 != 0) continue;
-    // the group's ring: the outer loop, then its holes in loop order; the
-    // hole starts go to the end of the depth array's unused tail is not
-    // needed: holeStart values are kept in `parent`-free scratch (starts)
+    // the group's ring: the outer loop, then its holes in loop order (hole
+    // starts kept in `starts`, free once the loops are walked); the loops'
+    // vertices are copied by all lanes at once
     uint32_t nAll = 0, nHoles = 0;
-    uint32_t* hs = starts;  // reused: the loop walk is done
+    uint32_t* hs = starts;
     auto append = [&](uint32_t li) {
-      for (uint32_t k = loopS[li]; k < loopS[li + 1]; k++) {
-        gid[nAll] = loopV[k];
-        gxy[2 * nAll] = l2[2 * k];
-        gxy[2 * nAll + 1] = l2[2 * k + 1];
-        nAll++;
+      const uint32_t s0 = loopS[li], len = loopS[li + 1] - s0;
+      for (uint32_t q = lane; q < len; q += 32) {
+        gid[nAll + q] = loopV[s0 + q];
+        gxy[2 * (nAll + q)] = l2[2 * (s0 + q)];
+        gxy[2 * (nAll + q) + 1] = l2[2 * (s0 + q) + 1];
       }
+      nAll += len;
     };
     append(i);
     for (uint32_t j = 0; j < nLoops; j++)
@@ -1105,7 +1167,9 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
         hs[nHoles++] = nAll;
         append(j);
       }
+    __syncwarp();
     const uint32_t expected = nAll + 2 * nHoles - 2;
+    Ring& P = nAll + 2 * nHoles <= Ps.cap ? Ps : Pg;
     if (nCap + nAll + 2 * nHoles > capMax || nAll + 2 * nHoles > P.cap) {
       failWith(CUT_SCRATCH);
       return;
@@ -1125,9 +1189,11 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
         }
       continue;
     }
-    // one flip for the whole cap, decided by its largest triangle
+    // one flip for the whole cap, decided by its largest triangle (the
+    // first of the largest |n . normal|, as a sequential scan keeps it)
     double bestAbs = 0, bestDot = 0;
-    for (uint32_t k = 0; k < got; k++) {
+    uint32_t bestK = CUT_NONE;
+    for (uint32_t k = lane; k < got; k += 32) {
       const uint32_t* t = capT + 3 * (nCap + k);
       double p0x, p0y, p0z, p1x, p1y, p1z, p2x, p2y, p2z;
       ctx.pos(gid[t[0]], p0x, p0y, p0z);
@@ -1142,17 +1208,28 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
       if (fabs(dd) > bestAbs) {
         bestAbs = fabs(dd);
         bestDot = dd;
+        bestK = k;
+      }
+    }
+    for (int dl = 16; dl > 0; dl >>= 1) {
+      const double oa = __shfl_xor_sync(CUT_FULL, bestAbs, dl), od = __shfl_xor_sync(CUT_FULL, bestDot, dl);
+      const uint32_t ok = __shfl_xor_sync(CUT_FULL, bestK, dl);
+      if (oa > bestAbs || (oa == bestAbs && ok < bestK)) {
+        bestAbs = oa;
+        bestDot = od;
+        bestK = ok;
       }
     }
     const bool flip = bestDot * dir < 0;
     __syncwarp();
-    for (uint32_t k = 0; k < got; k++) {
+    for (uint32_t k = lane; k < got; k += 32) {
       uint32_t* t = capT + 3 * (nCap + k);
       const uint32_t a = gid[t[0]], b = gid[t[1]], cc = gid[t[2]];
       t[0] = a;
       t[1] = flip ? cc : b;
       t[2] = flip ? b : cc;
     }
+    __syncwarp();
     nCap += got;
     __syncwarp();
   }
@@ -1614,7 +1691,10 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
                                                       e->sgn.as<int8_t>(), e->pre.as<uint4>(),
                                                       e->hashKeys.as<unsigned long long>(), e->hashXYZ.as<double>(),
                                                       e->surfT.as<uint32_t>(), e->candE.as<uint2>(), dOpen, dO);
-  k_cut_cap<<<blocks(2ull * n * 32, 128), 128, 0, s>>>(dD, dL, dO, n, e->surfT.as<uint32_t>(), e->candE.as<uint2>(),
+  // the cap warps' shared ring (above the 48 KB default); set on every run,
+  // so it holds on whichever device is current
+  CUTCK(cudaFuncSetAttribute(k_cut_cap, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CAP_SM_BYTES));
+  k_cut_cap<<<2 * n, 32, CAP_SM_BYTES, s>>>(dD, dL, dO, n, e->surfT.as<uint32_t>(), e->candE.as<uint2>(),
                                                        e->sgn.as<int8_t>(), e->hashXYZ.as<double>(),
                                                        e->inV.as<float>(), e->words.as<uint32_t>(),
                                                        e->dbls.as<double>(), e->inT.as<uint32_t>(), dOpen,
