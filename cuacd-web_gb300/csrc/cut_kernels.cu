@@ -104,10 +104,11 @@ struct CutOut {
 enum { CUT_OK = 0, CUT_NO_SPLIT = 1, CUT_OPEN_CHAIN = 2, CUT_DEAD_END = 3, CUT_CYCLE = 4, CUT_SCRATCH = 5 };
 
 constexpr double ON_PLANE_EPS = 1e-6;  // the host cut's default eps
-// ear-clip nodes a cap warp keeps in shared memory (X, Y, index, links,
-// alive flag, grid: 36 bytes each plus the cell starts)
+// ear-clip nodes a cap warp keeps in shared memory (X, Y, their float
+// copies, index, links, alive flag, grid: 44 bytes each plus the cell starts)
 constexpr uint32_t CAP_SM_NODES = 2048;
-constexpr size_t CAP_SM_BYTES = 16 * CAP_SM_NODES + 4 * 5 * CAP_SM_NODES + 4 * 2 * (CAP_SM_NODES / 2 + 2);
+constexpr size_t CAP_SM_BYTES = 16 * CAP_SM_NODES + 4 * 5 * CAP_SM_NODES + 4 * 2 * (CAP_SM_NODES / 2 + 2) +
+                                8 * CAP_SM_NODES;
 constexpr unsigned long long EMPTY_KEY = ~0ull;
 
 // the cap step's scratch of one half, carved from m = its plane-edge bound
@@ -124,6 +125,7 @@ struct CapCarve {
   uint32_t gId;             // a group's ring: vertex ids (m)
   uint32_t holeL;           // a group's holes: leftmost node (m)
   uint32_t gCnt, gStart, gNodes;  // the ear test's uniform grid: per-cell fill, starts, nodes (nd each)
+  uint32_t ndXf, ndYf;      // the nodes' float32 coordinates (nd each)
   uint32_t capT;            // cap triangles, 3 words each (capMax)
   uint32_t words;
   uint32_t l2, area, ndX, ndY, gXY, holeX, cent;  // double arena
@@ -167,6 +169,8 @@ __host__ __device__ inline CapCarve carve(uint32_t m, uint32_t capMax) {
   c.gCnt = o; o += c.nd + 1;
   c.gStart = o; o += c.nd + 1;
   c.gNodes = o; o += c.nd;
+  c.ndXf = o; o += c.nd;
+  c.ndYf = o; o += c.nd;
   c.capT = o; o += 3 * capMax;
   c.words = (o + 1) & ~1u;
   uint32_t d = 0;
@@ -456,59 +460,29 @@ __device__ uint32_t uh_find(uint32_t* keys, uint32_t size, uint32_t key, bool in
 struct Ring {  // ear-clip node arrays of one half (warp-uniform)
   uint32_t *I, *prev, *next, *alive;
   double *X, *Y;
+  float *Xf, *Yf;  // the coordinates rounded to float32 (the ear test's prefilter)
   uint32_t n, cap;
-  // uniform grid over the nodes (built once the holes are bridged in): the
-  // ear test looks only at the nodes in the cells its triangle's bounding
-  // box covers, and whether any node lies in the triangle does not depend
-  // on the order it looks in
+  // uniform grid over the nodes (built once the holes are bridged in), in
+  // the float32 coordinates: the ear test looks only at the nodes in the
+  // cells its triangle's bounding box covers (rounding is monotonic, so a
+  // node inside the box falls in a covered cell), and whether any node lies
+  // in the triangle does not depend on the order it looks in
   uint32_t *gCnt, *gStart, *gNodes;
   uint32_t gnx, gny;
-  double gx0, gy0, ginvx, ginvy;
-  __device__ uint32_t cell_x(double x) const {
-    const double f = (x - gx0) * ginvx;
-    return f <= 0.0 ? 0u : min(gnx - 1, (uint32_t)f);
+  float gx0, gy0, ginvx, ginvy;
+  __device__ uint32_t cell_x(float x) const {
+    const float f = (x - gx0) * ginvx;
+    return f <= 0.0f ? 0u : min(gnx - 1, (uint32_t)f);
   }
-  __device__ uint32_t cell_y(double y) const {
-    const double f = (y - gy0) * ginvy;
-    return f <= 0.0 ? 0u : min(gny - 1, (uint32_t)f);
-  }
-  __device__ int32_t add(uint32_t i, double x, double y, int32_t last) {
-    const uint32_t k = n++;
-    I[k] = i;
-    X[k] = x;
-    Y[k] = y;
-    alive[k] = 1;
-    if (last < 0) {
-      prev[k] = next[k] = k;
-    } else {
-      next[k] = next[last];
-      prev[k] = (uint32_t)last;
-      prev[next[last]] = k;
-      next[last] = k;
-    }
-    return (int32_t)k;
-  }
-  // ring vertices [s, e) of the group, counter-clockwise (ccw) or clockwise
-  __device__ int32_t ring(const uint32_t* gid, const double* gxy, uint32_t s, uint32_t e, bool ccw) {
-    double a = 0;
-    for (uint32_t k = s; k < e; k++) {
-      const uint32_t j = k + 1 < e ? k + 1 : s;
-      a += gxy[2 * k] * gxy[2 * j + 1] - gxy[2 * j] * gxy[2 * k + 1];
-    }
-    int32_t last = -1;
-    if ((a > 0) == ccw) {
-      for (uint32_t k = s; k < e; k++) last = add(k, gxy[2 * k], gxy[2 * k + 1], last);
-    } else {
-      for (uint32_t k = e; k-- > s;) last = add(k, gxy[2 * k], gxy[2 * k + 1], last);
-    }
-    (void)gid;
-    return last;
+  __device__ uint32_t cell_y(float y) const {
+    const float f = (y - gy0) * ginvy;
+    return f <= 0.0f ? 0u : min(gny - 1, (uint32_t)f);
   }
   __device__ void bridge(uint32_t a, uint32_t b) {
     const uint32_t a2 = n++;
-    I[a2] = I[a]; X[a2] = X[a]; Y[a2] = Y[a]; alive[a2] = 1;
+    I[a2] = I[a]; X[a2] = X[a]; Y[a2] = Y[a]; Xf[a2] = Xf[a]; Yf[a2] = Yf[a]; alive[a2] = 1;
     const uint32_t b2 = n++;
-    I[b2] = I[b]; X[b2] = X[b]; Y[b2] = Y[b]; alive[b2] = 1;
+    I[b2] = I[b]; X[b2] = X[b]; Y[b2] = Y[b]; Xf[b2] = Xf[b]; Yf[b2] = Yf[b]; alive[b2] = 1;
     const uint32_t an = next[a], bp = prev[b];
     next[a] = b;
     prev[b] = a;
@@ -525,10 +499,10 @@ struct Ring {  // ear-clip node arrays of one half (warp-uniform)
 };
 
 // ring vertices [s, e) of the group as nodes P.n .. P.n + (e - s) - 1,
-// counter-clockwise (ccw) or clockwise, as Ring::ring adds them (nodes in
-// creation order, each linked after the previous): the signed area's terms
-// in parallel and their sum in order, then every node at once; returns the
-// last node
+// counter-clockwise (ccw) or clockwise, as the host clipper's ring() adds
+// them (nodes in creation order, each linked after the previous): the
+// signed area's terms in parallel and their sum in order, then every node at
+// once; returns the last node
 __device__ uint32_t ring_par(Ring& P, const double* gxy, uint32_t s, uint32_t e, bool ccw, int lane) {
   const uint32_t base = P.n, len = e - s;
   double* terms = P.X + base;  // scratch until the nodes are written
@@ -546,6 +520,8 @@ __device__ uint32_t ring_par(Ring& P, const double* gxy, uint32_t s, uint32_t e,
     P.I[nd] = k;
     P.X[nd] = gxy[2 * k];
     P.Y[nd] = gxy[2 * k + 1];
+    P.Xf[nd] = (float)gxy[2 * k];
+    P.Yf[nd] = (float)gxy[2 * k + 1];
     P.alive[nd] = 1;
     P.next[nd] = base + (i + 1 == len ? 0 : i + 1);
     P.prev[nd] = base + (i == 0 ? len - 1 : i - 1);
@@ -605,8 +581,37 @@ __device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
   return m;
 }
 
+// orient2 in float32 of float-rounded coordinates, and whether it decides
+// the sign of the double orient2 of the original coordinates: with u = 2^-24
+// and S the largest coordinate magnitude, the float result is within 48.5 u
+// S^2 of the exact value (inputs rounded to float: 2 u S per difference,
+// then three roundings) and the double result within 1e-14 S^2 of it, so a
+// float result beyond 50 u S^2 has the double result's sign (and is not 0)
+__device__ __forceinline__ float orient2f(float ax, float ay, float bx, float by, float cx, float cy) {
+  return __fsub_rn(__fmul_rn(__fsub_rn(bx, ax), __fsub_rn(cy, ay)), __fmul_rn(__fsub_rn(by, ay), __fsub_rn(cx, ax)));
+}
+
+// the double test orient2(a, b, c) >= 0, decided in float when the float
+// value is clear of its error bound e (e < 0: always in double)
+__device__ __forceinline__ bool orient_nonneg(const Ring& P, uint32_t a, uint32_t b, uint32_t c, float e) {
+  if (e >= 0.0f) {
+    const float o = orient2f(P.Xf[a], P.Yf[a], P.Xf[b], P.Yf[b], P.Xf[c], P.Yf[c]);
+    if (o > e) return true;
+    if (o < -e) return false;
+  }
+  return orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]) >= 0;
+}
+
+// x >= b exactly, from the float roundings unless they tie (rounding is
+// monotonic: fl(x) < fl(b) implies x < b, fl(x) > fl(b) implies x > b)
+__device__ __forceinline__ bool ge_exact(float xf, double x, float bf, double b) {
+  return xf != bf ? xf > bf : x >= b;
+}
+
 // no other live node inside (or on) the triangle of ear k; the lanes split
-// the nodes and vote
+// the nodes and vote. Each node test is the host clipper's double test; the
+// float copies decide it exactly where they can, and the double arithmetic
+// (slow on this GPU) runs only for ties and near-zero orientations
 __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const uint32_t a = P.prev[k], b = k, c = P.next[k];
   const double ax = P.X[a], ay = P.Y[a], bx = P.X[b], by = P.Y[b], cx = P.X[c], cy = P.Y[c];
@@ -616,20 +621,34 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   // the node must lie in the triangle's bounding box (as in the host
   // clipper), so only the cells the box covers are looked at
   const double bx0 = fmin(lx, bx), bx1 = fmax(hx, bx), by0 = fmin(ly, by), by1 = fmax(hy, by);
-  const uint32_t x0 = P.cell_x(bx0), x1 = P.cell_x(bx1);
-  const uint32_t y0 = P.cell_y(by0), y1 = P.cell_y(by1);
+  const float fbx0 = (float)bx0, fbx1 = (float)bx1, fby0 = (float)by0, fby1 = (float)by1;
+  const uint32_t x0 = P.cell_x(fbx0), x1 = P.cell_x(fbx1);
+  const uint32_t y0 = P.cell_y(fby0), y1 = P.cell_y(fby1);
   const uint32_t w = x1 - x0 + 1, nCells = w * (y1 - y0 + 1);
+  const float axf = P.Xf[a], ayf = P.Yf[a], bxf = P.Xf[b], byf = P.Yf[b], cxf = P.Xf[c], cyf = P.Yf[c];
+  const float s3 = fmaxf(fmaxf(fmaxf(fabsf(axf), fabsf(ayf)), fmaxf(fabsf(bxf), fabsf(byf))),
+                         fmaxf(fabsf(cxf), fabsf(cyf)));
   bool hit = false;
   for (uint32_t ci = lane; ci < nCells && !hit; ci += 32) {
     const uint32_t cell = (y0 + ci / w) * P.gnx + x0 + ci % w;
     for (uint32_t e = P.gStart[cell]; e < P.gStart[cell + 1]; e++) {
       const uint32_t q = P.gNodes[e];
       if (!P.alive[q] || q == a || q == b || q == c) continue;
+      const float qxf = P.Xf[q], qyf = P.Yf[q];
       const double qx = P.X[q], qy = P.Y[q];
-      if (qx < bx0 || qx > bx1 || qy < by0 || qy > by1) continue;
-      if ((qx == ax && qy == ay) || (qx == bx && qy == by) || (qx == cx && qy == cy)) continue;
-      if (orient2(ax, ay, bx, by, qx, qy) >= 0 && orient2(bx, by, cx, cy, qx, qy) >= 0 &&
-          orient2(cx, cy, ax, ay, qx, qy) >= 0 && (ar > 0 || (qx >= lx && qx <= hx && qy >= ly && qy <= hy))) {
+      // in the bounding box, exactly
+      if (!ge_exact(qxf, qx, fbx0, bx0) || !ge_exact(fbx1, bx1, qxf, qx) || !ge_exact(qyf, qy, fby0, by0) ||
+          !ge_exact(fby1, by1, qyf, qy))
+        continue;
+      // not at a corner's position (equal doubles have equal floats)
+      if ((qxf == axf && qyf == ayf && qx == ax && qy == ay) || (qxf == bxf && qyf == byf && qx == bx && qy == by) ||
+          (qxf == cxf && qyf == cyf && qx == cx && qy == cy))
+        continue;
+      const float s = fmaxf(s3, fmaxf(fabsf(qxf), fabsf(qyf)));
+      // 52 u S^2, or the double path when S^2 is out of float range
+      const float eb = (s > 1e-15f && s < 1e15f) ? 52.0f * 5.9604645e-8f * s * s : -1.0f;
+      if (orient_nonneg(P, a, b, q, eb) && orient_nonneg(P, b, c, q, eb) && orient_nonneg(P, c, a, q, eb) &&
+          (ar > 0 || (qx >= lx && qx <= hx && qy >= ly && qy <= hy))) {
         hit = true;
         break;
       }
@@ -642,18 +661,18 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
 // their bounding box, nodes listed per cell (lanes split the work; the order
 // within a cell does not matter)
 __device__ void build_grid(Ring& P, int lane) {
-  double x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
+  float x0 = INFINITY, y0 = INFINITY, x1 = -INFINITY, y1 = -INFINITY;
   for (uint32_t q = lane; q < P.n; q += 32) {
-    x0 = fmin(x0, P.X[q]);
-    x1 = fmax(x1, P.X[q]);
-    y0 = fmin(y0, P.Y[q]);
-    y1 = fmax(y1, P.Y[q]);
+    x0 = fminf(x0, P.Xf[q]);
+    x1 = fmaxf(x1, P.Xf[q]);
+    y0 = fminf(y0, P.Yf[q]);
+    y1 = fmaxf(y1, P.Yf[q]);
   }
   for (int d = 16; d > 0; d >>= 1) {
-    x0 = fmin(x0, __shfl_xor_sync(CUT_FULL, x0, d));
-    x1 = fmax(x1, __shfl_xor_sync(CUT_FULL, x1, d));
-    y0 = fmin(y0, __shfl_xor_sync(CUT_FULL, y0, d));
-    y1 = fmax(y1, __shfl_xor_sync(CUT_FULL, y1, d));
+    x0 = fminf(x0, __shfl_xor_sync(CUT_FULL, x0, d));
+    x1 = fmaxf(x1, __shfl_xor_sync(CUT_FULL, x1, d));
+    y0 = fminf(y0, __shfl_xor_sync(CUT_FULL, y0, d));
+    y1 = fmaxf(y1, __shfl_xor_sync(CUT_FULL, y1, d));
   }
   uint32_t g = 1;
   while (2 * (g + 1) * (g + 1) <= P.n) g++;
@@ -661,12 +680,12 @@ __device__ void build_grid(Ring& P, int lane) {
   P.gny = y1 > y0 ? g : 1u;
   P.gx0 = x0;
   P.gy0 = y0;
-  P.ginvx = x1 > x0 ? (double)P.gnx / (x1 - x0) : 0.0;
-  P.ginvy = y1 > y0 ? (double)P.gny / (y1 - y0) : 0.0;
+  P.ginvx = x1 > x0 ? (float)P.gnx / (x1 - x0) : 0.0f;
+  P.ginvy = y1 > y0 ? (float)P.gny / (y1 - y0) : 0.0f;
   const uint32_t cells = P.gnx * P.gny;
   for (uint32_t i = lane; i <= cells; i += 32) P.gCnt[i] = 0;
   __syncwarp();
-  for (uint32_t q = lane; q < P.n; q += 32) atomicAdd(P.gCnt + P.cell_y(P.Y[q]) * P.gnx + P.cell_x(P.X[q]), 1u);
+  for (uint32_t q = lane; q < P.n; q += 32) atomicAdd(P.gCnt + P.cell_y(P.Yf[q]) * P.gnx + P.cell_x(P.Xf[q]), 1u);
   __syncwarp();
   uint32_t run = 0;
   for (uint32_t base = 0; base <= cells; base += 32) {
@@ -677,16 +696,14 @@ __device__ void build_grid(Ring& P, int lane) {
       const uint32_t u = __shfl_up_sync(CUT_FULL, inc, d);
       if (lane >= d) inc += u;
     }
-    if (i <= cells) {
-      P.gStart[i] = run + inc - v;
-    }
+    if (i <= cells) P.gStart[i] = run + inc - v;
     run += __shfl_sync(CUT_FULL, inc, 31);
   }
   __syncwarp();
   for (uint32_t i = lane; i < cells; i += 32) P.gCnt[i] = P.gStart[i];
   __syncwarp();
   for (uint32_t q = lane; q < P.n; q += 32) {
-    const uint32_t cell = P.cell_y(P.Y[q]) * P.gnx + P.cell_x(P.X[q]);
+    const uint32_t cell = P.cell_y(P.Yf[q]) * P.gnx + P.cell_x(P.Xf[q]);
     P.gNodes[atomicAdd(P.gCnt + cell, 1u)] = q;
   }
   __syncwarp();
@@ -1125,6 +1142,8 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
   Pg.gCnt = w + cv.gCnt;
   Pg.gStart = w + cv.gStart;
   Pg.gNodes = w + cv.gNodes;
+  Pg.Xf = reinterpret_cast<float*>(w + cv.ndXf);
+  Pg.Yf = reinterpret_cast<float*>(w + cv.ndYf);
   Ring Ps;
   {
     double* sx = reinterpret_cast<double*>(capSm);
@@ -1138,6 +1157,8 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
     Ps.gNodes = su + 4 * CAP_SM_NODES;
     Ps.gCnt = su + 5 * CAP_SM_NODES;
     Ps.gStart = Ps.gCnt + CAP_SM_NODES / 2 + 2;
+    Ps.Xf = reinterpret_cast<float*>(Ps.gStart + CAP_SM_NODES / 2 + 2);
+    Ps.Yf = Ps.Xf + CAP_SM_NODES;
     Ps.cap = CAP_SM_NODES;
     Ps.n = 0;
   }
