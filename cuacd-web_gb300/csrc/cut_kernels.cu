@@ -602,58 +602,79 @@ __device__ __forceinline__ bool orient_nonneg(const Ring& P, uint32_t a, uint32_
   return orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]) >= 0;
 }
 
-// x >= b exactly, from the float roundings unless they tie (rounding is
-// monotonic: fl(x) < fl(b) implies x < b, fl(x) > fl(b) implies x > b)
-__device__ __forceinline__ bool ge_exact(float xf, double x, float bf, double b) {
-  return xf != bf ? xf > bf : x >= b;
-}
-
 // no other live node inside (or on) the triangle of ear k; the lanes split
 // the nodes and vote. Each node test is the host clipper's double test; the
 // float copies decide it exactly where they can, and the double arithmetic
 // (slow on this GPU) runs only for ties and near-zero orientations
 __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const uint32_t a = P.prev[k], b = k, c = P.next[k];
-  const double ax = P.X[a], ay = P.Y[a], bx = P.X[b], by = P.Y[b], cx = P.X[c], cy = P.Y[c];
-  const double ar = orient2(ax, ay, bx, by, cx, cy);
-  if (ar < 0 || (ar == 0 && !allowFlat)) return false;
-  const double lx = fmin(ax, cx), hx = fmax(ax, cx), ly = fmin(ay, cy), hy = fmax(ay, cy);
-  // the node must lie in the triangle's bounding box (as in the host
-  // clipper), so only the cells the box covers are looked at
-  const double bx0 = fmin(lx, bx), bx1 = fmax(hx, bx), by0 = fmin(ly, by), by1 = fmax(hy, by);
-  const float fbx0 = (float)bx0, fbx1 = (float)bx1, fby0 = (float)by0, fby1 = (float)by1;
-  const uint32_t x0 = P.cell_x(fbx0), x1 = P.cell_x(fbx1);
-  const uint32_t y0 = P.cell_y(fby0), y1 = P.cell_y(fby1);
-  const uint32_t w = x1 - x0 + 1, nCells = w * (y1 - y0 + 1);
   const float axf = P.Xf[a], ayf = P.Yf[a], bxf = P.Xf[b], byf = P.Yf[b], cxf = P.Xf[c], cyf = P.Yf[c];
   const float s3 = fmaxf(fmaxf(fmaxf(fabsf(axf), fabsf(ayf)), fmaxf(fabsf(bxf), fabsf(byf))),
                          fmaxf(fabsf(cxf), fabsf(cyf)));
+  const bool fl3 = s3 > 1e-15f && s3 < 1e15f;
+  // the ear's orientation sign: from float beyond its error bound, else in
+  // double (arPos: ar > 0; flatEar: ar == 0)
+  bool arPos, flatEar;
+  {
+    const float o = orient2f(axf, ayf, bxf, byf, cxf, cyf);
+    const float eb = fl3 ? 52.0f * 5.9604645e-8f * s3 * s3 : -1.0f;
+    if (eb >= 0.0f && o > eb) {
+      arPos = true;
+      flatEar = false;
+    } else if (eb >= 0.0f && o < -eb) {
+      return false;
+    } else {
+      const double ar = orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]);
+      if (ar < 0 || (ar == 0 && !allowFlat)) return false;
+      arPos = ar > 0;
+      flatEar = ar == 0;
+    }
+  }
+  // the node must lie in the triangle's bounding box (as in the host
+  // clipper), so only the cells the box covers are looked at; the box's
+  // float bounds are the float roundings of its double bounds (rounding is
+  // monotonic, so it commutes with min and max)
+  const float fbx0 = fminf(fminf(axf, cxf), bxf), fbx1 = fmaxf(fmaxf(axf, cxf), bxf);
+  const float fby0 = fminf(fminf(ayf, cyf), byf), fby1 = fmaxf(fmaxf(ayf, cyf), byf);
+  const uint32_t x0 = P.cell_x(fbx0), x1 = P.cell_x(fbx1);
+  const uint32_t y0 = P.cell_y(fby0), y1 = P.cell_y(fby1);
+  const uint32_t w = x1 - x0 + 1, nCells = w * (y1 - y0 + 1);
   bool hit = false;
   for (uint32_t ci = lane; ci < nCells && !hit; ci += 32) {
-    const uint32_t cell = (y0 + ci / w) * P.gnx + x0 + ci % w;
+    const uint32_t row = ci / w;
+    const uint32_t cell = (y0 + row) * P.gnx + x0 + (ci - row * w);
     for (uint32_t e = P.gStart[cell]; e < P.gStart[cell + 1]; e++) {
       const uint32_t q = P.gNodes[e];
       if (!P.alive[q] || q == a || q == b || q == c) continue;
       const float qxf = P.Xf[q], qyf = P.Yf[q];
-      const double qx = P.X[q], qy = P.Y[q];
-      // in the bounding box, exactly
-      if (!ge_exact(qxf, qx, fbx0, bx0) || !ge_exact(fbx1, bx1, qxf, qx) || !ge_exact(qyf, qy, fby0, by0) ||
-          !ge_exact(fby1, by1, qyf, qy))
-        continue;
-      // not at a corner's position (equal doubles have equal floats)
-      if ((qxf == axf && qyf == ayf && qx == ax && qy == ay) || (qxf == bxf && qyf == byf && qx == bx && qy == by) ||
-          (qxf == cxf && qyf == cyf && qx == cx && qy == cy))
-        continue;
-      const float s = fmaxf(s3, fmaxf(fabsf(qxf), fabsf(qyf)));
-      // 52 u S^2, or the double path when S^2 is out of float range
-      const float eb = (s > 1e-15f && s < 1e15f) ? 52.0f * 5.9604645e-8f * s * s : -1.0f;
-      if (orient_nonneg(P, a, b, q, eb) && orient_nonneg(P, b, c, q, eb) && orient_nonneg(P, c, a, q, eb) &&
-          (ar > 0 || (qx >= lx && qx <= hx && qy >= ly && qy <= hy))) {
-        hit = true;
-        break;
+      // in the bounding box, exactly: float decides unless it ties
+      if (qxf < fbx0 || qxf > fbx1 || qyf < fby0 || qyf > fby1) continue;
+      if (qxf == fbx0 || qxf == fbx1 || qyf == fby0 || qyf == fby1) {
+        const double qx = P.X[q], qy = P.Y[q];
+        const double ax = P.X[a], ay = P.Y[a], bx = P.X[b], by = P.Y[b], cx = P.X[c], cy = P.Y[c];
+        if (qx < fmin(fmin(ax, cx), bx) || qx > fmax(fmax(ax, cx), bx) || qy < fmin(fmin(ay, cy), by) ||
+            qy > fmax(fmax(ay, cy), by))
+          continue;
       }
+      // not at a corner's position (equal doubles have equal floats)
+      if ((qxf == axf && qyf == ayf && P.X[q] == P.X[a] && P.Y[q] == P.Y[a]) ||
+          (qxf == bxf && qyf == byf && P.X[q] == P.X[b] && P.Y[q] == P.Y[b]) ||
+          (qxf == cxf && qyf == cyf && P.X[q] == P.X[c] && P.Y[q] == P.Y[c]))
+        continue;
+      const float sq = fmaxf(s3, fmaxf(fabsf(qxf), fabsf(qyf)));
+      // 52 u S^2, or the double path when S^2 is out of float range
+      const float eb = (sq > 1e-15f && sq < 1e15f) ? 52.0f * 5.9604645e-8f * sq * sq : -1.0f;
+      if (!orient_nonneg(P, a, b, q, eb) || !orient_nonneg(P, b, c, q, eb) || !orient_nonneg(P, c, a, q, eb)) continue;
+      if (!arPos) {
+        // a flat ear: only nodes within the box of its two ends count
+        const double qx = P.X[q], qy = P.Y[q], ax = P.X[a], ay = P.Y[a], cx = P.X[c], cy = P.Y[c];
+        if (!(qx >= fmin(ax, cx) && qx <= fmax(ax, cx) && qy >= fmin(ay, cy) && qy <= fmax(ay, cy))) continue;
+      }
+      hit = true;
+      break;
     }
   }
+  (void)flatEar;
   return !__any_sync(CUT_FULL, hit);
 }
 
