@@ -109,6 +109,11 @@ constexpr double ON_PLANE_EPS = 1e-6;  // the host cut's default eps
 constexpr uint32_t CAP_SM_NODES = 2048;
 constexpr size_t CAP_SM_BYTES = 16 * CAP_SM_NODES + 4 * 5 * CAP_SM_NODES + 4 * 2 * (CAP_SM_NODES / 2 + 2) +
                                 8 * CAP_SM_NODES;
+// boundary edges whose walk runs in shared memory: a source hash of up to
+// 2 * 2048 entries (key, head, tail) and next, used, source and destination
+// per edge, 80 KB, within CAP_SM_BYTES
+constexpr uint32_t CAP_SM_WALK_B = 2048;
+static_assert(3 * 4 * 2 * CAP_SM_WALK_B + 4 * 4 * CAP_SM_WALK_B <= CAP_SM_BYTES, "walk fits the cap shared memory");
 constexpr unsigned long long EMPTY_KEY = ~0ull;
 
 // the cap step's scratch of one half, carved from m = its plane-edge bound
@@ -950,17 +955,42 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
   // steps on the same data (stores are identical), lanes split only the ear
   // test and the per-loop work
 
-  // 3. boundary edges grouped by source vertex, in first-seen order
+  // 3. boundary edges grouped by source vertex, in first-seen order. The
+  // walk below follows these lists edge by edge, so for up to
+  // CAP_SM_WALK_B edges the lists, the source-vertex hash and the edges'
+  // ends live in the block's shared memory (free until the ear clipping)
   uint32_t* bNext = w + cv.bNext;
   uint32_t* bUsed = w + cv.bUsed;
   uint32_t* shKey = w + cv.shKey;
   uint32_t* shHead = w + cv.shHead;
   uint32_t* shTail = w + cv.shTail;
   uint32_t* starts = w + cv.starts;
+  uint32_t shSize = cv.sh;
+  const uint32_t* bSrcW = bSrc;
+  const uint32_t* bDstW = bDst;
+  if (B <= CAP_SM_WALK_B) {
+    uint32_t* su = reinterpret_cast<uint32_t*>(capSm);
+    shSize = pow2_at_least(2 * B);
+    shKey = su;
+    shHead = shKey + shSize;
+    shTail = shHead + shSize;
+    bNext = shTail + shSize;
+    bUsed = bNext + B;
+    uint32_t* sSrc = bUsed + B;
+    uint32_t* sDst = sSrc + B;
+    for (uint32_t i = lane; i < shSize; i += 32) shKey[i] = CUT_NONE;
+    for (uint32_t i = lane; i < B; i += 32) {
+      sSrc[i] = bSrc[i];
+      sDst[i] = bDst[i];
+    }
+    bSrcW = sSrc;
+    bDstW = sDst;
+    __syncwarp();
+  }
   uint32_t nStarts = 0;
   for (uint32_t i = 0; i < B; i++) {
     bool ins;
-    const uint32_t h = uh_find(shKey, cv.sh, bSrc[i], true, &ins);
+    const uint32_t h = uh_find(shKey, shSize, bSrcW[i], true, &ins);
     if (h == CUT_NONE) {
       failWith(CUT_SCRATCH);
       return;
@@ -970,7 +1000,7 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
     if (ins) {
       shHead[h] = i;
       shTail[h] = i;
-      starts[nStarts++] = bSrc[i];
+      starts[nStarts++] = bSrcW[i];
     } else {
       bNext[shTail[h]] = i;
       shTail[h] = i;
@@ -986,7 +1016,7 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
   for (uint32_t si = 0; si < nStarts; si++) {
     const uint32_t start = starts[si];
     bool ins;
-    const uint32_t hs = uh_find(shKey, cv.sh, start, false, &ins);
+    const uint32_t hs = uh_find(shKey, shSize, start, false, &ins);
     for (uint32_t e = shHead[hs]; e != CUT_NONE; e = bNext[e]) {
       if (bUsed[e]) continue;
       if (nLV >= m) {
@@ -996,7 +1026,7 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
       const uint32_t lvStart = nLV;
       loopV[nLV++] = start;
       bUsed[e] = 1;
-      uint32_t cur = bDst[e];
+      uint32_t cur = bDstW[e];
       uint32_t guard = 0;
       while (cur != start) {
         if (nLV >= m) {
@@ -1004,7 +1034,7 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
           return;
         }
         loopV[nLV++] = cur;
-        const uint32_t hc = uh_find(shKey, cv.sh, cur, false, &ins);
+        const uint32_t hc = uh_find(shKey, shSize, cur, false, &ins);
         if (hc == CUT_NONE) {
           failWith(CUT_OPEN_CHAIN);
           return;
@@ -1020,7 +1050,7 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
           return;
         }
         bUsed[nx] = 1;
-        cur = bDst[nx];
+        cur = bDstW[nx];
         if (++guard > B + 1) {
           failWith(CUT_CYCLE);
           return;
@@ -1390,39 +1420,46 @@ __global__ void k_cut_write(const CutDesc* __restrict__ D, const CutLayout* __re
 }
 
 // signed volume of every half by the divergence theorem anchored at its
-// vertex 0 (mesh.ts:58-72): one block per half, each thread sums its
-// strided triangles in order, then a fixed-order tree across the threads
-// (the same value on every run; it differs from a sequential sum in the last
-// bits)
-__global__ void k_cut_volume(uint32_t n2, const unsigned long long* __restrict__ vOff,
-                             const unsigned long long* __restrict__ tOff, const uint32_t* __restrict__ halfNt,
-                             const float* __restrict__ outV, const uint32_t* __restrict__ outT,
-                             double* __restrict__ vol) {
-  __shared__ double part[32];
-  const uint32_t k = blockIdx.x;
-  if (k >= n2) return;
-  const uint32_t nt = halfNt[k];
-  const float* v = outV + 3 * vOff[k];
-  const uint32_t* t = outT + tOff[k];
+// vertex 0 (mesh.ts:58-72), in two fixed-order steps so that large halves
+// spread over many blocks: each chunk of up to VOL_CHUNK triangles is one
+// block (every thread sums its strided triangles in order, then a fixed tree
+// over the threads), and each half adds its chunks in order (the same value
+// on every run; it differs from a sequential sum in the last bits)
+constexpr uint32_t VOL_CHUNK = 4096;
+
+__global__ void k_cut_vol_chunks(const uint4* __restrict__ chunks, const unsigned long long* __restrict__ vOff,
+                                 const unsigned long long* __restrict__ tOff, const float* __restrict__ outV,
+                                 const uint32_t* __restrict__ outT, double* __restrict__ part) {
+  __shared__ double ws[32];
+  const uint4 ch = chunks[blockIdx.x];  // half, first triangle, end triangle
+  const float* v = outV + 3 * vOff[ch.x];
+  const uint32_t* t = outT + tOff[ch.x];
+  const double ox = v[0], oy = v[1], oz = v[2];
   double s = 0.0;
-  if (nt > 0) {
-    const double ox = v[0], oy = v[1], oz = v[2];
-    for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) {
-      const uint32_t a = 3 * t[3 * i], b = 3 * t[3 * i + 1], c = 3 * t[3 * i + 2];
-      const double ax = v[a] - ox, ay = v[a + 1] - oy, az = v[a + 2] - oz;
-      const double bx = v[b] - ox, by = v[b + 1] - oy, bz = v[b + 2] - oz;
-      const double cx = v[c] - ox, cy = v[c + 1] - oy, cz = v[c + 2] - oz;
-      s += ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
-    }
+  for (uint32_t i = ch.y + threadIdx.x; i < ch.z; i += blockDim.x) {
+    const uint32_t a = 3 * t[3 * i], b = 3 * t[3 * i + 1], c = 3 * t[3 * i + 2];
+    const double ax = v[a] - ox, ay = v[a + 1] - oy, az = v[a + 2] - oz;
+    const double bx = v[b] - ox, by = v[b + 1] - oy, bz = v[b + 2] - oz;
+    const double cx = v[c] - ox, cy = v[c + 1] - oy, cz = v[c + 2] - oz;
+    s += ax * (by * cz - bz * cy) + ay * (bz * cx - bx * cz) + az * (bx * cy - by * cx);
   }
   for (int d = 16; d > 0; d >>= 1) s += __shfl_down_sync(CUT_FULL, s, d);
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
   __syncthreads();
   if (threadIdx.x == 0) {
     double tot = 0.0;
-    for (uint32_t w = 0; w < (blockDim.x >> 5); w++) tot += part[w];
-    vol[k] = tot / 6.0;
+    for (uint32_t w = 0; w < (blockDim.x >> 5); w++) tot += ws[w];
+    part[blockIdx.x] = tot;
   }
+}
+
+__global__ void k_cut_vol_sum(uint32_t n2, const uint32_t* __restrict__ chunkPre, const double* __restrict__ part,
+                              double* __restrict__ vol) {
+  const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n2) return;
+  double s = 0.0;
+  for (uint32_t c = chunkPre[k]; c < chunkPre[k + 1]; c++) s += part[c];
+  vol[k] = s / 6.0;
 }
 
 // open edges of the input meshes (used when the caller does not vouch for
@@ -1503,7 +1540,8 @@ struct Buf {
 
 struct Engine {
   Buf inV, inT, desc, vPre, tPre, sizes, layout, out, cPre, dist, sgn, cnt, pre, tiles, hashKeys, hashXYZ, surfT,
-      candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT, halfNt, vol, openBits, openKeys, openMeta;
+      candE, firstPos, flag, fpre, words, dbls, outVOff, outTOff, outV, outT, vol, openBits, openKeys, openMeta,
+      volChunks, volPre, volPart;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   void* stage = nullptr;  // pinned staging of the halves' readback
   size_t stageBytes = 0;
@@ -1776,10 +1814,9 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
     }
   }
   if ((rc = e->outV.ensure(12 * outVTot)) || (rc = e->outT.ensure(12 * outTTot)) ||
-      (rc = e->halfNt.ensure(4 * 2 * n)) || (rc = e->vol.ensure(8 * 2 * n)))
+      (rc = e->vol.ensure(8 * 2 * n)))
     return rc;
   for (auto& x : to) x *= 3;  // corner offsets
-  CUTCK(cudaMemcpyAsync(e->halfNt.p, out->nt.data(), 4 * 2 * n, cudaMemcpyHostToDevice, s));
   CUTCK(cudaMemcpyAsync(e->outVOff.p, vo.data(), 8 * 2 * n, cudaMemcpyHostToDevice, s));
   CUTCK(cudaMemcpyAsync(e->outTOff.p, to.data(), 8 * 2 * n, cudaMemcpyHostToDevice, s));
   if (corners)
@@ -1790,10 +1827,29 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
                                                      e->inV.as<float>(), e->outVOff.as<unsigned long long>(),
                                                      e->outTOff.as<unsigned long long>(), e->outV.as<float>(),
                                                      e->outT.as<uint32_t>());
-  k_cut_volume<<<2 * n, 256, 0, s>>>(2 * n, e->outVOff.as<unsigned long long>(),
-                                                          e->outTOff.as<unsigned long long>(), e->halfNt.as<uint32_t>(),
-                                                          e->outV.as<float>(), e->outT.as<uint32_t>(),
-                                                          e->vol.as<double>());
+  {
+    // chunks of the halves' triangles for the volume sums
+    std::vector<uint4> chunks;
+    std::vector<uint32_t> chunkPre(2 * (size_t)n + 1, 0);
+    for (uint32_t k = 0; k < 2 * n; k++) {
+      for (uint32_t t0 = 0; t0 < out->nt[k]; t0 += VOL_CHUNK)
+        chunks.push_back(make_uint4(k, t0, std::min<uint32_t>(out->nt[k], t0 + VOL_CHUNK), 0));
+      chunkPre[k + 1] = (uint32_t)chunks.size();
+    }
+    if ((rc = e->volChunks.ensure(16 * std::max<size_t>(chunks.size(), 1))) ||
+        (rc = e->volPre.ensure(4 * chunkPre.size())) || (rc = e->volPart.ensure(8 * std::max<size_t>(chunks.size(), 1))))
+      return rc;
+    if (!chunks.empty()) {
+      CUTCK(cudaMemcpyAsync(e->volChunks.p, chunks.data(), 16 * chunks.size(), cudaMemcpyHostToDevice, s));
+      k_cut_vol_chunks<<<(uint32_t)chunks.size(), 256, 0, s>>>(e->volChunks.as<uint4>(),
+                                                              e->outVOff.as<unsigned long long>(),
+                                                              e->outTOff.as<unsigned long long>(), e->outV.as<float>(),
+                                                              e->outT.as<uint32_t>(), e->volPart.as<double>());
+    }
+    CUTCK(cudaMemcpyAsync(e->volPre.p, chunkPre.data(), 4 * chunkPre.size(), cudaMemcpyHostToDevice, s));
+    k_cut_vol_sum<<<blocks(2ull * n, 128), 128, 0, s>>>(2 * n, e->volPre.as<uint32_t>(), e->volPart.as<double>(),
+                                                        e->vol.as<double>());
+  }
   CUTCK(cudaGetLastError());
   out->vol.assign(2 * (size_t)n, 0.0);
   CUTCK(cudaMemcpyAsync(out->vol.data(), e->vol.p, 8 * 2 * n, cudaMemcpyDeviceToHost, s));
