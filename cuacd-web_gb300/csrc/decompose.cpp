@@ -192,6 +192,7 @@ class Engine {
   std::vector<PairEval> evals;  // merge pair evaluations of the current call
   // whole-call timings
   double treeMs = 0, cutMs = 0, concaveMs = 0, hullMs = 0, hdMs = 0, mergeMs = 0, gpuMs = 0;
+  double cutGpuMs = 0;  // of cutMs: the GPU cut batch and its readback
 
   ~Engine() {
     if (tree) cuacd_tree_destroy(tree);
@@ -593,6 +594,7 @@ class Engine {
       c.neg.t.assign(t[1], t[1] + 3 * (size_t)nt[1]);
     }
     if (halvesH) cuacd_cuts_free(halvesH);
+    const double cutGpu = ms_since(ta);
     parallel_for(seeds.size(), threads, [&](size_t k) {
       Part& p = seeds[k].job->parts[seeds[k].part];
       const cuacd_seed_result& r = best[k];
@@ -618,6 +620,7 @@ class Engine {
       cuts[k].neg = std::move(c.neg);
     });
     cutMs += ms_since(ta);
+    cutGpuMs += cutGpu;
     // hulls and Hausdorff distances of every new half in one submission
     std::vector<const Mesh*> halves;
     std::vector<double> heps;
@@ -637,8 +640,11 @@ class Engine {
       size_t nParts = 0, nTris = 0;
       for (Job* j : jobs) nParts += j->parts.size();
       for (const Mesh* m : halves) nTris += m->nt();
-      fprintf(stderr, "[iter %d] cutting %zu parts, %zu cuts applied, %zu half triangles, %zu parts; tree %.1f ms, hull %.1f ms\n",
-              iterShown, seeds.size(), which.size(), nTris, nParts + which.size(), treeMs, hullMs);
+      fprintf(stderr,
+              "[iter %d] cutting %zu parts, %zu cuts applied, %zu half triangles, %zu parts; tree %.1f ms, hull %.1f ms, "
+              "cut %.1f ms (GPU batch and readback %.1f), concave %.1f ms\n",
+              iterShown, seeds.size(), which.size(), nTris, nParts + which.size(), treeMs, hullMs, cutMs, cutGpuMs,
+              concaveMs);
     }
     // per job, in cutting order: the positive half replaces the part, the
     // negative half is appended
@@ -1010,7 +1016,7 @@ class Engine {
   std::vector<std::unique_ptr<Engine>> peers;
   void reset_timers() {
     evals.clear();
-    treeMs = cutMs = concaveMs = hullMs = hdMs = mergeMs = gpuMs = 0;
+    treeMs = cutMs = concaveMs = hullMs = hdMs = mergeMs = gpuMs = cutGpuMs = 0;
   }
   // The batch split over `streams` engines by triangle count (largest mesh
   // to the least loaded group), each group run on its own host thread; each
