@@ -544,7 +544,7 @@ __device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
   const double hx = P.X[h], hy = P.Y[h];
   double qx = -INFINITY;
   int32_t m = -1;
-  uint32_t p = outer;
+  uint32_t p = outer, guard = 0;
   do {
     const uint32_t an = P.next[p];
     const double ax = P.X[p], ay = P.Y[p], bx = P.X[an], by = P.Y[an];
@@ -560,7 +560,7 @@ __device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
       }
     }
     p = an;
-  } while (p != outer);
+  } while (p != outer && ++guard <= P.n);
   if (m < 0) return -1;
   if (hx == qx) return m;
   const uint32_t stop = (uint32_t)m;
@@ -582,7 +582,7 @@ __device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
       }
     }
     p = P.next[p];
-  } while (p != stop);
+  } while (p != stop && ++guard <= 2 * P.n);
   return m;
 }
 
@@ -749,11 +749,11 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
     const uint32_t s = hs[k], e = k + 1 < nHoles ? hs[k + 1] : nAll;
     if (e <= s) continue;
     const uint32_t h = ring_par(P, gxy, s, e, false, lane);
-    uint32_t left = h, p = h;
+    uint32_t left = h, p = h, guard = 0;
     do {
       if (P.X[p] < P.X[left] || (P.X[p] == P.X[left] && P.Y[p] < P.Y[left])) left = p;
       p = P.next[p];
-    } while (p != h);
+    } while (p != h && ++guard <= P.n);
     // stable insertion by leftmost x
     uint32_t j = nh;
     while (j > 0 && holeX[j - 1] > P.X[left]) {
@@ -764,11 +764,17 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
     holeX[j] = P.X[left];
     holeL[j] = left;
     nh++;
+    // every lane has finished reading the sorted list before the next hole
+    // shifts it (warp-uniform code stays correct only if no lane runs ahead
+    // into a write that another lane has not read past)
+    __syncwarp();
   }
   for (uint32_t k = 0; k < nh; k++) {
     const int32_t m = find_bridge(P, holeL[k], outer);
+    __syncwarp();
     if (m < 0) return 0;
     P.bridge((uint32_t)m, holeL[k]);
+    __syncwarp();
   }
   __syncwarp();
   build_grid(P, lane);
@@ -778,12 +784,18 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
     do {
       count++;
       p = P.next[p];
-    } while (p != outer);
+    } while (p != outer && count <= P.n);
+    if (count > P.n) return 0;  // not a ring: never for a well-formed group
   }
   uint32_t nOut = 0;
   uint32_t ear = outer, stop = outer;
   bool flat = false;
+  // each pass over the ring clips an ear or ends the clipping, so 2 n^2
+  // steps are never reached; the bound only keeps a malformed ring finite
+  const unsigned long long maxSteps = 2ull * count * count + 16;
+  unsigned long long steps = 0;
   while (count > 3) {
+    if (++steps > maxSteps) return nOut;
     if (is_ear(P, ear, flat, lane)) {
       const uint32_t a = P.prev[ear], c = P.next[ear];
       out[3 * nOut] = P.I[a];
@@ -987,80 +999,98 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
     bDstW = sDst;
     __syncwarp();
   }
-  uint32_t nStarts = 0;
-  for (uint32_t i = 0; i < B; i++) {
-    bool ins;
-    const uint32_t h = uh_find(shKey, shSize, bSrcW[i], true, &ins);
-    if (h == CUT_NONE) {
-      failWith(CUT_SCRATCH);
-      return;
-    }
-    bNext[i] = CUT_NONE;
-    bUsed[i] = 0;
-    if (ins) {
-      shHead[h] = i;
-      shTail[h] = i;
-      starts[nStarts++] = bSrcW[i];
-    } else {
-      bNext[shTail[h]] = i;
-      shTail[h] = i;
-    }
-  }
-  __syncwarp();
-  // 4. boundary loops: from each start, each unused out-edge in order, then
-  // the first unused out-edge at every vertex
+  // Steps 3 and 4 are sequential and each decision reads what earlier
+  // iterations wrote (hash inserts, used flags), so they run on lane 0 alone
+  // while the other lanes wait; every list walk is bounded.
   uint32_t* loopV = w + cv.loopV;
   uint32_t* loopS = w + cv.loopS;
   uint32_t nLoops = 0, nLV = 0;
-  loopS[0] = 0;
-  for (uint32_t si = 0; si < nStarts; si++) {
-    const uint32_t start = starts[si];
-    bool ins;
-    const uint32_t hs = uh_find(shKey, shSize, start, false, &ins);
-    for (uint32_t e = shHead[hs]; e != CUT_NONE; e = bNext[e]) {
-      if (bUsed[e]) continue;
-      if (nLV >= m) {
-        failWith(CUT_SCRATCH);
-        return;
+  int walkFail = 0;
+  if (lane == 0) {
+    uint32_t nStarts = 0;
+    for (uint32_t i = 0; i < B && !walkFail; i++) {
+      bool ins;
+      const uint32_t h = uh_find(shKey, shSize, bSrcW[i], true, &ins);
+      if (h == CUT_NONE) {
+        walkFail = CUT_SCRATCH;
+        break;
       }
-      const uint32_t lvStart = nLV;
-      loopV[nLV++] = start;
-      bUsed[e] = 1;
-      uint32_t cur = bDstW[e];
-      uint32_t guard = 0;
-      while (cur != start) {
+      bNext[i] = CUT_NONE;
+      bUsed[i] = 0;
+      if (ins) {
+        shHead[h] = i;
+        shTail[h] = i;
+        starts[nStarts++] = bSrcW[i];
+      } else {
+        bNext[shTail[h]] = i;
+        shTail[h] = i;
+      }
+    }
+    // 4. boundary loops: from each start, each unused out-edge in order,
+    // then the first unused out-edge at every vertex
+    loopS[0] = 0;
+    for (uint32_t si = 0; si < nStarts && !walkFail; si++) {
+      const uint32_t start = starts[si];
+      bool ins;
+      const uint32_t hs = uh_find(shKey, shSize, start, false, &ins);
+      uint32_t steps = 0;
+      for (uint32_t e = shHead[hs]; e != CUT_NONE && !walkFail; e = bNext[e]) {
+        if (++steps > B) {
+          walkFail = CUT_CYCLE;
+          break;
+        }
+        if (bUsed[e]) continue;
         if (nLV >= m) {
-          failWith(CUT_SCRATCH);
-          return;
+          walkFail = CUT_SCRATCH;
+          break;
         }
-        loopV[nLV++] = cur;
-        const uint32_t hc = uh_find(shKey, shSize, cur, false, &ins);
-        if (hc == CUT_NONE) {
-          failWith(CUT_OPEN_CHAIN);
-          return;
-        }
-        uint32_t nx = CUT_NONE;
-        for (uint32_t e2 = shHead[hc]; e2 != CUT_NONE; e2 = bNext[e2])
-          if (!bUsed[e2]) {
-            nx = e2;
+        const uint32_t lvStart = nLV;
+        loopV[nLV++] = start;
+        bUsed[e] = 1;
+        uint32_t cur = bDstW[e];
+        uint32_t guard = 0;
+        while (cur != start) {
+          if (nLV >= m) {
+            walkFail = CUT_SCRATCH;
             break;
           }
-        if (nx == CUT_NONE) {
-          failWith(CUT_DEAD_END);
-          return;
+          loopV[nLV++] = cur;
+          const uint32_t hc = uh_find(shKey, shSize, cur, false, &ins);
+          if (hc == CUT_NONE) {
+            walkFail = CUT_OPEN_CHAIN;
+            break;
+          }
+          uint32_t nx = CUT_NONE, n2 = 0;
+          for (uint32_t e2 = shHead[hc]; e2 != CUT_NONE && n2 <= B; e2 = bNext[e2], n2++)
+            if (!bUsed[e2]) {
+              nx = e2;
+              break;
+            }
+          if (nx == CUT_NONE) {
+            walkFail = CUT_DEAD_END;
+            break;
+          }
+          bUsed[nx] = 1;
+          cur = bDstW[nx];
+          if (++guard > B + 1) {
+            walkFail = CUT_CYCLE;
+            break;
+          }
         }
-        bUsed[nx] = 1;
-        cur = bDstW[nx];
-        if (++guard > B + 1) {
-          failWith(CUT_CYCLE);
-          return;
-        }
+        if (walkFail) break;
+        if (nLV - lvStart >= 3) loopS[++nLoops] = nLV;
+        else nLV = lvStart;
       }
-      if (nLV - lvStart >= 3) loopS[++nLoops] = nLV;
-      else nLV = lvStart;
     }
   }
   __syncwarp();
+  walkFail = __shfl_sync(CUT_FULL, walkFail, 0);
+  nLoops = __shfl_sync(CUT_FULL, nLoops, 0);
+  nLV = __shfl_sync(CUT_FULL, nLV, 0);
+  if (walkFail) {
+    failWith(walkFail);
+    return;
+  }
   if (nLoops == 0) return;
   // 5. loop coordinates in the plane's basis (every loop vertex at once) and
   // signed areas: the terms at once, each loop's sum in order by one lane
