@@ -607,6 +607,24 @@ __device__ __forceinline__ bool orient_nonneg(const Ring& P, uint32_t a, uint32_
   return orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]) >= 0;
 }
 
+// the orientation gate of the ear test at vertex k (is_ear returns false at
+// once when it fails): the triangle (prev, k, next) turns left, or is flat in
+// flat mode; decided in float beyond the error bound, else in double
+__device__ bool ear_gate(const Ring& P, uint32_t k, bool allowFlat) {
+  const uint32_t a = P.prev[k], c = P.next[k];
+  const float axf = P.Xf[a], ayf = P.Yf[a], bxf = P.Xf[k], byf = P.Yf[k], cxf = P.Xf[c], cyf = P.Yf[c];
+  const float s3 = fmaxf(fmaxf(fmaxf(fabsf(axf), fabsf(ayf)), fmaxf(fabsf(bxf), fabsf(byf))),
+                         fmaxf(fabsf(cxf), fabsf(cyf)));
+  if (s3 > 1e-15f && s3 < 1e15f) {
+    const float o = orient2f(axf, ayf, bxf, byf, cxf, cyf);
+    const float eb = 52.0f * 5.9604645e-8f * s3 * s3;
+    if (o > eb) return true;
+    if (o < -eb) return false;
+  }
+  const double ar = orient2(P.X[a], P.Y[a], P.X[k], P.Y[k], P.X[c], P.Y[c]);
+  return ar > 0 || (ar == 0 && allowFlat);
+}
+
 // no other live node inside (or on) the triangle of ear k; the lanes split
 // the nodes and vote. Each node test is the host clipper's double test; the
 // float copies decide it exactly where they can, and the double arithmetic
@@ -790,18 +808,58 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
   uint32_t nOut = 0;
   uint32_t ear = outer, stop = outer;
   bool flat = false;
-  // each pass over the ring clips an ear or ends the clipping, so 2 n^2
-  // steps are never reached; the bound only keeps a malformed ring finite
+  // The host clipper tests ear, next(ear), ... one at a time; most tests
+  // fail at the orientation gate (reflex, or flat outside flat mode), and a
+  // flat stretch can cost a full pass per clipped ear. Here the warp looks
+  // at the next 32 vertices at once: each lane applies the gate to one, and
+  // the full test runs on the gate's survivors in ring order; the first
+  // that passes is the ear the host finds. Reaching `stop` ends the batch
+  // there, where the host switches to flat mode (or gives up).
+  __shared__ uint32_t ring33[33];
+  // each batch clips an ear, ends a pass, or advances 32 vertices, so
+  // 2 n^2 + 16 batches are never reached; the bound keeps a malformed ring
+  // finite
   const unsigned long long maxSteps = 2ull * count * count + 16;
   unsigned long long steps = 0;
   while (count > 3) {
     if (++steps > maxSteps) return nOut;
-    if (is_ear(P, ear, flat, lane)) {
+    if (lane == 0) {
+      uint32_t cv = ear;
+      for (int i = 0; i < 33; i++) {
+        ring33[i] = cv;
+        cv = P.next[cv];
+      }
+    }
+    __syncwarp();
+    // the batch: positions [0, jStop), jStop = first return to `stop`
+    uint32_t jStop = 33;
+    {
+      const bool isStop = lane >= 1 && ring33[lane] == stop;
+      const bool isStop32 = ring33[32] == stop;
+      const uint32_t bal = __ballot_sync(CUT_FULL, isStop);
+      jStop = bal ? (uint32_t)(__ffs(bal) - 1) : (isStop32 ? 32u : 33u);
+    }
+    const uint32_t nTest = min(jStop, 32u);
+    const uint32_t mine = ring33[lane];
+    const bool gate = (uint32_t)lane < nTest && ear_gate(P, mine, flat);
+    uint32_t cand = __ballot_sync(CUT_FULL, gate);
+    int found = -1;
+    while (cand) {
+      const int i = __ffs(cand) - 1;
+      cand &= cand - 1;
+      if (is_ear(P, ring33[i], flat, lane)) {
+        found = i;
+        break;
+      }
+    }
+    if (found >= 0) {
+      ear = ring33[found];
       const uint32_t a = P.prev[ear], c = P.next[ear];
       out[3 * nOut] = P.I[a];
       out[3 * nOut + 1] = P.I[ear];
       out[3 * nOut + 2] = P.I[c];
       nOut++;
+      __syncwarp();
       P.next[a] = c;
       P.prev[c] = a;
       P.alive[ear] = 0;
@@ -812,11 +870,15 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
       __syncwarp();
       continue;
     }
-    ear = P.next[ear];
-    if (ear == stop) {
+    if (jStop <= 32) {
+      // the walk reached `stop`: the host switches to flat mode or gives up
+      ear = stop;
       if (flat) return nOut;
       flat = true;
+    } else {
+      ear = ring33[32];
     }
+    __syncwarp();
   }
   const uint32_t a = P.prev[ear], c = P.next[ear];
   out[3 * nOut] = P.I[a];
