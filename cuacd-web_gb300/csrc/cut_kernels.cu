@@ -105,10 +105,11 @@ enum { CUT_OK = 0, CUT_NO_SPLIT = 1, CUT_OPEN_CHAIN = 2, CUT_DEAD_END = 3, CUT_C
 
 constexpr double ON_PLANE_EPS = 1e-6;  // the host cut's default eps
 // ear-clip nodes a cap warp keeps in shared memory (X, Y, their float
-// copies, index, links, alive flag, grid: 44 bytes each plus the cell starts)
+// hi/lo copies, index, links, alive flag, grid: 52 bytes each plus the cell
+// starts)
 constexpr uint32_t CAP_SM_NODES = 2048;
 constexpr size_t CAP_SM_BYTES = 16 * CAP_SM_NODES + 4 * 5 * CAP_SM_NODES + 4 * 2 * (CAP_SM_NODES / 2 + 2) +
-                                8 * CAP_SM_NODES;
+                                16 * CAP_SM_NODES;
 // boundary edges whose walk runs in shared memory: a source hash of up to
 // 2 * 2048 entries (key, head, tail) and next, used, source and destination
 // per edge, 80 KB, within CAP_SM_BYTES
@@ -131,6 +132,7 @@ struct CapCarve {
   uint32_t holeL;           // a group's holes: leftmost node (m)
   uint32_t gCnt, gStart, gNodes;  // the ear test's uniform grid: per-cell fill, starts, nodes (nd each)
   uint32_t ndXf, ndYf;      // the nodes' float32 coordinates (nd each)
+  uint32_t ndXl, ndYl;      // and their float32 remainders (nd each)
   uint32_t capT;            // cap triangles, 3 words each (capMax)
   uint32_t words;
   uint32_t l2, area, ndX, ndY, gXY, holeX, cent;  // double arena
@@ -176,6 +178,8 @@ __host__ __device__ inline CapCarve carve(uint32_t m, uint32_t capMax) {
   c.gNodes = o; o += c.nd;
   c.ndXf = o; o += c.nd;
   c.ndYf = o; o += c.nd;
+  c.ndXl = o; o += c.nd;
+  c.ndYl = o; o += c.nd;
   c.capT = o; o += 3 * capMax;
   c.words = (o + 1) & ~1u;
   uint32_t d = 0;
@@ -466,6 +470,7 @@ struct Ring {  // ear-clip node arrays of one half (warp-uniform)
   uint32_t *I, *prev, *next, *alive;
   double *X, *Y;
   float *Xf, *Yf;  // the coordinates rounded to float32 (the ear test's prefilter)
+  float *Xl, *Yl;  // and the float32 rounding of what that rounding left out
   uint32_t n, cap;
   // uniform grid over the nodes (built once the holes are bridged in), in
   // the float32 coordinates: the ear test looks only at the nodes in the
@@ -485,9 +490,11 @@ struct Ring {  // ear-clip node arrays of one half (warp-uniform)
   }
   __device__ void bridge(uint32_t a, uint32_t b) {
     const uint32_t a2 = n++;
-    I[a2] = I[a]; X[a2] = X[a]; Y[a2] = Y[a]; Xf[a2] = Xf[a]; Yf[a2] = Yf[a]; alive[a2] = 1;
+    I[a2] = I[a]; X[a2] = X[a]; Y[a2] = Y[a]; Xf[a2] = Xf[a]; Yf[a2] = Yf[a]; Xl[a2] = Xl[a]; Yl[a2] = Yl[a];
+    alive[a2] = 1;
     const uint32_t b2 = n++;
-    I[b2] = I[b]; X[b2] = X[b]; Y[b2] = Y[b]; Xf[b2] = Xf[b]; Yf[b2] = Yf[b]; alive[b2] = 1;
+    I[b2] = I[b]; X[b2] = X[b]; Y[b2] = Y[b]; Xf[b2] = Xf[b]; Yf[b2] = Yf[b]; Xl[b2] = Xl[b]; Yl[b2] = Yl[b];
+    alive[b2] = 1;
     const uint32_t an = next[a], bp = prev[b];
     next[a] = b;
     prev[b] = a;
@@ -525,8 +532,11 @@ __device__ uint32_t ring_par(Ring& P, const double* gxy, uint32_t s, uint32_t e,
     P.I[nd] = k;
     P.X[nd] = gxy[2 * k];
     P.Y[nd] = gxy[2 * k + 1];
-    P.Xf[nd] = (float)gxy[2 * k];
-    P.Yf[nd] = (float)gxy[2 * k + 1];
+    const float hx = (float)gxy[2 * k], hy = (float)gxy[2 * k + 1];
+    P.Xf[nd] = hx;
+    P.Yf[nd] = hy;
+    P.Xl[nd] = (float)(gxy[2 * k] - (double)hx);  // exact in double (Sterbenz)
+    P.Yl[nd] = (float)(gxy[2 * k + 1] - (double)hy);
     P.alive[nd] = 1;
     P.next[nd] = base + (i + 1 == len ? 0 : i + 1);
     P.prev[nd] = base + (i == 0 ? len - 1 : i - 1);
@@ -586,43 +596,48 @@ __device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
   return m;
 }
 
-// orient2 in float32 of float-rounded coordinates, and whether it decides
-// the sign of the double orient2 of the original coordinates: with u = 2^-24
-// and S the largest coordinate magnitude, the float result is within 48.5 u
-// S^2 of the exact value (inputs rounded to float: 2 u S per difference,
-// then three roundings) and the double result within 1e-14 S^2 of it, so a
-// float result beyond 50 u S^2 has the double result's sign (and is not 0)
-__device__ __forceinline__ float orient2f(float ax, float ay, float bx, float by, float cx, float cy) {
-  return __fsub_rn(__fmul_rn(__fsub_rn(bx, ax), __fsub_rn(cy, ay)), __fmul_rn(__fsub_rn(by, ay), __fsub_rn(cx, ax)));
+// orient2 of three ring nodes, decided in float32 where the float value is
+// clear of its error bound. Each coordinate x is kept as hi = fl(x) and lo =
+// fl(x - hi); a difference b - a is (b.hi - a.hi) + (b.lo - a.lo) in float,
+// within 2.01 u |b - a| + 6 u^2 S of the exact one (u = 2^-24, S the largest
+// |coordinate|), so the float orient2 d1 d2 - d3 d4 is within 6.2 u (|d1 d2|
+// + |d3 d4|) + 6.1 u^2 S (|d1| + |d2| + |d3| + |d4|) of the exact value, and
+// the double orient2 within 4 2^-53 (|d1 d2| + |d3 d4|) of it. Beyond the sum
+// of both (taken as 8 u (...) + 8 u^2 S (...)), the float value has the
+// double result's sign; otherwise the double orient2 is computed.
+// Returns +1, -1, or 0 for an exact double zero.
+__device__ __forceinline__ float ring_diff(const float* h, const float* l, uint32_t b, uint32_t a) {
+  return __fadd_rn(__fsub_rn(h[b], h[a]), __fsub_rn(l[b], l[a]));
 }
 
-// the double test orient2(a, b, c) >= 0, decided in float when the float
-// value is clear of its error bound e (e < 0: always in double)
-__device__ __forceinline__ bool orient_nonneg(const Ring& P, uint32_t a, uint32_t b, uint32_t c, float e) {
-  if (e >= 0.0f) {
-    const float o = orient2f(P.Xf[a], P.Yf[a], P.Xf[b], P.Yf[b], P.Xf[c], P.Yf[c]);
-    if (o > e) return true;
-    if (o < -e) return false;
+__device__ int orient_sign(const Ring& P, uint32_t a, uint32_t b, uint32_t c) {
+  const float d1 = ring_diff(P.Xf, P.Xl, b, a), d2 = ring_diff(P.Yf, P.Yl, c, a);
+  const float d3 = ring_diff(P.Yf, P.Yl, b, a), d4 = ring_diff(P.Xf, P.Xl, c, a);
+  const float p1 = __fmul_rn(d1, d2), p2 = __fmul_rn(d3, d4);
+  const float o = __fsub_rn(p1, p2);
+  const float S = fmaxf(fmaxf(fmaxf(fabsf(P.Xf[a]), fabsf(P.Yf[a])), fmaxf(fabsf(P.Xf[b]), fabsf(P.Yf[b]))),
+                        fmaxf(fabsf(P.Xf[c]), fabsf(P.Yf[c])));
+  if (S < 1e15f) {
+    const float u = 5.9604645e-8f;
+    const float eb = __fadd_rn(__fmul_rn(8.0f * u, __fadd_rn(fabsf(p1), fabsf(p2))),
+                               __fmul_rn(__fmul_rn(8.0f * u * u, S),
+                                         __fadd_rn(__fadd_rn(fabsf(d1), fabsf(d2)), __fadd_rn(fabsf(d3), fabsf(d4)))));
+    // a bound in the subnormal range is not trusted
+    if (eb > 1e-30f) {
+      if (o > eb) return 1;
+      if (o < -eb) return -1;
+    }
   }
-  return orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]) >= 0;
+  const double r = orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]);
+  return r > 0 ? 1 : (r < 0 ? -1 : 0);
 }
 
 // the orientation gate of the ear test at vertex k (is_ear returns false at
 // once when it fails): the triangle (prev, k, next) turns left, or is flat in
-// flat mode; decided in float beyond the error bound, else in double
+// flat mode
 __device__ bool ear_gate(const Ring& P, uint32_t k, bool allowFlat) {
-  const uint32_t a = P.prev[k], c = P.next[k];
-  const float axf = P.Xf[a], ayf = P.Yf[a], bxf = P.Xf[k], byf = P.Yf[k], cxf = P.Xf[c], cyf = P.Yf[c];
-  const float s3 = fmaxf(fmaxf(fmaxf(fabsf(axf), fabsf(ayf)), fmaxf(fabsf(bxf), fabsf(byf))),
-                         fmaxf(fabsf(cxf), fabsf(cyf)));
-  if (s3 > 1e-15f && s3 < 1e15f) {
-    const float o = orient2f(axf, ayf, bxf, byf, cxf, cyf);
-    const float eb = 52.0f * 5.9604645e-8f * s3 * s3;
-    if (o > eb) return true;
-    if (o < -eb) return false;
-  }
-  const double ar = orient2(P.X[a], P.Y[a], P.X[k], P.Y[k], P.X[c], P.Y[c]);
-  return ar > 0 || (ar == 0 && allowFlat);
+  const int sg = orient_sign(P, P.prev[k], k, P.next[k]);
+  return sg > 0 || (sg == 0 && allowFlat);
 }
 
 // no other live node inside (or on) the triangle of ear k; the lanes split
@@ -632,27 +647,10 @@ __device__ bool ear_gate(const Ring& P, uint32_t k, bool allowFlat) {
 __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const uint32_t a = P.prev[k], b = k, c = P.next[k];
   const float axf = P.Xf[a], ayf = P.Yf[a], bxf = P.Xf[b], byf = P.Yf[b], cxf = P.Xf[c], cyf = P.Yf[c];
-  const float s3 = fmaxf(fmaxf(fmaxf(fabsf(axf), fabsf(ayf)), fmaxf(fabsf(bxf), fabsf(byf))),
-                         fmaxf(fabsf(cxf), fabsf(cyf)));
-  const bool fl3 = s3 > 1e-15f && s3 < 1e15f;
-  // the ear's orientation sign: from float beyond its error bound, else in
-  // double (arPos: ar > 0; flatEar: ar == 0)
-  bool arPos, flatEar;
-  {
-    const float o = orient2f(axf, ayf, bxf, byf, cxf, cyf);
-    const float eb = fl3 ? 52.0f * 5.9604645e-8f * s3 * s3 : -1.0f;
-    if (eb >= 0.0f && o > eb) {
-      arPos = true;
-      flatEar = false;
-    } else if (eb >= 0.0f && o < -eb) {
-      return false;
-    } else {
-      const double ar = orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]);
-      if (ar < 0 || (ar == 0 && !allowFlat)) return false;
-      arPos = ar > 0;
-      flatEar = ar == 0;
-    }
-  }
+  // the ear's orientation (arPos: ar > 0; otherwise ar == 0 in flat mode)
+  const int sg = orient_sign(P, a, b, c);
+  if (sg < 0 || (sg == 0 && !allowFlat)) return false;
+  const bool arPos = sg > 0;
   // the node must lie in the triangle's bounding box (as in the host
   // clipper), so only the cells the box covers are looked at; the box's
   // float bounds are the float roundings of its double bounds (rounding is
@@ -684,10 +682,7 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
           (qxf == bxf && qyf == byf && P.X[q] == P.X[b] && P.Y[q] == P.Y[b]) ||
           (qxf == cxf && qyf == cyf && P.X[q] == P.X[c] && P.Y[q] == P.Y[c]))
         continue;
-      const float sq = fmaxf(s3, fmaxf(fabsf(qxf), fabsf(qyf)));
-      // 52 u S^2, or the double path when S^2 is out of float range
-      const float eb = (sq > 1e-15f && sq < 1e15f) ? 52.0f * 5.9604645e-8f * sq * sq : -1.0f;
-      if (!orient_nonneg(P, a, b, q, eb) || !orient_nonneg(P, b, c, q, eb) || !orient_nonneg(P, c, a, q, eb)) continue;
+      if (orient_sign(P, a, b, q) < 0 || orient_sign(P, b, c, q) < 0 || orient_sign(P, c, a, q) < 0) continue;
       if (!arPos) {
         // a flat ear: only nodes within the box of its two ends count
         const double qx = P.X[q], qy = P.Y[q], ax = P.X[a], ay = P.Y[a], cx = P.X[c], cy = P.Y[c];
@@ -697,7 +692,6 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
       break;
     }
   }
-  (void)flatEar;
   return !__any_sync(CUT_FULL, hit);
 }
 
@@ -1287,6 +1281,8 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
   Pg.gNodes = w + cv.gNodes;
   Pg.Xf = reinterpret_cast<float*>(w + cv.ndXf);
   Pg.Yf = reinterpret_cast<float*>(w + cv.ndYf);
+  Pg.Xl = reinterpret_cast<float*>(w + cv.ndXl);
+  Pg.Yl = reinterpret_cast<float*>(w + cv.ndYl);
   Ring Ps;
   {
     double* sx = reinterpret_cast<double*>(capSm);
@@ -1302,6 +1298,8 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
     Ps.gStart = Ps.gCnt + CAP_SM_NODES / 2 + 2;
     Ps.Xf = reinterpret_cast<float*>(Ps.gStart + CAP_SM_NODES / 2 + 2);
     Ps.Yf = Ps.Xf + CAP_SM_NODES;
+    Ps.Xl = Ps.Yf + CAP_SM_NODES;
+    Ps.Yl = Ps.Xl + CAP_SM_NODES;
     Ps.cap = CAP_SM_NODES;
     Ps.n = 0;
   }
