@@ -712,10 +712,24 @@ __device__ void build_grid(Ring& P, int lane) {
     y0 = fminf(y0, __shfl_xor_sync(CUT_FULL, y0, d));
     y1 = fmaxf(y1, __shfl_xor_sync(CUT_FULL, y1, d));
   }
-  uint32_t g = 1;
-  while (2 * (g + 1) * (g + 1) <= P.n) g++;
-  P.gnx = x1 > x0 ? g : 1u;
-  P.gny = y1 > y0 ? g : 1u;
+  // about two nodes per cell, the cells shaped like the box (a long thin
+  // cap gets one row of cells along its length, not a square grid whose
+  // few occupied cells each hold many nodes)
+  const uint32_t C = max(1u, P.n / 2);
+  const float bw = x1 - x0, bh = y1 - y0;
+  if (!(bw > 0.0f) && !(bh > 0.0f)) {
+    P.gnx = P.gny = 1;
+  } else if (!(bh > 0.0f)) {
+    P.gnx = C;
+    P.gny = 1;
+  } else if (!(bw > 0.0f)) {
+    P.gnx = 1;
+    P.gny = C;
+  } else {
+    const float gx = sqrtf((float)C * bw / bh);
+    P.gnx = gx < 1.0f ? 1u : (gx > (float)C ? C : (uint32_t)gx);
+    P.gny = max(1u, C / P.gnx);
+  }
   P.gx0 = x0;
   P.gy0 = y0;
   P.ginvx = x1 > x0 ? (float)P.gnx / (x1 - x0) : 0.0f;
