@@ -370,6 +370,10 @@ def run_engine(args):
         # the metric's second half: whole decompositions per second, the
         # uneven batch decomposed together against one mesh at a time
         line["decompose"] = decompose_measure(args.meshes)
+    if world == 1 and not args.no_serve:
+        # the serving configuration: 60 s of Poisson arrivals at 200 req/s
+        # under the device-memory budget, p50 / p99 latency beside the rate
+        line["serving"] = serve_measure(args.rate, args.duration, args.pool, args.admit_bytes, args.slots, args.max_queue)
     print(json.dumps(line), flush=True)
 
 
@@ -624,17 +628,23 @@ def decompose_measure(n_meshes, big_steps=2):
     }
 
 
-def serve_session(dec, pool, rate, duration, admit_tris, seed=1, clocks=False):
+def serve_session(dec, pool, rate, duration, admit_bytes=0, max_active=0, max_queue=0, seed=1, clocks=False):
     """One serving session: Poisson arrivals at `rate` for `duration`
-    seconds into a fresh server, then drained. Returns (latencies in ms,
-    per-kind latencies, wall seconds, requests, clock summary)."""
+    seconds into a fresh server (device budget admit_bytes, 0 = 80 % of the
+    GPU's memory; max_active slots; at most max_queue waiting requests, 0 =
+    no bound), then
+    drained. Returns a dict: latencies in ms (completion minus arrival,
+    queueing included) overall and per mesh kind, wall seconds, requests
+    offered, submissions refused with a full queue, the server's memory
+    figures and the clock summary."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
     arr = np.cumsum(rng.exponential(1.0 / rate, size=int(rate * duration * 2) + 16))
     arr = arr[arr < duration]
     pick = rng.integers(0, len(pool), size=len(arr))
-    srv = dec.Server(admit_tris=admit_tris, threshold=0.05, width=6, width2=3, depth=2, tree=DEC_TREE)
+    srv = dec.Server(admit_bytes=admit_bytes, max_active=max_active, max_queue=max_queue, threshold=0.05, width=6,
+                     width2=3, depth=2, tree=DEC_TREE)
     clk_summary = None
     try:
         # warm-up: the two trees (one per threshold) and their buffers
@@ -643,16 +653,22 @@ def serve_session(dec, pool, rate, duration, admit_tris, seed=1, clocks=False):
             while srv.take(t) is None:
                 srv.step()
         t0 = time.perf_counter()
-        i, out, lat, kinds = 0, {}, [], {}
+        i, out, lat, kinds, refused, most_active = 0, {}, [], {}, 0, 0
         with ClockSampler(0 if clocks else None) as clk:
             while i < len(arr) or srv.pending:
                 now = time.perf_counter() - t0
                 while i < len(arr) and arr[i] <= now:
                     kind, m, thr = pool[pick[i]]
-                    out[srv.submit(m, thr)] = (arr[i], kind)
+                    try:
+                        out[srv.submit(m, thr)] = (arr[i], kind)
+                    except dec.CuacdError as e:
+                        if e.code != dec.Server.E_BUSY:
+                            raise
+                        refused += 1
                     i += 1
                 if srv.pending:
                     srv.step()
+                    most_active = max(most_active, srv.stats()["active"])
                 elif i < len(arr):
                     time.sleep(max(0.0, arr[i] - (time.perf_counter() - t0)))
                 for t in list(out):
@@ -665,9 +681,14 @@ def serve_session(dec, pool, rate, duration, admit_tris, seed=1, clocks=False):
         wall = time.perf_counter() - t0
         if clocks:
             clk_summary = clk.summary()
+        st = srv.stats()
     finally:
         srv.destroy()
-    return np.array(lat), kinds, wall, len(arr), clk_summary
+    return {"lat": np.array(lat), "kinds": kinds, "wall": wall, "offered": len(arr), "refused": refused,
+            "most_active": most_active, "memory": {"budget_bytes": st["budgetBytes"],
+                                                   "peak_device_bytes": st["peakDeviceBytes"],
+                                                   "device_bytes_at_end": st["deviceBytes"]},
+            "clocks": clk_summary}
 
 
 def _lat_summary(lat, kinds):
@@ -678,31 +699,51 @@ def _lat_summary(lat, kinds):
              for k, v in kinds.items()})
 
 
-def run_serve(args):
-    """Serving: Poisson arrivals of decomposition requests (40% staircases of
-    4..16 steps, 40% blobs of 2k..60k triangles, 20% carved icospheres of
-    level 3..5; thresholds 0.05 or 0.1) into the continuous-batching server
-    for `duration` seconds, then drained. Latency = completion time minus
-    arrival time, queueing included. A second session at 2 req/s (below the
-    server's capacity) reports the latency without a growing queue."""
+SERVE_MIX = "40% staircases 4..16 steps, 40% blobs 2k..60k tris, 20% carved icospheres L3..5"
+
+
+def serve_measure(rate=200.0, duration=60.0, pool_size=48, admit_bytes=0, max_active=32, max_queue=64, low_rate=2.0,
+                  low_duration=15.0, clocks=False):
+    """The serving configuration: Poisson arrivals of decomposition
+    requests (40% staircases of 4..16 steps, 40% blobs of 2k..60k triangles,
+    20% carved icospheres of level 3..5; thresholds 0.05 or 0.1) into the
+    continuous-batching server for `duration` seconds under a device budget
+    (0 = 80 % of the GPU's memory) and max_active slots, with at most
+    max_queue waiting requests,
+    then drained. A second session at low_rate (below the server's
+    capacity) reports the latency without a standing queue."""
     dec = importlib.import_module("cuacd-web_gb300.decompose")
     gen = importlib.import_module("cuacd-web_gb300.meshgen")
-    pool = gen.serving_mix(args.pool, seed=0)
-    lat, kinds, wall, n, clk = serve_session(dec, pool, args.rate, args.duration, args.admit_tris, clocks=True)
-    p, pk = _lat_summary(lat, kinds)
-    line = {"metric": "decomposition requests served/s", "value": len(lat) / wall, "unit": "requests/s", "n_gpus": 1,
-            "steps": 1, "warmup": 1, "ms_per_step": 1000 * wall, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"Poisson arrivals at {args.rate} req/s for {args.duration} s "
-                                   f"({n} requests from {args.pool} distinct meshes), then drained",
-                       "mix": "40% staircases 4..16 steps, 40% blobs 2k..60k tris, 20% carved icospheres L3..5",
-                       "thresholds": [0.05, 0.1], "admit_tris": args.admit_tris, "width": 6, "depth": 2},
-            "latency_ms": p, "latency_ms_by_kind": pk, "offered_rate": args.rate, "clocks": clk}
-    if args.rate > 2.0:
-        lat2, kinds2, wall2, n2, _ = serve_session(dec, pool, 2.0, 15.0, args.admit_tris, seed=2)
-        p2, pk2 = _lat_summary(lat2, kinds2)
-        line["below_capacity"] = {"offered_rate": 2.0, "duration_s": 15.0, "requests": n2,
-                                  "served_per_s": len(lat2) / wall2, "latency_ms": p2, "latency_ms_by_kind": pk2}
+    pool = gen.serving_mix(pool_size, seed=0)
+    hi = serve_session(dec, pool, rate, duration, admit_bytes, max_active, max_queue, clocks=clocks)
+    p, pk = _lat_summary(hi["lat"], hi["kinds"])
+    out = {"metric": "decomposition requests served/s", "value": len(hi["lat"]) / hi["wall"], "unit": "requests/s",
+           "seconds": hi["wall"], "offered_rate": rate, "offered": hi["offered"], "served": len(hi["lat"]),
+           "refused_queue_full": hi["refused"], "most_running": hi["most_active"], "latency_ms": p,
+           "latency_ms_by_kind": pk, "memory": hi["memory"],
+           "config": {"workload": f"Poisson arrivals at {rate} req/s for {duration} s ({hi['offered']} requests "
+                                  f"from {pool_size} distinct meshes), then drained",
+                      "mix": SERVE_MIX, "thresholds": [0.05, 0.1], "width": 6, "width2": 3, "depth": 2,
+                      "admission": "device memory: 80 % of the GPU's" if admit_bytes == 0 else f"{admit_bytes} bytes",
+                      "slots": max_active, "max_queue": max_queue}}
+    if clocks:
+        out["clocks"] = hi["clocks"]
+    if low_rate and low_rate < rate:
+        lo = serve_session(dec, pool, low_rate, low_duration, admit_bytes, max_active, max_queue, seed=2)
+        p2, pk2 = _lat_summary(lo["lat"], lo["kinds"])
+        out["below_capacity"] = {"offered_rate": low_rate, "duration_s": low_duration, "offered": lo["offered"],
+                                 "served": len(lo["lat"]), "refused_queue_full": lo["refused"],
+                                 "served_per_s": len(lo["lat"]) / lo["wall"], "latency_ms": p2,
+                                 "latency_ms_by_kind": pk2, "memory": lo["memory"]}
+    return out
+
+
+def run_serve(args):
+    m = serve_measure(args.rate, args.duration, args.pool, args.admit_bytes, args.slots, args.max_queue, clocks=True)
+    line = {"metric": m["metric"], "value": m["value"], "unit": m["unit"], "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1000 * m["seconds"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic", "config": m.pop("config"), "clocks": m.pop("clocks", None)}
+    line.update({k: v for k, v in m.items() if k not in ("metric", "value", "unit")})
     print(json.dumps(line), flush=True)
 
 
@@ -777,9 +818,12 @@ def main():
     ap.add_argument("--meshes", type=int, default=32, help="meshes of the uneven decomposition batch")
     ap.add_argument("--no-decompose", action="store_true", help="leave the decomposition summary out of the tree line")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
-    ap.add_argument("--duration", type=float, default=2.0, help="serving: seconds of arrivals")
+    ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of arrivals")
     ap.add_argument("--pool", type=int, default=48, help="serving: distinct request meshes")
-    ap.add_argument("--admit-tris", type=int, default=1 << 20, help="serving: triangles admitted at once")
+    ap.add_argument("--admit-bytes", type=int, default=0, help="serving: device budget in bytes (0: 80%% of the GPU's)")
+    ap.add_argument("--slots", type=int, default=32, help="serving: decompositions running at once (0: no bound)")
+    ap.add_argument("--max-queue", type=int, default=64, help="serving: waiting requests at most (0: no bound)")
+    ap.add_argument("--no-serve", action="store_true", help="leave the serving session out of the tree line")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

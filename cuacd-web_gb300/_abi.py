@@ -265,6 +265,22 @@ class MergeOpts(C.Structure):
     ]
 
 
+class ServerStats(C.Structure):
+    """cuacd_server_state — device memory and queue of a server."""
+
+    _fields_ = [
+        ("budgetBytes", C.c_uint64),
+        ("deviceBytes", C.c_uint64),
+        ("peakDeviceBytes", C.c_uint64),
+        ("workingSetBytes", C.c_uint64),
+        ("projectedBytes", C.c_uint64),
+        ("admitted", C.c_uint64),
+        ("rejected", C.c_uint64),
+        ("queued", C.c_int32),
+        ("active", C.c_int32),
+    ]
+
+
 class MergeStats(C.Structure):
     """cuacd_merge_stats — MergeStats (merge.ts:54-66)."""
 

@@ -14,6 +14,8 @@ namespace conc {
 struct Engine;
 Engine* engine_create();
 void engine_destroy(Engine* e);
+// device bytes the engine's buffers hold (they grow with the largest batch)
+size_t engine_device_bytes(const Engine* e);
 // concaveEdgePlanes of every mesh on `stream`: mesh k's planes (at most
 // 4 * nConcaveEdges, 4 floats each) go to out + 16 * nConcaveEdges * k and
 // their count to counts[k]; seeds[k] is its reservoir seed.

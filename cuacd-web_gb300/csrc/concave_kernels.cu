@@ -279,6 +279,15 @@ void engine_destroy(Engine* e) {
   delete e;
 }
 
+size_t engine_device_bytes(const Engine* e) {
+  if (!e) return 0;
+  size_t n = 0;
+  for (const Buf* b : {&e->inV, &e->inT, &e->desc, &e->vPre, &e->ePre, &e->deg, &e->off, &e->fill, &e->list, &e->slots,
+                       &e->cnt, &e->cpre, &e->ordered, &e->res, &e->out, &e->counts, &e->tiles})
+    n += b->bytes;
+  return n;
+}
+
 #define CONCK(x)                                                                                 \
   do {                                                                                           \
     cudaError_t err_ = (x);                                                                      \

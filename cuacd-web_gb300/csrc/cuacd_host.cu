@@ -819,6 +819,68 @@ void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
 
 void cuacd_tree_destroy(void* t) { delete (Tree*)t; }
 
+int cuacd_device_memory(uint64_t* total, uint64_t* freeBytes) {
+  size_t f = 0, t = 0;
+  const cudaError_t e = cudaMemGetInfo(&f, &t);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(e == cudaErrorNoDevice ? CUACD_E_NODEVICE : CUACD_E_CUDA,
+                std::string("cuacd_device_memory: ") + cudaGetErrorString(e));
+  }
+  if (total) *total = t;
+  if (freeBytes) *freeBytes = f;
+  return CUACD_OK;
+}
+
+int cuacd_tree_memory(const void* tree, uint64_t* deviceBytes, uint64_t* caps4) {
+  const Tree* t = (const Tree*)tree;
+  if (!t) return fail(CUACD_E_INVALID, "cuacd_tree_memory: null tree");
+  uint64_t n = cut::engine_device_bytes(t->cutter) + conc::engine_device_bytes(t->concave);
+  for (const DevBuf* b : {&t->bV, &t->bT, &t->bE, &t->bS, &t->bCtr, &t->bSlab, &t->bParts, &t->bItems, &t->bJobs,
+                          &t->bPlanes, &t->bSnap, &t->bHd, &t->bScan, &t->bWork, &t->bUb})
+    n += b->bytes;
+  if (deviceBytes) *deviceBytes = n;
+  if (caps4) {
+    caps4[0] = t->cfg.vertexCap;
+    caps4[1] = t->cfg.triCap;
+    caps4[2] = t->cfg.edgeCap;
+    caps4[3] = t->cfg.scratchWords;
+  }
+  return CUACD_OK;
+}
+
+int cuacd_tree_reserve_pools(void* tree, const uint64_t* caps4) {
+  Tree* t = (Tree*)tree;
+  if (!t || !caps4) return fail(CUACD_E_INVALID, "cuacd_tree_reserve_pools: invalid argument");
+  uint64_t* cur[4] = {&t->cfg.vertexCap, &t->cfg.triCap, &t->cfg.edgeCap, &t->cfg.scratchWords};
+  DevBuf* buf[4] = {&t->bV, &t->bT, &t->bE, &t->bS};
+  const uint64_t unit[4] = {4, 4, 32, 4};
+  bool grow = false;
+  for (int k = 0; k < 4; k++) {
+    if (caps4[k] > 0xffffffffull) return fail(CUACD_E_CAPACITY, "cuacd_tree_reserve_pools: pools exceed 32-bit offsets");
+    grow |= caps4[k] > *cur[k];
+  }
+  if (!grow) return CUACD_OK;
+  cudaStreamSynchronize(t->stream);
+  // a pool that cannot grow is allocated again at its old size, so the
+  // handle stays usable after a refusal
+  int rc = 0;
+  for (int k = 0; k < 4 && rc == 0; k++) {
+    if (caps4[k] <= *cur[k]) continue;
+    if (buf[k]->ensure(caps4[k] * unit[k])) {
+      const std::string m = g_err;
+      buf[k]->ensure(std::max<uint64_t>(*cur[k], 4) * unit[k]);
+      rc = fail(CUACD_E_CUDA, "cuacd_tree_reserve_pools: " + m);
+      break;
+    }
+    *cur[k] = caps4[k];
+  }
+  t->prepared = false;
+  t->gvalid = false;
+  t->bind();
+  return rc;
+}
+
 int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, const int32_t* meshOfCut,
                           const double* planes, int nCuts, int flags, void** halves) {
   Tree* t = (Tree*)tree;

@@ -38,6 +38,8 @@ struct Halves {
 struct Engine;
 Engine* engine_create();
 void engine_destroy(Engine* e);
+// device bytes the engine's buffers hold (they grow with the largest batch)
+size_t engine_device_bytes(const Engine* e);
 // Cuts meshes[cuts[k].mesh] by each plane on `stream`. Mesh indices must be
 // in range. closed = the caller vouches that every mesh is closed (each
 // directed edge has a reverse), as the decomposer's parts are: the pass that

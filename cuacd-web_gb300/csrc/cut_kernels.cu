@@ -1670,6 +1670,18 @@ void engine_destroy(Engine* e) {
   delete e;
 }
 
+size_t engine_device_bytes(const Engine* e) {
+  if (!e) return 0;
+  size_t n = 0;
+  for (const Buf* b : {&e->inV, &e->inT, &e->desc, &e->vPre, &e->tPre, &e->sizes, &e->layout, &e->out, &e->cPre,
+                       &e->dist, &e->sgn, &e->cnt, &e->pre, &e->tiles, &e->hashKeys, &e->hashXYZ, &e->surfT, &e->candE,
+                       &e->firstPos, &e->flag, &e->fpre, &e->words, &e->dbls, &e->outVOff, &e->outTOff, &e->outV,
+                       &e->outT, &e->vol, &e->openBits, &e->openKeys, &e->openMeta, &e->volChunks, &e->volPre,
+                       &e->volPart})
+    n += b->bytes;
+  return n;
+}
+
 #define CUTCK(x)                                                                             \
   do {                                                                                       \
     cudaError_t err_ = (x);                                                                  \

@@ -1117,26 +1117,44 @@ Engine* make_engine(const cuacd_decompose_opts& o, int* err) {
 }
 
 // ---------------------------------------------------------------------------
-// Serving: continuous batching of decompositions. Requests wait in a queue
-// and are admitted in arrival order while the triangles of the admitted
-// meshes stay within a budget (at least one is always admitted). Every step
-// runs one iteration of every admitted decomposition together (one tree
-// launch per threshold), then finishes the ones with nothing left to cut
-// (merge pass included), so a request that arrives while others are on the
-// GPU joins them at the next step. A decomposition's parts do not depend on
-// what else was admitted with it.
+// Serving: continuous batching of decompositions under a device-memory
+// budget. Requests wait in a queue (of at most maxQueue; a submission to a
+// full queue is refused) and are admitted in arrival order while the device
+// bytes of the server's trees, with the pools grown for every admitted
+// request's working set, stay within the budget (one request is always
+// admitted when none runs). A request's working set is the pool space of one
+// lookahead run with its mesh as the seed: every job of level l splits a
+// copy of at most the seed plus the intersection points (the halves hold the
+// split triangles of the crossing edges), level 0 has width + planeSlots jobs
+// per seed and each deeper level width2 times its parent level's; the
+// estimate takes the seed's vertices and triangles once per job, with half
+// again for the crossings. Every step runs one iteration of every admitted
+// decomposition together (one tree launch per threshold, its pools grown
+// beforehand so the launch needs no split), then finishes the ones with
+// nothing left to cut (merge pass included), so a request that arrives while
+// others are on the GPU joins them at the next step. A decomposition's parts
+// do not depend on what else was admitted with it.
+// bytes of pools with these capacities (vertex floats, triangle u32, open
+// edges of 32 bytes, scratch u32)
+static uint64_t pool_bytes(const uint64_t* c) { return 4 * c[0] + 4 * c[1] + 32 * c[2] + 4 * c[3]; }
+
 struct Request {
   uint64_t ticket = 0;
   std::unique_ptr<Job> job;
   Clock::time_point submitted;
   float threshold = 0;
-  uint64_t tris = 0;
+  uint64_t need[4] = {0, 0, 0, 0};  // working set in the pools: vertex floats, triangle u32, open edges, scratch u32
+  uint64_t aux = 0;                  // allowance for the cut, concave-plane and Hausdorff buffers
+  uint64_t bytes() const { return pool_bytes(need) + aux; }
 };
 
 class Server {
  public:
   cuacd_decompose_opts base{};
-  uint64_t admitTris = 0;
+  uint64_t budget = 0;   // device bytes the server may hold
+  size_t maxQueue = 0;   // 0: unbounded
+  size_t maxActive = 0;  // running requests at most (slots); 0: unbounded
+  int planeSlots = 0;
   std::map<uint32_t, std::unique_ptr<Engine>> engines;  // by threshold bits
   std::vector<Request> queue;                           // FIFO
   size_t queueHead = 0;
@@ -1144,11 +1162,15 @@ class Server {
   std::map<uint64_t, std::unique_ptr<Result>> done;
   std::map<uint64_t, std::pair<int, std::string>> failed;
   uint64_t nextTicket = 1;
-  uint64_t activeTris = 0;
+  uint64_t rejected = 0, peakBytes = 0, admittedTotal = 0;
 
-  Engine* engine_for(float thr) {
+  static uint32_t key_of(float thr) {
     uint32_t key;
     std::memcpy(&key, &thr, 4);
+    return key;
+  }
+  Engine* engine_for(float thr) {
+    const uint32_t key = key_of(thr);
     auto it = engines.find(key);
     if (it != engines.end()) return it->second.get();
     cuacd_decompose_opts o = base;
@@ -1158,6 +1180,85 @@ class Server {
     if (!e) throw Failure{err, cuacd_last_error()};
     engines.emplace(key, std::unique_ptr<Engine>(e));
     return e;
+  }
+  // pool space of one lookahead run with an (nv, nt) seed. Level l has
+  // J_l jobs (J_0 = width + planeSlots, J_l+1 = width2 J_l); a job's two
+  // children hold up to 2.5 nv + 64 vertices together (the children keep
+  // the parent's vertices on their side plus the intersection points), the
+  // children of the levels that keep topology (all but the last) 1.5 nt + 64
+  // triangles and 16 sqrt(nt) + 64 open rim edges; a level's plan scratch is
+  // 2 words per parent vertex of each of its jobs. These bounds hold with a
+  // margin of 1.2 or more on every seed measured (icospheres, staircases,
+  // blobs of 100 to 4,000 triangles, depth 2 and 3, with refinement).
+  void working_set(uint64_t nv, uint64_t nt, uint64_t* need) const {
+    uint64_t jobs = (uint64_t)base.width + (uint64_t)planeSlots, all = 0, topo = 0, last = 0;
+    for (int l = 0; l < base.depth; l++) {
+      all += jobs;
+      if (l + 1 < base.depth) topo += jobs;
+      last = jobs;
+      jobs *= (uint64_t)base.width2;
+    }
+    const uint64_t rim = 16 * (uint64_t)std::ceil(std::sqrt((double)nt)) + 64;
+    need[0] = all * 3 * (5 * nv / 2 + 64) + 3 * nv + 4096;
+    need[1] = topo * 3 * (3 * nt / 2 + 64) + 3 * nt + 4096;
+    need[2] = topo * rim + 4096;
+    need[3] = 2 * last * (3 * nv / 2 + 64) + 4096;
+  }
+  // the buffers of the passes outside the tree pools grow with the work of
+  // a step: the cut's inputs, classification, hash tables, cap arenas and
+  // halves with the parts cut (at most the mesh and its caps), the tables
+  // with the seeds, and the merge pass's hull and Hausdorff batches (chunks
+  // of 256 pairs) with the parts. A tree counts 64 MB for its batches and
+  // each request 64 bytes per input byte, twice the growth measured on
+  // icospheres of 1,280 triangles decomposed alone.
+  static uint64_t aux_bytes(uint64_t nv, uint64_t nt) { return 64 * 12 * (nv + nt) + (1 << 20); }
+  static constexpr uint64_t kTreeBatchBytes = 64ull << 20;
+  struct Mem {
+    uint64_t nonPool = 0, aux = 0, cap[4] = {0, 0, 0, 0}, need[4] = {0, 0, 0, 0};
+    bool built = false;
+  };
+  // per tree at creation: bytes besides the pools, and the pools'
+  // capacities; the hull slabs (up to hullBudgetBytes) and the buffers of
+  // the cut, concave-plane and Hausdorff passes grow later
+  uint64_t createdNonPool = 0, createdCap[4] = {0, 0, 0, 0}, hullBudget = 0;
+  uint64_t mem_total(const Mem& x) const {
+    const uint64_t fixed = std::max(x.nonPool, createdNonPool + hullBudget + kTreeBatchBytes + x.aux);
+    uint64_t c[4];
+    for (int k = 0; k < 4; k++) c[k] = std::max(x.cap[k], x.need[k]);
+    return fixed + pool_bytes(c);
+  }
+  // device bytes of every tree (one not built yet counts as built), with
+  // its pools grown to the working sets of the active requests and `extra`
+  std::map<uint32_t, Mem> memory(const Request* extra) const {
+    std::map<uint32_t, Mem> m;
+    for (const auto& kv : engines) {
+      uint64_t held = 0;
+      Mem& x = m[kv.first];
+      cuacd_tree_memory(kv.second->tree, &held, x.cap);
+      x.nonPool = held - pool_bytes(x.cap);
+      x.built = true;
+    }
+    auto add = [&](const Request& r) {
+      Mem& x = m[key_of(r.threshold)];
+      if (!x.built)
+        for (int k = 0; k < 4; k++) x.cap[k] = createdCap[k];
+      for (int k = 0; k < 4; k++) x.need[k] += r.need[k];
+      x.aux += r.aux;
+    };
+    for (const Request& r : active)
+      if (r.job) add(r);
+    if (extra) add(*extra);
+    return m;
+  }
+  uint64_t projected(const Request* extra) const {
+    uint64_t n = 0;
+    for (const auto& kv : memory(extra)) n += mem_total(kv.second);
+    return n;
+  }
+  bool engine_busy(uint32_t key) const {
+    for (const Request& r : active)
+      if (r.job && key_of(r.threshold) == key) return true;
+    return false;
   }
 
   void complete(Request& r) {
@@ -1172,14 +1273,31 @@ class Server {
 
   int step(int* completed) {
     int nDone = 0;
-    // admission
+    // admission by device memory; a tree with no active request gives its
+    // pools back (it is built again when a request needs it) when the next
+    // request would not fit beside them
     std::vector<size_t> admitted;
     while (queueHead < queue.size()) {
       Request& q = queue[queueHead];
-      if (!active.empty() && activeTris + q.tris > admitTris) break;
-      activeTris += q.tris;
+      if (maxActive && active.size() >= maxActive) break;
+      if (!active.empty()) {
+        if (projected(&q) > budget) {
+          bool freed = false;
+          for (auto it = engines.begin(); it != engines.end();) {
+            if (!engine_busy(it->first)) {
+              it = engines.erase(it);
+              freed = true;
+            } else {
+              ++it;
+            }
+          }
+          if (!freed || projected(&q) > budget) break;
+        }
+      }
+      engine_for(q.threshold);
       active.push_back(std::move(q));
       admitted.push_back(active.size() - 1);
+      admittedTotal++;
       queueHead++;
     }
     if (queueHead == queue.size()) {
@@ -1198,11 +1316,35 @@ class Server {
       fresh[engine_for(r.threshold)].push_back(r.job.get());
     }
     for (auto& kv : fresh) kv.first->begin(kv.second);
+    // the pools of each tree grow to its requests' working sets, so one
+    // launch per threshold runs the whole step
+    for (const auto& kv : memory(nullptr)) {
+      auto it = engines.find(kv.first);
+      if (it == engines.end()) continue;
+      uint64_t c[4];
+      for (int k = 0; k < 4; k++) c[k] = std::min<uint64_t>(std::max(kv.second.cap[k], kv.second.need[k]), 0xffffffffull);
+      const int rc = cuacd_tree_reserve_pools(it->second->tree, c);
+      if (rc != CUACD_OK) throw Failure{rc, cuacd_last_error()};
+    }
+    uint64_t held = 0;
+    for (const auto& kv : engines) {
+      uint64_t b = 0;
+      cuacd_tree_memory(kv.second->tree, &b, nullptr);
+      held += b;
+    }
     // one iteration of every admitted decomposition, per threshold
     std::map<Engine*, std::vector<Job*>> groups;
     for (Request& r : active)
       if (r.job) groups[engine_for(r.threshold)].push_back(r.job.get());
     for (auto& kv : groups) kv.first->iterate(kv.second);
+    // the buffers of the cut and concave passes grow inside the step
+    uint64_t after = 0;
+    for (const auto& kv : engines) {
+      uint64_t b = 0;
+      cuacd_tree_memory(kv.second->tree, &b, nullptr);
+      after += b;
+    }
+    peakBytes = std::max({peakBytes, held, after});
     // decompositions with nothing left to cut finish together
     std::map<Engine*, std::vector<Job*>> fin;
     for (Request& r : active)
@@ -1210,12 +1352,8 @@ class Server {
     for (auto& kv : fin) kv.first->finish(kv.second);
     std::vector<Request> keep;
     for (Request& r : active) {
-      if (!r.job) {
-        activeTris -= r.tris;
-        continue;
-      }
+      if (!r.job) continue;
       if (r.job->cutting_done) {
-        activeTris -= r.tris;
         complete(r);
         nDone++;
       } else {
@@ -1517,16 +1655,33 @@ void cuacd_result_free(void* r) { delete static_cast<Result*>(r); }
 
 // ---- serving -----------------------------------------------------------
 
-void* cuacd_server_create(const cuacd_decompose_opts* o, uint64_t admitTris, int* err) {
-  if (!o) {
-    if (err) *err = set_error(CUACD_E_INVALID, "cuacd_server_create: null options");
+void* cuacd_server_create(const cuacd_decompose_opts* o, uint64_t admitBytes, int32_t maxActive, int32_t maxQueue,
+                          int* err) {
+  if (!o || maxQueue < 0 || maxActive < 0) {
+    if (err) *err = set_error(CUACD_E_INVALID, "cuacd_server_create: null options or negative bound");
     return nullptr;
   }
   std::unique_ptr<Server> s(new Server());
   s->base = *o;
-  s->admitTris = admitTris;
+  s->maxQueue = (size_t)maxQueue;
+  s->maxActive = (size_t)maxActive;
+  if (admitBytes == 0) {
+    uint64_t total = 0;
+    const int rc = cuacd_device_memory(&total, nullptr);
+    if (rc != CUACD_OK) {
+      if (err) *err = rc;
+      return nullptr;
+    }
+    admitBytes = total / 5 * 4;  // 20 % headroom
+  }
+  s->budget = admitBytes;
   try {
-    s->engine_for(o->threshold);  // validates the options and builds the first tree
+    Engine* e = s->engine_for(o->threshold);  // validates the options and builds the first tree
+    s->planeSlots = e->planeSlots;
+    uint64_t held = 0;
+    cuacd_tree_memory(e->tree, &held, s->createdCap);
+    s->createdNonPool = held - pool_bytes(s->createdCap);
+    s->hullBudget = e->o.tree.hullBudgetBytes;
   } catch (const Failure& f) {
     if (err) *err = set_error(f.code, f.msg.c_str());
     return nullptr;
@@ -1541,18 +1696,48 @@ int cuacd_server_submit(void* sv, const cuacd_mesh* m, float threshold, uint64_t
   Server* s = static_cast<Server*>(sv);
   if (!s || !m || !ticket || (m->nv && !m->verts) || (m->nt && !m->tris))
     return set_error(CUACD_E_INVALID, "cuacd_server_submit: invalid argument");
+  for (size_t k = 0; k < 3 * (size_t)m->nt; k++)
+    if (m->tris[k] >= m->nv) return set_error(CUACD_E_INVALID, "cuacd_server_submit: triangle index out of range");
   Request r;
+  s->working_set(m->nv, m->nt, r.need);
+  r.aux = Server::aux_bytes(m->nv, m->nt);
+  if (r.bytes() > s->budget)
+    return set_error(CUACD_E_CAPACITY, ("cuacd_server_submit: the mesh's working set (" + std::to_string(r.bytes()) +
+                                        " bytes) exceeds the server's device budget")
+                                           .c_str());
+  if (s->maxQueue && s->queue.size() - s->queueHead >= s->maxQueue) {
+    s->rejected++;
+    return set_error(CUACD_E_BUSY, "cuacd_server_submit: queue full");
+  }
   r.ticket = s->nextTicket++;
   r.job.reset(new Job());
   r.job->input.v.assign(m->verts, m->verts + 3 * (size_t)m->nv);
   r.job->input.t.assign(m->tris, m->tris + 3 * (size_t)m->nt);
-  for (uint32_t x : r.job->input.t)
-    if (x >= m->nv) return set_error(CUACD_E_INVALID, "cuacd_server_submit: triangle index out of range");
   r.submitted = Clock::now();
   r.threshold = threshold > 0 ? threshold : s->base.threshold;
-  r.tris = m->nt;
   *ticket = r.ticket;
   s->queue.push_back(std::move(r));
+  return CUACD_OK;
+}
+
+int cuacd_server_stats(const void* sv, cuacd_server_state* out) {
+  const Server* s = static_cast<const Server*>(sv);
+  if (!s || !out) return set_error(CUACD_E_INVALID, "cuacd_server_stats: invalid argument");
+  std::memset(out, 0, sizeof *out);
+  out->budgetBytes = s->budget;
+  for (const auto& kv : s->engines) {
+    uint64_t b = 0;
+    cuacd_tree_memory(kv.second->tree, &b, nullptr);
+    out->deviceBytes += b;
+  }
+  out->peakDeviceBytes = std::max(s->peakBytes, out->deviceBytes);
+  out->projectedBytes = s->projected(nullptr);
+  for (const Request& r : s->active)
+    if (r.job) out->workingSetBytes += r.bytes();
+  out->admitted = s->admittedTotal;
+  out->rejected = s->rejected;
+  out->queued = (int32_t)(s->queue.size() - s->queueHead);
+  out->active = (int32_t)s->active.size();
   return CUACD_OK;
 }
 

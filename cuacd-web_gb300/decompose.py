@@ -74,7 +74,8 @@ def _lib():
         L.cuacd_concave_planes.argtypes = [P(A.MeshRef), C.c_int, C.c_double, C.c_double, C.c_uint32, P(C.c_float),
                                            C.c_int]
         L.cuacd_server_create.restype = C.c_void_p
-        L.cuacd_server_create.argtypes = [P(A.DecomposeOpts), C.c_uint64, P(C.c_int)]
+        L.cuacd_server_create.argtypes = [P(A.DecomposeOpts), C.c_uint64, C.c_int32, C.c_int32, P(C.c_int)]
+        L.cuacd_server_stats.argtypes = [C.c_void_p, P(A.ServerStats)]
         L.cuacd_server_destroy.argtypes = [C.c_void_p]
         L.cuacd_server_submit.argtypes = [C.c_void_p, P(A.MeshRef), C.c_float, P(C.c_uint64)]
         L.cuacd_server_step.argtypes = [C.c_void_p, P(C.c_int)]
@@ -273,16 +274,29 @@ class Server:
     """Continuous batching of decompositions (cuacd_server_*): submit
     meshes at any time, step the server, take finished results. Each step
     runs one iteration of every admitted decomposition together; requests
-    are admitted in arrival order while the admitted triangles stay within
-    admit_tris."""
+    are admitted in arrival order while one of max_active slots is free (0:
+    no bound) and the server's device memory, with its pools grown for every
+    admitted request's working set, stays within admit_bytes (0: 80 % of the
+    device's memory). At most max_queue requests wait (0: no bound); submit
+    raises CuacdError with CUACD_E_BUSY (-6) when the queue is full."""
 
-    def __init__(self, admit_tris: int = 8 << 20, **options):
+    E_BUSY = -6
+
+    def __init__(self, admit_bytes: int = 0, max_active: int = 0, max_queue: int = 0, **options):
         L = _lib()
         self.opts = _opts(dict(options))
         err = C.c_int(0)
-        self.h = L.cuacd_server_create(C.byref(self.opts), C.c_uint64(int(admit_tris)), C.byref(err))
+        self.h = L.cuacd_server_create(C.byref(self.opts), C.c_uint64(int(admit_bytes)), C.c_int32(int(max_active)),
+                                       C.c_int32(int(max_queue)), C.byref(err))
         if not self.h:
             raise CuacdError(err.value, L.cuacd_last_error().decode())
+
+    def stats(self) -> dict:
+        """Device budget and bytes held, working sets, admitted / rejected
+        counts and queue lengths (cuacd_server_stats)."""
+        st = A.ServerStats()
+        _check(_lib().cuacd_server_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in A.ServerStats._fields_}
 
     def destroy(self):
         if getattr(self, "h", None):

@@ -52,6 +52,9 @@ def load_library():
     L.cuacd_tree_create.argtypes = [P(A.TreeConfig), P(C.c_int)]
     L.cuacd_tree_destroy.argtypes = [C.c_void_p]
     L.cuacd_plane_slots.argtypes = [C.c_void_p]
+    L.cuacd_device_memory.argtypes = [P(C.c_uint64), P(C.c_uint64)]
+    L.cuacd_tree_memory.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_uint64)]
+    L.cuacd_tree_reserve_pools.argtypes = [C.c_void_p, P(C.c_uint64)]
     L.cuacd_set_profile.argtypes = [C.c_void_p, C.c_int]
     L.cuacd_tree_kernel_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.cuacd_tree_kernel_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
@@ -90,6 +93,13 @@ def load_library():
     return L
 
 
+def device_memory():
+    """(total, free) bytes of the current device (cudaMemGetInfo)."""
+    tot, free = C.c_uint64(), C.c_uint64()
+    _check(load_library().cuacd_device_memory(C.byref(tot), C.byref(free)))
+    return tot.value, free.value
+
+
 def _check(rc):
     if rc != 0:
         msg = load_library().cuacd_last_error().decode()
@@ -114,6 +124,18 @@ class GpuTree:
             raise CuacdError(err.value, L.cuacd_last_error().decode())
         self.plane_slots = L.cuacd_plane_slots(self.h)
         self.last_hull_fails = []
+
+    def memory(self):
+        """(device bytes held, {vertexCap, triCap, edgeCap, scratchWords})."""
+        b, caps = C.c_uint64(), (C.c_uint64 * 4)()
+        _check(load_library().cuacd_tree_memory(self.h, C.byref(b), caps))
+        return b.value, dict(zip(("vertexCap", "triCap", "edgeCap", "scratchWords"), list(caps)))
+
+    def reserve_pools(self, vertexCap=0, triCap=0, edgeCap=0, scratchWords=0):
+        """Grows the pools to at least these capacities (the configuration's
+        units); never shrinks them."""
+        caps = (C.c_uint64 * 4)(vertexCap, triCap, edgeCap, scratchWords)
+        _check(load_library().cuacd_tree_reserve_pools(self.h, caps))
 
     def destroy(self):
         if getattr(self, "h", None):

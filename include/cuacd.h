@@ -36,6 +36,7 @@ extern "C" {
 #define CUACD_E_SCRATCH (-3)  /* Hausdorff sample scratch exceeded (tree.ts:345) */
 #define CUACD_E_CUDA (-4)     /* CUDA runtime error (allocation, launch) */
 #define CUACD_E_NODEVICE (-5) /* no CUDA device */
+#define CUACD_E_BUSY (-6)     /* a server's queue is full */
 
 /* Maximum pairs of one Hausdorff call (HD_MAX_PAIRS, tree.ts:12). */
 #define CUACD_HD_MAX_PAIRS 1024
@@ -122,6 +123,24 @@ void* cuacd_tree_create(const cuacd_tree_config* cfg, int* err);
 
 /* GpuTree.destroy (tree.ts:813-815). */
 void cuacd_tree_destroy(void* tree);
+
+/* cudaMemGetInfo of the current device: total and free bytes (either
+ * pointer may be NULL). */
+int cuacd_device_memory(uint64_t* total, uint64_t* freeBytes);
+
+/* Device memory of a handle (no counterpart in the reference, whose pools
+ * are fixed at construction, tree.ts:150-176): *deviceBytes = bytes held by
+ * its pools, tables, hull slabs and the buffers of its GPU cut and
+ * concave-plane passes; caps4 = the pools' current capacities in the
+ * configuration's units: vertexCap (floats), triCap (u32), edgeCap (open
+ * edges, 32 bytes each), scratchWords (u32). Either output may be NULL. */
+int cuacd_tree_memory(const void* tree, uint64_t* deviceBytes, uint64_t* caps4);
+
+/* Grows the pools to at least caps4 = {vertexCap, triCap, edgeCap,
+ * scratchWords} (pools never shrink; at most 2^32 - 1 each). Waits for the
+ * handle's stream and drops a prepared run. When the device refuses an
+ * allocation that pool keeps its old capacity and CUACD_E_CUDA is returned. */
+int cuacd_tree_reserve_pools(void* tree, const uint64_t* caps4);
 
 /* GpuTree.planeSlots (tree.ts:759-761): plane slots per seed. */
 int cuacd_plane_slots(const void* tree);
@@ -422,10 +441,28 @@ int cuacd_filtered_concat(const cuacd_mesh* a, const cuacd_mesh* b, const double
                           uint32_t* outTris, int cap);
 
 /* Serving (no counterpart in the reference, whose decompose serves one mesh
- * per call): continuous batching of decompositions. Requests queue in
- * arrival order and are admitted while the admitted meshes' triangles stay
- * within admitTris (one is always admitted). Each cuacd_server_step runs one
- * iteration of every admitted decomposition together, one tree launch per
+ * per call): continuous batching of decompositions under a device-memory
+ * budget. admitBytes = device bytes the server may hold (0: 80 % of the
+ * device's memory); maxActive = decompositions running at once (slots; 0 =
+ * no bound besides memory). Requests queue in arrival order (at most maxQueue of them
+ * wait, 0 = no bound; a submission to a full queue returns CUACD_E_BUSY and
+ * counts as rejected) and are admitted while a slot is free and the server's trees, with their
+ * vertex and triangle pools grown to the working sets of every admitted
+ * request, fit in the budget (one request is always admitted when none runs;
+ * a tree with no running request gives its memory back when the next request
+ * would not fit beside it). A request's working set is the pool space of one
+ * lookahead run with its mesh (nv vertices, nt triangles) as the seed: level
+ * l has J_l jobs (J_0 = width + planeSlots, J_l+1 = width2 J_l), each job's
+ * children hold up to 2.5 nv + 64 vertices, the children of every level but
+ * the last 1.5 nt + 64 triangles and 16 sqrt(nt) + 64 open edges, and a
+ * level's plan scratch is 2 words per parent vertex per job; 64 bytes per
+ * input byte are added for the buffers of the cut, concave-plane and
+ * Hausdorff passes, and a tree counts its hull slabs at hullBudgetBytes plus
+ * 64 MB for the merge pass's hull and Hausdorff batches.
+ * Before each step every tree's pools grow to its running requests' working
+ * sets. A mesh whose working set alone exceeds the budget is
+ * refused with CUACD_E_CAPACITY at submission. Each cuacd_server_step runs
+ * one iteration of every admitted decomposition together, one tree launch per
  * threshold, and finishes (merge pass included) the decompositions with
  * nothing left to cut; a request submitted between steps joins at the next
  * one. A decomposition's parts are the same as cuacd_decompose gives it.
@@ -434,12 +471,29 @@ int cuacd_filtered_concat(const cuacd_mesh* a, const cuacd_mesh* b, const double
  * CUACD_OK with a one-mesh result handle (cuacd_result_* accessors; stats
  * totalMs = time from submission to completion) once the request finished,
  * 1 while it is queued or running, or the request's error. */
-void* cuacd_server_create(const cuacd_decompose_opts* o, uint64_t admitTris, int* err);
+typedef struct {
+  uint64_t budgetBytes;     /* the device budget */
+  uint64_t deviceBytes;     /* device bytes the server's trees hold now */
+  uint64_t peakDeviceBytes; /* the most they held at any step */
+  uint64_t workingSetBytes; /* working sets of the running requests */
+  uint64_t projectedBytes;  /* what admission compares with the budget: the
+                               trees with their pools grown to the running
+                               requests' working sets, plus allowances for
+                               their hull slabs and cut / concave-plane /
+                               Hausdorff buffers (at least the bytes held) */
+  uint64_t admitted;        /* requests admitted so far */
+  uint64_t rejected;        /* submissions refused with a full queue */
+  int32_t queued;           /* requests waiting */
+  int32_t active;           /* requests running */
+} cuacd_server_state;
+void* cuacd_server_create(const cuacd_decompose_opts* o, uint64_t admitBytes, int32_t maxActive, int32_t maxQueue,
+                          int* err);
 void cuacd_server_destroy(void* server);
 int cuacd_server_submit(void* server, const cuacd_mesh* mesh, float threshold, uint64_t* ticket);
 int cuacd_server_step(void* server, int* completed);
 int cuacd_server_pending(const void* server);
 int cuacd_server_take(void* server, uint64_t ticket, void** result);
+int cuacd_server_stats(const void* server, cuacd_server_state* out);
 
 /* planeCut with caps (src/cpu/cut.ts:33-315) on the host, for callers that
  * apply a cut themselves. plane = a, b, c, d (a x + b y + c z + d = 0). On

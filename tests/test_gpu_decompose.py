@@ -9,6 +9,7 @@ from fixtures import M, square_torus, stairs
 
 D = pkg("decompose")
 G = pkg("meshgen")
+T = pkg("tree")
 P = pkg("part")
 
 # smallTree (tests/decompose.test.ts:8)
@@ -93,28 +94,113 @@ def test_batched_equals_one_at_a_time():
 
 def test_server_same_alone_and_in_the_mix():
     """Continuous batching: requests arrive while others run, with two
-    thresholds; every result equals the mesh decomposed alone."""
+    thresholds; every result equals the mesh decomposed alone, and the
+    admission's projection of device memory is never below what the trees
+    hold."""
     opts = dict(maxIters=20, threshold=0.05, width=6, depth=2, tree=SMALL_TREE)
     meshes = [M.l_shape(), stairs(), square_torus(), G.staircase(6), G.noisy_icosphere(2, seed=4), M.unit_cube()]
     thresholds = [0.05, 0.1, 0.05, 0.1, 0.05, 0.05]
-    s = D.Server(admit_tris=200, **opts)
+    s = D.Server(**opts)
     try:
         tickets = {}
         arrivals = {0: [0, 1], 1: [2], 2: [3, 4], 4: [5]}
-        step = 0
+        step, most_active = 0, 0
         while step < 200 and (len(tickets) < len(meshes) or s.pending):
             for k in arrivals.get(step, []):
                 tickets[k] = s.submit(meshes[k], thresholds[k])
             s.step()
+            st = s.stats()
+            most_active = max(most_active, st["active"])
+            assert st["projectedBytes"] >= st["deviceBytes"], st
             step += 1
         got = {k: s.take(t) for k, t in tickets.items()}
+        st = s.stats()
     finally:
         s.destroy()
+    assert st["admitted"] == len(meshes) and st["rejected"] == 0 and most_active >= 3
+    assert st["peakDeviceBytes"] <= st["budgetBytes"]
     assert all(r is not None for r in got.values())
     for k, m in enumerate(meshes):
         alone = D.decompose(m, **dict(opts, threshold=thresholds[k]))
         _same(got[k], alone)
         assert got[k].stats["totalMs"] > 0
+
+
+def test_server_admits_by_device_memory():
+    """Two meshes whose pools must grow: with a budget between the projected
+    bytes of the first alone and of both, the second waits in the queue
+    until the first finishes, and the trees never hold more than the
+    budget; both results equal the meshes decomposed alone."""
+    tree = dict(SMALL_TREE, vertexCap=1 << 16, triCap=1 << 16)
+    opts = dict(maxIters=20, threshold=0.05, width=6, depth=2, tree=tree)
+    a, b = G.noisy_icosphere(3, seed=1), G.noisy_icosphere(3, seed=2)
+
+    def run(budget):
+        s = D.Server(admit_bytes=budget, **opts)
+        try:
+            ta = s.submit(a)
+            s.step()
+            p1 = s.stats()["projectedBytes"]
+            tb = s.submit(b)
+            s.step()
+            st = s.stats()
+            p2, queued, most_active = st["projectedBytes"], st["queued"], st["active"]
+            n = 0
+            while s.pending and n < 100:
+                s.step()
+                st = s.stats()
+                most_active = max(most_active, st["active"])
+                assert st["deviceBytes"] <= st["projectedBytes"] <= budget or st["active"] <= 1, st
+                n += 1
+            return p1, p2, queued, most_active, s.take(ta), s.take(tb), s.stats()
+        finally:
+            s.destroy()
+
+    p1, p2, queued, most_active, _, _, _ = run(1 << 40)
+    assert queued == 0 and most_active == 2 and p2 > p1
+    budget = (p1 + p2) // 2
+    _, _, queued, most_active, ra, rb, st = run(budget)
+    print(f"admission: one request {p1} bytes projected, two {p2}; budget {budget}, peak held "
+          f"{st['peakDeviceBytes']}")
+    assert queued == 1 and most_active == 1 and st["peakDeviceBytes"] <= budget
+    # alone on pools large enough from the start (the parts do not depend on
+    # the pools' sizes)
+    _same(ra, D.decompose(a, **dict(opts, tree=SMALL_TREE)))
+    _same(rb, D.decompose(b, **dict(opts, tree=SMALL_TREE)))
+
+
+def test_server_slots_queue_bound_and_oversize_requests():
+    opts = dict(maxIters=20, threshold=0.05, width=6, depth=2, tree=SMALL_TREE)
+    s = D.Server(max_active=1, max_queue=2, **opts)
+    try:
+        st = s.stats()
+        total, _ = T.device_memory()
+        assert st["budgetBytes"] == total // 5 * 4 and st["deviceBytes"] > 0
+        t = [s.submit(M.l_shape()), s.submit(stairs())]
+        with pytest.raises(T.CuacdError) as e:
+            s.submit(M.unit_cube())
+        assert e.value.code == D.Server.E_BUSY
+        assert s.stats()["rejected"] == 1 and s.stats()["queued"] == 2
+        s.step()  # one slot: one runs, one waits, and the queue has room again
+        st = s.stats()
+        assert st["active"] <= 1 and st["queued"] <= 1
+        t.append(s.submit(M.unit_cube()))
+        n = 0
+        while s.pending and n < 200:
+            s.step()
+            assert s.stats()["active"] <= 1
+            n += 1
+        assert all(s.take(x) is not None for x in t)
+    finally:
+        s.destroy()
+    # a mesh whose working set alone exceeds the budget is refused at once
+    s = D.Server(admit_bytes=1 << 20, **opts)
+    try:
+        with pytest.raises(T.CuacdError) as e:
+            s.submit(G.noisy_icosphere(3, seed=1))
+        assert e.value.code == -2 and "working set" in str(e.value)
+    finally:
+        s.destroy()
 
 
 def test_staircase_configuration():

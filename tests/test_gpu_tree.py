@@ -103,6 +103,29 @@ def test_empty_and_pool_overflow(GpuTree, oracle):
     assert rg["overflow"] and ro["overflow"]
 
 
+def test_reserved_pools_end_the_overflow(GpuTree, oracle):
+    """cuacd_tree_reserve_pools: the run that overflowed the small pools
+    fits once they grow, equals the run on pools of that size from the
+    start, and the handle's device bytes grow by the pools' growth."""
+    cfg = dict(width=6, width2=3, depth=2, nConcaveEdges=0, vertexCap=3000, triCap=1 << 16, edgeCap=1 << 14,
+               scratchWords=1 << 16, hullBudgetBytes=16 << 20, hullMaxVerts=256)
+    seed = gen.noisy_icosphere(3)
+    g = GpuTree(**cfg)
+    assert g.run([seed])["overflow"]
+    b0, c0 = g.memory()
+    big = dict(vertexCap=1 << 20, triCap=1 << 20, edgeCap=1 << 15, scratchWords=1 << 17)
+    g.reserve_pools(**big)
+    b1, c1 = g.memory()
+    assert c1 == big
+    unit = dict(vertexCap=4, triCap=4, edgeCap=32, scratchWords=4)
+    assert b1 - b0 == sum(unit[k] * (c1[k] - c0[k]) for k in unit)
+    g.reserve_pools(vertexCap=1000, triCap=1000)  # pools never shrink
+    assert g.memory()[1] == big
+    r = g.run([seed])
+    ref = GpuTree(**dict(cfg, **big)).run([seed])
+    assert not r["overflow"] and r["seeds"] == ref["seeds"] and r["validJobs"] == ref["validJobs"]
+
+
 def test_invalid_config_raises(GpuTree):
     with pytest.raises(Exception):
         GpuTree(width=4)
