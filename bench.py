@@ -252,8 +252,13 @@ def run_engine(args):
         if world > 1:
             torch.distributed.barrier()
 
+    # the autotuner's trials for this distribution of part sizes (one run per
+    # schedule), untimed; the runs below use the schedule it kept
+    for _ in range(4):
+        g.run(seeds, planes, refine=refine)
     # ---- value: seeds resident on the device ----
     g.prepare(seeds, planes, refine=refine)
+    schedule = g.schedule()
     for _ in range(args.warmup):
         g.launch()
         r = g.collect()
@@ -354,6 +359,8 @@ def run_engine(args):
             # per level: plan, scan sums, scan, emit, two hull widths,
             # record; per stage the last level's seed bound and one evaluate
             "gpu_launches": args.steps * stages * (depth * 7 + 2),
+            "schedule": {"warp_max_nv": schedule["warpMaxNv"], "big_job_nv": schedule["bigJobNv"],
+                         "autotuned": not schedule["trial"] and schedule["tuned"] > 0},
             "candidates_per_step": cands / args.steps}
     if world == 1 and not args.no_cpu_baseline:
         nthr = host_threads()

@@ -28,7 +28,7 @@ class TreeConfig(C.Structure):
         ("pruneLastLevel", C.c_int32),
         ("warpMaxNv", C.c_int32),
         ("hdScreenMinTris", C.c_int32),
-        ("reserved", C.c_int32),
+        ("autotune", C.c_int32),
     ]
 
 
@@ -106,7 +106,7 @@ DEFAULT_TREE_CONFIG = dict(
     pruneLastLevel=1,
     warpMaxNv=0,
     hdScreenMinTris=0,
-    reserved=0,
+    autotune=1,
 )
 
 

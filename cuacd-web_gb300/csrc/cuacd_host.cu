@@ -13,6 +13,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -62,6 +63,48 @@ static const uint32_t VIS_MAX = CUACD_VIS_MAX;
 static const uint32_t SMALL_NV = 1024;
 // parents with more points than this get a block per plan / emit job
 static const uint32_t BIG_JOB_NV = 2048;
+
+// Schedules the autotuner chooses between: the largest part a warp hulls
+// (larger ones go to blocks) and the largest parent a warp plans and emits.
+// The kernels' outputs do not depend on which group shape handles a part,
+// so every schedule gives the same results; they differ in speed with the
+// distribution of part sizes. The first is the fixed default.
+struct Schedule {
+  uint32_t smallNv, bigJobNv;
+};
+static const Schedule kSchedules[] = {{SMALL_NV, BIG_JOB_NV}, {512, BIG_JOB_NV}, {256, BIG_JOB_NV}, {SMALL_NV, 4096}};
+static const int kNumSchedules = (int)(sizeof(kSchedules) / sizeof(kSchedules[0]));
+// per key: device time of one run or batch under each schedule tried so far
+struct TuneEntry {
+  float ms[kNumSchedules];
+  int tried = 0;
+  int best = 0;
+};
+static uint32_t log2_bucket(uint64_t x) {
+  uint32_t b = 0;
+  while (b < 63 && (1ull << b) < x) b++;
+  return b;
+}
+// the key of a batch's part-size distribution: log2 buckets of its largest,
+// median and total point counts and of its part count, with the kind of
+// work (tree run layout or hull batch) in the low bits
+static uint64_t size_key(uint64_t kind, const cuacd_mesh* m, int n) {
+  std::vector<uint32_t> nv((size_t)std::max(n, 0));
+  uint64_t sum = 0;
+  uint32_t mx = 0;
+  for (int k = 0; k < n; k++) {
+    nv[(size_t)k] = m[k].nv;
+    sum += m[k].nv;
+    mx = std::max(mx, m[k].nv);
+  }
+  uint32_t med = 0;
+  if (n > 0) {
+    std::nth_element(nv.begin(), nv.begin() + n / 2, nv.end());
+    med = nv[(size_t)n / 2];
+  }
+  return (kind & 0xffffull) | ((uint64_t)log2_bucket(mx) << 16) | ((uint64_t)log2_bucket(med) << 24) |
+         ((uint64_t)log2_bucket(sum) << 32) | ((uint64_t)log2_bucket((uint64_t)std::max(n, 0)) << 40);
+}
 
 struct LevelLayout {
   uint32_t itemsInBase, nItemsIn, itemsOutBase, jobBase, partBase, nJobs, width, nEdgeCuts, totalWidth;
@@ -148,6 +191,46 @@ struct Tree {
   std::vector<uint64_t> gsig;
   bool gvalid = false;
 
+  // autotuner (cfg.autotune and no fixed warpMaxNv): each new key tries the
+  // schedules in turn on real work, one run or batch each, then keeps the
+  // fastest
+  std::map<uint64_t, TuneEntry> tuneTable;
+  uint64_t tuneKey = 0;
+  int sched = 0;
+  bool tuneOpen = false;  // the prepared run or batch times a schedule under trial
+  bool lastTrial = false;  // the last prepared run or batch tried a schedule
+  bool autotuned() const { return cfg.autotune != 0 && cfg.warpMaxNv <= 0; }
+  void choose(uint64_t key) {
+    tuneKey = key;
+    tuneOpen = false;
+    lastTrial = false;
+    sched = 0;
+    if (!autotuned()) return;
+    TuneEntry& e = tuneTable[key];
+    if (e.tried < kNumSchedules) {
+      sched = e.tried;
+      tuneOpen = true;
+      lastTrial = true;
+    } else {
+      sched = e.best;
+    }
+  }
+  void record(float ms) {
+    if (!tuneOpen) return;
+    tuneOpen = false;
+    TuneEntry& e = tuneTable[tuneKey];
+    if (e.tried != sched) return;
+    e.ms[sched] = ms;
+    e.tried++;
+    if (e.tried == kNumSchedules) {
+      e.best = 0;
+      for (int k = 1; k < kNumSchedules; k++)
+        if (e.ms[k] < e.ms[e.best]) e.best = k;
+    }
+  }
+  uint32_t smallNv() const { return cfg.warpMaxNv > 0 ? (uint32_t)cfg.warpMaxNv : kSchedules[sched].smallNv; }
+  uint32_t bigJobNv() const { return kSchedules[sched].bigJobNv; }
+
   cut::Engine* cutter = nullptr;  // the GPU capped cut, created on first use
   conc::Engine* concave = nullptr;  // the GPU concave-edge planes, created on first use
   float lastConcaveMs = 0.0f;
@@ -229,7 +312,7 @@ struct Tree {
     P.minEdgeDist = cfg.minEdgeDist;
     P.hullSlabWords = slabWords;
     P.slabStride = slabStride;
-    P.smallNv = cfg.warpMaxNv > 0 ? (uint32_t)cfg.warpMaxNv : SMALL_NV;
+    P.smallNv = smallNv();
     return P;
   }
   // hull launches of one level, warp groups then block groups; work
@@ -331,6 +414,8 @@ struct Tree {
     if (rc) return rc;
     maxSeedNv = 0;
     for (int k = 0; k < n; k++) maxSeedNv = std::max(maxSeedNv, seeds[k].nv);
+    choose(size_key(1u | (dep << 1) | ((refine ? 1u : 0u) << 4) | ((width0 / 3) << 5) | ((nEdge0 > 0 ? 1u : 0u) << 12),
+                    seeds, n));
     tree = layout(nSeeds, depth, width0, nEdge0);
     probe = refine ? layout(nSeeds, depth, 0, nProbes) : std::vector<LevelLayout>();
     uint32_t maxChild = 0;
@@ -423,7 +508,7 @@ struct Tree {
         P.nSeeds = cfg.pruneLastLevel ? nSeeds : 0;
         P.workSlot = l;
         // parents shrink roughly by half per level
-        bool big = (maxSeedNv >> l) > BIG_JOB_NV;
+        bool big = (maxSeedNv >> l) > bigJobNv();
         launch_plan(P, D, big, stream);
         mark(1);
         launch_scan(P, D, stream);
@@ -450,12 +535,13 @@ struct Tree {
   }
   std::vector<uint64_t> signature() const {
     std::vector<uint64_t> s = {nSeeds, depth, nProbes, rounds, slabWords, slabStride, nSlabsSmall, nSlabsBig,
-                               maxSeedNv > BIG_JOB_NV ? maxSeedNv : 0, edgePlaneBase, stateBase, (uint64_t)bSnap.p,
+                               maxSeedNv > bigJobNv() ? maxSeedNv : 0, edgePlaneBase, stateBase, (uint64_t)bSnap.p,
                                (uint64_t)bSlab.p, (uint64_t)bParts.p, (uint64_t)bItems.p, (uint64_t)bJobs.p,
                                (uint64_t)bPlanes.p, (uint64_t)bCtr.p, snapBytes, (uint64_t)bScan.p,
                                (uint64_t)bWork.p};
     for (auto& L : tree) { s.push_back(L.nJobs); s.push_back(L.totalWidth); s.push_back(L.width); }
-    for (uint32_t l = 0; l < depth; l++) s.push_back((maxSeedNv >> l) > BIG_JOB_NV);
+    for (uint32_t l = 0; l < depth; l++) s.push_back((maxSeedNv >> l) > bigJobNv());
+    s.push_back(smallNv());
     return s;
   }
   int launch() {
@@ -516,9 +602,12 @@ struct Tree {
       st->validJobs = (uint64_t)ctr[CTR_VALID_LO] | ((uint64_t)ctr[CTR_VALID_HI] << 32);
       st->hullSlabWords = slabWords;
       st->hullChunkSize = nSlabsSmall;
+    }
+    {
       float ms = 0;
-      cudaEventElapsedTime(&ms, ev0, ev1);
-      st->gpuMs = ms;
+      if (cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess) cudaGetLastError();
+      if (st) st->gpuMs = ms;
+      record(ms);
     }
     for (int c = 0; c < 7; c++) kernelMs[c] = 0;
     std::memcpy(bytes, ctr + CTR_BYTES_PLAN, sizeof(bytes));
@@ -548,6 +637,7 @@ struct Tree {
     if ((rc = ensurePartSlots(withHd ? 2 * n : n))) return rc;
     uint32_t maxNv = 0;
     for (int k = 0; k < n; k++) maxNv = std::max(maxNv, m[k].nv);
+    choose(size_key(2u | ((withHd ? 1u : 0u) << 2), m, n));
     if ((rc = planSlabs(maxNv, (uint32_t)n))) return rc;
     std::vector<PartDesc> parts;
     if ((rc = uploadMeshes(m, (uint32_t)n, parts))) return rc;
@@ -604,6 +694,11 @@ struct Tree {
     if (tb) CK(cudaMemcpyAsync(h + pb, D.T + tTop, tb, cudaMemcpyDeviceToHost, stream));
     if (withHd) CK(cudaMemcpyAsync(h + pb + tb, D.ctr + CTR_HD, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
+    {
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess) cudaGetLastError();
+      record(ms);
+    }
     const PartDesc* pd = (const PartDesc*)h;
     const uint32_t* tw = (const uint32_t*)(h + pb);
     const uint32_t* hdw = (const uint32_t*)(h + pb + tb);
@@ -769,6 +864,7 @@ void cuacd_tree_config_default(cuacd_tree_config* c) {
   c->scratchWords = 48ull << 20;
   c->hullBudgetBytes = 256ull << 20;
   c->pruneLastLevel = 1;
+  c->autotune = 1;
 }
 
 void* cuacd_tree_create(const cuacd_tree_config* c, int* err) {
@@ -846,6 +942,18 @@ int cuacd_tree_memory(const void* tree, uint64_t* deviceBytes, uint64_t* caps4) 
     caps4[2] = t->cfg.edgeCap;
     caps4[3] = t->cfg.scratchWords;
   }
+  return CUACD_OK;
+}
+
+int cuacd_tree_schedule(const void* tree, int32_t* out4) {
+  const Tree* t = (const Tree*)tree;
+  if (!t || !out4) return fail(CUACD_E_INVALID, "cuacd_tree_schedule: invalid argument");
+  out4[0] = (int32_t)t->smallNv();
+  out4[1] = (int32_t)t->bigJobNv();
+  out4[2] = t->lastTrial ? 1 : 0;
+  int32_t done = 0;
+  for (const auto& kv : t->tuneTable) done += kv.second.tried == kNumSchedules ? 1 : 0;
+  out4[3] = done;
   return CUACD_OK;
 }
 

@@ -22,12 +22,19 @@
 //              first-seen order, their loops, the loops' classification
 //              (outer or hole by signed area, parent by the hole centroid's
 //              crossing number) and the caps (ear clipping with holes
-//              bridged in, or centroid fans). The sequential steps run on
-//              every lane of the warp with identical data (warp-uniform
-//              code: identical stores, no divergence); the ear test, the
-//              edge gathering and the twin search split their loops over
-//              the lanes, and the ear test looks only at the nodes in the
-//              cells of a uniform grid that the ear's bounding box covers;
+//              bridged in, or centroid fans). Steps whose decisions read
+//              what earlier iterations wrote (grouping the boundary edges,
+//              walking the loops) run on lane 0 while the other lanes wait;
+//              sorting and bridging the holes run on every lane with the
+//              same data (identical stores) with a warp sync after each
+//              step, so no lane writes what another has yet to read;
+//              the loops' areas and classification, the edge gathering and
+//              the twin search split their work over the lanes, and the ear
+//              clipper tests the orientation of the next 32 ring vertices
+//              at once (one per lane) and the full ear test only on the
+//              survivors, looking at the nodes in the cells of a uniform
+//              grid that the ear's bounding box covers. Every loop over a
+//              list or ring is bounded by its length;
 //   compact    one thread per triangle corner: first use of every vertex
 //              (atomicMin), a scan of the first uses numbers the vertices,
 //              then the halves are written to the output pools.
@@ -449,7 +456,7 @@ __device__ uint32_t kh_find(unsigned long long* keys, uint32_t size, unsigned lo
   return CUT_NONE;
 }
 
-// warp-uniform hash of 32-bit keys (every lane performs the same stores)
+// open-addressing hash of 32-bit keys for one lane (the caller's lane 0)
 __device__ uint32_t uh_find(uint32_t* keys, uint32_t size, uint32_t key, bool insert, bool* inserted) {
   uint32_t h = mix_key(key) & (size - 1);
   *inserted = false;
@@ -610,6 +617,60 @@ __device__ __forceinline__ float ring_diff(const float* h, const float* l, uint3
   return __fadd_rn(__fsub_rn(h[b], h[a]), __fsub_rn(l[b], l[a]));
 }
 
+// s + e = a + b exactly (Knuth's two-sum; no overflow in range)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bv = __fsub_rn(s, a), av = __fsub_rn(s, bv);
+  e = __fadd_rn(__fsub_rn(a, av), __fsub_rn(b, bv));
+}
+
+// the difference of two ring coordinates as an unevaluated float pair
+// (s, r): s + e = hi_b - hi_a exactly, r = fl(e + fl(lo_b - lo_a))
+__device__ __forceinline__ void ring_diff2(const float* h, const float* l, uint32_t b, uint32_t a, float& s, float& r) {
+  float e;
+  two_sum(h[b], -h[a], s, e);
+  r = __fadd_rn(e, __fsub_rn(l[b], l[a]));
+}
+
+// The second filter: orient2 in float-float arithmetic. With u = 2^-24 and
+// S the largest |coordinate|: a coordinate is hi + lo within u^2 |x| (+
+// 2^-149), a difference (s, r) is within 9 u^2 S (+ 2^-148) of the exact
+// one, with |r| <= u |s| + 2.02 u S; a product is p + q + c with (p, q)
+// the exact product s1 s2 (fma) and c = fl(fl(s1 r2 + r1 s2) + r1 r2),
+// within 6 u^2 |s1 s2| + 6.1 u^2 S (|s1| + |s2|) + 25 u^3 S^2; the tail sum
+// of the two products' low parts and the two-sum error of p1 - p2 adds 12
+// u^2 (|p1| + |p2|) + 6.1 u^2 S sum|s|; the host's double orient2 is within
+// 0.13 u^2 (|d1 d2| + |d3 d4|) of the exact value. So beyond E = 20 u^2
+// (|p1| + |p2|) + 24 u^2 S sum|s| + 128 u^3 S^2 (+ 2^-140 (sum|s| + 1)) the
+// float-float value has the double result's sign. Returns +1, -1, or 2
+// when undecided.
+__device__ int orient_ff(const Ring& P, uint32_t a, uint32_t b, uint32_t c, float S) {
+  float s1, r1, s2, r2, s3, r3, s4, r4;
+  ring_diff2(P.Xf, P.Xl, b, a, s1, r1);
+  ring_diff2(P.Yf, P.Yl, c, a, s2, r2);
+  ring_diff2(P.Yf, P.Yl, b, a, s3, r3);
+  ring_diff2(P.Xf, P.Xl, c, a, s4, r4);
+  const float p1 = __fmul_rn(s1, s2), q1 = __fmaf_rn(s1, s2, -p1);
+  const float p2 = __fmul_rn(s3, s4), q2 = __fmaf_rn(s3, s4, -p2);
+  const float c1 = __fadd_rn(__fadd_rn(__fmul_rn(s1, r2), __fmul_rn(r1, s2)), __fmul_rn(r1, r2));
+  const float c2 = __fadd_rn(__fadd_rn(__fmul_rn(s3, r4), __fmul_rn(r3, s4)), __fmul_rn(r3, r4));
+  float h, g;
+  two_sum(p1, -p2, h, g);
+  const float tail = __fadd_rn(__fadd_rn(__fsub_rn(q1, q2), __fsub_rn(c1, c2)), g);
+  const float o = __fadd_rn(h, tail);
+  const float u2 = 3.5527137e-15f;  // 2^-48
+  const float ss = __fadd_rn(__fadd_rn(fabsf(s1), fabsf(s2)), __fadd_rn(fabsf(s3), fabsf(s4)));
+  float E = __fmul_rn(20.0f * u2, __fadd_rn(fabsf(p1), fabsf(p2)));
+  E = __fadd_rn(E, __fmul_rn(__fmul_rn(24.0f * u2, S), ss));
+  E = __fadd_rn(E, __fmul_rn(__fmul_rn(128.0f * u2 * 5.9604645e-8f, S), S));
+  E = __fadd_rn(E, __fmul_rn(7.2e-43f, __fadd_rn(ss, 1.0f)));
+  // the bound's own roundings and the rounding of o: a 2 % margin
+  E = __fmul_rn(E, 1.02f);
+  if (o > E) return 1;
+  if (o < -E) return -1;
+  return 2;
+}
+
 __device__ int orient_sign(const Ring& P, uint32_t a, uint32_t b, uint32_t c) {
   const float d1 = ring_diff(P.Xf, P.Xl, b, a), d2 = ring_diff(P.Yf, P.Yl, c, a);
   const float d3 = ring_diff(P.Yf, P.Yl, b, a), d4 = ring_diff(P.Xf, P.Xl, c, a);
@@ -627,16 +688,40 @@ __device__ int orient_sign(const Ring& P, uint32_t a, uint32_t b, uint32_t c) {
       if (o > eb) return 1;
       if (o < -eb) return -1;
     }
+    // near-collinear: the float-float filter, then double for what it
+    // cannot decide (this GPU's FP64 rate is a small fraction of FP32's)
+    const int f = orient_ff(P, a, b, c, S);
+    if (f != 2) return f;
   }
   const double r = orient2(P.X[a], P.Y[a], P.X[b], P.Y[b], P.X[c], P.Y[c]);
   return r > 0 ? 1 : (r < 0 ? -1 : 0);
+}
+
+// Memo of the ear test, packed with the alive flag in alive[k]: bit 0
+// alive, bits 1-2 the sign of orient2(prev, k, next) plus 2 (0: not known),
+// bits 3-31 one plus a live node found inside the triangle (prev, k, next)
+// (0: none known; node indices stay below 2^28, the 32-bit word arena
+// holding more than 16 words per node). Both depend only on k's neighbours and the coordinates,
+// so they stay valid until a clip changes k's neighbours, which resets the
+// memo of the clipped ear's two neighbours. A retest whose witness is still
+// alive fails at once: the host clipper's test on the same triangle finds
+// that node inside again. On degenerate rings (long runs of collinear
+// vertices, where each pass re-tests the same vertices and their
+// orientations need double arithmetic) this removes the repeated tests.
+__device__ __forceinline__ int gate_sign(const Ring& P, uint32_t k) {
+  const uint32_t m = P.alive[k];
+  const uint32_t code = (m >> 1) & 3u;
+  if (code) return (int)code - 2;
+  const int sg = orient_sign(P, P.prev[k], k, P.next[k]);
+  P.alive[k] = (m & ~6u) | ((uint32_t)(sg + 2) << 1);
+  return sg;
 }
 
 // the orientation gate of the ear test at vertex k (is_ear returns false at
 // once when it fails): the triangle (prev, k, next) turns left, or is flat in
 // flat mode
 __device__ bool ear_gate(const Ring& P, uint32_t k, bool allowFlat) {
-  const int sg = orient_sign(P, P.prev[k], k, P.next[k]);
+  const int sg = gate_sign(P, k);
   return sg > 0 || (sg == 0 && allowFlat);
 }
 
@@ -648,9 +733,14 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const uint32_t a = P.prev[k], b = k, c = P.next[k];
   const float axf = P.Xf[a], ayf = P.Yf[a], bxf = P.Xf[b], byf = P.Yf[b], cxf = P.Xf[c], cyf = P.Yf[c];
   // the ear's orientation (arPos: ar > 0; otherwise ar == 0 in flat mode)
-  const int sg = orient_sign(P, a, b, c);
+  const int sg = gate_sign(P, k);
   if (sg < 0 || (sg == 0 && !allowFlat)) return false;
   const bool arPos = sg > 0;
+  {
+    // a known witness that is still alive is still inside
+    const uint32_t wit = P.alive[k] >> 3;
+    if (wit && (P.alive[wit - 1] & 1u)) return false;
+  }
   // the node must lie in the triangle's bounding box (as in the host
   // clipper), so only the cells the box covers are looked at; the box's
   // float bounds are the float roundings of its double bounds (rounding is
@@ -661,12 +751,13 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const uint32_t y0 = P.cell_y(fby0), y1 = P.cell_y(fby1);
   const uint32_t w = x1 - x0 + 1, nCells = w * (y1 - y0 + 1);
   bool hit = false;
+  uint32_t hitQ = 0;
   for (uint32_t ci = lane; ci < nCells && !hit; ci += 32) {
     const uint32_t row = ci / w;
     const uint32_t cell = (y0 + row) * P.gnx + x0 + (ci - row * w);
     for (uint32_t e = P.gStart[cell]; e < P.gStart[cell + 1]; e++) {
       const uint32_t q = P.gNodes[e];
-      if (!P.alive[q] || q == a || q == b || q == c) continue;
+      if (!(P.alive[q] & 1u) || q == a || q == b || q == c) continue;
       const float qxf = P.Xf[q], qyf = P.Yf[q];
       // in the bounding box, exactly: float decides unless it ties
       if (qxf < fbx0 || qxf > fbx1 || qyf < fby0 || qyf > fby1) continue;
@@ -689,10 +780,18 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
         if (!(qx >= fmin(ax, cx) && qx <= fmax(ax, cx) && qy >= fmin(ay, cy) && qy <= fmax(ay, cy))) continue;
       }
       hit = true;
+      hitQ = q;
       break;
     }
   }
-  return !__any_sync(CUT_FULL, hit);
+  const uint32_t hb = __ballot_sync(CUT_FULL, hit);
+  if (hb) {
+    const uint32_t q = __shfl_sync(CUT_FULL, hitQ, __ffs(hb) - 1);
+    __syncwarp();
+    if (lane == 0) P.alive[k] = (P.alive[k] & 7u) | ((q + 1) << 3);
+    __syncwarp();
+  }
+  return hb == 0;
 }
 
 // the uniform grid of the ring's P.n nodes: about two nodes per cell over
@@ -850,6 +949,7 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
     const uint32_t nTest = min(jStop, 32u);
     const uint32_t mine = ring33[lane];
     const bool gate = (uint32_t)lane < nTest && ear_gate(P, mine, flat);
+    __syncwarp();  // the gates' memo writes before the ear tests read them
     uint32_t cand = __ballot_sync(CUT_FULL, gate);
     int found = -1;
     while (cand) {
@@ -871,6 +971,8 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
       P.next[a] = c;
       P.prev[c] = a;
       P.alive[ear] = 0;
+      P.alive[a] = 1;  // new neighbours: the memo starts over
+      P.alive[c] = 1;
       count--;
       ear = c;
       stop = c;
@@ -1033,9 +1135,9 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
   __syncwarp();
   if (B == 0) return;
 
-  // ---- from here on warp-uniform: every lane runs the same sequential
-  // steps on the same data (stores are identical), lanes split only the ear
-  // test and the per-loop work
+  // ---- from here on the cap's sequential steps: the lanes split the
+  // per-edge, per-loop and per-node work, and steps whose decisions read
+  // earlier writes run on lane 0 between warp syncs
 
   // 3. boundary edges grouped by source vertex, in first-seen order. The
   // walk below follows these lists edge by edge, so for up to

@@ -55,6 +55,7 @@ def load_library():
     L.cuacd_device_memory.argtypes = [P(C.c_uint64), P(C.c_uint64)]
     L.cuacd_tree_memory.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_uint64)]
     L.cuacd_tree_reserve_pools.argtypes = [C.c_void_p, P(C.c_uint64)]
+    L.cuacd_tree_schedule.argtypes = [C.c_void_p, P(C.c_int32)]
     L.cuacd_set_profile.argtypes = [C.c_void_p, C.c_int]
     L.cuacd_tree_kernel_ms.argtypes = [C.c_void_p, C.POINTER(C.c_float)]
     L.cuacd_tree_kernel_bytes.argtypes = [C.c_void_p, C.POINTER(C.c_uint64)]
@@ -130,6 +131,12 @@ class GpuTree:
         b, caps = C.c_uint64(), (C.c_uint64 * 4)()
         _check(load_library().cuacd_tree_memory(self.h, C.byref(b), caps))
         return b.value, dict(zip(("vertexCap", "triCap", "edgeCap", "scratchWords"), list(caps)))
+
+    def schedule(self) -> dict:
+        """The autotuner's state after the last run or hull batch."""
+        out = (C.c_int32 * 4)()
+        _check(load_library().cuacd_tree_schedule(self.h, out))
+        return dict(warpMaxNv=out[0], bigJobNv=out[1], trial=bool(out[2]), tuned=out[3])
 
     def reserve_pools(self, vertexCap=0, triCap=0, edgeCap=0, scratchWords=0):
         """Grows the pools to at least these capacities (the configuration's

@@ -66,7 +66,14 @@ typedef struct {
                                triangles go through the tensor-core screen
                                (0: 256, < 0: never); the results do not
                                depend on it */
-  int32_t reserved;
+  int32_t autotune;         /* 1 (the default): when warpMaxNv is 0, the
+                               warp/block thresholds of the hull and of
+                               plan/emit are chosen per distribution of part
+                               sizes (log2 buckets of the largest, median and
+                               total point counts and of the part count): the
+                               first runs or hull batches of each distribution
+                               try the schedules in turn, later ones use the
+                               fastest; the results do not depend on it */
 } cuacd_tree_config;
 
 /* Mesh (mesh.ts:7-10): nv vertices (3 floats each), nt triangles (3 u32). */
@@ -135,6 +142,13 @@ int cuacd_device_memory(uint64_t* total, uint64_t* freeBytes);
  * configuration's units: vertexCap (floats), triCap (u32), edgeCap (open
  * edges, 32 bytes each), scratchWords (u32). Either output may be NULL. */
 int cuacd_tree_memory(const void* tree, uint64_t* deviceBytes, uint64_t* caps4);
+
+/* The autotuner's state (no reference counterpart): out4[0] = the largest
+ * part a warp hulls and out4[1] = the largest parent a warp plans and emits
+ * in the last prepared run or hull batch, out4[2] = 1 when that run tries a
+ * schedule for its distribution of part sizes, out4[3] = distributions whose
+ * trials are complete. */
+int cuacd_tree_schedule(const void* tree, int32_t* out4);
 
 /* Grows the pools to at least caps4 = {vertexCap, triCap, edgeCap,
  * scratchWords} (pools never shrink; at most 2^32 - 1 each). Waits for the

@@ -126,6 +126,34 @@ def test_reserved_pools_end_the_overflow(GpuTree, oracle):
     assert not r["overflow"] and r["seeds"] == ref["seeds"] and r["validJobs"] == ref["validJobs"]
 
 
+def test_autotuned_schedules_match_oracle(GpuTree, oracle):
+    """The autotuner tries each schedule (warp/block thresholds of the hull
+    and of plan/emit) on the first runs of a part-size distribution, then
+    keeps the fastest. Seeds of 642, ~3,000 and 50 points put parts on both
+    sides of every threshold; every run's tables equal the oracle's."""
+    seeds = [gen.noisy_icosphere(3, seed=1), M.normalize(gen.blob_mesh(10, 36, seed=3))[0], gen.staircase(8)]
+    assert 2048 < seeds[1].nv <= 4096
+    cfg = {**SMALL, **dict(width=3, width2=3, depth=2, nConcaveEdges=0, hullMaxVerts=4096)}
+    g = GpuTree(**cfg)
+    o = oracle.OracleTree(**cfg)
+    ro = o.run(seeds)
+    seen = []
+    for k in range(6):
+        rg = g.run(seeds)
+        seen.append(g.schedule())
+        assert not rg["overflow"]
+        parity.compare_level_tables(g, o, rg, ro, len(seeds), label=f"run {k}")
+        parity.compare_seeds(rg, ro, label=f"run {k}")
+    assert [s["trial"] for s in seen] == [True] * 4 + [False] * 2
+    assert {(s["warpMaxNv"], s["bigJobNv"]) for s in seen[:4]} == {(1024, 2048), (512, 2048), (256, 2048),
+                                                                      (1024, 4096)}
+    assert seen[4] == seen[5] and seen[5]["tuned"] >= 1
+    # a fixed warpMaxNv turns the tuner off
+    g2 = GpuTree(**{**cfg, "warpMaxNv": 512})
+    g2.run(seeds)
+    assert g2.schedule() == dict(warpMaxNv=512, bigJobNv=2048, trial=False, tuned=0)
+
+
 def test_invalid_config_raises(GpuTree):
     with pytest.raises(Exception):
         GpuTree(width=4)
