@@ -115,8 +115,16 @@ constexpr double ON_PLANE_EPS = 1e-6;  // the host cut's default eps
 // hi/lo copies, index, links, alive flag, grid: 52 bytes each plus the cell
 // starts)
 constexpr uint32_t CAP_SM_NODES = 2048;
-constexpr size_t CAP_SM_BYTES = 16 * CAP_SM_NODES + 4 * 5 * CAP_SM_NODES + 4 * 2 * (CAP_SM_NODES / 2 + 2) +
-                                16 * CAP_SM_NODES;
+constexpr size_t CAP_SM_RING_BYTES = 16 * CAP_SM_NODES + 4 * 5 * CAP_SM_NODES + 4 * 2 * (CAP_SM_NODES / 2 + 2) +
+                                     16 * CAP_SM_NODES;
+// a larger ring keeps its links and ear-test memo (12 bytes a node) in
+// shared memory up to CAP_SM_LINK_NODES nodes, its coordinates and grid in
+// the global scratch: the ear search walks the links node by node, and on
+// long degenerate rings that walk is most of the cap's time. One 32-thread
+// block per SM fits either way.
+constexpr uint32_t CAP_SM_LINK_NODES = 16384;
+constexpr size_t CAP_SM_BYTES =
+    CAP_SM_RING_BYTES > 12 * (size_t)CAP_SM_LINK_NODES ? CAP_SM_RING_BYTES : 12 * (size_t)CAP_SM_LINK_NODES;
 // boundary edges whose walk runs in shared memory: a source hash of up to
 // 2 * 2048 entries (key, head, tail) and next, used, source and destination
 // per edge, 80 KB, within CAP_SM_BYTES
@@ -749,49 +757,57 @@ __device__ bool is_ear(const Ring& P, uint32_t k, bool allowFlat, int lane) {
   const float fby0 = fminf(fminf(ayf, cyf), byf), fby1 = fmaxf(fmaxf(ayf, cyf), byf);
   const uint32_t x0 = P.cell_x(fbx0), x1 = P.cell_x(fbx1);
   const uint32_t y0 = P.cell_y(fby0), y1 = P.cell_y(fby1);
-  const uint32_t w = x1 - x0 + 1, nCells = w * (y1 - y0 + 1);
+  // the nodes of one row of covered cells are contiguous in the grid's node
+  // list: the lanes take 32 consecutive entries at a time (coalesced, the
+  // loads of the whole warp in flight together) and the warp stops at the
+  // first batch holding a node inside
+  auto inside = [&](uint32_t q) -> bool {
+    if (!(P.alive[q] & 1u) || q == a || q == b || q == c) return false;
+    const float qxf = P.Xf[q], qyf = P.Yf[q];
+    // in the bounding box, exactly: float decides unless it ties
+    if (qxf < fbx0 || qxf > fbx1 || qyf < fby0 || qyf > fby1) return false;
+    if (qxf == fbx0 || qxf == fbx1 || qyf == fby0 || qyf == fby1) {
+      const double qx = P.X[q], qy = P.Y[q];
+      const double ax = P.X[a], ay = P.Y[a], bx = P.X[b], by = P.Y[b], cx = P.X[c], cy = P.Y[c];
+      if (qx < fmin(fmin(ax, cx), bx) || qx > fmax(fmax(ax, cx), bx) || qy < fmin(fmin(ay, cy), by) ||
+          qy > fmax(fmax(ay, cy), by))
+        return false;
+    }
+    // not at a corner's position (equal doubles have equal floats)
+    if ((qxf == axf && qyf == ayf && P.X[q] == P.X[a] && P.Y[q] == P.Y[a]) ||
+        (qxf == bxf && qyf == byf && P.X[q] == P.X[b] && P.Y[q] == P.Y[b]) ||
+        (qxf == cxf && qyf == cyf && P.X[q] == P.X[c] && P.Y[q] == P.Y[c]))
+      return false;
+    if (orient_sign(P, a, b, q) < 0 || orient_sign(P, b, c, q) < 0 || orient_sign(P, c, a, q) < 0) return false;
+    if (!arPos) {
+      // a flat ear: only nodes within the box of its two ends count
+      const double qx = P.X[q], qy = P.Y[q], ax = P.X[a], ay = P.Y[a], cx = P.X[c], cy = P.Y[c];
+      if (!(qx >= fmin(ax, cx) && qx <= fmax(ax, cx) && qy >= fmin(ay, cy) && qy <= fmax(ay, cy))) return false;
+    }
+    return true;
+  };
   bool hit = false;
   uint32_t hitQ = 0;
-  for (uint32_t ci = lane; ci < nCells && !hit; ci += 32) {
-    const uint32_t row = ci / w;
-    const uint32_t cell = (y0 + row) * P.gnx + x0 + (ci - row * w);
-    for (uint32_t e = P.gStart[cell]; e < P.gStart[cell + 1]; e++) {
-      const uint32_t q = P.gNodes[e];
-      if (!(P.alive[q] & 1u) || q == a || q == b || q == c) continue;
-      const float qxf = P.Xf[q], qyf = P.Yf[q];
-      // in the bounding box, exactly: float decides unless it ties
-      if (qxf < fbx0 || qxf > fbx1 || qyf < fby0 || qyf > fby1) continue;
-      if (qxf == fbx0 || qxf == fbx1 || qyf == fby0 || qyf == fby1) {
-        const double qx = P.X[q], qy = P.Y[q];
-        const double ax = P.X[a], ay = P.Y[a], bx = P.X[b], by = P.Y[b], cx = P.X[c], cy = P.Y[c];
-        if (qx < fmin(fmin(ax, cx), bx) || qx > fmax(fmax(ax, cx), bx) || qy < fmin(fmin(ay, cy), by) ||
-            qy > fmax(fmax(ay, cy), by))
-          continue;
+  for (uint32_t y = y0; y <= y1 && !hit; y++) {
+    const uint32_t e0 = P.gStart[y * P.gnx + x0], e1 = P.gStart[y * P.gnx + x1 + 1];
+    for (uint32_t base = e0; base < e1; base += 32) {
+      const uint32_t e = base + (uint32_t)lane;
+      const uint32_t q = e < e1 ? P.gNodes[e] : 0u;
+      const bool h = e < e1 && inside(q);
+      const uint32_t hb = __ballot_sync(CUT_FULL, h);
+      if (hb) {
+        hit = true;
+        hitQ = __shfl_sync(CUT_FULL, q, __ffs(hb) - 1);
+        break;
       }
-      // not at a corner's position (equal doubles have equal floats)
-      if ((qxf == axf && qyf == ayf && P.X[q] == P.X[a] && P.Y[q] == P.Y[a]) ||
-          (qxf == bxf && qyf == byf && P.X[q] == P.X[b] && P.Y[q] == P.Y[b]) ||
-          (qxf == cxf && qyf == cyf && P.X[q] == P.X[c] && P.Y[q] == P.Y[c]))
-        continue;
-      if (orient_sign(P, a, b, q) < 0 || orient_sign(P, b, c, q) < 0 || orient_sign(P, c, a, q) < 0) continue;
-      if (!arPos) {
-        // a flat ear: only nodes within the box of its two ends count
-        const double qx = P.X[q], qy = P.Y[q], ax = P.X[a], ay = P.Y[a], cx = P.X[c], cy = P.Y[c];
-        if (!(qx >= fmin(ax, cx) && qx <= fmax(ax, cx) && qy >= fmin(ay, cy) && qy <= fmax(ay, cy))) continue;
-      }
-      hit = true;
-      hitQ = q;
-      break;
     }
   }
-  const uint32_t hb = __ballot_sync(CUT_FULL, hit);
-  if (hb) {
-    const uint32_t q = __shfl_sync(CUT_FULL, hitQ, __ffs(hb) - 1);
+  if (hit) {
     __syncwarp();
-    if (lane == 0) P.alive[k] = (P.alive[k] & 7u) | ((q + 1) << 3);
+    if (lane == 0) P.alive[k] = (P.alive[k] & 7u) | ((hitQ + 1) << 3);
     __syncwarp();
   }
-  return hb == 0;
+  return !hit;
 }
 
 // the uniform grid of the ring's P.n nodes: about two nodes per cell over
@@ -1382,7 +1398,8 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
       return;
     }
   // the ear clipper's nodes and grid: in shared memory when the group fits
-  // CAP_SM_NODES nodes, else in the global scratch
+  // CAP_SM_NODES nodes, else in the global scratch with the links and memo
+  // in shared memory up to CAP_SM_LINK_NODES nodes
   Ring Pg;
   Pg.I = w + cv.ndI;
   Pg.prev = w + cv.ndPrev;
@@ -1447,7 +1464,18 @@ __global__ void k_cut_cap(const CutDesc* __restrict__ D, const CutLayout* __rest
       }
     __syncwarp();
     const uint32_t expected = nAll + 2 * nHoles - 2;
-    Ring& P = nAll + 2 * nHoles <= Ps.cap ? Ps : Pg;
+    const uint32_t ringNodes = nAll + 2 * nHoles;
+    if (ringNodes > Ps.cap && ringNodes <= CAP_SM_LINK_NODES) {
+      uint32_t* su = reinterpret_cast<uint32_t*>(capSm);
+      Pg.prev = su;
+      Pg.next = su + CAP_SM_LINK_NODES;
+      Pg.alive = su + 2 * CAP_SM_LINK_NODES;
+    } else {
+      Pg.prev = w + cv.ndPrev;
+      Pg.next = w + cv.ndNext;
+      Pg.alive = w + cv.ndAlive;
+    }
+    Ring& P = ringNodes <= Ps.cap ? Ps : Pg;
     if (nCap + nAll + 2 * nHoles > capMax || nAll + 2 * nHoles > P.cap) {
       failWith(CUT_SCRATCH);
       return;
