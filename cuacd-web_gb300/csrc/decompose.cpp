@@ -1141,6 +1141,30 @@ Engine* make_engine(const cuacd_decompose_opts& o, int* err) {
 // edges of 32 bytes, scratch u32)
 static uint64_t pool_bytes(const uint64_t* c) { return 4 * c[0] + 4 * c[1] + 32 * c[2] + 4 * c[3]; }
 
+// Pool space of one lookahead run with an (nv, nt) seed. Level l has J_l
+// jobs (J_0 = width + planeSlots, J_l+1 = width2 J_l); a job's two children
+// hold up to 2.5 nv + 64 vertices together (the children keep the parent's
+// vertices on their side plus the intersection points), the children of the
+// levels that keep topology (all but the last) 1.5 nt + 64 triangles and
+// 16 sqrt(nt) + 64 open rim edges; a level's plan scratch is 2 words per
+// parent vertex of each of its jobs. The oracle's tree runs on pools of
+// exactly these sizes without overflow (tests/test_pool_estimate.py).
+static void pool_working_set(int width, int width2, int depth, int planeSlots, uint64_t nv, uint64_t nt,
+                             uint64_t* need) {
+  uint64_t jobs = (uint64_t)width + (uint64_t)planeSlots, all = 0, topo = 0, last = 0;
+  for (int l = 0; l < depth; l++) {
+    all += jobs;
+    if (l + 1 < depth) topo += jobs;
+    last = jobs;
+    jobs *= (uint64_t)width2;
+  }
+  const uint64_t rim = 16 * (uint64_t)std::ceil(std::sqrt((double)nt)) + 64;
+  need[0] = all * 3 * (5 * nv / 2 + 64) + 3 * nv + 4096;
+  need[1] = topo * 3 * (3 * nt / 2 + 64) + 3 * nt + 4096;
+  need[2] = topo * rim + 4096;
+  need[3] = 2 * last * (3 * nv / 2 + 64) + 4096;
+}
+
 struct Request {
   uint64_t ticket = 0;
   std::unique_ptr<Job> job;
@@ -1184,34 +1208,14 @@ class Server {
     engines.emplace(key, std::unique_ptr<Engine>(e));
     return e;
   }
-  // pool space of one lookahead run with an (nv, nt) seed. Level l has
-  // J_l jobs (J_0 = width + planeSlots, J_l+1 = width2 J_l); a job's two
-  // children hold up to 2.5 nv + 64 vertices together (the children keep
-  // the parent's vertices on their side plus the intersection points), the
-  // children of the levels that keep topology (all but the last) 1.5 nt + 64
-  // triangles and 16 sqrt(nt) + 64 open rim edges; a level's plan scratch is
-  // 2 words per parent vertex of each of its jobs. These bounds hold with a
-  // margin of 1.2 or more on every seed measured (icospheres, staircases,
-  // blobs of 100 to 4,000 triangles, depth 2 and 3, with refinement).
   void working_set(uint64_t nv, uint64_t nt, uint64_t* need) const {
-    uint64_t jobs = (uint64_t)base.width + (uint64_t)planeSlots, all = 0, topo = 0, last = 0;
-    for (int l = 0; l < base.depth; l++) {
-      all += jobs;
-      if (l + 1 < base.depth) topo += jobs;
-      last = jobs;
-      jobs *= (uint64_t)base.width2;
-    }
-    const uint64_t rim = 16 * (uint64_t)std::ceil(std::sqrt((double)nt)) + 64;
-    need[0] = all * 3 * (5 * nv / 2 + 64) + 3 * nv + 4096;
-    need[1] = topo * 3 * (3 * nt / 2 + 64) + 3 * nt + 4096;
-    need[2] = topo * rim + 4096;
-    need[3] = 2 * last * (3 * nv / 2 + 64) + 4096;
+    pool_working_set(base.width, base.width2, base.depth, planeSlots, nv, nt, need);
   }
   // the buffers of the passes outside the tree pools grow with the work of
   // a step: the cut's inputs, classification, hash tables, cap arenas and
   // halves with the parts cut (at most the mesh and its caps), the tables
   // with the seeds, and the merge pass's hull and Hausdorff batches (chunks
-  // of 256 pairs) with the parts. A tree counts 64 MB for its batches and
+  // of up to 1024 pairs) with the parts. A tree counts 64 MB for its batches and
   // each request 64 bytes per input byte, twice the growth measured on
   // icospheres of 1,280 triangles decomposed alone.
   static uint64_t aux_bytes(uint64_t nv, uint64_t nt) { return 64 * 12 * (nv + nt) + (1 << 20); }
@@ -1720,6 +1724,13 @@ int cuacd_server_submit(void* sv, const cuacd_mesh* m, float threshold, uint64_t
   r.threshold = threshold > 0 ? threshold : s->base.threshold;
   *ticket = r.ticket;
   s->queue.push_back(std::move(r));
+  return CUACD_OK;
+}
+
+int cuacd_pool_working_set(const cuacd_tree_config* cfg, uint32_t nv, uint32_t nt, uint64_t* caps4) {
+  if (!cfg || !caps4 || cfg->depth < 1 || cfg->width < 0 || cfg->width2 < 0)
+    return set_error(CUACD_E_INVALID, "cuacd_pool_working_set: invalid argument");
+  pool_working_set(cfg->width, cfg->width2, cfg->depth, std::max(4 * cfg->nConcaveEdges, 32), nv, nt, caps4);
   return CUACD_OK;
 }
 

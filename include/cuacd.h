@@ -143,6 +143,16 @@ int cuacd_device_memory(uint64_t* total, uint64_t* freeBytes);
  * edges, 32 bytes each), scratchWords (u32). Either output may be NULL. */
 int cuacd_tree_memory(const void* tree, uint64_t* deviceBytes, uint64_t* caps4);
 
+/* Pool space of one lookahead run with an (nv, nt) seed on a tree of this
+ * configuration (no reference counterpart; the server's working-set
+ * estimate): caps4 = {vertex floats, triangle u32, open edges, scratch u32}.
+ * Level l has J_l jobs (J_0 = width + max(4 nConcaveEdges, 32), J_l+1 =
+ * width2 J_l); each job's children hold up to 2.5 nv + 64 vertices, the
+ * children of every level but the last 1.5 nt + 64 triangles and
+ * 16 sqrt(nt) + 64 open edges, and a level's plan scratch is 2 words per
+ * parent vertex per job. A run on pools of these sizes does not overflow. */
+int cuacd_pool_working_set(const cuacd_tree_config* cfg, uint32_t nv, uint32_t nt, uint64_t* caps4);
+
 /* The autotuner's state (no reference counterpart): out4[0] = the largest
  * part a warp hulls and out4[1] = the largest parent a warp plans and emits
  * in the last prepared run or hull batch, out4[2] = 1 when that run tries a
