@@ -584,13 +584,16 @@ def _parts_equal(ra, rb):
                and a.hausdorff == b.hausdorff for a, b in zip(ra.parts, rb.parts))
 
 
-def decompose_measure(n_meshes, big_steps=2):
+def decompose_measure(n_meshes, big_steps=2, max_iters=0):
     """meshes/s of the uneven batch decomposed together and one at a time
-    (same decomposer, same parts), and the large mesh's latency."""
+    (same decomposer, same parts), and the large mesh's latency. max_iters
+    > 0 caps the iterations per mesh (the 256-mesh batch holds two meshes
+    that never reach the threshold at 100)."""
     dec = importlib.import_module("cuacd-web_gb300.decompose")
     gen = importlib.import_module("cuacd-web_gb300.meshgen")
     meshes = gen.blob_batch(n_meshes, seed=0)
-    d = dec.Decomposer(**DEC_OPTS)
+    opts = dict(DEC_OPTS, **({"maxIters": max_iters} if max_iters > 0 else {}))
+    d = dec.Decomposer(**opts)
     try:
         small = sorted(meshes, key=lambda m: m.nt)[:2]
         d.decompose_many(small, batched=True)  # warm-up: tree buffers and graphs
@@ -627,6 +630,7 @@ def decompose_measure(n_meshes, big_steps=2):
         "stuck": sum(p.stuck for r in rb for p in r.parts),
         "config": {"workload": f"{n_meshes} blob meshes (2..32 Gaussian blobs, marching tetrahedra, triangles "
                                f"log-uniform in 500..60k, seed 0)", "tris": sum(m.nt for m in meshes),
+                   "maxIters": opts.get("maxIters", 100),
                    "threshold": 0.05, "width": 6, "width2": 3, "depth": 2, "maxNCutting": 16, "nConcaveEdges": 16,
                    "refineRounds": 2, "mergeHulls": True, "hullMaxVerts": DEC_TREE["hullMaxVerts"]},
         "e2e_bytes": {"h2d": h2d, "d2h": d2h},
@@ -800,7 +804,7 @@ def run_refmeshes(args):
 
 
 def run_decompose(args):
-    m = decompose_measure(args.meshes, big_steps=max(args.steps, 1))
+    m = decompose_measure(args.meshes, big_steps=max(args.steps, 1), max_iters=args.max_iters)
     line = {"metric": m["metric"], "value": m["batched"]["value"], "unit": "meshes/s", "n_gpus": 1,
             "steps": 1, "warmup": 1, "ms_per_step": 1000 * m["batched"]["seconds"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": m["config"],
@@ -824,6 +828,7 @@ def main():
     ap.add_argument("--pairs", type=int, default=256)
     ap.add_argument("--meshes", type=int, default=32, help="meshes of the uneven decomposition batch")
     ap.add_argument("--no-decompose", action="store_true", help="leave the decomposition summary out of the tree line")
+    ap.add_argument("--max-iters", type=int, default=0, help="decompose workload: iterations per mesh at most (0: 100)")
     ap.add_argument("--rate", type=float, default=200.0, help="serving: arrivals per second")
     ap.add_argument("--duration", type=float, default=60.0, help="serving: seconds of arrivals")
     ap.add_argument("--pool", type=int, default=48, help="serving: distinct request meshes")
