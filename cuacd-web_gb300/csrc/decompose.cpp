@@ -224,8 +224,14 @@ class Engine {
   // allowFail, when the part gets a NaN hull volume.
   // defer: the output hulls' cleanup goes to the workers (the part's
   // hullTask) instead of finishing before the call returns
+  // keep: when given, a hull whose (mesh index, GPU hull volume) it rejects
+  // gets its volume only, without the host cleanup of its faces (the merge
+  // pass needs the cleaned hull only for pairs under the threshold: merge.ts
+  // cleans every pair's hull, merge.ts:213, but keeps it only for those,
+  // merge.ts:221)
   void hulls(const std::vector<const Mesh*>& ms, const std::vector<double>& eps, bool withHd, std::vector<Part>& out,
-             bool allowFail = false, bool defer = false) {
+             bool allowFail = false, bool defer = false,
+             const std::function<bool(size_t, double)>* keep = nullptr) {
     out.resize(ms.size());
     if (defer && !pool) pool = std::make_unique<TaskPool>(threads);
     size_t chunk = CUACD_HD_MAX_PAIRS;
@@ -271,6 +277,10 @@ class Engine {
         }
         if (status[k] != 0) {
           p.hullVol = NAN;
+          return;
+        }
+        if (keep && !(*keep)(s + k, (double)vol[k])) {
+          p.hullVol = vol[k];
           return;
         }
         // output faces cleaned (decompose.ts:189, merge.ts:213); the kernel's
@@ -821,7 +831,12 @@ class Engine {
           ptr[k] = &pts[k];
           peps[k] = todo[k].job->hullEps;
         }
-        hulls(ptr, peps, false, hp, true);
+        const std::function<bool(size_t, double)> underThreshold = [&](size_t k, double hv) {
+          const Part& A = todo[k].job->parts[todo[k].i];
+          const Part& B = todo[k].job->parts[todo[k].j];
+          return rv_cost(A.meshVol + B.meshVol, hv) < o.threshold;
+        };
+        hulls(ptr, peps, false, hp, true, false, &underThreshold);
       }
       hullMs += ms_since(th);
       const size_t base = evals.size();
