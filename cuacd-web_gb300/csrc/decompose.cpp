@@ -216,11 +216,12 @@ class Engine {
   // ---- GPU services ------------------------------------------------------
 
   // hulls (and, when withHd, Hausdorff distances to them) of meshes, in
-  // chunks of at most 1024 (the reference's chunks hold 256, decompose.ts:
-  // 180; a hull does not depend on its chunk, and larger chunks fill the GPU:
-  // 1,535 merge-pair hulls took 67 ms of device time in chunks of 256 and
-  // 53 ms in chunks of 1024), halved when a chunk's hull export does not fit
-  // the triangle pool. A failed hull is an error unless
+  // chunks of at most 1024 (the reference hulls new parts in chunks of 256,
+  // decompose.ts:178, and merge pairs in chunks of 1024, merge.ts:209; a hull
+  // does not depend on its chunk, and larger chunks fill the GPU: 1,535
+  // merge-pair hulls took 67 ms of device time in chunks of 256 and 53 ms in
+  // chunks of 1024), halved when a chunk's hull export does not fit the
+  // triangle pool. A failed hull is an error unless
   // allowFail, when the part gets a NaN hull volume.
   // defer: the output hulls' cleanup goes to the workers (the part's
   // hullTask) instead of finishing before the call returns
