@@ -803,6 +803,75 @@ def run_refmeshes(args):
     print(json.dumps(line), flush=True)
 
 
+def run_cuts(args):
+    """The capped winning cut on the GPU (cuacd_tree_plane_cuts): the
+    icosphere configuration's mesh (level 4, 2,562 vertices, 5,120
+    triangles, radial noise) cut by its 96 seeded planes in one batch, the
+    halves read back to host memory. value: cuts/s of device time; e2e: the
+    public call with host buffers (mesh and planes in, every half out).
+    Roofline: per cut the mesh is read once and both halves written once
+    (12 bytes per vertex and per triangle each way), over the batch's
+    device time."""
+    import ctypes as C
+
+    import numpy as np
+
+    gen = importlib.import_module("cuacd-web_gb300.meshgen")
+    tree_mod = importlib.import_module("cuacd-web_gb300.tree")
+    A = importlib.import_module("cuacd-web_gb300._abi")
+    m = gen.noisy_icosphere(4, noise=0.15, seed=0)
+    planes = np.ascontiguousarray(gen.random_planes(m, 96, seed=0).astype(np.float64))
+    n = planes.shape[0]
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=4096)
+    L = tree_mod.load_library()
+    ma = A.MeshArray([A.as_mesh(m)])
+    idx = np.zeros(n, np.int32)
+
+    def batch():
+        h = C.c_void_p()
+        t0 = time.perf_counter()
+        rc = L.cuacd_tree_plane_cuts(g.h, ma.arr, 1, idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                     planes.ctypes.data_as(C.POINTER(C.c_double)), n, 1, C.byref(h))
+        wall = time.perf_counter() - t0
+        assert rc == 0, L.cuacd_last_error().decode()
+        ms = float(L.cuacd_cuts_gpu_ms(h))
+        sizes = []
+        for k in range(n):
+            for side in (0, 1):
+                v, t = C.POINTER(C.c_float)(), C.POINTER(C.c_uint32)()
+                nv, nt = C.c_uint32(), C.c_uint32()
+                if L.cuacd_cuts_half(h, k, side, C.byref(v), C.byref(nv), C.byref(t), C.byref(nt)) == 0:
+                    sizes.append((nv.value, nt.value))
+        L.cuacd_cuts_free(h)
+        return wall, ms, sizes
+
+    for _ in range(args.warmup):
+        batch()
+    walls, devs, sizes = [], [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            w, ms, sizes = batch()
+            walls.append(w)
+            devs.append(ms)
+    dev = statistics.median(devs) / 1000.0
+    wall = statistics.median(walls)
+    out_bytes = sum(12 * (nv + nt) for nv, nt in sizes)
+    alg = n * 12 * (m.nv + m.nt) + out_bytes
+    peak, peak_kind = peaks()
+    achieved = alg / dev / 1e9
+    line = {"metric": "capped plane cuts/s", "value": n / dev, "unit": "cuts/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * dev, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "noisy icosphere L4 (2,562 verts, 5,120 tris) cut by 96 seeded planes in one batch",
+                       "halves": len(sizes), "closed": True},
+            "e2e": {"value": n / wall, "unit": "cuts/s", "h2d_bytes_per_step": m.verts.nbytes + m.tris.nbytes +
+                    planes.nbytes, "d2h_bytes_per_step": out_bytes},
+            "roofline": {"bound": "latency", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_source": peak_kind, "algorithmic_bytes_per_step": alg},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_decompose(args):
     m = decompose_measure(args.meshes, big_steps=max(args.steps, 1), max_iters=args.max_iters)
     line = {"metric": m["metric"], "value": m["batched"]["value"], "unit": "meshes/s", "n_gpus": 1,
@@ -824,7 +893,7 @@ def main():
     ap.add_argument("--seeds", type=int, default=160)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="tree",
-                    choices=["tree", "hausdorff", "hulls", "bighulls", "decompose", "serve", "refmeshes"])
+                    choices=["tree", "hausdorff", "hulls", "bighulls", "decompose", "serve", "refmeshes", "cuts"])
     ap.add_argument("--pairs", type=int, default=256)
     ap.add_argument("--meshes", type=int, default=32, help="meshes of the uneven decomposition batch")
     ap.add_argument("--no-decompose", action="store_true", help="leave the decomposition summary out of the tree line")
@@ -845,6 +914,8 @@ def main():
         run_serve(args)
     elif args.workload == "refmeshes":
         run_refmeshes(args)
+    elif args.workload == "cuts":
+        run_cuts(args)
     elif args.workload != "tree":
         run_secondary(args)
     else:
