@@ -564,35 +564,75 @@ __device__ uint32_t ring_par(Ring& P, const double* gxy, uint32_t s, uint32_t e,
 // an outer vertex visible from hole vertex h (leftmost of its loop), as the
 // host clipper's find_bridge: the nearest crossing of the leftward ray with
 // a downward edge of the counter-clockwise outer loop, its endpoint of larger
-// x, replaced by the reflex vertex of smallest angle inside the triangle
-__device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
+// x, replaced by the reflex vertex of smallest angle inside the triangle.
+// The host walks the ring once for each; here lane 0 lists the ring in order
+// from `outer` (order[i], and i in pos[] of each node) and the lanes split
+// the edges and nodes by ring position. The host keeps the first crossing in
+// ring order among those of largest x (a later one must be strictly larger)
+// and the first candidate in ring order from m among those of smallest
+// tangent, then largest x (the same strict tests), so each lane keeps its
+// own first best and the warp takes the best of the lanes' with the lowest
+// ring position. Every value is the host's double expression on the same
+// operands. order and pos are scratch (the grid's node list and the alive
+// words, both rebuilt before the ear clipping).
+__device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer, uint32_t* order, uint32_t* pos,
+                               int lane) {
+  uint32_t len = 0;
+  if (lane == 0) {
+    uint32_t p = outer;
+    do {
+      if (len >= P.n) {  // more steps than nodes: not a ring
+        len = P.n + 1;
+        break;
+      }
+      order[len] = p;
+      pos[p] = len;
+      len++;
+      p = P.next[p];
+    } while (p != outer);
+  }
+  len = __shfl_sync(CUT_FULL, len, 0);
+  __syncwarp();
+  if (len > P.n) return -1;  // not a ring: never for a well-formed group
   const double hx = P.X[h], hy = P.Y[h];
-  double qx = -INFINITY;
-  int32_t m = -1;
-  uint32_t p = outer, guard = 0;
-  do {
-    const uint32_t an = P.next[p];
+  // 1. the first crossing of largest x at most hx
+  double bx1 = -INFINITY;
+  uint32_t bi = CUT_NONE;
+  for (uint32_t i = lane; i < len; i += 32) {
+    const uint32_t p = order[i], an = P.next[p];
     const double ax = P.X[p], ay = P.Y[p], bx = P.X[an], by = P.Y[an];
     if (hy <= ay && hy >= by && by != ay) {
       const double x = ax + (hy - ay) * (bx - ax) / (by - ay);
-      if (x <= hx && x > qx) {
-        qx = x;
-        if (x == hx) {
-          if (hy == ay) return (int32_t)p;
-          if (hy == by) return (int32_t)an;
-        }
-        m = ax < bx ? (int32_t)an : (int32_t)p;
+      if (x <= hx && x > bx1) {
+        bx1 = x;
+        bi = i;
       }
     }
-    p = an;
-  } while (p != outer && ++guard <= P.n);
-  if (m < 0) return -1;
+  }
+  double qx = bx1;
+  for (int d = 16; d > 0; d >>= 1) qx = fmax(qx, __shfl_xor_sync(CUT_FULL, qx, d));
+  uint32_t first = (bi != CUT_NONE && bx1 == qx) ? bi : CUT_NONE;
+  for (int d = 16; d > 0; d >>= 1) first = min(first, __shfl_xor_sync(CUT_FULL, first, d));
+  if (first == CUT_NONE) return -1;
+  int32_t m;
+  {
+    const uint32_t p = order[first], an = P.next[p];
+    const double ax = P.X[p], ay = P.Y[p], bx = P.X[an], by = P.Y[an];
+    if (qx == hx) {
+      if (hy == ay) return (int32_t)p;
+      if (hy == by) return (int32_t)an;
+    }
+    m = ax < bx ? (int32_t)an : (int32_t)p;
+  }
   if (hx == qx) return m;
-  const uint32_t stop = (uint32_t)m;
+  // 2. from m once around: reflex nodes inside the triangle, smallest
+  // tangent, then largest x, then first
   const double mx = P.X[m], my = P.Y[m];
-  double tanMin = INFINITY;
-  p = (uint32_t)m;
-  do {
+  const uint32_t base = pos[m];
+  double tBest = INFINITY, cBest = -INFINITY;
+  uint32_t jBest = CUT_NONE;
+  for (uint32_t j = lane; j < len; j += 32) {
+    const uint32_t p = order[base + j < len ? base + j : base + j - len];
     const double cx = P.X[p], cy = P.Y[p];
     if (hx >= cx && cx >= mx && hx != cx) {
       const double d1 = orient2(hx, hy, qx, hy, cx, cy), d2 = orient2(qx, hy, mx, my, cx, cy),
@@ -600,14 +640,24 @@ __device__ int32_t find_bridge(const Ring& P, uint32_t h, uint32_t outer) {
       const bool inTri = (d1 >= 0 && d2 >= 0 && d3 >= 0) || (d1 <= 0 && d2 <= 0 && d3 <= 0);
       if (inTri && P.reflex(p)) {
         const double tn = fabs(hy - cy) / (hx - cx);
-        if (tn < tanMin || (tn == tanMin && cx > P.X[m])) {
-          m = (int32_t)p;
-          tanMin = tn;
+        if (tn < tBest || (tn == tBest && cx > cBest)) {
+          tBest = tn;
+          cBest = cx;
+          jBest = j;
         }
       }
     }
-    p = P.next[p];
-  } while (p != stop && ++guard <= 2 * P.n);
+  }
+  for (int d = 16; d > 0; d >>= 1) {
+    const double t2 = __shfl_xor_sync(CUT_FULL, tBest, d), c2 = __shfl_xor_sync(CUT_FULL, cBest, d);
+    const uint32_t j2 = __shfl_xor_sync(CUT_FULL, jBest, d);
+    if (t2 < tBest || (t2 == tBest && (c2 > cBest || (c2 == cBest && j2 < jBest)))) {
+      tBest = t2;
+      cBest = c2;
+      jBest = j2;
+    }
+  }
+  if (jBest != CUT_NONE) m = (int32_t)order[base + jBest < len ? base + jBest : base + jBest - len];
   return m;
 }
 
@@ -911,11 +961,15 @@ __device__ uint32_t ear_clip(Ring& P, const uint32_t* gid, const double* gxy, ui
     __syncwarp();
   }
   for (uint32_t k = 0; k < nh; k++) {
-    const int32_t m = find_bridge(P, holeL[k], outer);
+    const int32_t m = find_bridge(P, holeL[k], outer, P.gNodes, P.alive, lane);
     __syncwarp();
     if (m < 0) return 0;
     P.bridge((uint32_t)m, holeL[k]);
     __syncwarp();
+  }
+  // the alive words held ring positions while the holes were bridged
+  if (nh > 0) {
+    for (uint32_t q = lane; q < P.n; q += 32) P.alive[q] = 1;
   }
   __syncwarp();
   build_grid(P, lane);
