@@ -235,13 +235,20 @@ class Engine {
              const std::function<bool(size_t, double)>* keep = nullptr) {
     out.resize(ms.size());
     if (defer && !pool) pool = std::make_unique<TaskPool>(threads);
+    // chunks hold meshes of similar size (ascending point count): a chunk's
+    // export stride and readback follow its largest mesh, so one large
+    // merged hull no longer sizes a thousand small ones (a hull and its
+    // Hausdorff samples do not depend on their chunk)
+    std::vector<size_t> order(ms.size());
+    for (size_t k = 0; k < order.size(); k++) order[k] = k;
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return ms[a]->nv() < ms[b]->nv(); });
     size_t chunk = CUACD_HD_MAX_PAIRS;
     for (size_t s = 0; s < ms.size();) {
       const size_t n = std::min(chunk, ms.size() - s);
       std::vector<cuacd_mesh> cm(n);
       uint32_t maxNv = 0;
       for (size_t k = 0; k < n; k++) {
-        const Mesh& m = *ms[s + k];
+        const Mesh& m = *ms[order[s + k]];
         cm[k] = cuacd_mesh{m.v.data(), m.t.data(), (uint32_t)m.nv(), (uint32_t)m.nt()};
         maxNv = std::max(maxNv, (uint32_t)m.nv());
       }
@@ -262,8 +269,9 @@ class Engine {
       }
       if (rc != CUACD_OK) cuda_fail(rc, "hull batch");
       parallel_for(n, threads, [&](size_t k) {
-        Part& p = out[s + k];
-        const Mesh& m = *ms[s + k];
+        const size_t i = order[s + k];
+        Part& p = out[i];
+        const Mesh& m = *ms[i];
         p.mesh = m;
         p.meshVol = host::volume(m);
         if (status[k] == 8) {
@@ -280,7 +288,7 @@ class Engine {
           p.hullVol = NAN;
           return;
         }
-        if (keep && !(*keep)(s + k, (double)vol[k])) {
+        if (keep && !(*keep)(i, (double)vol[k])) {
           p.hullVol = vol[k];
           return;
         }
@@ -290,13 +298,13 @@ class Engine {
         if (defer) {
           std::vector<uint32_t> rt(raw, raw + 3 * (size_t)ntri[k]);
           std::vector<float> pv(m.v);
-          const double e = eps[s + k];
+          const double e = eps[i];
           p.hullTask = clean_pool().submit([pv = std::move(pv), rt = std::move(rt), e]() {
             const std::vector<uint32_t> ct = host::clean_hull_faces(pv.data(), pv.size() / 3, rt.data(), rt.size(), e);
             return host::compact_hull(pv.data(), ct.data(), ct.size() / 3, nullptr);
           });
         } else {
-          const std::vector<uint32_t> ct = host::clean_hull_faces(m.v.data(), m.nv(), raw, 3 * (size_t)ntri[k], eps[s + k]);
+          const std::vector<uint32_t> ct = host::clean_hull_faces(m.v.data(), m.nv(), raw, 3 * (size_t)ntri[k], eps[i]);
           p.hull = host::compact_hull(m.v.data(), ct.data(), ct.size() / 3, nullptr);
         }
         p.hullVol = vol[k];
@@ -310,8 +318,9 @@ class Engine {
       // point, where the reference falls back to its CPU hull (decompose.ts:
       // 183-188, merge.ts:371)
       for (size_t k = 0; k < n; k++) {
-        if (!std::isnan(out[s + k].hullVol)) continue;
-        if (!retry_hull(*ms[s + k], eps[s + k], withHd, out[s + k]) && !allowFail) {
+        const size_t i = order[s + k];
+        if (!std::isnan(out[i].hullVol)) continue;
+        if (!retry_hull(*ms[i], eps[i], withHd, out[i]) && !allowFail) {
           char msg[160];
           snprintf(msg, sizeof msg, "GPU hull failed (code %d) for a part with %u vertices", status[k], cm[k].nv);
           throw Failure{CUACD_E_CAPACITY, msg};
