@@ -1953,13 +1953,12 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   const uint8_t* dOpen = nullptr;
   if (!closed && mt[nMeshes] > 0) {
     const uint32_t nm = (uint32_t)nMeshes;
-    std::vector<uint32_t> meta(5 * (size_t)nm + 2, 0);  // edge prefix, triangle prefix, tOff, hash offset, size
+    // edge prefix, triangle prefix, tOff, hash offset; the hash sizes follow
+    std::vector<uint32_t> meta(4 * (size_t)nm + 2, 0);
     uint32_t* ePreH = meta.data();
     uint32_t* mtPreH = ePreH + nm + 1;
     uint32_t* tOffH = mtPreH + nm + 1;
     uint32_t* hOffH = tOffH + nm;
-    uint32_t* hSizeH = hOffH + nm;
-    (void)hSizeH;
     std::vector<uint32_t> hs(nm);
     uint64_t hTot = 0;
     for (uint32_t i = 0; i < nm; i++) {
@@ -1970,7 +1969,7 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
       hs[i] = pow2_at_least(std::max<uint32_t>(16, 6 * meshes[i].nt));
       hTot += hs[i];
     }
-    std::vector<uint32_t> metaAll(meta.begin(), meta.begin() + 4 * (size_t)nm + 2);
+    std::vector<uint32_t> metaAll(meta);
     metaAll.insert(metaAll.end(), hs.begin(), hs.end());
     if ((rc = e->openBits.ensure(mt[nMeshes])) || (rc = e->openKeys.ensure(8 * hTot)) ||
         (rc = e->openMeta.ensure(4 * metaAll.size())))

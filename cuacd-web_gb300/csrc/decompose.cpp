@@ -4,11 +4,12 @@
 //
 // One Engine owns one GPU tree. A call decomposes n meshes: one after
 // another, or all together, when every iteration gathers the cutting parts
-// of all meshes into one tree run, the new halves of all meshes into one
-// hull + Hausdorff submission, and every merge round's pairs into shared hull
-// and Hausdorff batches. The GPU work per seed and per part does not depend
-// on its batch, so both ways give the same parts. Host geometry (capped cuts,
-// concave planes, seam planes) runs on a thread pool.
+// of all meshes into one concave-plane batch and one tree run, the winning
+// cuts of all meshes into one GPU cut batch, the new halves into one hull +
+// Hausdorff submission, and every merge round's pairs into shared hull and
+// Hausdorff batches. The GPU work per seed and per part does not depend on
+// its batch, so both ways give the same parts. Host geometry (seam planes,
+// filtered unions, the output hulls' cleanup) runs on a thread pool.
 #include <algorithm>
 #include <array>
 #include <atomic>
@@ -1079,7 +1080,7 @@ void Engine::run_groups(std::vector<Job*>& jobs, std::vector<Engine*>& ranBy) {
     load[g] += jobs[k]->input.nt() + 1;
     ranBy[k] = g == 0 ? this : peers[g - 1].get();
   }
-  // the host threads of the cut and merge geometry are shared out
+  // the host threads of the merge geometry and hull cleanup are shared out
   const unsigned hc = std::max(1u, std::thread::hardware_concurrency());
   const int per = std::max(2, (int)(hc / (unsigned)G));
   std::vector<Failure> errs(G);

@@ -2,9 +2,10 @@
 (src/decompose.ts:404-415, Decomposer at :128-392) with its options
 (DecomposeOptions, :26-78) and result (DecomposeResult, :107-121).
 
-The loop itself runs inside the library (csrc/decompose.cpp): capped cuts,
-concave-edge planes and merge geometry on host threads, the tree search,
-hulls and Hausdorff distances on the GPU. `decompose_batch` decomposes many
+The loop itself runs inside the library (csrc/decompose.cpp): the tree
+search, capped cuts, concave-edge planes, hulls and Hausdorff distances on
+the GPU, the merge pass's pairing and the output hulls' cleanup on host
+threads. `decompose_batch` decomposes many
 meshes in one call; with batched=True every iteration and merge round
 serves all meshes with shared GPU launches, which gives the same parts as
 decomposing them one at a time.

@@ -344,7 +344,7 @@ typedef struct {
   int32_t mergeRounds;
   float mergePlaneTol;
   int32_t profile;
-  int32_t threads; /* host threads for cuts and merge geometry, 0 = all cores */
+  int32_t threads; /* host threads for hull cleanup and merge geometry, 0 = all cores */
   int32_t verbose; /* 1: one line per iteration and merge round on stderr;
                       2: also every applied cut (part, plane, half sizes) */
   int32_t streams; /* batched decompositions: meshes are split (by triangle
