@@ -37,7 +37,7 @@ UNITS = {
     "decompose.cpp": ["-Xcompiler", "-ffp-contract=off"],
     "cpu_hull.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
-HEADERS = ["cuacd_dev.cuh", "host_mesh.h", "cut_engine.h", "dev_scan.cuh", "concave_engine.h"]
+HEADERS = ["cuacd_dev.cuh", "host_mesh.h", "cut_engine.h", "dev_scan.cuh", "concave_engine.h", "dev_ptr.h", "tree_internal.h"]
 
 
 def nvcc() -> str:

@@ -31,6 +31,7 @@
 
 #include "../../include/cuacd.h"
 #include "concave_engine.h"
+#include "dev_ptr.h"
 #include "dev_scan.cuh"
 
 #define CONC_NONE 0xffffffffu
@@ -311,8 +312,14 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   for (uint32_t i = 0; i < nm; i++) {
     const cuacd_mesh& m = meshes[i];
     if ((m.nv && !m.verts) || (m.nt && !m.tris)) return set_error(CUACD_E_INVALID, "concave: null mesh buffer");
-    for (uint64_t k = 0; k < 3ull * m.nt; k++)
-      if (m.tris[k] >= m.nv) return set_error(CUACD_E_INVALID, "concave: triangle index out of range");
+    // a device mesh is copied on the device and its indices are the
+    // caller's to vouch for; a host mesh is checked
+    const bool dv = is_device_ptr(m.verts), dt = is_device_ptr(m.tris);
+    if ((m.nv && m.nt && dv != dt) || (!m.nv && dt) || (!m.nt && dv))
+      return set_error(CUACD_E_INVALID, "concave: a mesh's buffers must both be host or both be device memory");
+    if (!dt)
+      for (uint64_t k = 0; k < 3ull * m.nt; k++)
+        if (m.tris[k] >= m.nv) return set_error(CUACD_E_INVALID, "concave: triangle index out of range");
     MeshDesc& d = desc[i];
     d.vOff = (uint32_t)totV;
     d.nv = m.nv;
@@ -342,9 +349,9 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   CONCK(cudaEventRecord(e->ev0, s));
   for (uint32_t i = 0; i < nm; i++) {
     const cuacd_mesh& m = meshes[i];
-    if (m.nv) CONCK(cudaMemcpyAsync(e->inV.as<float>() + 3 * (size_t)desc[i].vOff, m.verts, 12ull * m.nv, cudaMemcpyHostToDevice, s));
+    if (m.nv) CONCK(cudaMemcpyAsync(e->inV.as<float>() + 3 * (size_t)desc[i].vOff, m.verts, 12ull * m.nv, cudaMemcpyDefault, s));
     if (desc[i].nt)
-      CONCK(cudaMemcpyAsync(e->inT.as<uint32_t>() + 3 * (size_t)desc[i].tOff, m.tris, 12ull * m.nt, cudaMemcpyHostToDevice, s));
+      CONCK(cudaMemcpyAsync(e->inT.as<uint32_t>() + 3 * (size_t)desc[i].tOff, m.tris, 12ull * m.nt, cudaMemcpyDefault, s));
   }
   CONCK(cudaMemcpyAsync(e->desc.p, desc.data(), sizeof(MeshDesc) * nm, cudaMemcpyHostToDevice, s));
   CONCK(cudaMemcpyAsync(e->vPre.p, vPre.data(), 4 * (nm + 1), cudaMemcpyHostToDevice, s));

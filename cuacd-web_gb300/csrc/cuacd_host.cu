@@ -21,6 +21,7 @@
 #include "cuacd_dev.cuh"
 #include "concave_engine.h"
 #include "cut_engine.h"
+#include "dev_ptr.h"
 #include "host_mesh.h"
 
 namespace cuacd {
@@ -340,24 +341,41 @@ struct Tree {
   }
   // upload meshes at the start of the pools and write their part descriptors
   // (tree.ts:233-278); returns the host-side descriptors in parts
+  // Host meshes are staged in pinned memory and uploaded in two copies;
+  // device meshes (both buffers in device memory, e.g. the halves of the
+  // last GPU cut batch) are copied on the device after the upload, into the
+  // places the staging left for them.
   int uploadMeshes(const cuacd_mesh* m, uint32_t n, std::vector<PartDesc>& parts) {
     uint64_t totV = 0, totT = 0;
+    std::vector<char> dev(n, 0);
+    bool anyHost = false;
     for (uint32_t k = 0; k < n; k++) {
       if (m[k].nv && !m[k].verts) return fail(CUACD_E_INVALID, "mesh has vertices but no vertex pointer");
       if (m[k].nt && !m[k].tris) return fail(CUACD_E_INVALID, "mesh has triangles but no index pointer");
+      const bool dv = is_device_ptr(m[k].verts), dt = is_device_ptr(m[k].tris);
+      if ((m[k].nv && m[k].nt && dv != dt) || (!m[k].nv && dt) || (!m[k].nt && dv))
+        return fail(CUACD_E_INVALID, "a mesh's buffers must both be host or both be device memory");
+      dev[k] = dv || dt;
+      anyHost |= !dev[k];
       totV += 3ull * m[k].nv;
       totT += 3ull * m[k].nt;
     }
     if (totV > cfg.vertexCap || totT > cfg.triCap) return fail(CUACD_E_CAPACITY, "seed meshes exceed pool capacity");
-    int rc = hStage.ensure(std::max<size_t>((totV + totT) * 4, 64));
-    if (rc) return rc;
-    float* hv = (float*)hStage.p;
-    uint32_t* ht = (uint32_t*)(hv + totV);
+    float* hv = nullptr;
+    uint32_t* ht = nullptr;
+    if (anyHost) {
+      int rc = hStage.ensure(std::max<size_t>((totV + totT) * 4, 64));
+      if (rc) return rc;
+      hv = (float*)hStage.p;
+      ht = (uint32_t*)(hv + totV);
+    }
     parts.assign(n, PartDesc{});
     uint32_t vt = 0, tt = 0;
     for (uint32_t k = 0; k < n; k++) {
-      std::memcpy(hv + vt, m[k].verts, 12ull * m[k].nv);
-      if (m[k].nt) std::memcpy(ht + tt, m[k].tris, 12ull * m[k].nt);
+      if (!dev[k]) {
+        std::memcpy(hv + vt, m[k].verts, 12ull * m[k].nv);
+        if (m[k].nt) std::memcpy(ht + tt, m[k].tris, 12ull * m[k].nt);
+      }
       PartDesc& p = parts[k];
       std::memset(&p, 0, sizeof(p));
       p.vOff = vt; p.nv = m[k].nv; p.tOff = tt; p.nt = m[k].nt;
@@ -366,11 +384,25 @@ struct Tree {
       vt += 3 * m[k].nv;
       tt += 3 * m[k].nt;
     }
-    if (totV) CK(cudaMemcpyAsync(D.V, hv, totV * 4, cudaMemcpyHostToDevice, stream));
-    if (totT) CK(cudaMemcpyAsync(D.T, ht, totT * 4, cudaMemcpyHostToDevice, stream));
+    if (anyHost && totV) CK(cudaMemcpyAsync(D.V, hv, totV * 4, cudaMemcpyHostToDevice, stream));
+    if (anyHost && totT) CK(cudaMemcpyAsync(D.T, ht, totT * 4, cudaMemcpyHostToDevice, stream));
+    for (uint32_t k = 0; k < n; k++) {
+      if (!dev[k]) continue;
+      if (m[k].nv)
+        CK(cudaMemcpyAsync(D.V + parts[k].vOff, m[k].verts, 12ull * m[k].nv, cudaMemcpyDeviceToDevice, stream));
+      if (m[k].nt)
+        CK(cudaMemcpyAsync(D.T + parts[k].tOff, m[k].tris, 12ull * m[k].nt, cudaMemcpyDeviceToDevice, stream));
+    }
     vTop = vt;
     tTop = tt;
     return 0;
+  }
+  // host copies of the meshes of the next hull-with-Hausdorff or Hausdorff
+  // call, whose sample counts follow each mesh's area (computed on the
+  // host); needed when those meshes are in device memory
+  std::vector<cuacd_mesh> twins;
+  const cuacd_mesh& host_side(const cuacd_mesh* m, size_t k) const {
+    return k < twins.size() ? twins[k] : m[k];
   }
 
   std::vector<LevelLayout> layout(uint32_t n, uint32_t dep, uint32_t w0, uint32_t ne0) const {
@@ -627,8 +659,17 @@ struct Tree {
   // ---- hull batches (tree.ts:382-443, 671-756) ----
   int hulls(const cuacd_mesh* m, int n, int hullStage, uint32_t* trisOut, uint32_t exportStrideOut, float* volOut,
             uint32_t* ntOut, int32_t* status, float* hdOut) {
+    // the host twins serve this call only
+    struct ClearTwins {
+      std::vector<cuacd_mesh>& t;
+      ~ClearTwins() { t.clear(); }
+    } clearTwins{twins};
     if (n < 0) return fail(CUACD_E_INVALID, "negative mesh count");
     if (n == 0) return 0;
+    if (hdOut)
+      for (int k = 0; k < n; k++)
+        if ((size_t)k >= twins.size() && is_device_ptr(m[k].verts))
+          return fail(CUACD_E_INVALID, "hull with Hausdorff of a device mesh needs its host copy");
     CK(cudaStreamSynchronize(stream));
     bool withHd = hdOut != nullptr;
     if (withHd && n > CUACD_HD_MAX_PAIRS) return fail(CUACD_E_INVALID, "hullsWithHausdorff: at most 1024 meshes per call");
@@ -653,7 +694,7 @@ struct Tree {
       capN.resize(2 * n);
       uint64_t off = 0;
       for (int k = 0; k < n; k++) {
-        double area = mesh_area(m[k]);
+        double area = mesh_area(host_side(m, (size_t)k));
         uint64_t res = std::max<uint64_t>(1000, (uint64_t)std::floor(2000.0 * area));
         uint64_t cap = 2 * (2 * res + std::max<uint64_t>(m[k].nt, 2ull * m[k].nv) + 16);
         if (3 * (off + cap) > cfg.scratchWords) return fail(CUACD_E_SCRATCH, "hausdorff sample scratch exceeds capacity");
@@ -795,6 +836,9 @@ struct Tree {
   int hausdorff(const cuacd_mesh* a, const cuacd_mesh* b, int n, float* out) {
     if (n < 0) return fail(CUACD_E_INVALID, "negative pair count");
     if (n == 0) return 0;
+    for (int k = 0; k < n; k++)
+      if (is_device_ptr(a[k].verts) || is_device_ptr(b[k].verts))
+        return fail(CUACD_E_INVALID, "hausdorff: the sample counts follow host meshes' areas; pass host meshes");
     if (n > CUACD_HD_MAX_PAIRS) return fail(CUACD_E_INVALID, "hausdorff: at most 1024 pairs per call");
     CK(cudaStreamSynchronize(stream));
     int rc = ensureTables(1);
@@ -845,6 +889,18 @@ struct Tree {
     return 0;
   }
 };
+
+// the host copies of the meshes of the handle's next hull-with-Hausdorff
+// call (internal: the decomposer passes device meshes with their host
+// copies, tree_internal.h)
+namespace cuacd {
+int tree_set_host_twins(void* tree, const cuacd_mesh* twins, int n) {
+  Tree* t = (Tree*)tree;
+  if (!t || n < 0 || (n > 0 && !twins)) return fail(CUACD_E_INVALID, "host twins: invalid argument");
+  t->twins.assign(twins, twins + n);
+  return CUACD_OK;
+}
+}  // namespace cuacd
 
 extern "C" {
 
@@ -1030,6 +1086,17 @@ int cuacd_cuts_half(const void* halves, int cut, int side, const float** verts, 
   if (tris) *tris = st == 0 ? h->T + 3 * h->tOff[k] : nullptr;
   if (nv) *nv = st == 0 ? h->nv[k] : 0;
   if (nt) *nt = st == 0 ? h->nt[k] : 0;
+  return st;
+}
+
+int cuacd_cuts_half_device(const void* halves, int cut, int side, const float** verts, const uint32_t** tris) {
+  const cut::Halves* h = (const cut::Halves*)halves;
+  if (!h || cut < 0 || (size_t)cut >= h->status.size() || side < 0 || side > 1)
+    return fail(CUACD_E_INVALID, "cuacd_cuts_half_device: invalid argument");
+  const size_t k = 2 * (size_t)cut + side;
+  const int st = h->status[cut];
+  if (verts) *verts = st == 0 && h->dV ? h->dV + 3 * h->vOff[k] : nullptr;
+  if (tris) *tris = st == 0 && h->dT ? h->dT + 3 * h->tOff[k] : nullptr;
   return st;
 }
 

@@ -31,6 +31,10 @@ struct Halves {
   std::vector<double> vol;  // signed volume of each half (a fixed-order parallel sum)
   float* V = nullptr;     // into host
   uint32_t* T = nullptr;  // into host
+  // the same halves on the device, in the engine's output buffers (same
+  // offsets), valid until the engine's next batch
+  const float* dV = nullptr;
+  const uint32_t* dT = nullptr;
   float gpuMs = 0.0f;
   std::vector<uint32_t> host;  // every half's vertices, then every half's triangles
 };

@@ -58,6 +58,7 @@
 #include <vector>
 
 #include "cut_engine.h"
+#include "dev_ptr.h"
 #include "dev_scan.cuh"
 
 #define CUT_FULL 0xffffffffu
@@ -1898,8 +1899,14 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   for (int i = 0; i < nMeshes; i++) {
     const cuacd_mesh& m = meshes[i];
     if ((m.nv && !m.verts) || (m.nt && !m.tris)) return set_error(CUACD_E_INVALID, "cut: null mesh buffer");
-    for (uint64_t k = 0; k < 3ull * m.nt; k++)
-      if (m.tris[k] >= m.nv) return set_error(CUACD_E_INVALID, "cut: triangle index out of range");
+    // a device mesh (both buffers in device memory) is copied on the device
+    // and its indices are the caller's to vouch for; a host mesh is checked
+    const bool dv = is_device_ptr(m.verts), dt = is_device_ptr(m.tris);
+    if ((m.nv && m.nt && dv != dt) || (!m.nv && dt) || (!m.nt && dv))
+      return set_error(CUACD_E_INVALID, "cut: a mesh's buffers must both be host or both be device memory");
+    if (!dt)
+      for (uint64_t k = 0; k < 3ull * m.nt; k++)
+        if (m.tris[k] >= m.nv) return set_error(CUACD_E_INVALID, "cut: triangle index out of range");
     mv[i + 1] = mv[i] + m.nv;
     mt[i + 1] = mt[i] + m.nt;
   }
@@ -1942,8 +1949,8 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   CUTCK(cudaEventRecord(e->ev0, s));
   for (int i = 0; i < nMeshes; i++) {
     const cuacd_mesh& m = meshes[i];
-    if (m.nv) CUTCK(cudaMemcpyAsync(e->inV.as<float>() + 3 * mv[i], m.verts, 12ull * m.nv, cudaMemcpyHostToDevice, s));
-    if (m.nt) CUTCK(cudaMemcpyAsync(e->inT.as<uint32_t>() + 3 * mt[i], m.tris, 12ull * m.nt, cudaMemcpyHostToDevice, s));
+    if (m.nv) CUTCK(cudaMemcpyAsync(e->inV.as<float>() + 3 * mv[i], m.verts, 12ull * m.nv, cudaMemcpyDefault, s));
+    if (m.nt) CUTCK(cudaMemcpyAsync(e->inT.as<uint32_t>() + 3 * mt[i], m.tris, 12ull * m.nt, cudaMemcpyDefault, s));
   }
   CUTCK(cudaMemcpyAsync(e->desc.p, desc.data(), sizeof(CutDesc) * n, cudaMemcpyHostToDevice, s));
   CUTCK(cudaMemcpyAsync(e->vPre.p, vPre.data(), 4 * (n + 1), cudaMemcpyHostToDevice, s));
@@ -2173,6 +2180,9 @@ int engine_run(Engine* e, cudaStream_t s, const cuacd_mesh* meshes, int nMeshes,
   CUTCK(cudaStreamSynchronize(s));
   std::memcpy(out->V, stV, 12 * outVTot);
   std::memcpy(out->T, stT, 12 * outTTot);
+  // the halves stay in the engine's output buffers until its next batch
+  out->dV = e->outV.as<float>();
+  out->dT = e->outT.as<uint32_t>();
   cudaEventElapsedTime(&out->gpuMs, e->ev0, e->ev1);
   return CUACD_OK;
 }

@@ -30,6 +30,7 @@
 
 #include "../../include/cuacd.h"
 #include "host_mesh.h"
+#include "tree_internal.h"
 
 namespace cuacd {
 int set_error(int code, const char* msg);
@@ -61,6 +62,11 @@ struct Part {
   std::vector<Plane> seams;
   int merged = 1;
   uint64_t id = 0;  // identity for the merge pass's pair cache
+  // the part's geometry on the device: made by GPU cut batch `gen` of its
+  // engine, in that engine's cut output until the next batch
+  const float* dV = nullptr;
+  const uint32_t* dT = nullptr;
+  uint64_t gen = 0;
 };
 
 // partCost (part.ts:27-29)
@@ -210,6 +216,16 @@ class Engine {
     p.hullTask = std::shared_future<Mesh>();
   }
 
+  // GPU cut batches run so far: a part made by the latest one is still in
+  // the cut engine's output buffers, and the next concave-plane batch, tree
+  // run and cut batch read it there instead of uploading it again
+  uint64_t cutGen = 0;
+  cuacd_mesh resident(const Part& p) const {
+    if (p.gen != 0 && p.gen == cutGen && p.dV && p.dT)
+      return cuacd_mesh{p.dV, p.dT, (uint32_t)p.mesh.nv(), (uint32_t)p.mesh.nt()};
+    return cuacd_mesh{p.mesh.v.data(), p.mesh.t.data(), (uint32_t)p.mesh.nv(), (uint32_t)p.mesh.nt()};
+  }
+
   [[noreturn]] void cuda_fail(int rc, const char* what) {
     throw Failure{rc, std::string(what) + ": " + cuacd_last_error()};
   }
@@ -231,9 +247,12 @@ class Engine {
   // pass needs the cleaned hull only for pairs under the threshold: merge.ts
   // cleans every pair's hull, merge.ts:213, but keeps it only for those,
   // merge.ts:221)
+  // dev: the same meshes in device memory (the GPU then copies them on the
+  // device; ms stays the host copy for the sample counts and the cleanup)
   void hulls(const std::vector<const Mesh*>& ms, const std::vector<double>& eps, bool withHd, std::vector<Part>& out,
              bool allowFail = false, bool defer = false,
-             const std::function<bool(size_t, double)>* keep = nullptr) {
+             const std::function<bool(size_t, double)>* keep = nullptr,
+             const std::vector<cuacd_mesh>* dev = nullptr) {
     out.resize(ms.size());
     if (defer && !pool) pool = std::make_unique<TaskPool>(threads);
     // chunks hold meshes of similar size (ascending point count): a chunk's
@@ -246,12 +265,18 @@ class Engine {
     size_t chunk = CUACD_HD_MAX_PAIRS;
     for (size_t s = 0; s < ms.size();) {
       const size_t n = std::min(chunk, ms.size() - s);
-      std::vector<cuacd_mesh> cm(n);
+      std::vector<cuacd_mesh> cm(n), twins;
       uint32_t maxNv = 0;
       for (size_t k = 0; k < n; k++) {
         const Mesh& m = *ms[order[s + k]];
         cm[k] = cuacd_mesh{m.v.data(), m.t.data(), (uint32_t)m.nv(), (uint32_t)m.nt()};
         maxNv = std::max(maxNv, (uint32_t)m.nv());
+      }
+      if (dev) {
+        twins = cm;
+        for (size_t k = 0; k < n; k++) cm[k] = (*dev)[order[s + k]];
+        const int trc = tree_set_host_twins(tree, twins.data(), (int)n);
+        if (trc != CUACD_OK) cuda_fail(trc, "hull batch");
       }
       const uint32_t stride = 3 * 2 * std::min<uint32_t>((uint32_t)o.tree.hullMaxVerts, maxNv);
       std::vector<uint32_t> tris((size_t)n * stride + 1);
@@ -494,8 +519,7 @@ class Engine {
       for (size_t k = 0; k < seeds.size(); k++) {
         const int iter = seeds[k].job->iter - 1;
         if (iter >= o.concaveIters) continue;
-        const Mesh& m = seeds[k].job->parts[seeds[k].part].mesh;
-        cm.push_back(cuacd_mesh{m.v.data(), m.t.data(), (uint32_t)m.nv(), (uint32_t)m.nt()});
+        cm.push_back(resident(seeds[k].job->parts[seeds[k].part]));
         sd.push_back((uint32_t)(iter * 7919 + (int)seeds[k].part));
         which.push_back(k);
       }
@@ -525,9 +549,9 @@ class Engine {
       for (size_t k = 0; k < n; k++) per = std::max(per, planes[start + k].size() / 4);
       std::vector<float> flat(std::max<size_t>(n * per * 4, 1), 0.0f);
       for (size_t k = 0; k < n; k++) {
-        const Mesh& m = seeds[start + k].job->parts[seeds[start + k].part].mesh;
-        cm[k] = cuacd_mesh{m.v.data(), m.t.data(), (uint32_t)m.nv(), (uint32_t)m.nt()};
-        spacing[k] = refine ? (float)refine_spacing(m) : 0.0f;
+        const Part& sp = seeds[start + k].job->parts[seeds[start + k].part];
+        cm[k] = resident(sp);
+        spacing[k] = refine ? (float)refine_spacing(sp.mesh) : 0.0f;
         std::copy(planes[start + k].begin(), planes[start + k].end(), flat.begin() + k * per * 4);
       }
       cuacd_run_opts ro{};
@@ -589,7 +613,7 @@ class Engine {
         continue;
       }
       cutOf.push_back((int32_t)cm.size());
-      cm.push_back(cuacd_mesh{p.mesh.v.data(), p.mesh.t.data(), (uint32_t)p.mesh.nv(), (uint32_t)p.mesh.nt()});
+      cm.push_back(resident(p));
       for (int a = 0; a < 4; a++) cutPlanes.push_back((double)r.plane[a]);
       cutSeed.push_back(k);
     }
@@ -601,8 +625,11 @@ class Engine {
       const int rc = cuacd_tree_plane_cuts(tree, cm.data(), (int)cm.size(), cutOf.data(), cutPlanes.data(),
                                            (int)cm.size(), flags, &halvesH);
       if (rc != CUACD_OK) cuda_fail(rc, "plane cuts");
+      cutGen++;  // the batch's halves are the resident generation now
     }
     std::vector<host::CutResult> cutRes(seeds.size());
+    // device copies of each cut's halves (positive, negative)
+    std::vector<std::array<const void*, 4>> devHalf(seeds.size(), {nullptr, nullptr, nullptr, nullptr});
     for (size_t q = 0; q < cutSeed.size(); q++) {
       host::CutResult& c = cutRes[cutSeed[q]];
       const float* v[2];
@@ -611,6 +638,13 @@ class Engine {
       int st = 0;
       for (int sd = 0; sd < 2 && st == 0; sd++) st = cuacd_cuts_half(halvesH, (int)q, sd, &v[sd], &nv[sd], &t[sd], &nt[sd]);
       if (st != 0) continue;
+      for (int sd = 0; sd < 2; sd++) {
+        const float* dv = nullptr;
+        const uint32_t* dt = nullptr;
+        cuacd_cuts_half_device(halvesH, (int)q, sd, &dv, &dt);
+        devHalf[cutSeed[q]][2 * sd] = dv;
+        devHalf[cutSeed[q]][2 * sd + 1] = dt;
+      }
       c.ok = true;
       c.pos.v.assign(v[0], v[0] + 3 * (size_t)nv[0]);
       c.pos.t.assign(t[0], t[0] + 3 * (size_t)nt[0]);
@@ -647,18 +681,33 @@ class Engine {
     cutGpuMs += cutGpu;
     // hulls and Hausdorff distances of every new half in one submission
     std::vector<const Mesh*> halves;
+    std::vector<cuacd_mesh> halvesDev;  // the same halves in the cut engine's output
     std::vector<double> heps;
     std::vector<size_t> which;
+    bool allDev = true;
     for (size_t k = 0; k < seeds.size(); k++)
       if (cuts[k].ok) {
         halves.push_back(&cuts[k].pos);
         halves.push_back(&cuts[k].neg);
+        for (int sd = 0; sd < 2; sd++) {
+          const Mesh& h = sd == 0 ? cuts[k].pos : cuts[k].neg;
+          const float* dv = (const float*)devHalf[k][2 * sd];
+          const uint32_t* dt = (const uint32_t*)devHalf[k][2 * sd + 1];
+          allDev &= dv != nullptr && dt != nullptr;
+          halvesDev.push_back(cuacd_mesh{dv, dt, (uint32_t)h.nv(), (uint32_t)h.nt()});
+        }
         heps.insert(heps.end(), 2, seeds[k].job->hullEps);
         which.push_back(k);
       }
     const auto th = Clock::now();
     std::vector<Part> made;
-    hulls(halves, heps, true, made, false, true);
+    hulls(halves, heps, true, made, false, true, nullptr, allDev ? &halvesDev : nullptr);
+    for (size_t q = 0; q < which.size() && allDev; q++)
+      for (int sd = 0; sd < 2; sd++) {
+        made[2 * q + sd].dV = halvesDev[2 * q + sd].verts;
+        made[2 * q + sd].dT = halvesDev[2 * q + sd].tris;
+        made[2 * q + sd].gen = cutGen;
+      }
     hullMs += ms_since(th);
     if (o.verbose) {
       size_t nParts = 0, nTris = 0;

@@ -10,6 +10,13 @@
  * Conventions
  *   - Plain pointers and sizes only. Inputs are borrowed for the duration of
  *     the call and copied; outputs are caller-allocated.
+ *   - Device meshes: cuacd_tree_run / _prepare, cuacd_tree_hull_meshes,
+ *     cuacd_tree_plane_cuts and cuacd_tree_concave_planes also take meshes
+ *     whose two buffers are device memory of the handle's device (for
+ *     instance the halves cuacd_cuts_half_device returns): they are copied
+ *     on the device, in the handle's stream order, and their indices are not
+ *     checked on the host. The Hausdorff entry points take host meshes (the
+ *     sample counts follow each mesh's area, computed on the host).
  *   - Return codes: CUACD_OK (0) or a negative CUACD_E_* code; the message
  *     of the last failure on the calling thread is cuacd_last_error().
  *   - Recoverable conditions of a tree run (pool overflow, hull failures,
@@ -291,6 +298,13 @@ int cuacd_tree_plane_cuts(void* tree, const cuacd_mesh* meshes, int nMeshes, con
  * scratch bound was exceeded; or a negative error. */
 int cuacd_cuts_half(const void* halves, int cut, int side, const float** verts, uint32_t* nv, const uint32_t** tris,
                     uint32_t* nt);
+/* The same half in device memory (no counterpart in the reference): the
+ * GPU cut's output buffers keep every half of the batch until the next
+ * cuacd_tree_plane_cuts (or cuacd_tree_eval_cuts) on the same handle, also
+ * after cuacd_cuts_free, so the next steps can take the halves as device
+ * meshes (see the conventions on device meshes). Same return as
+ * cuacd_cuts_half. */
+int cuacd_cuts_half_device(const void* halves, int cut, int side, const float** verts, const uint32_t** tris);
 /* concaveEdgePlanes (src/cpu/concave.ts:25-92) of n meshes on the GPU, on
  * the tree handle's stream: mesh k's planes (at most 4 * nConcaveEdges, 4
  * floats each) go to out + 16 * nConcaveEdges * k and their count to

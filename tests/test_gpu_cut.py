@@ -226,3 +226,102 @@ def test_gpu_cut_closed_flag_gives_the_same_halves():
         assert x[0] == y[0]
         if x[0] == 0:
             assert _same(x[1], y[1]) and _same(x[2], y[2])
+
+
+def test_device_halves_feed_the_next_calls():
+    """cuacd_cuts_half_device: the halves of a GPU cut batch, passed as device
+    meshes to the next hull batch, concave-plane batch, tree run and cut
+    batch (the decomposer's resident parts), give the results of the same
+    halves passed from host memory. The last cut reads its inputs from the
+    output buffers it then overwrites."""
+    import ctypes as C
+
+    A = pkg("_abi")
+    L = T.load_library()
+    L.cuacd_cuts_half_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(C.POINTER(C.c_float)),
+                                         C.POINTER(C.POINTER(C.c_uint32))]
+    m = G.noisy_icosphere(3, seed=1)
+    g = T.GpuTree(width=6, width2=3, depth=2, nConcaveEdges=16, hullMaxVerts=4096)
+    c = (m.verts.min(0).astype(np.float64) + m.verts.max(0)) / 2
+    planes = np.ascontiguousarray([[1.0, 0.0, 0.0, -c[0] - 0.05], [0.0, 1.0, 0.0, -c[1] + 0.1]], np.float64)
+    ma = A.MeshArray([m])
+    idx = np.zeros(2, np.int32)
+    h = C.c_void_p()
+    assert L.cuacd_tree_plane_cuts(g.h, ma.arr, 1, idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   planes.ctypes.data_as(C.POINTER(C.c_double)), 2, 1, C.byref(h)) == 0
+    host, dev = [], (A.MeshRef * 4)()
+    for k in range(2):
+        for sd in range(2):
+            v, t = C.POINTER(C.c_float)(), C.POINTER(C.c_uint32)()
+            nv, nt = C.c_uint32(), C.c_uint32()
+            assert L.cuacd_cuts_half(h, k, sd, C.byref(v), C.byref(nv), C.byref(t), C.byref(nt)) == 0
+            host.append(M.Mesh(np.ctypeslib.as_array(v, shape=(3 * nv.value,)).reshape(-1, 3).copy(),
+                               np.ctypeslib.as_array(t, shape=(3 * nt.value,)).reshape(-1, 3).copy()))
+            dv, dt = C.POINTER(C.c_float)(), C.POINTER(C.c_uint32)()
+            assert L.cuacd_cuts_half_device(h, k, sd, C.byref(dv), C.byref(dt)) == 0
+            i = 2 * k + sd
+            dev[i].verts, dev[i].tris, dev[i].nv, dev[i].nt = dv, dt, nv.value, nt.value
+    L.cuacd_cuts_free(h)
+    n = 4
+    # hulls
+    hh, _ = g.hull_meshes(host)
+    stride = 3 * 2 * max(x.nv for x in host)
+    tris = np.zeros(n * stride, np.uint32)
+    vol = np.zeros(n, np.float32)
+    ntr = np.zeros(n, np.uint32)
+    st = np.zeros(n, np.int32)
+    assert L.cuacd_tree_hull_meshes(g.h, dev, n, 0, A.uptr(tris), stride, A.fptr(vol), A.uptr(ntr),
+                                    st.ctypes.data_as(C.POINTER(C.c_int32))) == 0
+    for k in range(n):
+        assert st[k] == 0 and vol[k] == hh[k]["volume"]
+        assert np.array_equal(tris[k * stride: k * stride + 3 * ntr[k]].reshape(-1, 3), hh[k]["tris"])
+    # concave planes
+    ph = g.concave_planes(host, 16)
+    out = np.zeros((n, 64, 4), np.float32)
+    cnt = np.zeros(n, np.int32)
+    seeds = np.full(n, 12345, np.uint32)
+    assert L.cuacd_tree_concave_planes(g.h, dev, n, 16, 0.005, 3.49, A.uptr(seeds), A.fptr(out),
+                                       cnt.ctypes.data_as(C.POINTER(C.c_int32))) == 0
+    for k in range(n):
+        assert np.array_equal(out[k, : cnt[k]], ph[k])
+    # tree run
+    rh = g.run(host, ph)
+    ep = np.zeros((n, g.plane_slots, 4), np.float32)
+    for k in range(n):
+        ep[k, : len(ph[k])] = ph[k]
+    res = (A.SeedResult * n)()
+    rs = A.RunStats()
+    opts = A.RunOpts(depth=0, width=-1, nEdgeCuts=-1)
+    assert L.cuacd_tree_run(g.h, dev, n, A.fptr(ep), g.plane_slots, C.byref(opts), res, C.byref(rs)) == 0
+    rd = T._result(res, rs, n)
+    assert rd["seeds"] == rh["seeds"] and rd["validJobs"] == rh["validJobs"]
+    # a cut of the device halves, which overwrites the buffers they live in
+    cp = np.ascontiguousarray([[0.0, 0.0, 1.0, -c[2] - 0.02]] * n, np.float64)
+    ref = g.plane_cuts(host, cp, np.arange(n, dtype=np.int32), closed=True)
+    # the host-mesh cut above replaced the batch the device halves lived in:
+    # cut once more from host so that the device halves are fresh, then cut them
+    h2 = C.c_void_p()
+    assert L.cuacd_tree_plane_cuts(g.h, ma.arr, 1, idx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   planes.ctypes.data_as(C.POINTER(C.c_double)), 2, 1, C.byref(h2)) == 0
+    for k in range(2):
+        for sd in range(2):
+            dv, dt = C.POINTER(C.c_float)(), C.POINTER(C.c_uint32)()
+            assert L.cuacd_cuts_half_device(h2, k, sd, C.byref(dv), C.byref(dt)) == 0
+            dev[2 * k + sd].verts, dev[2 * k + sd].tris = dv, dt
+    L.cuacd_cuts_free(h2)
+    h3 = C.c_void_p()
+    cidx = np.arange(n, dtype=np.int32)
+    assert L.cuacd_tree_plane_cuts(g.h, dev, n, cidx.ctypes.data_as(C.POINTER(C.c_int32)),
+                                   cp.ctypes.data_as(C.POINTER(C.c_double)), n, 1, C.byref(h3)) == 0
+    for k in range(n):
+        st_ref, pos, neg = ref[k]
+        for sd, want in enumerate((pos, neg)):
+            v, t = C.POINTER(C.c_float)(), C.POINTER(C.c_uint32)()
+            nv, nt = C.c_uint32(), C.c_uint32()
+            s = L.cuacd_cuts_half(h3, k, sd, C.byref(v), C.byref(nv), C.byref(t), C.byref(nt))
+            assert (s == 0) == (st_ref == 0)
+            if s == 0:
+                got = M.Mesh(np.ctypeslib.as_array(v, shape=(3 * nv.value,)).reshape(-1, 3).copy(),
+                             np.ctypeslib.as_array(t, shape=(3 * nt.value,)).reshape(-1, 3).copy())
+                assert _same(got, want)
+    L.cuacd_cuts_free(h3)
