@@ -1249,7 +1249,10 @@ int cuacd_tree_hull_meshes(void* t, const cuacd_mesh* m, int n, int hullStage, u
 int cuacd_tree_hulls_with_hausdorff(void* t, const cuacd_mesh* m, int n, uint32_t* trisOut, uint32_t exportStride,
                                     float* volOut, uint32_t* ntOut, float* hdOut, int32_t* status) {
   if (!t) return fail(CUACD_E_INVALID, "null tree");
-  if (!hdOut) return fail(CUACD_E_INVALID, "null Hausdorff output");
+  if (!hdOut) {
+    ((Tree*)t)->twins.clear();  // the host twins serve one call, even a refused one
+    return fail(CUACD_E_INVALID, "null Hausdorff output");
+  }
   return ((Tree*)t)->hulls(m, n, 0, trisOut, exportStride, volOut, ntOut, status, hdOut);
 }
 int cuacd_tree_read_items(void* tp, uint32_t first, uint32_t n, uint32_t* out) {
