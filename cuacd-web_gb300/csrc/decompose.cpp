@@ -1311,12 +1311,19 @@ class Server {
   }
   // device bytes of every tree (one not built yet counts as built), with
   // its pools grown to the working sets of the active requests and `extra`
+  // device bytes of an engine's trees: its tree and, once a hull outgrew
+  // that tree's bound, the larger tree that rebuilds such hulls
+  static uint64_t engine_bytes(const Engine& e, uint64_t* caps4) {
+    uint64_t held = 0, extra = 0;
+    cuacd_tree_memory(e.tree, &held, caps4);
+    if (e.bigTree) cuacd_tree_memory(e.bigTree, &extra, nullptr);
+    return held + extra;
+  }
   std::map<uint32_t, Mem> memory(const Request* extra) const {
     std::map<uint32_t, Mem> m;
     for (const auto& kv : engines) {
-      uint64_t held = 0;
       Mem& x = m[kv.first];
-      cuacd_tree_memory(kv.second->tree, &held, x.cap);
+      const uint64_t held = engine_bytes(*kv.second, x.cap);
       x.nonPool = held - pool_bytes(x.cap);
       x.built = true;
     }
@@ -1409,11 +1416,7 @@ class Server {
       if (rc != CUACD_OK) throw Failure{rc, cuacd_last_error()};
     }
     uint64_t held = 0;
-    for (const auto& kv : engines) {
-      uint64_t b = 0;
-      cuacd_tree_memory(kv.second->tree, &b, nullptr);
-      held += b;
-    }
+    for (const auto& kv : engines) held += engine_bytes(*kv.second, nullptr);
     // one iteration of every admitted decomposition, per threshold
     std::map<Engine*, std::vector<Job*>> groups;
     for (Request& r : active)
@@ -1421,11 +1424,7 @@ class Server {
     for (auto& kv : groups) kv.first->iterate(kv.second);
     // the buffers of the cut and concave passes grow inside the step
     uint64_t after = 0;
-    for (const auto& kv : engines) {
-      uint64_t b = 0;
-      cuacd_tree_memory(kv.second->tree, &b, nullptr);
-      after += b;
-    }
+    for (const auto& kv : engines) after += engine_bytes(*kv.second, nullptr);
     peakBytes = std::max({peakBytes, held, after});
     // decompositions with nothing left to cut finish together
     std::map<Engine*, std::vector<Job*>> fin;
@@ -1814,11 +1813,7 @@ int cuacd_server_stats(const void* sv, cuacd_server_state* out) {
   if (!s || !out) return set_error(CUACD_E_INVALID, "cuacd_server_stats: invalid argument");
   std::memset(out, 0, sizeof *out);
   out->budgetBytes = s->budget;
-  for (const auto& kv : s->engines) {
-    uint64_t b = 0;
-    cuacd_tree_memory(kv.second->tree, &b, nullptr);
-    out->deviceBytes += b;
-  }
+  for (const auto& kv : s->engines) out->deviceBytes += Server::engine_bytes(*kv.second, nullptr);
   out->peakDeviceBytes = std::max(s->peakBytes, out->deviceBytes);
   out->projectedBytes = s->projected(nullptr);
   for (const Request& r : s->active)
