@@ -728,21 +728,52 @@ struct Tree {
     }
     CK(cudaEventRecord(ev1, stream));
     CK(cudaGetLastError());
-    size_t pb = (size_t)n * sizeof(PartDesc), tb = (size_t)n * stride * 4;
-    if ((rc = hRead.ensure(pb + tb + 4 * (size_t)n + 64))) return rc;
+    // the faces come back either as the whole export range (small strides)
+    // or, when that range is large and mostly unused (a chunk's stride
+    // follows its largest mesh), as each hull's own faces after the face
+    // counts are known
+    const size_t pb = (size_t)n * sizeof(PartDesc), hb = withHd ? 4 * (size_t)n : 0;
+    const bool wantTris = trisOut != nullptr && exportStrideOut > 0 && stride > 0;
+    const bool compact = wantTris && (size_t)n * stride * 4 > (16u << 20);
+    const size_t tb = wantTris && !compact ? (size_t)n * stride * 4 : 0;
+    if ((rc = hRead.ensure(pb + hb + tb + 64))) return rc;
     uint8_t* h = (uint8_t*)hRead.p;
     CK(cudaMemcpyAsync(h, D.parts, pb, cudaMemcpyDeviceToHost, stream));
-    if (tb) CK(cudaMemcpyAsync(h + pb, D.T + tTop, tb, cudaMemcpyDeviceToHost, stream));
-    if (withHd) CK(cudaMemcpyAsync(h + pb + tb, D.ctr + CTR_HD, 4 * (size_t)n, cudaMemcpyDeviceToHost, stream));
+    if (withHd) CK(cudaMemcpyAsync(h + pb, D.ctr + CTR_HD, hb, cudaMemcpyDeviceToHost, stream));
+    if (tb) CK(cudaMemcpyAsync(h + pb + hb, D.T + tTop, tb, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
     {
       float ms = 0;
       if (cudaEventElapsedTime(&ms, ev0, ev1) != cudaSuccess) cudaGetLastError();
       record(ms);
     }
+    std::vector<size_t> faceOff;  // compact readback: word offset of hull k's faces
+    if (compact) {
+      const PartDesc* pd0 = (const PartDesc*)h;
+      faceOff.assign((size_t)n, 0);
+      size_t words = 0;
+      for (int k = 0; k < n; k++) {
+        faceOff[k] = words;
+        if (pd0[k].hullVol >= 0.0f && pd0[k].pad0 >= 4) words += std::min<size_t>(3 * (size_t)pd0[k].pad0, stride);
+      }
+      std::vector<PartDesc> keep(pd0, pd0 + n);  // hRead may move when it grows
+      std::vector<uint32_t> hdKeep;
+      if (withHd) hdKeep.assign((const uint32_t*)(h + pb), (const uint32_t*)(h + pb) + n);
+      if ((rc = hRead.ensure(pb + hb + 4 * words + 64))) return rc;
+      h = (uint8_t*)hRead.p;
+      std::memcpy(h, keep.data(), pb);
+      if (withHd) std::memcpy(h + pb, hdKeep.data(), hb);
+      for (int k = 0; k < n; k++) {
+        const size_t w = (k + 1 < n ? faceOff[k + 1] : words) - faceOff[k];
+        if (w)
+          CK(cudaMemcpyAsync(h + pb + hb + 4 * faceOff[k], D.T + tTop + (size_t)k * stride, 4 * w,
+                             cudaMemcpyDeviceToHost, stream));
+      }
+      CK(cudaStreamSynchronize(stream));
+    }
     const PartDesc* pd = (const PartDesc*)h;
-    const uint32_t* tw = (const uint32_t*)(h + pb);
-    const uint32_t* hdw = (const uint32_t*)(h + pb + tb);
+    const uint32_t* tw = (const uint32_t*)(h + pb + hb);
+    const uint32_t* hdw = (const uint32_t*)(h + pb);
     for (int k = 0; k < n; k++) {
       float vol = pd[k].hullVol;
       uint32_t nf = doExport ? pd[k].pad0 : 4;
@@ -752,9 +783,10 @@ struct Tree {
       if (status) status[k] = s;
       if (volOut) volOut[k] = vol;
       if (ntOut) ntOut[k] = s == 0 && doExport ? nf : 0;
-      if (trisOut && s == 0 && exportStrideOut) {
-        uint32_t cpy = std::min(3 * nf, exportStrideOut);
-        std::memcpy(trisOut + (size_t)k * exportStrideOut, tw + (size_t)k * stride, 4ull * cpy);
+      if (wantTris && s == 0) {
+        const uint32_t cpy = std::min({3 * nf, exportStrideOut, stride});
+        const uint32_t* src = compact ? tw + faceOff[k] : tw + (size_t)k * stride;
+        std::memcpy(trisOut + (size_t)k * exportStrideOut, src, 4ull * cpy);
       }
       if (withHd) {
         float w;

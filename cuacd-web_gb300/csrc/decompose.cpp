@@ -279,14 +279,15 @@ class Engine {
         if (trc != CUACD_OK) cuda_fail(trc, "hull batch");
       }
       const uint32_t stride = 3 * 2 * std::min<uint32_t>((uint32_t)o.tree.hullMaxVerts, maxNv);
-      std::vector<uint32_t> tris((size_t)n * stride + 1);
+      // not zeroed: only each hull's own faces are written and read
+      std::unique_ptr<uint32_t[]> tris(new uint32_t[(size_t)n * stride + 1]);
       std::vector<float> vol(n), hd(n);
       std::vector<uint32_t> ntri(n);
       std::vector<int32_t> status(n);
       const auto t0 = Clock::now();
-      const int rc = withHd ? cuacd_tree_hulls_with_hausdorff(tree, cm.data(), (int)n, tris.data(), stride, vol.data(),
+      const int rc = withHd ? cuacd_tree_hulls_with_hausdorff(tree, cm.data(), (int)n, tris.get(), stride, vol.data(),
                                                               ntri.data(), hd.data(), status.data())
-                            : cuacd_tree_hull_meshes(tree, cm.data(), (int)n, 0, tris.data(), stride, vol.data(),
+                            : cuacd_tree_hull_meshes(tree, cm.data(), (int)n, 0, tris.get(), stride, vol.data(),
                                                      ntri.data(), status.data());
       gpuMs += ms_since(t0);
       if (rc == CUACD_E_CAPACITY && n > 1) {
@@ -320,7 +321,7 @@ class Engine {
         }
         // output faces cleaned (decompose.ts:189, merge.ts:213); the kernel's
         // volume stays the part's hull volume
-        const uint32_t* raw = tris.data() + (size_t)k * stride;
+        const uint32_t* raw = tris.get() + (size_t)k * stride;
         if (defer) {
           std::vector<uint32_t> rt(raw, raw + 3 * (size_t)ntri[k]);
           std::vector<float> pv(m.v);

@@ -233,3 +233,18 @@ def test_empty_batches(tree_mod):
     assert len(g.hausdorff([])) == 0
     assert g.hull_meshes([])[0] == []
     assert g.hulls_with_hausdorff([]) == []
+
+
+def test_hull_batch_compact_readback_matches_single_batches(tree_mod):
+    """A hull batch whose export range is large (one 10,242-point hull sets
+    the stride of 80 meshes: about 20 MB) reads back each hull's own faces;
+    faces, counts and volumes equal those of the same meshes hulled one per
+    batch (whole-range readback)."""
+    meshes = [gen.noisy_icosphere(5, seed=1)] + [gen.noisy_icosphere(2 + (k % 2), seed=k) for k in range(79)]
+    g = tree_mod.GpuTree(width=3, width2=3, depth=1, nConcaveEdges=0, hullMaxVerts=16384, vertexCap=64 << 20,
+                         triCap=64 << 20, scratchWords=64 << 20, hullBudgetBytes=1 << 30)
+    many, st = g.hull_meshes(meshes)
+    assert all(s == 0 for s in st)
+    for m, h in zip(meshes, many):
+        (one,), (s1,) = g.hull_meshes([m])
+        assert s1 == 0 and one["volume"] == h["volume"] and np.array_equal(one["tris"], h["tris"])
