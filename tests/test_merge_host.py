@@ -66,3 +66,32 @@ def test_filtered_concat_drops_the_seam():
     on = lambda x: int(np.all(np.abs(x.verts[x.tris][:, :, 0] - 0.5) < 1e-6, axis=1).sum())  # noqa: E731
     assert on(a.mesh) == 6 and on(b.mesh) == 6
     assert m.nt == a.mesh.nt + b.mesh.nt - 12
+
+
+def test_seam_plane_and_filtered_concat_random_cuts(oracle):
+    """Pieces of noisy icospheres and blobs cut by seeded random planes: every
+    ordered pair's seam plane and filtered union equal the oracle's."""
+    rng = np.random.default_rng(11)
+    n = seams = 0
+    meshes = [G.noisy_icosphere(2, seed=5), G.noisy_icosphere(3, seed=6), M.normalize(G.blob_mesh(5, 22, seed=7))[0]]
+    for mesh in meshes:
+        lo, hi = mesh.verts.min(0).astype(np.float64), mesh.verts.max(0).astype(np.float64)
+        planes = []
+        for _ in range(3):
+            nrm = rng.normal(size=3)
+            nrm /= np.linalg.norm(nrm)
+            p = lo + rng.uniform(0.3, 0.7, 3) * (hi - lo)
+            planes.append([nrm[0], nrm[1], nrm[2], -float(nrm @ p)])
+        parts = MC.cut_parts(mesh, planes)
+        for a, b in itertools.permutations(parts, 2):
+            got = D.seam_plane(a, b, 1e-3)
+            ref = oracle.seam_plane(a, b, 1e-3)
+            assert (got is None) == (ref is None)
+            if got is not None:
+                assert np.array_equal(np.asarray(got), np.asarray(ref))
+                seams += 1
+            pl = ([got] if got else []) + [planes[0]]
+            assert np.array_equal(D.filtered_concat(a.mesh, b.mesh, pl, 1e-3).tris,
+                                  oracle.filtered_concat(a.mesh, b.mesh, pl, 1e-3))
+            n += 1
+    assert n > 60 and seams > 10, (n, seams)
