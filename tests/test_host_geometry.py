@@ -104,3 +104,48 @@ def test_concave_planes_reference_case():
     assert D.concave_planes(l_prism(), 8).shape == (4, 4)
     assert len(D.concave_planes(M.l_shape(), 8)) == 0
     assert len(D.concave_planes(M.unit_cube(), 8)) == 0
+
+
+def _slab(mesh, axis, at, width):
+    """The piece of mesh between two parallel planes `width` apart (the thin
+    slabs a decomposition slices off a flat stretch of surface)."""
+    n = [0.0, 0.0, 0.0]
+    n[axis] = 1.0
+    lo_pos, _ = D.plane_cut(mesh, n + [-at])  # x_axis >= at
+    _, slab = D.plane_cut(lo_pos, n + [-(at + width)])  # and <= at + width
+    return slab
+
+
+def test_plane_cut_of_thin_slabs_matches_oracle(oracle):
+    """Caps of thin slabs: long runs of nearly collinear boundary vertices
+    (the cut crosses the earlier caps along straight lines), the degenerate
+    polygons the ear clipper's flat mode handles."""
+    checked = 0
+    for mesh in (G.noisy_icosphere(3, seed=2), M.normalize(G.blob_mesh(6, 26, seed=3))[0], G.carved_sphere(3, 3, seed=2)):
+        v = mesh.verts.astype(np.float64)
+        lo, hi = v.min(0), v.max(0)
+        for axis, frac, width in ((1, 0.45, 0.004), (0, 0.6, 0.002), (2, 0.3, 0.01)):
+            try:
+                slab = _slab(mesh, axis, lo[axis] + frac * (hi[axis] - lo[axis]), width * (hi[axis] - lo[axis]))
+            except pkg("tree").CuacdError:
+                continue
+            sv = slab.verts.astype(np.float64)
+            c = (sv.min(0) + sv.max(0)) / 2
+            for pl in ([1, 0, 0, -c[0]], [0, 1, 0, -c[1]], [0, 0, 1, -c[2]], [0.6, 0.8, 0.0, -(0.6 * c[0] + 0.8 * c[1])]):
+                ref = oracle.plane_cut(slab, pl)
+                try:
+                    got = D.plane_cut(slab, pl)
+                except pkg("tree").CuacdError:
+                    got = None
+                assert (ref is None) == (got is None), (axis, pl)
+                if ref is None:
+                    continue
+                for r, g in zip(ref, got):
+                    rv = np.asarray(r.verts, np.float32).reshape(-1, 3)
+                    k = min(len(rv), len(g.verts))
+                    assert np.array_equal(rv[:k], g.verts[:k])
+                    assert M.is_closed(g)
+                    vr, vg = M.signed_volume(r), M.signed_volume(g)
+                    assert abs(vr - vg) <= 1e-6 * abs(vr) + 1e-12, (vr, vg)
+                checked += 1
+    assert checked >= 12, checked
